@@ -1,0 +1,218 @@
+/*
+ * nyxpm.h -- C ABI of the GB300-native particle-mesh (PM) gravity step for Nyx.
+ *
+ * One periodic, single-level, dark-matter-only grid ("box") per handle.  All
+ * particle and field state stays resident in GPU memory between calls; host
+ * buffers cross the boundary only in the upload / download calls and in the
+ * optional output pointers.  Every call is enqueued on the context's CUDA stream;
+ * calls that return host data synchronise that stream.  No call aborts the
+ * process: each returns an nyxpm_status and nyxpm_last_error() gives the text.
+ * One host thread per context.
+ *
+ * Each entry point names the Nyx interface it replaces (paths inside the Nyx
+ * source tree).  The plain FP64 form computes exactly what those routines
+ * compute on a periodic single level; the restated pieces that live in AMReX
+ * (CIC deposit, MLMG) follow the definitions written next to each call.
+ */
+#ifndef NYXPM_H
+#define NYXPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NYXPM_ABI_VERSION 1
+
+typedef enum nyxpm_status {
+    NYXPM_OK = 0,
+    NYXPM_INVALID_ARG = 1,    /* bad size, null pointer, unsupported grid */
+    NYXPM_OOM = 2,            /* device memory exhausted */
+    NYXPM_CUDA_ERROR = 3,     /* a CUDA runtime call or kernel failed */
+    NYXPM_NOT_CONVERGED = 4,  /* multigrid hit max_vcycles above tolerance */
+    NYXPM_TIMEOUT = 5,        /* a bounded device wait ran out */
+    NYXPM_NO_DEVICE = 6       /* no usable CUDA device */
+} nyxpm_status;
+
+/* Precision of a box's particle and field storage. */
+typedef enum nyxpm_precision {
+    NYXPM_FP64 = 0,           /* plain drop-in: FP64 everywhere */
+    NYXPM_MIXED = 1           /* FP32 cell-relative positions, FP32 deposit and V-cycles
+                                 inside FP64 defect correction */
+} nyxpm_precision;
+
+/* Flags of nyxpm_step. */
+#define NYXPM_STEP_REUSE_FIELD 1u  /* take the old-time field from the previous step's
+                                      new-time solve (one deposit + one solve per step)
+                                      instead of re-solving from the start-of-step
+                                      positions with a zero guess */
+
+typedef struct nyxpm_params {
+    int device;             /* CUDA device ordinal */
+    void* stream;           /* cudaStream_t to enqueue on; NULL: the context creates one */
+    double comoving_OmM;    /* nyx.comoving_OmM */
+    double comoving_OmR;    /* nyx.comoving_OmR */
+    double comoving_h;      /* nyx.comoving_h */
+    double gconst;          /* Gconst in code units (Mpc, M_sun, km/s) */
+    double rel_tol;         /* gravity.sl_tol / gravity.ml_tol */
+    int max_vcycles;        /* V-cycle limit per solve */
+    int nu1, nu2;           /* red-black Gauss-Seidel sweeps before / after the coarse correction */
+    int verbose;
+} nyxpm_params;
+
+typedef struct nyxpm_ctx nyxpm_ctx;
+typedef struct nyxpm_box nyxpm_box;
+
+/* Result of one solve (Gravity::solve_for_phi stores the final residual norm in
+ * level_solver_resnorm, Source/Gravity/Gravity.cpp:312-314). */
+typedef struct nyxpm_solve_info {
+    int vcycles;            /* V-cycles (FP64) or outer defect-correction iterations (mixed) */
+    int inner_vcycles;      /* FP32 V-cycles inside the defect correction (mixed only) */
+    double resnorm0;        /* ||rhs - L phi0||_inf */
+    double resnorm;         /* ||rhs - L phi||_inf at exit */
+    double bnorm;           /* ||rhs||_inf */
+} nyxpm_solve_info;
+
+typedef struct nyxpm_step_info {
+    nyxpm_solve_info old_solve;   /* zeroed when the old-time field was reused */
+    nyxpm_solve_info new_solve;
+} nyxpm_step_info;
+
+/* ---- context ---------------------------------------------------------------- */
+
+/* Defaults: device 0, own stream, Einstein-de Sitter with h = 0.675, Gconst of
+ * Source/Driver/constants_cosmo.H:15-16, rel_tol 1e-10, 100 V-cycles, nu1 = nu2 = 2. */
+void nyxpm_default_params(nyxpm_params* p);
+
+/* Replaces Gravity::Gravity (Source/Gravity/Gravity.cpp:49-68) and the particle
+ * container construction of Nyx::init_particles (Source/Particle/NyxParticles.cpp:378). */
+nyxpm_status nyxpm_create(const nyxpm_params* p, nyxpm_ctx** out);
+void nyxpm_destroy(nyxpm_ctx* ctx);
+const char* nyxpm_last_error(const nyxpm_ctx* ctx);
+int nyxpm_abi_version(void);
+/* The CUDA stream the context enqueues on (cudaStream_t). */
+void* nyxpm_stream(nyxpm_ctx* ctx);
+nyxpm_status nyxpm_synchronize(nyxpm_ctx* ctx);
+
+/* ---- boxes ------------------------------------------------------------------ */
+
+/* A periodic n^3 grid of side L (prob_lo = 0) holding up to np particles.
+ * n must be m * 2^k with m <= 8 (the multigrid coarsens by 2 down to m^3).
+ * All device memory the box needs is allocated here; no later call allocates. */
+nyxpm_status nyxpm_box_create(nyxpm_ctx* ctx, int n, double L, int64_t np,
+                              nyxpm_precision prec, nyxpm_box** out);
+nyxpm_status nyxpm_box_destroy(nyxpm_ctx* ctx, nyxpm_box* box);
+/* Device bytes held by a box of this shape (for admission by memory budget). */
+size_t nyxpm_box_bytes(int n, int64_t np, nyxpm_precision prec);
+
+/* Particle state in: pos and vel are np x 3 (x, y, z per particle), mass is np
+ * values or NULL for a uniform mass_scalar.  Particle ids are the row indices.
+ * (Replaces the AsciiFile/BinaryFile/cosmological fills of init_particles,
+ * Source/Particle/NyxParticles.cpp:378-591.) */
+nyxpm_status nyxpm_box_upload(nyxpm_ctx* ctx, nyxpm_box* box, const double* pos,
+                              const double* vel, const double* mass, double mass_scalar);
+/* Particle state out, in id order (row i = the particle uploaded in row i). */
+nyxpm_status nyxpm_box_download(nyxpm_ctx* ctx, nyxpm_box* box, double* pos, double* vel);
+
+/* Gravity::set_mass_offset (Source/Gravity/Gravity.cpp:975-1030) with
+ * NyxParticleContainer::sumParticleMass (Source/Particle/NyxParticleContainer.H:70-79):
+ * mass_offset = sum(m) / L^3.  Called by nyxpm_box_upload; returns the value. */
+nyxpm_status nyxpm_set_mass_offset(nyxpm_ctx* ctx, nyxpm_box* box, double* mass_offset);
+
+/* ---- the hot path -------------------------------------------------------------- */
+
+/* Periodic shift of positions into [0, L) and counting sort by deposit cell.
+ * Replaces NyxParticleContainer::RedistributeLocal (Source/Particle/NyxParticleContainer.H:123-136,
+ * called from Nyx::post_timestep, Source/Driver/Nyx.cpp:1421-1437).  Deterministic:
+ * equal keys keep their previous relative order. */
+nyxpm_status nyxpm_redistribute(nyxpm_ctx* ctx, nyxpm_box* box);
+
+/* CIC mass density of the particles (sorted first).  Replaces
+ * NyxParticleContainer::AssignDensitySingleLevel / AssignDensity
+ * (Source/Particle/NyxParticleContainer.H:90-97 -> AMReX AssignCellDensitySingleLevel;
+ * restated in-tree at Source/Particle/NeutrinoParticleContainer.cpp:160-320).
+ * The density stays on the device for nyxpm_solve_phi; rho_out (n^3, x fastest)
+ * may be NULL. */
+nyxpm_status nyxpm_deposit(nyxpm_ctx* ctx, nyxpm_box* box, double* rho_out);
+
+/* Gravity::solve_for_phi (Source/Gravity/Gravity.cpp:267-315): RHS = -4 pi G
+ * (rho - mass_offset - mean) / a from the last deposit, then multigrid V-cycles
+ * to ||r||_inf <= rel_tol * max(||rhs||_inf, ||r0||_inf).  zero_guess = 1 starts
+ * from phi = 0 (actual_multilevel_solve with use_previous_phi_as_guess = 0,
+ * Gravity.cpp:665-666); 0 starts from the current phi.  info may be NULL. */
+nyxpm_status nyxpm_solve_phi(nyxpm_ctx* ctx, nyxpm_box* box, double a, int zero_guess,
+                             nyxpm_solve_info* info);
+
+/* phi (PhiGrav_Type, n^3 x fastest) out / in. */
+nyxpm_status nyxpm_get_phi(nyxpm_ctx* ctx, nyxpm_box* box, double* phi);
+nyxpm_status nyxpm_set_phi(nyxpm_ctx* ctx, nyxpm_box* box, const double* phi);
+
+/* Cell-centred gravity vector g = average of the two face gradients of phi
+ * (Gravity::get_new_grav_vector, Source/Gravity/Gravity.cpp:817-850).  g_out
+ * receives 3 n^3 values, component-major; it may be NULL (the field then stays
+ * on the device). */
+nyxpm_status nyxpm_grav_vector(nyxpm_ctx* ctx, nyxpm_box* box, double* g_out);
+
+/* DarkMatterParticleContainer::moveKickDrift (Source/Particle/DarkMatterParticleContainer.cpp:76-181):
+ * CIC-interpolated g from the current phi (gradient fused), v = (a_old v + dt/2 g)/a_half,
+ * x += dt/a_half v (update_dm_particle_single, :250-306, do_move = 1). */
+nyxpm_status nyxpm_kick_drift(nyxpm_ctx* ctx, nyxpm_box* box, double dt, double a_old,
+                              double a_half);
+
+/* DarkMatterParticleContainer::moveKick (:184-247): v = (a_half v + dt/2 g)/a_new. */
+nyxpm_status nyxpm_kick(nyxpm_ctx* ctx, nyxpm_box* box, double dt, double a_new, double a_half);
+
+/* One PM step of Nyx::advance_particles_only on level 0
+ * (Source/TimeStep/Nyx_advance_particles.cpp:137-268) plus the periodic shift of
+ * Nyx::post_timestep: [old-time deposit + solve], kick-drift, deposit, new-time
+ * solve (old phi as guess), kick, wrap.  a_half = (a_old + a_new)/2.  flags:
+ * NYXPM_STEP_REUSE_FIELD.  info may be NULL. */
+nyxpm_status nyxpm_step(nyxpm_ctx* ctx, nyxpm_box* box, double a_old, double a_new, double dt,
+                        unsigned flags, nyxpm_step_info* info);
+
+/* The post_init solve (Nyx::post_init, Source/Driver/Nyx.cpp:1957-2005):
+ * redistribute, deposit, solve from phi = 0 at scale factor a. */
+nyxpm_status nyxpm_init_field(nyxpm_ctx* ctx, nyxpm_box* box, double a, nyxpm_solve_info* info);
+
+/* ---- a(t), FP64 on the host (Source/Driver/comoving.cpp) -------------------------- */
+
+/* Nyx::integrate_comoving_a(old_a, new_a, dt), comoving.cpp:629-688. */
+double nyxpm_integrate_a(const nyxpm_params* p, double a_old, double dt);
+/* Nyx::integrate_comoving_a_to_a, comoving.cpp:74-130 (dt_window = search window). */
+double nyxpm_dt_for_da(const nyxpm_params* p, double a_old, double a_value, double dt_window);
+
+/* ---- measurement ------------------------------------------------------------- */
+
+#define NYXPM_NUM_STAGES 12
+/* Stage ids of nyxpm_profile. */
+enum {
+    NYXPM_ST_KEYS = 0, NYXPM_ST_SCAN, NYXPM_ST_SCATTER, NYXPM_ST_GATHER, NYXPM_ST_DEPOSIT,
+    NYXPM_ST_RHS, NYXPM_ST_SMOOTH, NYXPM_ST_RESTRICT, NYXPM_ST_PROLONG, NYXPM_ST_BOTTOM,
+    NYXPM_ST_NORM, NYXPM_ST_KICK
+};
+
+typedef struct nyxpm_profile {
+    int64_t launches[NYXPM_NUM_STAGES];
+    double ms[NYXPM_NUM_STAGES];          /* summed CUDA-event time per stage */
+    double bytes[NYXPM_NUM_STAGES];       /* summed algorithmic bytes per stage */
+    /* finest-level red-black half sweeps only (the dominant kernel) */
+    int64_t fine_smooth_launches;
+    double fine_smooth_ms;
+    double fine_smooth_bytes;
+} nyxpm_profile;
+
+/* Record a CUDA event pair around every launch (off by default). */
+nyxpm_status nyxpm_set_profiling(nyxpm_ctx* ctx, int on);
+/* Synchronises, folds the recorded events into *out (accumulated since the last
+ * reset) and optionally resets. */
+nyxpm_status nyxpm_get_profile(nyxpm_ctx* ctx, nyxpm_profile* out, int reset);
+/* Number of kernels the context launched since creation. */
+int64_t nyxpm_launch_count(const nyxpm_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NYXPM_H */

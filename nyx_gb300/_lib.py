@@ -1,0 +1,134 @@
+"""ctypes binding of libnyxpm.so (include/nyxpm.h).
+
+The library is built in-tree by nyx_gb300/build.py.  There is no fallback: if
+the shared library is missing or cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnyxpm.so")
+
+NYXPM_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "NOT_CONVERGED",
+                5: "TIMEOUT", 6: "NO_DEVICE"}
+NYXPM_FP64 = 0
+NYXPM_MIXED = 1
+NYXPM_STEP_REUSE_FIELD = 1
+NUM_STAGES = 12
+STAGE_NAMES = ["keys", "scan", "scatter", "gather", "deposit", "rhs", "smooth", "restrict",
+               "prolong", "bottom", "norm", "kick"]
+
+# every symbol include/nyxpm.h declares
+EXPORTS = [
+    "nyxpm_default_params", "nyxpm_create", "nyxpm_destroy", "nyxpm_last_error",
+    "nyxpm_abi_version", "nyxpm_stream", "nyxpm_synchronize", "nyxpm_box_create",
+    "nyxpm_box_destroy", "nyxpm_box_bytes", "nyxpm_box_upload", "nyxpm_box_download",
+    "nyxpm_set_mass_offset", "nyxpm_redistribute", "nyxpm_deposit", "nyxpm_solve_phi",
+    "nyxpm_get_phi", "nyxpm_set_phi", "nyxpm_grav_vector", "nyxpm_kick_drift", "nyxpm_kick",
+    "nyxpm_step", "nyxpm_init_field", "nyxpm_integrate_a", "nyxpm_dt_for_da",
+    "nyxpm_set_profiling", "nyxpm_get_profile", "nyxpm_launch_count",
+]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("device", C.c_int),
+        ("stream", C.c_void_p),
+        ("comoving_OmM", C.c_double),
+        ("comoving_OmR", C.c_double),
+        ("comoving_h", C.c_double),
+        ("gconst", C.c_double),
+        ("rel_tol", C.c_double),
+        ("max_vcycles", C.c_int),
+        ("nu1", C.c_int),
+        ("nu2", C.c_int),
+        ("verbose", C.c_int),
+    ]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [
+        ("vcycles", C.c_int),
+        ("inner_vcycles", C.c_int),
+        ("resnorm0", C.c_double),
+        ("resnorm", C.c_double),
+        ("bnorm", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class StepInfo(C.Structure):
+    _fields_ = [("old_solve", SolveInfo), ("new_solve", SolveInfo)]
+
+
+class Profile(C.Structure):
+    _fields_ = [
+        ("launches", C.c_int64 * NUM_STAGES),
+        ("ms", C.c_double * NUM_STAGES),
+        ("bytes", C.c_double * NUM_STAGES),
+        ("fine_smooth_launches", C.c_int64),
+        ("fine_smooth_ms", C.c_double),
+        ("fine_smooth_bytes", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load libnyxpm.so (building it first if the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    from . import build as _build
+    if path is None:
+        if not os.path.exists(LIB_PATH) or _build._stale():
+            _build.build()
+        path = LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"libnyxpm.so not found at {path}; run nyx_gb300/build.py")
+    L = C.CDLL(path)
+    vp, i64, d = C.c_void_p, C.c_int64, C.c_double
+    L.nyxpm_default_params.argtypes = [C.POINTER(Params)]
+    L.nyxpm_default_params.restype = None
+    L.nyxpm_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
+    L.nyxpm_destroy.argtypes = [vp]
+    L.nyxpm_destroy.restype = None
+    L.nyxpm_last_error.argtypes = [vp]
+    L.nyxpm_last_error.restype = C.c_char_p
+    L.nyxpm_abi_version.restype = C.c_int
+    L.nyxpm_stream.argtypes = [vp]
+    L.nyxpm_stream.restype = vp
+    L.nyxpm_synchronize.argtypes = [vp]
+    L.nyxpm_box_create.argtypes = [vp, C.c_int, d, i64, C.c_int, C.POINTER(vp)]
+    L.nyxpm_box_destroy.argtypes = [vp, vp]
+    L.nyxpm_box_bytes.argtypes = [C.c_int, i64, C.c_int]
+    L.nyxpm_box_bytes.restype = C.c_size_t
+    L.nyxpm_box_upload.argtypes = [vp, vp, vp, vp, vp, d]
+    L.nyxpm_box_download.argtypes = [vp, vp, vp, vp]
+    L.nyxpm_set_mass_offset.argtypes = [vp, vp, C.POINTER(d)]
+    L.nyxpm_redistribute.argtypes = [vp, vp]
+    L.nyxpm_deposit.argtypes = [vp, vp, vp]
+    L.nyxpm_solve_phi.argtypes = [vp, vp, d, C.c_int, C.POINTER(SolveInfo)]
+    L.nyxpm_get_phi.argtypes = [vp, vp, vp]
+    L.nyxpm_set_phi.argtypes = [vp, vp, vp]
+    L.nyxpm_grav_vector.argtypes = [vp, vp, vp]
+    L.nyxpm_kick_drift.argtypes = [vp, vp, d, d, d]
+    L.nyxpm_kick.argtypes = [vp, vp, d, d, d]
+    L.nyxpm_step.argtypes = [vp, vp, d, d, d, C.c_uint, C.POINTER(StepInfo)]
+    L.nyxpm_init_field.argtypes = [vp, vp, d, C.POINTER(SolveInfo)]
+    L.nyxpm_integrate_a.argtypes = [C.POINTER(Params), d, d]
+    L.nyxpm_integrate_a.restype = d
+    L.nyxpm_dt_for_da.argtypes = [C.POINTER(Params), d, d, d]
+    L.nyxpm_dt_for_da.restype = d
+    L.nyxpm_set_profiling.argtypes = [vp, C.c_int]
+    L.nyxpm_get_profile.argtypes = [vp, C.POINTER(Profile), C.c_int]
+    L.nyxpm_launch_count.argtypes = [vp]
+    L.nyxpm_launch_count.restype = i64
+    _lib = L
+    return L

@@ -1,0 +1,220 @@
+// Internal declarations shared by the translation units of libnyxpm.
+//
+// Layouts in device memory (one box = one periodic n^3 grid):
+//   particles  structure of arrays, FP64: x y z vx vy vz [m] id, kept sorted by
+//              deposit key (cell of floor(x/dx + 1/2)), double-buffered for the
+//              counting-sort gather;
+//   cell index c = i + n*(j + n*k), x fastest;
+//   rho        n^3, natural layout;
+//   multigrid  every smoothed level stores phi and rhs red-black split: the red
+//              cells ((i+j+k) even) and the black cells in two arrays of n^3/2,
+//              compact index (i>>1) + (n/2)*(j + n*k), so a half sweep streams
+//              exactly one array of each colour; the coarsest level (n <= 8) is
+//              natural layout.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/nyxpm.h"
+
+namespace nyxpm {
+
+constexpr int kMaxBottom = 8;          // coarsest grid edge solved exactly
+
+struct Level {
+    int n = 0;
+    int split = 0;                     // 1: red/black arrays, 0: natural layout
+    double h2 = 0, ih2 = 0;
+    double* phi_r = nullptr;           // split: red n^3/2; natural: n^3
+    double* phi_b = nullptr;           // split: black n^3/2; natural: unused
+    double* rhs_r = nullptr;
+    double* rhs_b = nullptr;
+    // FP32 copies for the mixed-precision inner V-cycles
+    float* fphi_r = nullptr;
+    float* fphi_b = nullptr;
+    float* frhs_r = nullptr;
+    float* frhs_b = nullptr;
+};
+
+// device view of one level
+struct LevelView {
+    int n, split;
+    double h2, ih2;
+    double* phi_r;
+    double* phi_b;
+    double* rhs_r;
+    double* rhs_b;
+};
+
+struct LevelViewF {
+    int n, split;
+    float h2, ih2;
+    float* phi_r;
+    float* phi_b;
+    float* rhs_r;
+    float* rhs_b;
+};
+
+inline LevelView view(const Level& l)
+{
+    return LevelView{l.n, l.split, l.h2, l.ih2, l.phi_r, l.phi_b, l.rhs_r, l.rhs_b};
+}
+
+inline LevelViewF viewf(const Level& l)
+{
+    return LevelViewF{l.n, l.split, (float)l.h2, (float)l.ih2, l.fphi_r, l.fphi_b, l.frhs_r,
+                      l.frhs_b};
+}
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+__host__ __device__ inline int wrapi(int i, int n)
+{
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+__host__ __device__ inline long long cidx(int i, int j, int k, int n)
+{
+    return (long long)i + (long long)n * ((long long)j + (long long)n * k);
+}
+
+// pointer to phi (or rhs) at cell (i,j,k) of a level in either layout
+template <typename T>
+__device__ inline T* lv_ptr(T* r, T* b, int n, int split, int i, int j, int k)
+{
+    if (!split) return r + cidx(i, j, k, n);
+    const int half = n >> 1;
+    T* base = ((i + j + k) & 1) ? b : r;
+    return base + (long long)(i >> 1) + (long long)half * ((long long)j + (long long)n * k);
+}
+
+// ---------------------------------------------------------------------------
+// box
+// ---------------------------------------------------------------------------
+struct ProfRec {
+    int stage;
+    int fine;
+    double bytes;
+};
+
+struct Ctx;
+
+struct Box {
+    int n = 0;
+    double L = 0, dx = 0, dxi = 0;
+    int64_t np = 0;
+    nyxpm_precision prec = NYXPM_FP64;
+    int uniform_mass = 1;
+    double mscalar = 0;
+    double mass_offset = 0;
+    int sorted = 0;
+    int uploaded = 0;
+    int have_phi = 0;
+
+    // particles (FP64 form)
+    double *x = nullptr, *y = nullptr, *z = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr,
+           *m = nullptr;
+    int* id = nullptr;
+    double *x2 = nullptr, *y2 = nullptr, *z2 = nullptr, *vx2 = nullptr, *vy2 = nullptr,
+           *vz2 = nullptr, *m2 = nullptr;
+    int* id2 = nullptr;
+
+    // particles (mixed form): cell-relative FP32
+    int* cell = nullptr;               // linear cell of floor(x/dx)
+    float *ox = nullptr, *oy = nullptr, *oz = nullptr;   // offset within the cell, [0,1)
+    float *fvx = nullptr, *fvy = nullptr, *fvz = nullptr;
+    float* fm = nullptr;
+    int* cell2 = nullptr;
+    float *ox2 = nullptr, *oy2 = nullptr, *oz2 = nullptr, *fvx2 = nullptr, *fvy2 = nullptr,
+          *fvz2 = nullptr, *fm2 = nullptr;
+
+    // sort scratch
+    int* key = nullptr;
+    int* perm = nullptr;
+    int* cell_count = nullptr;         // n^3, all zero between sorts
+    int* cell_start = nullptr;         // n^3 + 1
+    int* tile_sums = nullptr;
+    int ntiles = 0;
+    int* long_list = nullptr;          // keys of segments longer than a warp
+    int* long_count = nullptr;
+
+    // fields
+    double* rho = nullptr;             // n^3
+    float* frho = nullptr;             // n^3 (mixed)
+    double* g = nullptr;               // 3 n^3
+    double* rows = nullptr;            // n^2 row sums
+    double* planes = nullptr;          // n plane sums
+    double* scal = nullptr;            // [0] mean
+    unsigned long long* norms = nullptr;   // [0] ||rhs||inf, [1] ||r||inf, [2] bad uploads
+    unsigned long long* h_norms = nullptr; // pinned host mirror
+    double* G = nullptr;               // bottom Green's function
+    int nb = 0;
+    std::vector<Level> levels;
+    double* resid = nullptr;           // mixed: FP64 outer residual scratch (n^3, natural)
+
+    // host<->device staging: AoS pos (3 np), vel (3 np), mass (np) doubles
+    double* staging = nullptr;
+
+    std::vector<void*> allocs;
+};
+
+struct Ctx {
+    nyxpm_params p{};
+    cudaStream_t stream = nullptr;
+    int own_stream = 0;
+    std::string err;
+    int64_t launches = 0;
+    // profiling
+    int prof_on = 0;
+    std::vector<cudaEvent_t> ev_a, ev_b;
+    std::vector<ProfRec> recs;
+    nyxpm_profile acc{};
+    int sm_count = 0;
+};
+
+// launch bookkeeping: call prof_begin before and prof_end after each launch
+void prof_begin(Ctx& c);
+void prof_end(Ctx& c, int stage, double bytes, int fine = 0);
+nyxpm_status check_launch(Ctx& c, const char* what);
+
+// ---------------------------------------------------------------------------
+// launchers (defined in pm_particles.cu / pm_multigrid.cu / pm_mixed.cu)
+// ---------------------------------------------------------------------------
+nyxpm_status launch_unpack(Ctx& c, Box& b, const double* d_pos, const double* d_vel,
+                           const double* d_mass);
+nyxpm_status launch_pack(Ctx& c, Box& b, double* d_pos, double* d_vel);
+nyxpm_status launch_wrap(Ctx& c, Box& b);
+nyxpm_status launch_sort(Ctx& c, Box& b);
+nyxpm_status launch_deposit(Ctx& c, Box& b);
+nyxpm_status launch_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move,
+                         int do_wrap);
+
+nyxpm_status launch_make_rhs(Ctx& c, Box& b, double a);
+nyxpm_status launch_zero_phi(Ctx& c, Box& b);
+nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info);
+nyxpm_status launch_grav_vector(Ctx& c, Box& b);
+nyxpm_status launch_phi_to_natural(Ctx& c, Box& b, double* d_out);
+nyxpm_status launch_phi_from_natural(Ctx& c, Box& b, const double* d_in);
+
+// mixed-precision form
+nyxpm_status mixed_unpack(Ctx& c, Box& b, const double* d_pos, const double* d_vel,
+                          const double* d_mass);
+nyxpm_status mixed_pack(Ctx& c, Box& b, double* d_pos, double* d_vel);
+nyxpm_status mixed_sort(Ctx& c, Box& b);
+nyxpm_status mixed_deposit(Ctx& c, Box& b);
+nyxpm_status mixed_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move);
+nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info);
+
+// host-side helpers shared by the forms
+nyxpm_status scan_counts(Ctx& c, Box& b);   // cell_count -> cell_start
+nyxpm_status fix_segments(Ctx& c, Box& b);  // deterministic order inside each key segment
+
+}  // namespace nyxpm
+
+struct nyxpm_ctx : public nyxpm::Ctx {};
+struct nyxpm_box : public nyxpm::Box {};

@@ -1,0 +1,467 @@
+// Comoving Poisson solve of the FP64 PM step: RHS assembly with the mean
+// density removed (Gravity::solve_for_phi + CorrectRhsUsingOffset,
+// Source/Gravity/Gravity.cpp:267-315, 1207-1244) and a geometric multigrid
+// V-cycle with red-black Gauss-Seidel smoothing on the red-black split layout,
+// the GB300-native replacement of the AMReX MLMG solve that
+// Gravity::solve_with_MLMG (Gravity.cpp:1318-1416) calls.
+//
+// Built with --fmad=false so that every expression rounds as written.
+#include "pm_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace nyxpm {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr double kSixth = 1.0 / 6.0;
+
+inline unsigned blocks_for(long long n, int t = kThreads)
+{
+    long long b = (n + t - 1) / t;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+// ---------------------------------------------------------------------------
+// RHS: canonical sum of (rho - mass_offset), then
+// rhs = (((rho - mass_offset) - mean) * ggrav) * (1/a)
+// ---------------------------------------------------------------------------
+// one warp per row: 32 strided lane partials, then a halving tree
+__global__ void k_rowsum(int n, const double* __restrict__ rho, double mo, double* rows)
+{
+    const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= (long long)n * n) return;
+    const double* r = rho + row * n;
+    double s = 0.0;
+    for (int i = lane; i < n; i += 32) s = s + (r[i] - mo);
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const double t = __shfl_down_sync(0xffffffffu, s, off);
+        if (lane < off) s = s + t;
+    }
+    if (lane == 0) rows[row] = s;
+}
+
+__global__ void k_planesum(int n, const double* __restrict__ rows, double* planes)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) s = s + rows[(long long)k * n + j];
+    planes[k] = s;
+}
+
+__global__ void k_mean(int n, double dx, double L, const double* __restrict__ planes, double* scal)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0;
+    for (int k = 0; k < n; ++k) s = s + planes[k];
+    scal[0] = (s * (dx * dx * dx)) / (L * L * L);
+}
+
+__global__ void k_make_rhs(int n, int split, const double* __restrict__ rho, double mo,
+                           const double* __restrict__ scal, double ggrav, double ainv, double* rhs_r,
+                           double* rhs_b)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nc = (long long)n * n * n;
+    if (c >= nc) return;
+    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
+    const double mean = scal[0];
+    *lv_ptr<double>(rhs_r, rhs_b, n, split, i, j, k) = (((rho[c] - mo) - mean) * ggrav) * ainv;
+}
+
+// ---------------------------------------------------------------------------
+// norms (max is order independent; non-negative doubles compare as their bits)
+// ---------------------------------------------------------------------------
+// max that keeps a NaN (so a diverged solve is seen by the host)
+__device__ __forceinline__ double nanmax(double a, double b)
+{
+    return (a != a) ? a : ((b != b) ? b : (a > b ? a : b));
+}
+
+__device__ __forceinline__ void block_max_store(double v, unsigned long long* out)
+{
+    __shared__ double sm[32];
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, off));
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, off));
+        if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+__global__ void k_absmax(long long cnt, const double* __restrict__ a, unsigned long long* out)
+{
+    double v = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < cnt;
+         t += (long long)gridDim.x * blockDim.x) {
+        const double u = fabs(a[t]);
+        v = (u > v || u != u) ? u : v;
+    }
+    block_max_store(v, out);
+}
+
+// neighbour sum in the oracle's order: x-, x+, y-, y+, z-, z+
+__device__ __forceinline__ double nbr_sum(const LevelView& L, int i, int j, int k)
+{
+    const int n = L.n;
+    const int im = i == 0 ? n - 1 : i - 1, ip = i == n - 1 ? 0 : i + 1;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    double s = *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, im, j, k) +
+               *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, ip, j, k);
+    s = s + *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, i, jm, k);
+    s = s + *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, i, jp, k);
+    s = s + *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, i, j, km);
+    s = s + *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, i, j, kp);
+    return s;
+}
+
+__device__ __forceinline__ double resid_at(const LevelView& L, int i, int j, int k)
+{
+    const double s = nbr_sum(L, i, j, k);
+    const double c = *lv_ptr<double>(L.phi_r, L.phi_b, L.n, L.split, i, j, k);
+    const double r = *lv_ptr<double>(L.rhs_r, L.rhs_b, L.n, L.split, i, j, k);
+    return r - (s - 6.0 * c) * L.ih2;
+}
+
+__global__ void k_resnorm(LevelView L, unsigned long long* out)
+{
+    const long long nc = (long long)L.n * L.n * L.n;
+    double v = 0.0;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % L.n), j = (int)((c / L.n) % L.n), k = (int)(c / ((long long)L.n * L.n));
+        const double u = fabs(resid_at(L, i, j, k));
+        v = (u > v || u != u) ? u : v;
+    }
+    block_max_store(v, out);
+}
+
+// ---------------------------------------------------------------------------
+// red-black Gauss-Seidel half sweep on a split level: one thread per cell of
+// the colour being updated; reads the other colour's array, writes this one.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_gsrb(int n, double h2, int color, double* __restrict__ mine,
+                                              const double* __restrict__ other,
+                                              const double* __restrict__ rhs)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int half = n >> 1;
+    const long long cnt = (long long)half * n * n;
+    if (t >= cnt) return;
+    const int ih = (int)(t % half);
+    const long long row = t / half;
+    const int j = (int)(row % n), k = (int)(row / n);
+    const int q = (j + k + color) & 1;  // this cell is i = 2*ih + q
+    const int ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
+    const int ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    const long long rb = row * half;
+    double s = other[rb + ihm] + other[rb + ihp];
+    s = s + other[(long long)half * (jm + (long long)n * k) + ih];
+    s = s + other[(long long)half * (jp + (long long)n * k) + ih];
+    s = s + other[(long long)half * (j + (long long)n * km) + ih];
+    s = s + other[(long long)half * (j + (long long)n * kp) + ih];
+    mine[t] = (s - h2 * rhs[t]) * kSixth;
+}
+
+// coarse rhs = 1/8 of the 8 fine residuals (summed dk, dj, di); coarse phi = 0
+__global__ void k_restrict(LevelView F, LevelView Cv)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nc = Cv.n;
+    if (c >= (long long)nc * nc * nc) return;
+    const int I = (int)(c % nc), J = (int)((c / nc) % nc), K = (int)(c / ((long long)nc * nc));
+    double s = 0.0;
+#pragma unroll
+    for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+            for (int di = 0; di < 2; ++di) s = s + resid_at(F, 2 * I + di, 2 * J + dj, 2 * K + dk);
+    *lv_ptr<double>(Cv.rhs_r, Cv.rhs_b, nc, Cv.split, I, J, K) = s * 0.125;
+    *lv_ptr<double>(Cv.phi_r, Cv.phi_b, nc, Cv.split, I, J, K) = 0.0;
+}
+
+// trilinear cell-centred prolongation of the coarse correction, added to the fine phi
+__global__ void k_prolong(LevelView Cv, LevelView F)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = F.n, nc = Cv.n;
+    if (c >= (long long)n * n * n) return;
+    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
+    const double w[2] = {0.75, 0.25};
+    const int I = i >> 1, J = j >> 1, K = k >> 1;
+    const int Is[2] = {I, wrapi((i & 1) ? I + 1 : I - 1, nc)};
+    const int Js[2] = {J, wrapi((j & 1) ? J + 1 : J - 1, nc)};
+    const int Ks[2] = {K, wrapi((k & 1) ? K + 1 : K - 1, nc)};
+    double s = 0.0;
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int t = 0; t < 2; ++t)
+                s = s + ((w[t] * w[a]) * w[b]) *
+                            *lv_ptr<const double>(Cv.phi_r, Cv.phi_b, nc, Cv.split, Is[t], Js[a], Ks[b]);
+    double* p = lv_ptr<double>(F.phi_r, F.phi_b, n, F.split, i, j, k);
+    *p = *p + s;
+}
+
+// exact coarsest solve: phi = G * rhs (circulant pseudo-inverse), one block
+__global__ void k_bottom(int nb, const double* __restrict__ G, const double* __restrict__ rhs,
+                         double* phi)
+{
+    __shared__ double r[kMaxBottom * kMaxBottom * kMaxBottom];
+    const int nc = nb * nb * nb;
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) r[t] = rhs[t];
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const int i = c % nb, j = (c / nb) % nb, k = c / (nb * nb);
+        double s = 0.0;
+        for (int y = 0; y < nc; ++y) {
+            const int yi = y % nb, yj = (y / nb) % nb, yk = y / (nb * nb);
+            const int d = wrapi(i - yi, nb) + nb * (wrapi(j - yj, nb) + nb * wrapi(k - yk, nb));
+            s = s + G[d] * r[y];
+        }
+        phi[c] = s;
+    }
+}
+
+// g_d(c) = 0.5*((phi_c - phi_{c-e_d})*dxi + (phi_{c+e_d} - phi_c)*dxi), component-major
+__global__ void k_grav(LevelView L, double dxi, double* g)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = L.n;
+    const long long nc = (long long)n * n * n;
+    if (c >= nc) return;
+    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
+    auto P = [&](int a, int b, int d) {
+        return *lv_ptr<const double>(L.phi_r, L.phi_b, n, L.split, wrapi(a, n), wrapi(b, n), wrapi(d, n));
+    };
+    const double pc = P(i, j, k);
+    g[c] = 0.5 * ((pc - P(i - 1, j, k)) * dxi + (P(i + 1, j, k) - pc) * dxi);
+    g[nc + c] = 0.5 * ((pc - P(i, j - 1, k)) * dxi + (P(i, j + 1, k) - pc) * dxi);
+    g[2 * nc + c] = 0.5 * ((pc - P(i, j, k - 1)) * dxi + (P(i, j, k + 1) - pc) * dxi);
+}
+
+__global__ void k_to_natural(LevelView L, double* out)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = L.n;
+    if (c >= (long long)n * n * n) return;
+    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
+    out[c] = *lv_ptr<const double>(L.phi_r, L.phi_b, n, L.split, i, j, k);
+}
+
+__global__ void k_from_natural(LevelView L, const double* __restrict__ in)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = L.n;
+    if (c >= (long long)n * n * n) return;
+    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
+    *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, i, j, k) = in[c];
+}
+
+inline unsigned norm_blocks(Ctx& c, long long cnt)
+{
+    long long b = (cnt + kThreads - 1) / kThreads;
+    long long cap = (long long)c.sm_count * 8;
+    return (unsigned)std::max<long long>(1, std::min(b, cap));
+}
+
+nyxpm_status gsrb_sweep(Ctx& c, const Level& l, int fine)
+{
+    const long long half_cells = (long long)l.n * l.n * l.n / 2;
+    for (int color = 0; color < 2; ++color) {
+        double* mine = color ? l.phi_b : l.phi_r;
+        const double* other = color ? l.phi_r : l.phi_b;
+        const double* rhs = color ? l.rhs_b : l.rhs_r;
+        prof_begin(c);
+        k_gsrb<<<blocks_for(half_cells), kThreads, 0, c.stream>>>(l.n, l.h2, color, mine, other, rhs);
+        prof_end(c, NYXPM_ST_SMOOTH, 24.0 * half_cells, fine);
+    }
+    return check_launch(c, "gsrb");
+}
+
+nyxpm_status vcycle(Ctx& c, Box& b, size_t li)
+{
+    nyxpm_status st;
+    const Level& f = b.levels[li];
+    if (li + 1 == b.levels.size()) {
+        prof_begin(c);
+        k_bottom<<<1, 512, 0, c.stream>>>(b.nb, b.G, f.rhs_r, f.phi_r);
+        prof_end(c, NYXPM_ST_BOTTOM, 16.0 * f.n * f.n * f.n);
+        return check_launch(c, "bottom");
+    }
+    const int nu1 = c.p.nu1, nu2 = c.p.nu2;
+    for (int s = 0; s < nu1; ++s)
+        if ((st = gsrb_sweep(c, f, li == 0)) != NYXPM_OK) return st;
+    const Level& cl = b.levels[li + 1];
+    const long long ncc = (long long)cl.n * cl.n * cl.n;
+    const long long ncf = (long long)f.n * f.n * f.n;
+    prof_begin(c);
+    k_restrict<<<blocks_for(ncc), kThreads, 0, c.stream>>>(view(f), view(cl));
+    prof_end(c, NYXPM_ST_RESTRICT, 16.0 * ncf + 16.0 * ncc);
+    if ((st = check_launch(c, "restrict")) != NYXPM_OK) return st;
+    if ((st = vcycle(c, b, li + 1)) != NYXPM_OK) return st;
+    prof_begin(c);
+    k_prolong<<<blocks_for(ncf), kThreads, 0, c.stream>>>(view(cl), view(f));
+    prof_end(c, NYXPM_ST_PROLONG, 16.0 * ncf + 8.0 * ncc);
+    if ((st = check_launch(c, "prolong")) != NYXPM_OK) return st;
+    for (int s = 0; s < nu2; ++s)
+        if ((st = gsrb_sweep(c, f, li == 0)) != NYXPM_OK) return st;
+    return NYXPM_OK;
+}
+
+// launch ||r||_inf of level 0 into norms[slot]
+nyxpm_status launch_resnorm(Ctx& c, Box& b, int slot)
+{
+    const Level& l = b.levels[0];
+    const long long nc = (long long)l.n * l.n * l.n;
+    prof_begin(c);
+    cudaMemsetAsync(b.norms + slot, 0, sizeof(unsigned long long), c.stream);
+    k_resnorm<<<norm_blocks(c, nc), kThreads, 0, c.stream>>>(view(l), b.norms + slot);
+    prof_end(c, NYXPM_ST_NORM, 16.0 * nc);
+    return check_launch(c, "resnorm");
+}
+
+double read_norm(Box& b, int slot)
+{
+    double v;
+    std::memcpy(&v, &b.h_norms[slot], sizeof(v));
+    return v;
+}
+
+}  // namespace
+
+nyxpm_status launch_make_rhs(Ctx& c, Box& b, double a)
+{
+    const int n = b.n;
+    const long long nc = (long long)n * n * n;
+    const Level& l0 = b.levels[0];
+    const double dx = b.L / n;
+    prof_begin(c);
+    k_rowsum<<<blocks_for((long long)n * n * 32), kThreads, 0, c.stream>>>(n, b.rho, b.mass_offset,
+                                                                          b.rows);
+    k_planesum<<<blocks_for(n, 128), 128, 0, c.stream>>>(n, b.rows, b.planes);
+    k_mean<<<1, 32, 0, c.stream>>>(n, dx, b.L, b.planes, b.scal);
+    k_make_rhs<<<blocks_for(nc), kThreads, 0, c.stream>>>(n, l0.split, b.rho, b.mass_offset, b.scal,
+                                                          -4.0 * M_PI * c.p.gconst, 1.0 / a,
+                                                          l0.rhs_r, l0.rhs_b);
+    prof_end(c, NYXPM_ST_RHS, 24.0 * nc);
+    c.launches += 3;
+    return check_launch(c, "make rhs");
+}
+
+nyxpm_status launch_zero_phi(Ctx& c, Box& b)
+{
+    const Level& l0 = b.levels[0];
+    const size_t nc = (size_t)l0.n * l0.n * l0.n;
+    if (l0.split) {
+        cudaMemsetAsync(l0.phi_r, 0, sizeof(double) * nc / 2, c.stream);
+        cudaMemsetAsync(l0.phi_b, 0, sizeof(double) * nc / 2, c.stream);
+    } else {
+        cudaMemsetAsync(l0.phi_r, 0, sizeof(double) * nc, c.stream);
+    }
+    return check_launch(c, "zero phi");
+}
+
+nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
+{
+    nyxpm_status st;
+    const Level& l0 = b.levels[0];
+    const long long nc = (long long)l0.n * l0.n * l0.n;
+    // ||rhs||_inf and ||r0||_inf
+    prof_begin(c);
+    cudaMemsetAsync(b.norms, 0, sizeof(unsigned long long), c.stream);
+    if (l0.split) {
+        k_absmax<<<norm_blocks(c, nc / 2), kThreads, 0, c.stream>>>(nc / 2, l0.rhs_r, b.norms);
+        k_absmax<<<norm_blocks(c, nc / 2), kThreads, 0, c.stream>>>(nc / 2, l0.rhs_b, b.norms);
+        c.launches += 1;
+    } else {
+        k_absmax<<<norm_blocks(c, nc), kThreads, 0, c.stream>>>(nc, l0.rhs_r, b.norms);
+    }
+    prof_end(c, NYXPM_ST_NORM, 8.0 * nc);
+    if ((st = check_launch(c, "rhs norm")) != NYXPM_OK) return st;
+    if ((st = launch_resnorm(c, b, 1)) != NYXPM_OK) return st;
+    cudaMemcpyAsync(b.h_norms, b.norms, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                    c.stream);
+    if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "solve sync");
+    const double bnorm = read_norm(b, 0);
+    const double r0 = read_norm(b, 1);
+    const double target = c.p.rel_tol * std::max(bnorm, r0);
+    double r = r0;
+    int it = 0;
+    nyxpm_status result = NYXPM_OK;
+    if (!(r0 <= target)) {
+        for (it = 1; it <= c.p.max_vcycles; ++it) {
+            if ((st = vcycle(c, b, 0)) != NYXPM_OK) return st;
+            if ((st = launch_resnorm(c, b, 1)) != NYXPM_OK) return st;
+            cudaMemcpyAsync(b.h_norms + 1, b.norms + 1, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, c.stream);
+            if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "solve sync");
+            r = read_norm(b, 1);
+            if (r != r) {
+                c.err = "multigrid residual is NaN";
+                return NYXPM_NOT_CONVERGED;
+            }
+            if (r <= target) break;
+        }
+        if (it > c.p.max_vcycles) {
+            it = c.p.max_vcycles;
+            result = NYXPM_NOT_CONVERGED;
+            c.err = "multigrid reached max_vcycles above tolerance";
+        }
+    }
+    b.have_phi = 1;
+    if (info) {
+        info->vcycles = it;
+        info->inner_vcycles = 0;
+        info->resnorm0 = r0;
+        info->resnorm = r;
+        info->bnorm = bnorm;
+    }
+    return result;
+}
+
+nyxpm_status launch_grav_vector(Ctx& c, Box& b)
+{
+    const long long nc = (long long)b.n * b.n * b.n;
+    prof_begin(c);
+    k_grav<<<blocks_for(nc), kThreads, 0, c.stream>>>(view(b.levels[0]), b.dxi, b.g);
+    prof_end(c, NYXPM_ST_KICK, 32.0 * nc);
+    return check_launch(c, "grav vector");
+}
+
+nyxpm_status launch_phi_to_natural(Ctx& c, Box& b, double* d_out)
+{
+    const long long nc = (long long)b.n * b.n * b.n;
+    prof_begin(c);
+    k_to_natural<<<blocks_for(nc), kThreads, 0, c.stream>>>(view(b.levels[0]), d_out);
+    prof_end(c, NYXPM_ST_GATHER, 16.0 * nc);
+    return check_launch(c, "phi to natural");
+}
+
+nyxpm_status launch_phi_from_natural(Ctx& c, Box& b, const double* d_in)
+{
+    const long long nc = (long long)b.n * b.n * b.n;
+    prof_begin(c);
+    k_from_natural<<<blocks_for(nc), kThreads, 0, c.stream>>>(view(b.levels[0]), d_in);
+    prof_end(c, NYXPM_ST_GATHER, 16.0 * nc);
+    return check_launch(c, "phi from natural");
+}
+
+}  // namespace nyxpm

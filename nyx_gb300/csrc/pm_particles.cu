@@ -1,0 +1,583 @@
+// Particle kernels of the FP64 PM step: upload/download, periodic wrap, the
+// per-step counting sort by deposit cell, the atomic-free CIC deposit and the
+// fused gradient + CIC interpolation + kick(-drift).
+//
+// Built with --fmad=false: every FP64 expression rounds exactly as written,
+// in the order written, which is what update_dm_particle_single
+// (Source/Particle/DarkMatterParticleContainer.cpp:250-306) and the CIC weights
+// (Source/Particle/NeutrinoParticles_K.H:15-45) specify.
+#include "pm_common.cuh"
+
+#include <cstdio>
+
+namespace nyxpm {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned blocks_for(long long n, int t = kThreads)
+{
+    long long b = (n + t - 1) / t;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+// deposit key along one axis: floor(x*dxi + 1/2) wrapped into [0, n)
+__device__ __forceinline__ int key1(double x, double dxi, int n, double* frac)
+{
+    const double l = x * dxi + 0.5;
+    const int i = (int)floor(l);
+    *frac = l - (double)i;
+    return wrapi(i, n);
+}
+
+// ---------------------------------------------------------------------------
+// upload / download (AoS host layout <-> SoA device layout)
+// ---------------------------------------------------------------------------
+__global__ void k_unpack(long long np, const double* __restrict__ pos, const double* __restrict__ vel,
+                         const double* __restrict__ mass, double* x, double* y, double* z, double* vx,
+                         double* vy, double* vz, double* m, int* id, unsigned long long* bad)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) ok = ok && isfinite(pos[3 * q + d]) && isfinite(vel[3 * q + d]);
+    if (!ok) atomicAdd(bad, 1ULL);
+    x[q] = pos[3 * q];
+    y[q] = pos[3 * q + 1];
+    z[q] = pos[3 * q + 2];
+    vx[q] = vel[3 * q];
+    vy[q] = vel[3 * q + 1];
+    vz[q] = vel[3 * q + 2];
+    if (m) m[q] = mass[q];
+    id[q] = (int)q;
+}
+
+__global__ void k_pack(long long np, const double* __restrict__ x, const double* __restrict__ y,
+                       const double* __restrict__ z, const double* __restrict__ vx,
+                       const double* __restrict__ vy, const double* __restrict__ vz,
+                       const int* __restrict__ id, double* pos, double* vel)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const long long o = 3LL * id[q];
+    pos[o] = x[q];
+    pos[o + 1] = y[q];
+    pos[o + 2] = z[q];
+    vel[o] = vx[q];
+    vel[o + 1] = vy[q];
+    vel[o + 2] = vz[q];
+}
+
+__device__ __forceinline__ double wrap_pos(double v, double L)
+{
+    if (v >= L) v = v - L;
+    else if (v < 0.0) v = v + L;
+    if (v >= L) v = 0.0;
+    return v;
+}
+
+__global__ void k_wrap(long long np, double L, double* x, double* y, double* z)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    x[q] = wrap_pos(x[q], L);
+    y[q] = wrap_pos(y[q], L);
+    z[q] = wrap_pos(z[q], L);
+}
+
+// ---------------------------------------------------------------------------
+// counting sort
+// ---------------------------------------------------------------------------
+__global__ void k_keys(long long np, int n, double dxi, const double* __restrict__ x,
+                       const double* __restrict__ y, const double* __restrict__ z, int* key,
+                       int* count)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    double f;
+    const int i = key1(x[q], dxi, n, &f);
+    const int j = key1(y[q], dxi, n, &f);
+    const int k = key1(z[q], dxi, n, &f);
+    const int K = (int)cidx(i, j, k, n);
+    key[q] = K;
+    atomicAdd(count + K, 1);
+}
+
+// slot = start[key] + (remaining count - 1); leaves count all zero
+__global__ void k_scatter(long long np, const int* __restrict__ key, const int* __restrict__ start,
+                          int* count, int* perm)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const int K = key[q];
+    const int slot = start[K] + atomicSub(count + K, 1) - 1;
+    perm[slot] = (int)q;
+}
+
+// Sort every key segment by previous particle index so the result does not
+// depend on the order the atomics above were served in.  Segments up to 32
+// long are sorted by one thread in registers; longer ones are queued.
+__global__ void k_fix_short(int nc, const int* __restrict__ start, int* perm, int* long_list,
+                            int* long_count)
+{
+    int K = blockIdx.x * blockDim.x + threadIdx.x;
+    if (K >= nc) return;
+    const int s = start[K], e = start[K + 1];
+    const int len = e - s;
+    if (len <= 1) return;
+    if (len > 32) {
+        long_list[atomicAdd(long_count, 1)] = K;
+        return;
+    }
+    int v[32];
+#pragma unroll
+    for (int t = 0; t < 32; ++t)
+        if (t < len) v[t] = perm[s + t];
+    for (int a = 1; a < len; ++a) {
+        int cur = v[a];
+        int b = a - 1;
+        while (b >= 0 && v[b] > cur) {
+            v[b + 1] = v[b];
+            --b;
+        }
+        v[b + 1] = cur;
+    }
+#pragma unroll
+    for (int t = 0; t < 32; ++t)
+        if (t < len) perm[s + t] = v[t];
+}
+
+// long segments: rank sort by one block per segment (values are distinct)
+constexpr int kLongSmem = 12288;
+
+__global__ void k_fix_long(const int* __restrict__ start, const int* __restrict__ long_list,
+                           const int* __restrict__ long_count, int* perm, int* tmp)
+{
+    __shared__ int sv[kLongSmem];
+    const int total = *long_count;
+    for (int li = blockIdx.x; li < total; li += gridDim.x) {
+        const int K = long_list[li];
+        const int s = start[K], len = start[K + 1] - s;
+        const bool in_smem = len <= kLongSmem;
+        __syncthreads();
+        if (in_smem)
+            for (int t = threadIdx.x; t < len; t += blockDim.x) sv[t] = perm[s + t];
+        __syncthreads();
+        for (int t = threadIdx.x; t < len; t += blockDim.x) {
+            const int v = in_smem ? sv[t] : perm[s + t];
+            int rank = 0;
+            if (in_smem) {
+                for (int u = 0; u < len; ++u) rank += sv[u] < v;
+            } else {
+                for (int u = 0; u < len; ++u) rank += perm[s + u] < v;
+            }
+            tmp[s + rank] = v;
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < len; t += blockDim.x) perm[s + t] = tmp[s + t];
+    }
+}
+
+__global__ void k_gather(long long np, const int* __restrict__ perm, const double* __restrict__ x,
+                         const double* __restrict__ y, const double* __restrict__ z,
+                         const double* __restrict__ vx, const double* __restrict__ vy,
+                         const double* __restrict__ vz, const double* __restrict__ m,
+                         const int* __restrict__ id, double* x2, double* y2, double* z2,
+                         double* vx2, double* vy2, double* vz2, double* m2, int* id2)
+{
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= np) return;
+    const int q = perm[s];
+    x2[s] = x[q];
+    y2[s] = y[q];
+    z2[s] = z[q];
+    vx2[s] = vx[q];
+    vy2[s] = vy[q];
+    vz2[s] = vz[q];
+    if (m) m2[s] = m[q];
+    id2[s] = id[q];
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of the per-key counts (3 phases, 4096 keys per tile)
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int warp_incl_scan(int v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// block-wide exclusive scan of one int per thread; returns the block total in *total
+__device__ int block_excl_scan(int v, int* total)
+{
+    __shared__ int ws[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int inc = warp_incl_scan(v);
+    if (lane == 31) ws[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        int s = lane < nw ? ws[lane] : 0;
+        s = warp_incl_scan(s);
+        ws[lane] = s;
+    }
+    __syncthreads();
+    const int before = (w > 0 ? ws[w - 1] : 0) + inc - v;
+    *total = ws[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before;
+}
+
+__global__ void k_scan_reduce(const int* __restrict__ in, int n, int* tile_sums)
+{
+    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+    int s = 0;
+#pragma unroll
+    for (int t = 0; t < kScanItems; ++t)
+        if (base + t < n) s += in[base + t];
+    int total;
+    block_excl_scan(s, &total);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_top(int* tile_sums, int ntiles)
+{
+    int carry = 0;
+    for (int b0 = 0; b0 < ntiles; b0 += blockDim.x) {
+        const int i = b0 + threadIdx.x;
+        const int v = i < ntiles ? tile_sums[i] : 0;
+        int total;
+        const int ex = block_excl_scan(v, &total);
+        if (i < ntiles) tile_sums[i] = carry + ex;
+        carry += total;
+    }
+}
+
+__global__ void k_scan_down(const int* __restrict__ in, int n, const int* __restrict__ tile_off,
+                            int* out)
+{
+    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int t = 0; t < kScanItems; ++t) {
+        v[t] = base + t < n ? in[base + t] : 0;
+        s += v[t];
+    }
+    int total;
+    int run = block_excl_scan(s, &total) + tile_off[blockIdx.x];
+#pragma unroll
+    for (int t = 0; t < kScanItems; ++t) {
+        if (base + t < n) out[base + t] = run;
+        run += v[t];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = run;
+}
+
+// ---------------------------------------------------------------------------
+// CIC deposit: one block per 8x8x8 tile of cells.  Phase 1: one thread per key of
+// the 9x9x9 key window sums its segment's 8 corner weights sequentially (keys of
+// one row are contiguous in the sorted particle array).  Phase 2: each cell adds
+// the 8 corner partials of its keys in a fixed order.  No atomics; the order is
+// fixed, so the density is bitwise reproducible.
+// ---------------------------------------------------------------------------
+constexpr int kTx = 8, kTy = 8, kTz = 8;
+constexpr int kKx = kTx + 1, kKy = kTy + 1, kKz = kTz + 1;
+constexpr int kNKeys = kKx * kKy * kKz;
+
+__global__ void __launch_bounds__(256) k_deposit(int n, double dxi, double inv_vol,
+                                                 const double* __restrict__ x,
+                                                 const double* __restrict__ y,
+                                                 const double* __restrict__ z,
+                                                 const double* __restrict__ m, double mscalar,
+                                                 const int* __restrict__ start, double* rho)
+{
+    __shared__ double part[kNKeys * 8];
+    const int i0 = blockIdx.x * kTx, j0 = blockIdx.y * kTy, k0 = blockIdx.z * kTz;
+    for (int kl = threadIdx.x; kl < kNKeys; kl += blockDim.x) {
+        const int ki = kl % kKx, kj = (kl / kKx) % kKy, kk = kl / (kKx * kKy);
+        const long long K = cidx(wrapi(i0 + ki, n), wrapi(j0 + kj, n), wrapi(k0 + kk, n), n);
+        double s[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s[c] = 0.0;
+        const int e = start[K + 1];
+        for (int q = start[K]; q < e; ++q) {
+            double fx, fy, fz;
+            key1(x[q], dxi, n, &fx);
+            key1(y[q], dxi, n, &fy);
+            key1(z[q], dxi, n, &fz);
+            const double sx[2] = {1.0 - fx, fx};
+            const double sy[2] = {1.0 - fy, fy};
+            const double sz[2] = {1.0 - fz, fz};
+            const double mq = m ? m[q] : mscalar;
+#pragma unroll
+            for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+                for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                    for (int cx = 0; cx < 2; ++cx)
+                        s[cx + 2 * cy + 4 * cz] = s[cx + 2 * cy + 4 * cz] + ((sx[cx] * sy[cy]) * sz[cz]) * mq;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
+    }
+    __syncthreads();
+    for (int cl = threadIdx.x; cl < kTx * kTy * kTz; cl += blockDim.x) {
+        const int ci = cl % kTx, cj = (cl / kTx) % kTy, ck = cl / (kTx * kTy);
+        const int i = i0 + ci, j = j0 + cj, k = k0 + ck;
+        if (i >= n || j >= n || k >= n) continue;
+        double acc = 0.0;
+#pragma unroll
+        for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+            for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+                for (int di = 0; di < 2; ++di) {
+                    const int kl = (ci + di) + kKx * ((cj + dj) + kKy * (ck + dk));
+                    const int corner = (1 - di) + 2 * (1 - dj) + 4 * (1 - dk);
+                    acc = acc + part[kl * 8 + corner];
+                }
+        rho[cidx(i, j, k, n)] = acc * inv_vol;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fused gradient + CIC interpolation + kick (+ drift) (+ periodic wrap)
+// ---------------------------------------------------------------------------
+struct KickArgs {
+    int n, split;
+    double dxi, L;
+    const double* phi_r;
+    const double* phi_b;
+    double half_dt, a_prev, a_cur_inv, dt_a_cur_inv;
+    int do_move, do_wrap;
+};
+
+__device__ __forceinline__ double phi_at(const KickArgs& A, int i, int j, int k)
+{
+    return *lv_ptr<const double>(A.phi_r, A.phi_b, A.n, A.split, wrapi(i, A.n), wrapi(j, A.n),
+                                 wrapi(k, A.n));
+}
+
+__global__ void __launch_bounds__(256) k_kick(long long np, KickArgs A, double* x, double* y,
+                                              double* z, double* vx, double* vy, double* vz)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const double lx = x[q] * A.dxi + 0.5;
+    const double ly = y[q] * A.dxi + 0.5;
+    const double lz = z[q] * A.dxi + 0.5;
+    const int i = (int)floor(lx), j = (int)floor(ly), k = (int)floor(lz);
+    const double xint = lx - i, yint = ly - j, zint = lz - k;
+    const double sx[2] = {1.0 - xint, xint};
+    const double sy[2] = {1.0 - yint, yint};
+    const double sz[2] = {1.0 - zint, zint};
+    // phi on the 4x4x4 block around the 2x2x2 interpolation cells (offsets -2..1),
+    // loaded only where a central difference needs it
+    double P[4][4][4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const int inx = (a == 1 || a == 2), iny = (b == 1 || b == 2), inz = (c == 1 || c == 2);
+                if (inx + iny + inz >= 2) P[c][b][a] = phi_at(A, i - 2 + a, j - 2 + b, k - 2 + c);
+                else P[c][b][a] = 0.0;
+            }
+    // gravity vector at the 8 cells (i-ii, j-jj, k-kk): local index (2-ii, 2-jj, 2-kk)
+    double gv[2][2][2][3];
+#pragma unroll
+    for (int kk = 0; kk < 2; ++kk)
+#pragma unroll
+        for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+            for (int ii = 0; ii < 2; ++ii) {
+                const int a = 2 - ii, b = 2 - jj, c = 2 - kk;
+                const double pc = P[c][b][a];
+                gv[kk][jj][ii][0] = 0.5 * ((pc - P[c][b][a - 1]) * A.dxi + (P[c][b][a + 1] - pc) * A.dxi);
+                gv[kk][jj][ii][1] = 0.5 * ((pc - P[c][b - 1][a]) * A.dxi + (P[c][b + 1][a] - pc) * A.dxi);
+                gv[kk][jj][ii][2] = 0.5 * ((pc - P[c - 1][b][a]) * A.dxi + (P[c + 1][b][a] - pc) * A.dxi);
+            }
+    double v[3] = {vx[q], vy[q], vz[q]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double val = 0.0;
+#pragma unroll
+        for (int kk = 0; kk <= 1; ++kk)
+#pragma unroll
+            for (int jj = 0; jj <= 1; ++jj)
+#pragma unroll
+                for (int ii = 0; ii <= 1; ++ii)
+                    val = val + ((sx[1 - ii] * sy[1 - jj]) * sz[1 - kk]) * gv[kk][jj][ii][d];
+        const double u = A.a_prev * v[d] + A.half_dt * val;
+        v[d] = u * A.a_cur_inv;
+    }
+    vx[q] = v[0];
+    vy[q] = v[1];
+    vz[q] = v[2];
+    if (A.do_move == 1) {
+        double px = x[q] + A.dt_a_cur_inv * v[0];
+        double py = y[q] + A.dt_a_cur_inv * v[1];
+        double pz = z[q] + A.dt_a_cur_inv * v[2];
+        if (A.do_wrap) {
+            px = wrap_pos(px, A.L);
+            py = wrap_pos(py, A.L);
+            pz = wrap_pos(pz, A.L);
+        }
+        x[q] = px;
+        y[q] = py;
+        z[q] = pz;
+    } else if (A.do_wrap) {
+        x[q] = wrap_pos(x[q], A.L);
+        y[q] = wrap_pos(y[q], A.L);
+        z[q] = wrap_pos(z[q], A.L);
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+nyxpm_status launch_unpack(Ctx& c, Box& b, const double* d_pos, const double* d_vel,
+                           const double* d_mass)
+{
+    prof_begin(c);
+    k_unpack<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, d_pos, d_vel, d_mass, b.x, b.y, b.z,
+                                                           b.vx, b.vy, b.vz, d_mass ? b.m : nullptr,
+                                                           b.id, b.norms + 2);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "unpack");
+}
+
+nyxpm_status launch_pack(Ctx& c, Box& b, double* d_pos, double* d_vel)
+{
+    prof_begin(c);
+    k_pack<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.x, b.y, b.z, b.vx, b.vy, b.vz, b.id,
+                                                         d_pos, d_vel);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "pack");
+}
+
+nyxpm_status launch_wrap(Ctx& c, Box& b)
+{
+    prof_begin(c);
+    k_wrap<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.L, b.x, b.y, b.z);
+    prof_end(c, NYXPM_ST_KICK, 48.0 * b.np);
+    return check_launch(c, "wrap");
+}
+
+nyxpm_status scan_counts(Ctx& c, Box& b)
+{
+    const int nc = b.n * b.n * b.n;
+    const int nt = b.ntiles;
+    prof_begin(c);
+    k_scan_reduce<<<nt, kScanThreads, 0, c.stream>>>(b.cell_count, nc, b.tile_sums);
+    k_scan_top<<<1, 1024, 0, c.stream>>>(b.tile_sums, nt);
+    k_scan_down<<<nt, kScanThreads, 0, c.stream>>>(b.cell_count, nc, b.tile_sums, b.cell_start);
+    prof_end(c, NYXPM_ST_SCAN, 12.0 * nc);
+    c.launches += 2;
+    return check_launch(c, "scan");
+}
+
+nyxpm_status fix_segments(Ctx& c, Box& b)
+{
+    const int nc = b.n * b.n * b.n;
+    prof_begin(c);
+    cudaMemsetAsync(b.long_count, 0, sizeof(int), c.stream);
+    k_fix_short<<<blocks_for(nc), kThreads, 0, c.stream>>>(nc, b.cell_start, b.perm, b.long_list,
+                                                            b.long_count);
+    k_fix_long<<<c.sm_count * 2, 512, 0, c.stream>>>(b.cell_start, b.long_list, b.long_count, b.perm,
+                                                      b.key);
+    prof_end(c, NYXPM_ST_SCATTER, 4.0 * nc + 8.0 * b.np);
+    c.launches += 1;
+    return check_launch(c, "fix segments");
+}
+
+nyxpm_status launch_sort(Ctx& c, Box& b)
+{
+    nyxpm_status st;
+    prof_begin(c);
+    k_keys<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.n, b.dxi, b.x, b.y, b.z, b.key,
+                                                         b.cell_count);
+    prof_end(c, NYXPM_ST_KEYS, 32.0 * b.np);
+    if ((st = check_launch(c, "keys")) != NYXPM_OK) return st;
+    if ((st = scan_counts(c, b)) != NYXPM_OK) return st;
+    prof_begin(c);
+    k_scatter<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.key, b.cell_start, b.cell_count,
+                                                            b.perm);
+    prof_end(c, NYXPM_ST_SCATTER, 12.0 * b.np);
+    if ((st = check_launch(c, "scatter")) != NYXPM_OK) return st;
+    if ((st = fix_segments(c, b)) != NYXPM_OK) return st;
+    const int nvals = b.uniform_mass ? 6 : 7;
+    prof_begin(c);
+    k_gather<<<blocks_for(b.np), kThreads, 0, c.stream>>>(
+        b.np, b.perm, b.x, b.y, b.z, b.vx, b.vy, b.vz, b.uniform_mass ? nullptr : b.m, b.id, b.x2,
+        b.y2, b.z2, b.vx2, b.vy2, b.vz2, b.uniform_mass ? nullptr : b.m2, b.id2);
+    prof_end(c, NYXPM_ST_GATHER, (16.0 * nvals + 12.0) * b.np);
+    if ((st = check_launch(c, "gather")) != NYXPM_OK) return st;
+    std::swap(b.x, b.x2);
+    std::swap(b.y, b.y2);
+    std::swap(b.z, b.z2);
+    std::swap(b.vx, b.vx2);
+    std::swap(b.vy, b.vy2);
+    std::swap(b.vz, b.vz2);
+    std::swap(b.m, b.m2);
+    std::swap(b.id, b.id2);
+    b.sorted = 1;
+    return NYXPM_OK;
+}
+
+nyxpm_status launch_deposit(Ctx& c, Box& b)
+{
+    const int n = b.n;
+    dim3 grid((n + kTx - 1) / kTx, (n + kTy - 1) / kTy, (n + kTz - 1) / kTz);
+    const double dx = b.L / n;
+    const double inv_vol = 1.0 / (dx * dx * dx);
+    const double nc = (double)n * n * n;
+    prof_begin(c);
+    k_deposit<<<grid, 256, 0, c.stream>>>(n, b.dxi, inv_vol, b.x, b.y, b.z,
+                                          b.uniform_mass ? nullptr : b.m, b.mscalar, b.cell_start,
+                                          b.rho);
+    prof_end(c, NYXPM_ST_DEPOSIT, (b.uniform_mass ? 24.0 : 32.0) * b.np + 12.0 * nc);
+    return check_launch(c, "deposit");
+}
+
+nyxpm_status launch_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move,
+                         int do_wrap)
+{
+    const Level& l0 = b.levels[0];
+    KickArgs A;
+    A.n = b.n;
+    A.split = l0.split;
+    A.dxi = b.dxi;
+    A.L = b.L;
+    A.phi_r = l0.phi_r;
+    A.phi_b = l0.phi_b;
+    A.half_dt = 0.5 * dt;
+    A.a_prev = a_prev;
+    A.a_cur_inv = 1.0 / a_cur;
+    A.dt_a_cur_inv = dt * A.a_cur_inv;
+    A.do_move = do_move;
+    A.do_wrap = do_wrap;
+    prof_begin(c);
+    k_kick<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, A, b.x, b.y, b.z, b.vx, b.vy, b.vz);
+    const double nc = (double)b.n * b.n * b.n;
+    prof_end(c, NYXPM_ST_KICK, (do_move ? 96.0 : 72.0) * b.np + 8.0 * nc);
+    b.sorted = b.sorted && !do_move && !do_wrap;
+    return check_launch(c, "kick");
+}
+
+}  // namespace nyxpm

@@ -1,0 +1,361 @@
+"""Host-side mirror of Nyx's PM call surface over libnyxpm.
+
+Names and argument meanings follow the reference classes so a caller of Nyx's
+particle-mesh path finds the same operations:
+
+* ``DarkMatterParticleContainer`` -- moveKickDrift / moveKick
+  (Source/Particle/DarkMatterParticleContainer.cpp:76-247), AssignDensitySingleLevel /
+  AssignDensity (Source/Particle/NyxParticleContainer.H:90-97), RedistributeLocal
+  (:123-136), sumParticleMass (:70-79);
+* ``Gravity`` -- solve_for_phi / solve_for_old_phi / solve_for_new_phi
+  (Source/Gravity/Gravity.cpp:202-315), get_old_grav_vector / get_new_grav_vector
+  (:781-850), set_mass_offset (:975-1030);
+* ``Nyx`` -- advance_particles_only (Source/TimeStep/Nyx_advance_particles.cpp:9-272),
+  post_init solve, integrate_comoving_a / integrate_comoving_a_to_a
+  (Source/Driver/comoving.cpp).
+
+Where Nyx aborts (amrex::Abort / amrex::Error), these raise ``NyxPMError``.
+All state lives on the GPU inside the box; numpy arrays cross only on upload,
+download and the optional field read-backs.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib as _L
+from .ics import GCONST
+
+
+class NyxPMError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_L.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        a = a.reshape(shape)
+    return a
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """A CUDA device + stream + solver parameters (nyxpm_ctx)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None, OmM: float = 1.0,
+                 OmR: float = 0.0, h: float = 0.675, rel_tol: float = 1e-10,
+                 max_vcycles: int = 100, nu1: int = 2, nu2: int = 2, gconst: float | None = None):
+        self.lib = _L.load()
+        p = _L.Params()
+        self.lib.nyxpm_default_params(C.byref(p))
+        p.device = device
+        p.stream = stream
+        p.comoving_OmM, p.comoving_OmR, p.comoving_h = OmM, OmR, h
+        if gconst is not None:
+            p.gconst = gconst
+        p.rel_tol, p.max_vcycles, p.nu1, p.nu2 = rel_tol, max_vcycles, nu1, nu2
+        self.params = p
+        h_ = C.c_void_p()
+        st = self.lib.nyxpm_create(C.byref(p), C.byref(h_))
+        if st != _L.NYXPM_OK:
+            raise NyxPMError(st, "nyxpm_create failed")
+        self.handle = h_
+
+    def check(self, st: int, what: str = ""):
+        if st != _L.NYXPM_OK:
+            msg = self.lib.nyxpm_last_error(self.handle)
+            raise NyxPMError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    @property
+    def stream(self) -> int:
+        return self.lib.nyxpm_stream(self.handle) or 0
+
+    def synchronize(self):
+        self.check(self.lib.nyxpm_synchronize(self.handle), "synchronize")
+
+    def launch_count(self) -> int:
+        return int(self.lib.nyxpm_launch_count(self.handle))
+
+    def set_profiling(self, on: bool):
+        self.check(self.lib.nyxpm_set_profiling(self.handle, 1 if on else 0), "set_profiling")
+
+    def profile(self, reset: bool = False) -> dict:
+        pr = _L.Profile()
+        self.check(self.lib.nyxpm_get_profile(self.handle, C.byref(pr), 1 if reset else 0), "profile")
+        stages = {name: {"launches": int(pr.launches[i]), "ms": float(pr.ms[i]),
+                         "bytes": float(pr.bytes[i])} for i, name in enumerate(_L.STAGE_NAMES)}
+        return {"stages": stages, "fine_smooth": {"launches": int(pr.fine_smooth_launches),
+                                                  "ms": float(pr.fine_smooth_ms),
+                                                  "bytes": float(pr.fine_smooth_bytes)}}
+
+    # a(t), FP64 on the host (comoving.cpp)
+    def integrate_comoving_a(self, a_old: float, dt: float) -> float:
+        return self.lib.nyxpm_integrate_a(C.byref(self.params), a_old, dt)
+
+    def integrate_comoving_a_to_a(self, a_old: float, a_value: float, dt_window: float) -> float:
+        return self.lib.nyxpm_dt_for_da(C.byref(self.params), a_old, a_value, dt_window)
+
+    def hubble(self, a: float) -> float:
+        p = self.params
+        OmL = 1.0 - p.comoving_OmM - p.comoving_OmR
+        return p.comoving_h * 100.0 * math.sqrt(p.comoving_OmM / a ** 3 + p.comoving_OmR / a ** 4 + OmL)
+
+    def step_schedule(self, a_start: float, a_end: float, nsteps: int):
+        """Equal-delta-a steps: [(a_old, a_new, dt)], dt from integrate_comoving_a_to_a and
+        a_new re-integrated from dt as Nyx::integrate_comoving_a does."""
+        out = []
+        a = a_start
+        da = (a_end - a_start) / nsteps
+        for _ in range(nsteps):
+            target = a + da
+            adot_min = min(a * self.hubble(a), target * self.hubble(target))
+            window = 1.01 * da / adot_min
+            dt = self.integrate_comoving_a_to_a(a, target, window)
+            a_new = self.integrate_comoving_a(a, dt)
+            out.append((a, a_new, dt))
+            a = a_new
+        return out
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.nyxpm_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def box_bytes(n: int, np_: int, precision: str = "fp64") -> int:
+    lib = _L.load()
+    return int(lib.nyxpm_box_bytes(n, np_, _L.NYXPM_MIXED if precision == "mixed" else _L.NYXPM_FP64))
+
+
+class Box:
+    """One periodic n^3 grid with its particles, resident on the GPU (nyxpm_box)."""
+
+    def __init__(self, ctx: Context, n: int, L: float, np_: int, precision: str = "fp64"):
+        self.ctx, self.n, self.L, self.np = ctx, n, L, int(np_)
+        self.precision = precision
+        prec = _L.NYXPM_MIXED if precision == "mixed" else _L.NYXPM_FP64
+        h = C.c_void_p()
+        ctx.check(ctx.lib.nyxpm_box_create(ctx.handle, n, float(L), self.np, prec, C.byref(h)),
+                  "box_create")
+        self.handle = h
+
+    def _c(self, fn, *args, what=""):
+        self.ctx.check(fn(self.ctx.handle, self.handle, *args), what)
+
+    def upload(self, pos, vel, mass):
+        pos = _f64(pos, (self.np, 3))
+        vel = _f64(vel, (self.np, 3))
+        if np.ndim(mass) == 0:
+            self._c(self.ctx.lib.nyxpm_box_upload, _ptr(pos), _ptr(vel), None, float(mass), what="upload")
+        else:
+            m = _f64(mass, (self.np,))
+            self._c(self.ctx.lib.nyxpm_box_upload, _ptr(pos), _ptr(vel), _ptr(m), 0.0, what="upload")
+
+    def upload_ptr(self, pos_ptr: int, vel_ptr: int, mass: float):
+        """Upload from raw host pointers (pinned buffers), uniform mass."""
+        self._c(self.ctx.lib.nyxpm_box_upload, C.c_void_p(pos_ptr), C.c_void_p(vel_ptr), None,
+                float(mass), what="upload")
+
+    def download(self):
+        pos = np.empty((self.np, 3))
+        vel = np.empty((self.np, 3))
+        self._c(self.ctx.lib.nyxpm_box_download, _ptr(pos), _ptr(vel), what="download")
+        return pos, vel
+
+    def download_ptr(self, pos_ptr: int, vel_ptr: int):
+        self._c(self.ctx.lib.nyxpm_box_download, C.c_void_p(pos_ptr), C.c_void_p(vel_ptr),
+                what="download")
+
+    def mass_offset(self) -> float:
+        v = C.c_double()
+        self._c(self.ctx.lib.nyxpm_set_mass_offset, C.byref(v), what="set_mass_offset")
+        return v.value
+
+    def redistribute(self):
+        self._c(self.ctx.lib.nyxpm_redistribute, what="redistribute")
+
+    def deposit(self, read_back: bool = True):
+        rho = np.empty(self.n ** 3) if read_back else None
+        self._c(self.ctx.lib.nyxpm_deposit, _ptr(rho), what="deposit")
+        return rho
+
+    def solve_phi(self, a: float, zero_guess: bool = False) -> dict:
+        info = _L.SolveInfo()
+        self._c(self.ctx.lib.nyxpm_solve_phi, float(a), 1 if zero_guess else 0, C.byref(info),
+                what="solve_phi")
+        return info.as_dict()
+
+    def get_phi(self):
+        phi = np.empty(self.n ** 3)
+        self._c(self.ctx.lib.nyxpm_get_phi, _ptr(phi), what="get_phi")
+        return phi
+
+    def set_phi(self, phi):
+        phi = _f64(phi, (self.n ** 3,))
+        self._c(self.ctx.lib.nyxpm_set_phi, _ptr(phi), what="set_phi")
+
+    def grav_vector(self, read_back: bool = True):
+        g = np.empty(3 * self.n ** 3) if read_back else None
+        self._c(self.ctx.lib.nyxpm_grav_vector, _ptr(g), what="grav_vector")
+        return g
+
+    def kick_drift(self, dt, a_old, a_half):
+        self._c(self.ctx.lib.nyxpm_kick_drift, float(dt), float(a_old), float(a_half), what="kick_drift")
+
+    def kick(self, dt, a_new, a_half):
+        self._c(self.ctx.lib.nyxpm_kick, float(dt), float(a_new), float(a_half), what="kick")
+
+    def init_field(self, a: float) -> dict:
+        info = _L.SolveInfo()
+        self._c(self.ctx.lib.nyxpm_init_field, float(a), C.byref(info), what="init_field")
+        return info.as_dict()
+
+    def step(self, a_old, a_new, dt, reuse_field: bool = False) -> dict:
+        info = _L.StepInfo()
+        flags = _L.NYXPM_STEP_REUSE_FIELD if reuse_field else 0
+        self._c(self.ctx.lib.nyxpm_step, float(a_old), float(a_new), float(dt), flags,
+                C.byref(info), what="step")
+        return {"old_solve": info.old_solve.as_dict(), "new_solve": info.new_solve.as_dict()}
+
+    def close(self):
+        if getattr(self, "handle", None) and self.ctx.handle:
+            self.ctx.lib.nyxpm_box_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# the reference-named facade
+# ---------------------------------------------------------------------------
+class DarkMatterParticleContainer:
+    """Nyx's DM particle container on one periodic level, resident on the GPU."""
+
+    def __init__(self, box: Box):
+        self.box = box
+
+    def InitFromArrays(self, pos, vel, mass):
+        """Particle fill (init_particles AsciiFile/BinaryFile/Cosmological, NyxParticles.cpp:378-591)."""
+        self.box.upload(pos, vel, mass)
+
+    def moveKickDrift(self, acceleration=None, lev: int = 0, dt: float = 0.0, a_old: float = 1.0,
+                      a_half: float = 1.0, where_width: int = 0):
+        """Kick by dt/2 with the CIC-interpolated field of the current phi, then drift by dt.
+        ``acceleration`` is the box's own field (the gradient is fused); passing an array is
+        not supported because the field never leaves the device."""
+        if acceleration is not None:
+            raise NyxPMError(1, "moveKickDrift uses the box's own field; pass acceleration=None")
+        if lev != 0:
+            raise NyxPMError(1, "single level only")
+        self.box.kick_drift(dt, a_old, a_half)
+
+    def moveKick(self, acceleration=None, lev: int = 0, dt: float = 0.0, a_new: float = 1.0,
+                 a_half: float = 1.0):
+        if acceleration is not None:
+            raise NyxPMError(1, "moveKick uses the box's own field; pass acceleration=None")
+        if lev != 0:
+            raise NyxPMError(1, "single level only")
+        self.box.kick(dt, a_new, a_half)
+
+    def AssignDensitySingleLevel(self, mf=None, lev: int = 0, ncomp: int = 1,
+                                 particle_lvl_offset: int = 0):
+        """CIC mass density; fills ``mf`` (n^3 array) when given and returns it."""
+        if lev != 0 or ncomp != 1 or particle_lvl_offset != 0:
+            raise NyxPMError(1, "single level, one component, no level offset")
+        rho = self.box.deposit(read_back=True)
+        if mf is not None:
+            mf[...] = rho.reshape(mf.shape)
+            return mf
+        return rho
+
+    def AssignDensity(self, mf: list, lev_min: int = 0, ncomp: int = 1, finest_level: int = -1,
+                      ngrow: int = 1):
+        """Callee-allocating form: appends the level-0 density to ``mf``."""
+        if lev_min != 0 or finest_level not in (-1, 0):
+            raise NyxPMError(1, "single level only")
+        mf.clear()
+        mf.append(self.box.deposit(read_back=True).reshape(self.box.n, self.box.n, self.box.n))
+        return mf
+
+    def RedistributeLocal(self, lev_min: int = 0, lev_max: int = -1, nGrow: int = 0):
+        self.box.redistribute()
+
+    def sumParticleMass(self, lev: int = 0) -> float:
+        return self.box.mass_offset() * self.box.L ** 3
+
+    def GetParticles(self):
+        return self.box.download()
+
+
+class Gravity:
+    """The comoving Poisson solve of one periodic level."""
+
+    def __init__(self, box: Box):
+        self.box = box
+        self.mass_offset = 0.0
+        self.level_solver_resnorm = [0.0]
+        self.last_info: dict = {}
+
+    def set_mass_offset(self, time: float = 0.0) -> float:
+        self.mass_offset = self.box.mass_offset()
+        return self.mass_offset
+
+    def solve_for_phi(self, level: int, a: float, zero_guess: bool = False):
+        """Deposit already done; RHS from it, V-cycles (Gravity.cpp:267-315)."""
+        info = self.box.solve_phi(a, zero_guess)
+        self.level_solver_resnorm[0] = info["resnorm"]
+        self.last_info = info
+        return info
+
+    def solve_for_old_phi(self, level: int, a_old: float):
+        self.box.deposit(read_back=False)
+        return self.solve_for_phi(level, a_old, zero_guess=True)
+
+    def solve_for_new_phi(self, level: int, a_new: float):
+        self.box.deposit(read_back=False)
+        return self.solve_for_phi(level, a_new, zero_guess=False)
+
+    def get_phi(self):
+        return self.box.get_phi()
+
+    def get_new_grav_vector(self, level: int = 0):
+        return self.box.grav_vector(read_back=True).reshape(3, self.box.n, self.box.n, self.box.n)
+
+    get_old_grav_vector = get_new_grav_vector
+
+
+class Nyx:
+    """Level-0 driver of the particle-only PM step."""
+
+    def __init__(self, ctx: Context, n: int, L: float, pos, vel, mass):
+        self.ctx = ctx
+        self.box = Box(ctx, n, L, len(pos))
+        self.particles = DarkMatterParticleContainer(self.box)
+        self.particles.InitFromArrays(pos, vel, mass)
+        self.gravity = Gravity(self.box)
+        self.gravity.set_mass_offset()
+
+    def post_init(self, a: float):
+        """Nyx::post_init (Nyx.cpp:1957-2005): solve for phi at the initial a."""
+        return self.box.init_field(a)
+
+    def advance_particles_only(self, a_old: float, a_new: float, dt: float,
+                               reuse_field: bool = False) -> dict:
+        return self.box.step(a_old, a_new, dt, reuse_field=reuse_field)

@@ -509,6 +509,8 @@ nyxpm_status fix_segments(Ctx& c, Box& b)
 nyxpm_status launch_sort(Ctx& c, Box& b)
 {
     nyxpm_status st;
+    // the scatter leaves the counts at zero, but an interrupted sort may not have
+    cudaMemsetAsync(b.cell_count, 0, sizeof(int) * (size_t)b.n * b.n * b.n, c.stream);
     prof_begin(c);
     k_keys<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.n, b.dxi, b.x, b.y, b.z, b.key,
                                                          b.cell_count);

@@ -42,7 +42,15 @@ def parse():
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--quick", action="store_true",
+                    help="headline timing only (no reuse-field pass, e2e or CPU baseline); "
+                         "the command the ncu captures run")
+    a = ap.parse_args()
+    if a.quick:
+        a.no_cpu_baseline = a.no_e2e = a.no_reuse = True
+    else:
+        a.no_reuse = False
+    return a
 
 
 def workload_config(n, W, K):
@@ -343,20 +351,21 @@ def run_ours(args):
     }
 
     # ---- same workload with the old-time field reused (1 deposit + 1 solve per step) ----
-    box.upload(ic.pos, ic.vel, ic.mass)
-    box.init_field(A_START)
-    for a0, a1, dt in sched[:W]:
-        box.step(a0, a1, dt, reuse_field=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for a0, a1, dt in sched[W:W + K]:
-        box.step(a0, a1, dt, reuse_field=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_r = allreduce_max(ws, e0.elapsed_time(e1), torch.device("cuda", local))
-    line["reuse_field"] = {"value": allreduce_sum(ws, float(npart) * K, torch.device("cuda", local))
-                           / (ms_r / 1e3), "ms_per_step": ms_r / K,
-                           "note": "old-time field taken from the previous new-time solve"}
+    if not args.no_reuse:
+        box.upload(ic.pos, ic.vel, ic.mass)
+        box.init_field(A_START)
+        for a0, a1, dt in sched[:W]:
+            box.step(a0, a1, dt, reuse_field=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for a0, a1, dt in sched[W:W + K]:
+            box.step(a0, a1, dt, reuse_field=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_r = allreduce_max(ws, e0.elapsed_time(e1), torch.device("cuda", local))
+        line["reuse_field"] = {
+            "value": allreduce_sum(ws, float(npart) * K, torch.device("cuda", local)) / (ms_r / 1e3),
+            "ms_per_step": ms_r / K, "note": "old-time field taken from the previous new-time solve"}
 
     # ---- end to end through the C ABI with pinned host buffers ----
     if not args.no_e2e:

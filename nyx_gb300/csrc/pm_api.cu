@@ -76,7 +76,8 @@ int bottom_edge(int n)
 }
 
 // Green's function of the periodic 7-point Laplacian on nb^3 with spacing h,
-// without the constant mode (the exact coarsest-level solve).
+// without the constant mode, in smoother units (applied to beta = h^2 rhs / 6):
+// the exact coarsest-level solve.
 void bottom_green(int nb, double h, double* G)
 {
     const long nc = (long)nb * nb * nb;
@@ -89,6 +90,7 @@ void bottom_green(int nb, double h, double* G)
                          + (2.0 * std::cos(twopi * kz / nb) - 2.0);
                 lam[kx + nb * (ky + (long)nb * kz)] = l / (h * h);
             }
+    const double scale = 6.0 / (h * h);
     for (int dz = 0; dz < nb; ++dz)
         for (int dy = 0; dy < nb; ++dy)
             for (int dxx = 0; dxx < nb; ++dxx) {
@@ -100,7 +102,7 @@ void bottom_green(int nb, double h, double* G)
                             const long ph = ((long)kx * dxx + (long)ky * dy + (long)kz * dz) % nb;
                             s += std::cos(twopi * (double)ph / nb) / lam[kx + nb * (ky + (long)nb * kz)];
                         }
-                G[dxx + nb * (dy + (long)nb * dz)] = s / (double)nc;
+                G[dxx + nb * (dy + (long)nb * dz)] = (s / (double)nc) * scale;
             }
 }
 
@@ -122,12 +124,16 @@ nyxpm_status do_deposit(Ctx& c, Box& b)
     return b.prec == NYXPM_MIXED ? mixed_deposit(c, b) : launch_deposit(c, b);
 }
 
+// RHS, V-cycles, then the cell-centred gravity vector of the new phi
 nyxpm_status do_solve(Ctx& c, Box& b, double a, int zero_guess, nyxpm_solve_info* info)
 {
     nyxpm_status st;
     if ((st = launch_make_rhs(c, b, a)) != NYXPM_OK) return st;
     if (zero_guess && (st = launch_zero_phi(c, b)) != NYXPM_OK) return st;
-    return b.prec == NYXPM_MIXED ? mixed_solve(c, b, info) : mg_solve(c, b, info);
+    nyxpm_status solved = b.prec == NYXPM_MIXED ? mixed_solve(c, b, info) : mg_solve(c, b, info);
+    if (solved != NYXPM_OK && solved != NYXPM_NOT_CONVERGED) return solved;
+    if ((st = launch_grav_vector(c, b)) != NYXPM_OK) return st;
+    return solved;
 }
 
 nyxpm_status do_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move, int do_wrap)
@@ -308,6 +314,7 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
     ALLOC(b->long_count, 1);
     ALLOC(b->rho, nc);
     ALLOC(b->g, 3 * nc);
+    ALLOC(b->nat, nc);
     ALLOC(b->rows, (size_t)n * n);
     ALLOC(b->planes, n);
     ALLOC(b->scal, 4);
@@ -324,20 +331,17 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
         Level l;
         l.n = nl;
         l.split = nl > nbot ? 1 : 0;
-        const double h = L / nl;
-        l.h2 = h * h;
-        l.ih2 = 1.0 / (h * h);
         const size_t cnt = (size_t)nl * nl * nl;
         if (l.split) {
             ALLOC(l.phi_r, cnt / 2); ALLOC(l.phi_b, cnt / 2);
-            ALLOC(l.rhs_r, cnt / 2); ALLOC(l.rhs_b, cnt / 2);
+            ALLOC(l.beta_r, cnt / 2); ALLOC(l.beta_b, cnt / 2);
             if (prec == NYXPM_MIXED) {
                 ALLOC(l.fphi_r, cnt / 2); ALLOC(l.fphi_b, cnt / 2);
-                ALLOC(l.frhs_r, cnt / 2); ALLOC(l.frhs_b, cnt / 2);
+                ALLOC(l.fbeta_r, cnt / 2); ALLOC(l.fbeta_b, cnt / 2);
             }
         } else {
-            ALLOC(l.phi_r, cnt); ALLOC(l.rhs_r, cnt);
-            if (prec == NYXPM_MIXED) { ALLOC(l.fphi_r, cnt); ALLOC(l.frhs_r, cnt); }
+            ALLOC(l.phi_r, cnt); ALLOC(l.beta_r, cnt);
+            if (prec == NYXPM_MIXED) { ALLOC(l.fphi_r, cnt); ALLOC(l.fbeta_r, cnt); }
         }
         b->levels.push_back(l);
         if (nl == nbot) break;
@@ -489,8 +493,8 @@ nyxpm_status nyxpm_get_phi(nyxpm_ctx* c, nyxpm_box* b, double* phi)
     CHECK_BOX(c, b);
     if (!phi) return fail(c, NYXPM_INVALID_ARG, "null phi");
     const size_t nc = (size_t)b->n * b->n * b->n;
-    TRY(launch_phi_to_natural(*c, *b, b->g));
-    cudaMemcpyAsync(phi, b->g, sizeof(double) * nc, cudaMemcpyDeviceToHost, c->stream);
+    TRY(launch_phi_to_natural(*c, *b, b->nat));
+    cudaMemcpyAsync(phi, b->nat, sizeof(double) * nc, cudaMemcpyDeviceToHost, c->stream);
     TRY(check_launch(*c, "phi copy"));
     return nyxpm_synchronize(c);
 }
@@ -500,9 +504,10 @@ nyxpm_status nyxpm_set_phi(nyxpm_ctx* c, nyxpm_box* b, const double* phi)
     CHECK_BOX(c, b);
     if (!phi) return fail(c, NYXPM_INVALID_ARG, "null phi");
     const size_t nc = (size_t)b->n * b->n * b->n;
-    cudaMemcpyAsync(b->g, phi, sizeof(double) * nc, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(b->nat, phi, sizeof(double) * nc, cudaMemcpyHostToDevice, c->stream);
     TRY(check_launch(*c, "phi copy"));
-    TRY(launch_phi_from_natural(*c, *b, b->g));
+    TRY(launch_phi_from_natural(*c, *b, b->nat));
+    TRY(launch_grav_vector(*c, *b));
     b->have_phi = 1;
     return nyxpm_synchronize(c);
 }
@@ -510,7 +515,7 @@ nyxpm_status nyxpm_set_phi(nyxpm_ctx* c, nyxpm_box* b, const double* phi)
 nyxpm_status nyxpm_grav_vector(nyxpm_ctx* c, nyxpm_box* b, double* g_out)
 {
     CHECK_BOX(c, b);
-    TRY(launch_grav_vector(*c, *b));
+    if (!b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field: solve or set phi first");
     if (g_out) {
         const size_t nc = (size_t)b->n * b->n * b->n;
         cudaMemcpyAsync(g_out, b->g, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream);
@@ -524,6 +529,7 @@ nyxpm_status nyxpm_kick_drift(nyxpm_ctx* c, nyxpm_box* b, double dt, double a_ol
 {
     CHECK_BOX(c, b);
     if (!b->uploaded) return fail(c, NYXPM_INVALID_ARG, "box has no particles");
+    if (!b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field: solve or set phi first");
     if (!(a_half > 0) || !std::isfinite(dt)) return fail(c, NYXPM_INVALID_ARG, "bad dt / a");
     return do_kick(*c, *b, dt, a_old, a_half, 1, 0);
 }
@@ -532,6 +538,7 @@ nyxpm_status nyxpm_kick(nyxpm_ctx* c, nyxpm_box* b, double dt, double a_new, dou
 {
     CHECK_BOX(c, b);
     if (!b->uploaded) return fail(c, NYXPM_INVALID_ARG, "box has no particles");
+    if (!b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field: solve or set phi first");
     if (!(a_new > 0) || !std::isfinite(dt)) return fail(c, NYXPM_INVALID_ARG, "bad dt / a");
     return do_kick(*c, *b, dt, a_half, a_new, 0, 0);
 }

@@ -24,49 +24,71 @@ namespace nyxpm {
 
 constexpr int kMaxBottom = 8;          // coarsest grid edge solved exactly
 
+// One multigrid level.  The right-hand side is stored in smoother units,
+// beta = h^2 rhs / 6, so a Gauss-Seidel update is phi = s/6 - beta (s = sum of
+// the 6 neighbours) and the h factors of coarser levels are exact powers of 2.
 struct Level {
     int n = 0;
     int split = 0;                     // 1: red/black arrays, 0: natural layout
-    double h2 = 0, ih2 = 0;
     double* phi_r = nullptr;           // split: red n^3/2; natural: n^3
     double* phi_b = nullptr;           // split: black n^3/2; natural: unused
-    double* rhs_r = nullptr;
-    double* rhs_b = nullptr;
+    double* beta_r = nullptr;
+    double* beta_b = nullptr;
     // FP32 copies for the mixed-precision inner V-cycles
     float* fphi_r = nullptr;
     float* fphi_b = nullptr;
-    float* frhs_r = nullptr;
-    float* frhs_b = nullptr;
+    float* fbeta_r = nullptr;
+    float* fbeta_b = nullptr;
 };
 
 // device view of one level
 struct LevelView {
     int n, split;
-    double h2, ih2;
     double* phi_r;
     double* phi_b;
-    double* rhs_r;
-    double* rhs_b;
+    double* beta_r;
+    double* beta_b;
 };
 
 struct LevelViewF {
     int n, split;
-    float h2, ih2;
     float* phi_r;
     float* phi_b;
-    float* rhs_r;
-    float* rhs_b;
+    float* beta_r;
+    float* beta_b;
 };
 
 inline LevelView view(const Level& l)
 {
-    return LevelView{l.n, l.split, l.h2, l.ih2, l.phi_r, l.phi_b, l.rhs_r, l.rhs_b};
+    return LevelView{l.n, l.split, l.phi_r, l.phi_b, l.beta_r, l.beta_b};
 }
 
 inline LevelViewF viewf(const Level& l)
 {
-    return LevelViewF{l.n, l.split, (float)l.h2, (float)l.ih2, l.fphi_r, l.fphi_b, l.frhs_r,
-                      l.frhs_b};
+    return LevelViewF{l.n, l.split, l.fphi_r, l.fphi_b, l.fbeta_r, l.fbeta_b};
+}
+
+// 3-D launch geometry without index division: x over the fastest index
+// (rounded up to a power of two up to 32), y over rows, z over planes.
+struct Geo {
+    dim3 grid, block;
+};
+
+inline Geo geo3(int nx, int ny, int nz, int threads = 256)
+{
+    int bx = 1;
+    while (bx < nx && bx < 32) bx <<= 1;
+    int by = threads / bx;
+    if (by > ny) {
+        int p = 1;
+        while (p < ny) p <<= 1;
+        by = p;
+    }
+    if (bx * by < 32) by = 32 / bx;  // whole warps: the block reductions shuffle over 32 lanes
+    Geo g;
+    g.block = dim3(bx, by, 1);
+    g.grid = dim3((nx + bx - 1) / bx, (ny + by - 1) / by, nz);
+    return g;
 }
 
 // ---------------------------------------------------------------------------
@@ -146,7 +168,8 @@ struct Box {
     // fields
     double* rho = nullptr;             // n^3
     float* frho = nullptr;             // n^3 (mixed)
-    double* g = nullptr;               // 3 n^3
+    double* g = nullptr;               // 3 n^3, component-major, kept in step with phi
+    double* nat = nullptr;             // n^3 natural-layout scratch for phi in/out
     double* rows = nullptr;            // n^2 row sums
     double* planes = nullptr;          // n plane sums
     double* scal = nullptr;            // [0] mean
@@ -195,6 +218,7 @@ nyxpm_status launch_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur,
                          int do_wrap);
 
 nyxpm_status launch_make_rhs(Ctx& c, Box& b, double a);
+double beta_scale(const Box& b);  // (h*h)/6 of level 0: rhs -> smoother units
 nyxpm_status launch_zero_phi(Ctx& c, Box& b);
 nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info);
 nyxpm_status launch_grav_vector(Ctx& c, Box& b);

@@ -5,7 +5,13 @@
 // the GB300-native replacement of the AMReX MLMG solve that
 // Gravity::solve_with_MLMG (Gravity.cpp:1318-1416) calls.
 //
-// Built with --fmad=false so that every expression rounds as written.
+// GB300 executes FP64 at a small fraction of its FP32 rate, so these kernels
+// are written for the fewest FP64 instructions: the right-hand side is kept in
+// smoother units (beta = h^2 rhs / 6, one fused multiply-add per Gauss-Seidel
+// update), the trilinear prolongation weights are exact constants, and index
+// arithmetic uses 3-D launch geometry instead of integer division.  Built with
+// --fmad=false: only the explicit fma() calls fuse, in the same places the CPU
+// oracle fuses, so both round identically.
 #include "pm_common.cuh"
 
 #include <algorithm>
@@ -19,15 +25,20 @@ namespace {
 constexpr int kThreads = 256;
 constexpr double kSixth = 1.0 / 6.0;
 
+__constant__ double kProlongW[8] = {0.421875, 0.140625, 0.140625, 0.046875,
+                                    0.140625, 0.046875, 0.046875, 0.015625};
+
 inline unsigned blocks_for(long long n, int t = kThreads)
 {
     long long b = (n + t - 1) / t;
     return (unsigned)(b < 1 ? 1 : b);
 }
 
+__device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
 // ---------------------------------------------------------------------------
 // RHS: canonical sum of (rho - mass_offset), then
-// rhs = (((rho - mass_offset) - mean) * ggrav) * (1/a)
+// beta = ((((rho - mass_offset) - mean) * ggrav) * (1/a)) * (h^2/6)
 // ---------------------------------------------------------------------------
 // one warp per row: 32 strided lane partials, then a halving tree
 __global__ void k_rowsum(int n, const double* __restrict__ rho, double mo, double* rows)
@@ -63,16 +74,17 @@ __global__ void k_mean(int n, double dx, double L, const double* __restrict__ pl
     scal[0] = (s * (dx * dx * dx)) / (L * L * L);
 }
 
-__global__ void k_make_rhs(int n, int split, const double* __restrict__ rho, double mo,
-                           const double* __restrict__ scal, double ggrav, double ainv, double* rhs_r,
-                           double* rhs_b)
+__global__ void k_make_beta(int n, int split, const double* __restrict__ rho, double mo,
+                            const double* __restrict__ scal, double ggrav, double ainv, double k0,
+                            double* beta_r, double* beta_b)
 {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long nc = (long long)n * n * n;
-    if (c >= nc) return;
-    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n || j >= n) return;
     const double mean = scal[0];
-    *lv_ptr<double>(rhs_r, rhs_b, n, split, i, j, k) = (((rho[c] - mo) - mean) * ggrav) * ainv;
+    const double v = rho[cidx(i, j, k, n)];
+    *lv_ptr<double>(beta_r, beta_b, n, split, i, j, k) = ((((v - mo) - mean) * ggrav) * ainv) * k0;
 }
 
 // ---------------------------------------------------------------------------
@@ -87,13 +99,15 @@ __device__ __forceinline__ double nanmax(double a, double b)
 __device__ __forceinline__ void block_max_store(double v, unsigned long long* out)
 {
     __shared__ double sm[32];
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, off));
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lane = tid & 31, w = tid >> 5;
     if (lane == 0) sm[w] = v;
     __syncthreads();
     if (w == 0) {
-        v = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
+        v = lane < (nthreads >> 5) ? sm[lane] : 0.0;
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, off));
         if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
@@ -104,10 +118,8 @@ __global__ void k_absmax(long long cnt, const double* __restrict__ a, unsigned l
 {
     double v = 0.0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < cnt;
-         t += (long long)gridDim.x * blockDim.x) {
-        const double u = fabs(a[t]);
-        v = (u > v || u != u) ? u : v;
-    }
+         t += (long long)gridDim.x * blockDim.x)
+        v = nanmax(v, fabs(a[t]));
     block_max_store(v, out);
 }
 
@@ -127,24 +139,37 @@ __device__ __forceinline__ double nbr_sum(const LevelView& L, int i, int j, int 
     return s;
 }
 
+// residual in smoother units: beta - (s/6 - phi)
 __device__ __forceinline__ double resid_at(const LevelView& L, int i, int j, int k)
 {
     const double s = nbr_sum(L, i, j, k);
     const double c = *lv_ptr<double>(L.phi_r, L.phi_b, L.n, L.split, i, j, k);
-    const double r = *lv_ptr<double>(L.rhs_r, L.rhs_b, L.n, L.split, i, j, k);
-    return r - (s - 6.0 * c) * L.ih2;
+    const double b = *lv_ptr<double>(L.beta_r, L.beta_b, L.n, L.split, i, j, k);
+    return b - fma(s, kSixth, -c);
 }
 
-__global__ void k_resnorm(LevelView L, unsigned long long* out)
+// ||r_beta||_inf of a split level: one thread per (ih, j, k), both cells of the pair
+__global__ void k_resnorm_split(LevelView L, unsigned long long* out)
 {
-    const long long nc = (long long)L.n * L.n * L.n;
+    const int half = L.n >> 1;
+    const int ih = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
     double v = 0.0;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-         c += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(c % L.n), j = (int)((c / L.n) % L.n), k = (int)(c / ((long long)L.n * L.n));
-        const double u = fabs(resid_at(L, i, j, k));
-        v = (u > v || u != u) ? u : v;
+    if (ih < half && j < L.n) {
+        v = nanmax(v, fabs(resid_at(L, 2 * ih, j, k)));
+        v = nanmax(v, fabs(resid_at(L, 2 * ih + 1, j, k)));
     }
+    block_max_store(v, out);
+}
+
+__global__ void k_resnorm_nat(LevelView L, unsigned long long* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    double v = 0.0;
+    if (i < L.n && j < L.n) v = fabs(resid_at(L, i, j, k));
     block_max_store(v, out);
 }
 
@@ -152,38 +177,38 @@ __global__ void k_resnorm(LevelView L, unsigned long long* out)
 // red-black Gauss-Seidel half sweep on a split level: one thread per cell of
 // the colour being updated; reads the other colour's array, writes this one.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_gsrb(int n, double h2, int color, double* __restrict__ mine,
+__global__ void __launch_bounds__(256) k_gsrb(int n, int color, double* __restrict__ mine,
                                               const double* __restrict__ other,
-                                              const double* __restrict__ rhs)
+                                              const double* __restrict__ beta)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int half = n >> 1;
-    const long long cnt = (long long)half * n * n;
-    if (t >= cnt) return;
-    const int ih = (int)(t % half);
-    const long long row = t / half;
-    const int j = (int)(row % n), k = (int)(row / n);
+    const int ih = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (ih >= half || j >= n) return;
     const int q = (j + k + color) & 1;  // this cell is i = 2*ih + q
     const int ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
     const int ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
     const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
     const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
-    const long long rb = row * half;
-    double s = other[rb + ihm] + other[rb + ihp];
-    s = s + other[(long long)half * (jm + (long long)n * k) + ih];
-    s = s + other[(long long)half * (jp + (long long)n * k) + ih];
-    s = s + other[(long long)half * (j + (long long)n * km) + ih];
-    s = s + other[(long long)half * (j + (long long)n * kp) + ih];
-    mine[t] = (s - h2 * rhs[t]) * kSixth;
+    const long long row = (long long)j + (long long)n * k;
+    const long long t = row * half + ih;
+    double s = other[row * half + ihm] + other[row * half + ihp];
+    s = s + other[((long long)jm + (long long)n * k) * half + ih];
+    s = s + other[((long long)jp + (long long)n * k) * half + ih];
+    s = s + other[((long long)j + (long long)n * km) * half + ih];
+    s = s + other[((long long)j + (long long)n * kp) * half + ih];
+    mine[t] = fma(s, kSixth, -beta[t]);
 }
 
-// coarse rhs = 1/8 of the 8 fine residuals (summed dk, dj, di); coarse phi = 0
+// coarse beta = 1/2 of the 8 fine residuals (summed dk, dj, di); coarse phi = 0
 __global__ void k_restrict(LevelView F, LevelView Cv)
 {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nc = Cv.n;
-    if (c >= (long long)nc * nc * nc) return;
-    const int I = (int)(c % nc), J = (int)((c / nc) % nc), K = (int)(c / ((long long)nc * nc));
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z;
+    if (I >= nc || J >= nc) return;
     double s = 0.0;
 #pragma unroll
     for (int dk = 0; dk < 2; ++dk)
@@ -191,88 +216,110 @@ __global__ void k_restrict(LevelView F, LevelView Cv)
         for (int dj = 0; dj < 2; ++dj)
 #pragma unroll
             for (int di = 0; di < 2; ++di) s = s + resid_at(F, 2 * I + di, 2 * J + dj, 2 * K + dk);
-    *lv_ptr<double>(Cv.rhs_r, Cv.rhs_b, nc, Cv.split, I, J, K) = s * 0.125;
+    *lv_ptr<double>(Cv.beta_r, Cv.beta_b, nc, Cv.split, I, J, K) = s * 0.5;
     *lv_ptr<double>(Cv.phi_r, Cv.phi_b, nc, Cv.split, I, J, K) = 0.0;
 }
 
-// trilinear cell-centred prolongation of the coarse correction, added to the fine phi
+// trilinear cell-centred prolongation of the coarse correction, added to the
+// fine phi; one thread per fine pair (2ih, 2ih+1) of a split level
 __global__ void k_prolong(LevelView Cv, LevelView F)
 {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = F.n, nc = Cv.n;
-    if (c >= (long long)n * n * n) return;
-    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
-    const double w[2] = {0.75, 0.25};
-    const int I = i >> 1, J = j >> 1, K = k >> 1;
-    const int Is[2] = {I, wrapi((i & 1) ? I + 1 : I - 1, nc)};
-    const int Js[2] = {J, wrapi((j & 1) ? J + 1 : J - 1, nc)};
-    const int Ks[2] = {K, wrapi((k & 1) ? K + 1 : K - 1, nc)};
-    double s = 0.0;
+    const int n = F.n, nc = Cv.n, half = n >> 1;
+    const int ih = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (ih >= half || j >= n) return;
+    const int J = j >> 1, K = k >> 1;
+    const int Js[2] = {J, wrap1((j & 1) ? J + 1 : J - 1, nc)};
+    const int Ks[2] = {K, wrap1((k & 1) ? K + 1 : K - 1, nc)};
+    const long long t = ((long long)j + (long long)n * k) * half + ih;
 #pragma unroll
-    for (int b = 0; b < 2; ++b)
+    for (int odd = 0; odd < 2; ++odd) {
+        const int i = 2 * ih + odd;
+        const int I = ih;
+        const int Is[2] = {I, wrap1(odd ? I + 1 : I - 1, nc)};
+        double s = 0.0;
 #pragma unroll
-        for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
 #pragma unroll
-            for (int t = 0; t < 2; ++t)
-                s = s + ((w[t] * w[a]) * w[b]) *
-                            *lv_ptr<const double>(Cv.phi_r, Cv.phi_b, nc, Cv.split, Is[t], Js[a], Ks[b]);
-    double* p = lv_ptr<double>(F.phi_r, F.phi_b, n, F.split, i, j, k);
-    *p = *p + s;
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int tt = 0; tt < 2; ++tt)
+                    s = fma(kProlongW[tt + 2 * a + 4 * b],
+                            *lv_ptr<const double>(Cv.phi_r, Cv.phi_b, nc, Cv.split, Is[tt], Js[a], Ks[b]), s);
+        double* p = (((i + j + k) & 1) ? F.phi_b : F.phi_r) + t;
+        *p = *p + s;
+    }
 }
 
-// exact coarsest solve: phi = G * rhs (circulant pseudo-inverse), one block
-__global__ void k_bottom(int nb, const double* __restrict__ G, const double* __restrict__ rhs,
+// exact coarsest solve: phi = G * beta (cyclic convolution, y in storage order), one block
+__global__ void k_bottom(int nb, const double* __restrict__ G, const double* __restrict__ beta,
                          double* phi)
 {
     __shared__ double r[kMaxBottom * kMaxBottom * kMaxBottom];
+    __shared__ double g[kMaxBottom * kMaxBottom * kMaxBottom];
     const int nc = nb * nb * nb;
-    for (int t = threadIdx.x; t < nc; t += blockDim.x) r[t] = rhs[t];
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) {
+        r[t] = beta[t];
+        g[t] = G[t];
+    }
     __syncthreads();
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         const int i = c % nb, j = (c / nb) % nb, k = c / (nb * nb);
         double s = 0.0;
-        for (int y = 0; y < nc; ++y) {
-            const int yi = y % nb, yj = (y / nb) % nb, yk = y / (nb * nb);
-            const int d = wrapi(i - yi, nb) + nb * (wrapi(j - yj, nb) + nb * wrapi(k - yk, nb));
-            s = s + G[d] * r[y];
+        int y = 0;
+        for (int yk = 0; yk < nb; ++yk) {
+            const int dk = wrap1(k - yk, nb) * nb * nb;
+            for (int yj = 0; yj < nb; ++yj) {
+                const int djk = dk + wrap1(j - yj, nb) * nb;
+                for (int yi = 0; yi < nb; ++yi, ++y) s = fma(g[djk + wrap1(i - yi, nb)], r[y], s);
+            }
         }
         phi[c] = s;
     }
 }
 
-// g_d(c) = 0.5*((phi_c - phi_{c-e_d})*dxi + (phi_{c+e_d} - phi_c)*dxi), component-major
+// g_d(c) = 0.5*((phi_c - phi_{c-e_d})*dxi + (phi_{c+e_d} - phi_c)*dxi), second product fused;
+// component-major output
 __global__ void k_grav(LevelView L, double dxi, double* g)
 {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int n = L.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n || j >= n) return;
     const long long nc = (long long)n * n * n;
-    if (c >= nc) return;
-    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
+    const long long c = cidx(i, j, k, n);
     auto P = [&](int a, int b, int d) {
-        return *lv_ptr<const double>(L.phi_r, L.phi_b, n, L.split, wrapi(a, n), wrapi(b, n), wrapi(d, n));
+        return *lv_ptr<const double>(L.phi_r, L.phi_b, n, L.split, a, b, d);
     };
     const double pc = P(i, j, k);
-    g[c] = 0.5 * ((pc - P(i - 1, j, k)) * dxi + (P(i + 1, j, k) - pc) * dxi);
-    g[nc + c] = 0.5 * ((pc - P(i, j - 1, k)) * dxi + (P(i, j + 1, k) - pc) * dxi);
-    g[2 * nc + c] = 0.5 * ((pc - P(i, j, k - 1)) * dxi + (P(i, j, k + 1) - pc) * dxi);
+    const int im = i == 0 ? n - 1 : i - 1, ip = i == n - 1 ? 0 : i + 1;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    g[c] = 0.5 * fma(P(ip, j, k) - pc, dxi, (pc - P(im, j, k)) * dxi);
+    g[nc + c] = 0.5 * fma(P(i, jp, k) - pc, dxi, (pc - P(i, jm, k)) * dxi);
+    g[2 * nc + c] = 0.5 * fma(P(i, j, kp) - pc, dxi, (pc - P(i, j, km)) * dxi);
 }
 
 __global__ void k_to_natural(LevelView L, double* out)
 {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int n = L.n;
-    if (c >= (long long)n * n * n) return;
-    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
-    out[c] = *lv_ptr<const double>(L.phi_r, L.phi_b, n, L.split, i, j, k);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n || j >= n) return;
+    out[cidx(i, j, k, n)] = *lv_ptr<const double>(L.phi_r, L.phi_b, n, L.split, i, j, k);
 }
 
 __global__ void k_from_natural(LevelView L, const double* __restrict__ in)
 {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int n = L.n;
-    if (c >= (long long)n * n * n) return;
-    const int i = (int)(c % n), j = (int)((c / n) % n), k = (int)(c / ((long long)n * n));
-    *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, i, j, k) = in[c];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n || j >= n) return;
+    *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, i, j, k) = in[cidx(i, j, k, n)];
 }
 
 inline unsigned norm_blocks(Ctx& c, long long cnt)
@@ -285,12 +332,13 @@ inline unsigned norm_blocks(Ctx& c, long long cnt)
 nyxpm_status gsrb_sweep(Ctx& c, const Level& l, int fine)
 {
     const long long half_cells = (long long)l.n * l.n * l.n / 2;
+    const Geo g = geo3(l.n / 2, l.n, l.n);
     for (int color = 0; color < 2; ++color) {
         double* mine = color ? l.phi_b : l.phi_r;
         const double* other = color ? l.phi_r : l.phi_b;
-        const double* rhs = color ? l.rhs_b : l.rhs_r;
+        const double* beta = color ? l.beta_b : l.beta_r;
         prof_begin(c);
-        k_gsrb<<<blocks_for(half_cells), kThreads, 0, c.stream>>>(l.n, l.h2, color, mine, other, rhs);
+        k_gsrb<<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
         prof_end(c, NYXPM_ST_SMOOTH, 24.0 * half_cells, fine);
     }
     return check_launch(c, "gsrb");
@@ -302,7 +350,7 @@ nyxpm_status vcycle(Ctx& c, Box& b, size_t li)
     const Level& f = b.levels[li];
     if (li + 1 == b.levels.size()) {
         prof_begin(c);
-        k_bottom<<<1, 512, 0, c.stream>>>(b.nb, b.G, f.rhs_r, f.phi_r);
+        k_bottom<<<1, 512, 0, c.stream>>>(b.nb, b.G, f.beta_r, f.phi_r);
         prof_end(c, NYXPM_ST_BOTTOM, 16.0 * f.n * f.n * f.n);
         return check_launch(c, "bottom");
     }
@@ -312,28 +360,40 @@ nyxpm_status vcycle(Ctx& c, Box& b, size_t li)
     const Level& cl = b.levels[li + 1];
     const long long ncc = (long long)cl.n * cl.n * cl.n;
     const long long ncf = (long long)f.n * f.n * f.n;
-    prof_begin(c);
-    k_restrict<<<blocks_for(ncc), kThreads, 0, c.stream>>>(view(f), view(cl));
-    prof_end(c, NYXPM_ST_RESTRICT, 16.0 * ncf + 16.0 * ncc);
+    {
+        const Geo g = geo3(cl.n, cl.n, cl.n);
+        prof_begin(c);
+        k_restrict<<<g.grid, g.block, 0, c.stream>>>(view(f), view(cl));
+        prof_end(c, NYXPM_ST_RESTRICT, 16.0 * ncf + 16.0 * ncc);
+    }
     if ((st = check_launch(c, "restrict")) != NYXPM_OK) return st;
     if ((st = vcycle(c, b, li + 1)) != NYXPM_OK) return st;
-    prof_begin(c);
-    k_prolong<<<blocks_for(ncf), kThreads, 0, c.stream>>>(view(cl), view(f));
-    prof_end(c, NYXPM_ST_PROLONG, 16.0 * ncf + 8.0 * ncc);
+    {
+        const Geo g = geo3(f.n / 2, f.n, f.n);
+        prof_begin(c);
+        k_prolong<<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
+        prof_end(c, NYXPM_ST_PROLONG, 16.0 * ncf + 8.0 * ncc);
+    }
     if ((st = check_launch(c, "prolong")) != NYXPM_OK) return st;
     for (int s = 0; s < nu2; ++s)
         if ((st = gsrb_sweep(c, f, li == 0)) != NYXPM_OK) return st;
     return NYXPM_OK;
 }
 
-// launch ||r||_inf of level 0 into norms[slot]
+// launch ||r_beta||_inf of level 0 into norms[slot]
 nyxpm_status launch_resnorm(Ctx& c, Box& b, int slot)
 {
     const Level& l = b.levels[0];
     const long long nc = (long long)l.n * l.n * l.n;
     prof_begin(c);
     cudaMemsetAsync(b.norms + slot, 0, sizeof(unsigned long long), c.stream);
-    k_resnorm<<<norm_blocks(c, nc), kThreads, 0, c.stream>>>(view(l), b.norms + slot);
+    if (l.split) {
+        const Geo g = geo3(l.n / 2, l.n, l.n);
+        k_resnorm_split<<<g.grid, g.block, 0, c.stream>>>(view(l), b.norms + slot);
+    } else {
+        const Geo g = geo3(l.n, l.n, l.n);
+        k_resnorm_nat<<<g.grid, g.block, 0, c.stream>>>(view(l), b.norms + slot);
+    }
     prof_end(c, NYXPM_ST_NORM, 16.0 * nc);
     return check_launch(c, "resnorm");
 }
@@ -347,20 +407,27 @@ double read_norm(Box& b, int slot)
 
 }  // namespace
 
+double beta_scale(const Box& b)
+{
+    const double h = b.L / b.n;
+    return (h * h) * kSixth;
+}
+
 nyxpm_status launch_make_rhs(Ctx& c, Box& b, double a)
 {
     const int n = b.n;
     const long long nc = (long long)n * n * n;
     const Level& l0 = b.levels[0];
     const double dx = b.L / n;
+    const Geo g = geo3(n, n, n);
     prof_begin(c);
     k_rowsum<<<blocks_for((long long)n * n * 32), kThreads, 0, c.stream>>>(n, b.rho, b.mass_offset,
                                                                           b.rows);
     k_planesum<<<blocks_for(n, 128), 128, 0, c.stream>>>(n, b.rows, b.planes);
     k_mean<<<1, 32, 0, c.stream>>>(n, dx, b.L, b.planes, b.scal);
-    k_make_rhs<<<blocks_for(nc), kThreads, 0, c.stream>>>(n, l0.split, b.rho, b.mass_offset, b.scal,
-                                                          -4.0 * M_PI * c.p.gconst, 1.0 / a,
-                                                          l0.rhs_r, l0.rhs_b);
+    k_make_beta<<<g.grid, g.block, 0, c.stream>>>(n, l0.split, b.rho, b.mass_offset, b.scal,
+                                                  -4.0 * M_PI * c.p.gconst, 1.0 / a, beta_scale(b),
+                                                  l0.beta_r, l0.beta_b);
     prof_end(c, NYXPM_ST_RHS, 24.0 * nc);
     c.launches += 3;
     return check_launch(c, "make rhs");
@@ -384,15 +451,15 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
     nyxpm_status st;
     const Level& l0 = b.levels[0];
     const long long nc = (long long)l0.n * l0.n * l0.n;
-    // ||rhs||_inf and ||r0||_inf
+    // ||beta||_inf and ||r0||_inf
     prof_begin(c);
     cudaMemsetAsync(b.norms, 0, sizeof(unsigned long long), c.stream);
     if (l0.split) {
-        k_absmax<<<norm_blocks(c, nc / 2), kThreads, 0, c.stream>>>(nc / 2, l0.rhs_r, b.norms);
-        k_absmax<<<norm_blocks(c, nc / 2), kThreads, 0, c.stream>>>(nc / 2, l0.rhs_b, b.norms);
+        k_absmax<<<norm_blocks(c, nc / 2), kThreads, 0, c.stream>>>(nc / 2, l0.beta_r, b.norms);
+        k_absmax<<<norm_blocks(c, nc / 2), kThreads, 0, c.stream>>>(nc / 2, l0.beta_b, b.norms);
         c.launches += 1;
     } else {
-        k_absmax<<<norm_blocks(c, nc), kThreads, 0, c.stream>>>(nc, l0.rhs_r, b.norms);
+        k_absmax<<<norm_blocks(c, nc), kThreads, 0, c.stream>>>(nc, l0.beta_r, b.norms);
     }
     prof_end(c, NYXPM_ST_NORM, 8.0 * nc);
     if ((st = check_launch(c, "rhs norm")) != NYXPM_OK) return st;
@@ -428,11 +495,12 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
     }
     b.have_phi = 1;
     if (info) {
+        const double inv_k0 = 1.0 / beta_scale(b);
         info->vcycles = it;
         info->inner_vcycles = 0;
-        info->resnorm0 = r0;
-        info->resnorm = r;
-        info->bnorm = bnorm;
+        info->resnorm0 = r0 * inv_k0;
+        info->resnorm = r * inv_k0;
+        info->bnorm = bnorm * inv_k0;
     }
     return result;
 }
@@ -440,8 +508,9 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
 nyxpm_status launch_grav_vector(Ctx& c, Box& b)
 {
     const long long nc = (long long)b.n * b.n * b.n;
+    const Geo g = geo3(b.n, b.n, b.n);
     prof_begin(c);
-    k_grav<<<blocks_for(nc), kThreads, 0, c.stream>>>(view(b.levels[0]), b.dxi, b.g);
+    k_grav<<<g.grid, g.block, 0, c.stream>>>(view(b.levels[0]), b.dxi, b.g);
     prof_end(c, NYXPM_ST_KICK, 32.0 * nc);
     return check_launch(c, "grav vector");
 }
@@ -449,8 +518,9 @@ nyxpm_status launch_grav_vector(Ctx& c, Box& b)
 nyxpm_status launch_phi_to_natural(Ctx& c, Box& b, double* d_out)
 {
     const long long nc = (long long)b.n * b.n * b.n;
+    const Geo g = geo3(b.n, b.n, b.n);
     prof_begin(c);
-    k_to_natural<<<blocks_for(nc), kThreads, 0, c.stream>>>(view(b.levels[0]), d_out);
+    k_to_natural<<<g.grid, g.block, 0, c.stream>>>(view(b.levels[0]), d_out);
     prof_end(c, NYXPM_ST_GATHER, 16.0 * nc);
     return check_launch(c, "phi to natural");
 }
@@ -458,8 +528,9 @@ nyxpm_status launch_phi_to_natural(Ctx& c, Box& b, double* d_out)
 nyxpm_status launch_phi_from_natural(Ctx& c, Box& b, const double* d_in)
 {
     const long long nc = (long long)b.n * b.n * b.n;
+    const Geo g = geo3(b.n, b.n, b.n);
     prof_begin(c);
-    k_from_natural<<<blocks_for(nc), kThreads, 0, c.stream>>>(view(b.levels[0]), d_in);
+    k_from_natural<<<g.grid, g.block, 0, c.stream>>>(view(b.levels[0]), d_in);
     prof_end(c, NYXPM_ST_GATHER, 16.0 * nc);
     return check_launch(c, "phi from natural");
 }

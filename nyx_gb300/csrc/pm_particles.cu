@@ -1,11 +1,13 @@
 // Particle kernels of the FP64 PM step: upload/download, periodic wrap, the
 // per-step counting sort by deposit cell, the atomic-free CIC deposit and the
-// fused gradient + CIC interpolation + kick(-drift).
+// CIC interpolation + kick(-drift) (+ periodic wrap).
 //
-// Built with --fmad=false: every FP64 expression rounds exactly as written,
-// in the order written, which is what update_dm_particle_single
-// (Source/Particle/DarkMatterParticleContainer.cpp:250-306) and the CIC weights
-// (Source/Particle/NeutrinoParticles_K.H:15-45) specify.
+// Built with --fmad=false: every FP64 expression rounds exactly as written, in
+// the order written, with explicit fma() only where the CPU oracle uses fma()
+// too -- the arithmetic of update_dm_particle_single
+// (Source/Particle/DarkMatterParticleContainer.cpp:250-306) and of the CIC
+// weights (Source/Particle/NeutrinoParticles_K.H:15-45).  GB300 runs FP64 at a
+// small fraction of its FP32 rate, so every FP64 instruction saved counts.
 #include "pm_common.cuh"
 
 #include <cstdio>
@@ -22,13 +24,14 @@ inline unsigned blocks_for(long long n, int t = kThreads)
     return (unsigned)(b < 1 ? 1 : b);
 }
 
-// deposit key along one axis: floor(x*dxi + 1/2) wrapped into [0, n)
+// deposit key along one axis: floor(x*dxi + 1/2) (product and sum fused)
+// wrapped into [0, n)
 __device__ __forceinline__ int key1(double x, double dxi, int n, double* frac)
 {
-    const double l = x * dxi + 0.5;
-    const int i = (int)floor(l);
-    *frac = l - (double)i;
-    return wrapi(i, n);
+    const double l = fma(x, dxi, 0.5);
+    const double fl = floor(l);
+    *frac = l - fl;
+    return wrapi((int)fl, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -296,11 +299,11 @@ constexpr int kTx = 8, kTy = 8, kTz = 8;
 constexpr int kKx = kTx + 1, kKy = kTy + 1, kKz = kTz + 1;
 constexpr int kNKeys = kKx * kKy * kKz;
 
-__global__ void __launch_bounds__(256) k_deposit(int n, double dxi, double inv_vol,
+__global__ void __launch_bounds__(256) k_deposit(int n, double dxi, double scale,
                                                  const double* __restrict__ x,
                                                  const double* __restrict__ y,
                                                  const double* __restrict__ z,
-                                                 const double* __restrict__ m, double mscalar,
+                                                 const double* __restrict__ m,
                                                  const int* __restrict__ start, double* rho)
 {
     __shared__ double part[kNKeys * 8];
@@ -320,14 +323,24 @@ __global__ void __launch_bounds__(256) k_deposit(int n, double dxi, double inv_v
             const double sx[2] = {1.0 - fx, fx};
             const double sy[2] = {1.0 - fy, fy};
             const double sz[2] = {1.0 - fz, fz};
-            const double mq = m ? m[q] : mscalar;
+            if (m) {
+                const double mq = m[q];
 #pragma unroll
-            for (int cz = 0; cz < 2; ++cz)
+                for (int cz = 0; cz < 2; ++cz)
 #pragma unroll
-                for (int cy = 0; cy < 2; ++cy)
+                    for (int cy = 0; cy < 2; ++cy)
 #pragma unroll
-                    for (int cx = 0; cx < 2; ++cx)
-                        s[cx + 2 * cy + 4 * cz] = s[cx + 2 * cy + 4 * cz] + ((sx[cx] * sy[cy]) * sz[cz]) * mq;
+                        for (int cx = 0; cx < 2; ++cx)
+                            s[cx + 2 * cy + 4 * cz] = fma((sx[cx] * sy[cy]) * sz[cz], mq, s[cx + 2 * cy + 4 * cz]);
+            } else {
+#pragma unroll
+                for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+                    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                        for (int cx = 0; cx < 2; ++cx)
+                            s[cx + 2 * cy + 4 * cz] = s[cx + 2 * cy + 4 * cz] + (sx[cx] * sy[cy]) * sz[cz];
+            }
         }
 #pragma unroll
         for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
@@ -348,89 +361,68 @@ __global__ void __launch_bounds__(256) k_deposit(int n, double dxi, double inv_v
                     const int corner = (1 - di) + 2 * (1 - dj) + 4 * (1 - dk);
                     acc = acc + part[kl * 8 + corner];
                 }
-        rho[cidx(i, j, k, n)] = acc * inv_vol;
+        rho[cidx(i, j, k, n)] = acc * scale;
     }
 }
 
 // ---------------------------------------------------------------------------
-// fused gradient + CIC interpolation + kick (+ drift) (+ periodic wrap)
+// CIC interpolation of the cell-centred gravity vector + kick (+ drift)
+// (+ periodic wrap), update_dm_particle_single with the products of the
+// reference fused where the oracle fuses them
 // ---------------------------------------------------------------------------
 struct KickArgs {
-    int n, split;
+    int n;
     double dxi, L;
-    const double* phi_r;
-    const double* phi_b;
+    const double* g;   // 3 n^3, component-major
     double half_dt, a_prev, a_cur_inv, dt_a_cur_inv;
     int do_move, do_wrap;
 };
-
-__device__ __forceinline__ double phi_at(const KickArgs& A, int i, int j, int k)
-{
-    return *lv_ptr<const double>(A.phi_r, A.phi_b, A.n, A.split, wrapi(i, A.n), wrapi(j, A.n),
-                                 wrapi(k, A.n));
-}
 
 __global__ void __launch_bounds__(256) k_kick(long long np, KickArgs A, double* x, double* y,
                                               double* z, double* vx, double* vy, double* vz)
 {
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
-    const double lx = x[q] * A.dxi + 0.5;
-    const double ly = y[q] * A.dxi + 0.5;
-    const double lz = z[q] * A.dxi + 0.5;
-    const int i = (int)floor(lx), j = (int)floor(ly), k = (int)floor(lz);
-    const double xint = lx - i, yint = ly - j, zint = lz - k;
+    const int n = A.n;
+    const long long nc = (long long)n * n * n;
+    const double lx = fma(x[q], A.dxi, 0.5);
+    const double ly = fma(y[q], A.dxi, 0.5);
+    const double lz = fma(z[q], A.dxi, 0.5);
+    const double fi = floor(lx), fj = floor(ly), fk = floor(lz);
+    const int i = (int)fi, j = (int)fj, k = (int)fk;
+    const double xint = lx - fi, yint = ly - fj, zint = lz - fk;
     const double sx[2] = {1.0 - xint, xint};
     const double sy[2] = {1.0 - yint, yint};
     const double sz[2] = {1.0 - zint, zint};
-    // phi on the 4x4x4 block around the 2x2x2 interpolation cells (offsets -2..1),
-    // loaded only where a central difference needs it
-    double P[4][4][4];
+    double w[8];
+    long long cell[8];
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
+    for (int kk = 0; kk <= 1; ++kk)
 #pragma unroll
-        for (int b = 0; b < 4; ++b)
+        for (int jj = 0; jj <= 1; ++jj)
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                const int inx = (a == 1 || a == 2), iny = (b == 1 || b == 2), inz = (c == 1 || c == 2);
-                if (inx + iny + inz >= 2) P[c][b][a] = phi_at(A, i - 2 + a, j - 2 + b, k - 2 + c);
-                else P[c][b][a] = 0.0;
-            }
-    // gravity vector at the 8 cells (i-ii, j-jj, k-kk): local index (2-ii, 2-jj, 2-kk)
-    double gv[2][2][2][3];
-#pragma unroll
-    for (int kk = 0; kk < 2; ++kk)
-#pragma unroll
-        for (int jj = 0; jj < 2; ++jj)
-#pragma unroll
-            for (int ii = 0; ii < 2; ++ii) {
-                const int a = 2 - ii, b = 2 - jj, c = 2 - kk;
-                const double pc = P[c][b][a];
-                gv[kk][jj][ii][0] = 0.5 * ((pc - P[c][b][a - 1]) * A.dxi + (P[c][b][a + 1] - pc) * A.dxi);
-                gv[kk][jj][ii][1] = 0.5 * ((pc - P[c][b - 1][a]) * A.dxi + (P[c][b + 1][a] - pc) * A.dxi);
-                gv[kk][jj][ii][2] = 0.5 * ((pc - P[c - 1][b][a]) * A.dxi + (P[c + 1][b][a] - pc) * A.dxi);
+            for (int ii = 0; ii <= 1; ++ii) {
+                const int t = ii + 2 * jj + 4 * kk;
+                w[t] = (sx[1 - ii] * sy[1 - jj]) * sz[1 - kk];
+                cell[t] = cidx(wrapi(i - ii, n), wrapi(j - jj, n), wrapi(k - kk, n), n);
             }
     double v[3] = {vx[q], vy[q], vz[q]};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
+        const double* gd = A.g + d * nc;
         double val = 0.0;
 #pragma unroll
-        for (int kk = 0; kk <= 1; ++kk)
-#pragma unroll
-            for (int jj = 0; jj <= 1; ++jj)
-#pragma unroll
-                for (int ii = 0; ii <= 1; ++ii)
-                    val = val + ((sx[1 - ii] * sy[1 - jj]) * sz[1 - kk]) * gv[kk][jj][ii][d];
-        const double u = A.a_prev * v[d] + A.half_dt * val;
+        for (int t = 0; t < 8; ++t) val = fma(w[t], __ldg(gd + cell[t]), val);
+        const double u = fma(A.a_prev, v[d], A.half_dt * val);
         v[d] = u * A.a_cur_inv;
     }
     vx[q] = v[0];
     vy[q] = v[1];
     vz[q] = v[2];
     if (A.do_move == 1) {
-        double px = x[q] + A.dt_a_cur_inv * v[0];
-        double py = y[q] + A.dt_a_cur_inv * v[1];
-        double pz = z[q] + A.dt_a_cur_inv * v[2];
+        double px = fma(A.dt_a_cur_inv, v[0], x[q]);
+        double py = fma(A.dt_a_cur_inv, v[1], y[q]);
+        double pz = fma(A.dt_a_cur_inv, v[2], z[q]);
         if (A.do_wrap) {
             px = wrap_pos(px, A.L);
             py = wrap_pos(py, A.L);
@@ -548,11 +540,12 @@ nyxpm_status launch_deposit(Ctx& c, Box& b)
     dim3 grid((n + kTx - 1) / kTx, (n + kTy - 1) / kTy, (n + kTz - 1) / kTz);
     const double dx = b.L / n;
     const double inv_vol = 1.0 / (dx * dx * dx);
+    // per-particle masses: keys sum w*m, cells scale by 1/dx^3; uniform: keys sum w, cells by m/dx^3
+    const double scale = b.uniform_mass ? b.mscalar * inv_vol : inv_vol;
     const double nc = (double)n * n * n;
     prof_begin(c);
-    k_deposit<<<grid, 256, 0, c.stream>>>(n, b.dxi, inv_vol, b.x, b.y, b.z,
-                                          b.uniform_mass ? nullptr : b.m, b.mscalar, b.cell_start,
-                                          b.rho);
+    k_deposit<<<grid, 256, 0, c.stream>>>(n, b.dxi, scale, b.x, b.y, b.z,
+                                          b.uniform_mass ? nullptr : b.m, b.cell_start, b.rho);
     prof_end(c, NYXPM_ST_DEPOSIT, (b.uniform_mass ? 24.0 : 32.0) * b.np + 12.0 * nc);
     return check_launch(c, "deposit");
 }
@@ -560,14 +553,11 @@ nyxpm_status launch_deposit(Ctx& c, Box& b)
 nyxpm_status launch_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move,
                          int do_wrap)
 {
-    const Level& l0 = b.levels[0];
     KickArgs A;
     A.n = b.n;
-    A.split = l0.split;
     A.dxi = b.dxi;
     A.L = b.L;
-    A.phi_r = l0.phi_r;
-    A.phi_b = l0.phi_b;
+    A.g = b.g;
     A.half_dt = 0.5 * dt;
     A.a_prev = a_prev;
     A.a_cur_inv = 1.0 / a_cur;
@@ -577,7 +567,7 @@ nyxpm_status launch_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur,
     prof_begin(c);
     k_kick<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, A, b.x, b.y, b.z, b.vx, b.vy, b.vz);
     const double nc = (double)b.n * b.n * b.n;
-    prof_end(c, NYXPM_ST_KICK, (do_move ? 96.0 : 72.0) * b.np + 8.0 * nc);
+    prof_end(c, NYXPM_ST_KICK, (do_move ? 96.0 : 72.0) * b.np + 24.0 * nc);
     b.sorted = b.sorted && !do_move && !do_wrap;
     return check_launch(c, "kick");
 }

@@ -92,10 +92,11 @@ inline int wrapi(int i, int n) { i %= n; return i < 0 ? i + n : i; }
 inline long cidx(int i, int j, int k, int n) { return (long)i + (long)n * ((long)j + (long)n * k); }
 
 // deposit key of one coordinate: floor((x - plo) * dxi + 0.5), plo = 0
-// (NeutrinoParticles_K.H:15-21, DarkMatterParticleContainer.cpp:263-269)
+// (NeutrinoParticles_K.H:15-21, DarkMatterParticleContainer.cpp:263-269),
+// the product and the sum fused into one multiply-add
 inline int key1(double x, double dxi, int n, double* frac)
 {
-    double l = x * dxi + 0.5;
+    double l = std::fma(x, dxi, 0.5);
     int i = (int)std::floor(l);
     *frac = l - i;
     return wrapi(i, n);
@@ -170,8 +171,10 @@ int orc_sort(int n, double L, long np, double* x, double* y, double* z,
 // CIC deposit (AssignDensitySingleLevel).  Particles must be sorted by key
 // (orc_sort).  m == NULL means every particle has mass mscalar.
 // Per particle: l = x*dxi + 0.5, i = floor(l), f = l - i, weights
-// sx = {1-f, f} on cells {i-1, i}; value ((sx*sy)*sz)*m, then * 1/dx^3
-// (NeutrinoParticles_K.H:15-45, NeutrinoParticleContainer.cpp:300-302).
+// sx = {1-f, f} on cells {i-1, i}, w = (sx*sy)*sz (NeutrinoParticles_K.H:15-45).
+// Per-particle masses: the key sums w*m (fused), the cell sum is scaled by
+// 1/dx^3 (NeutrinoParticleContainer.cpp:300-302).  Uniform mass: the key sums w
+// and the cell sum is scaled once by m/dx^3.
 // ----------------------------------------------------------------------------
 void orc_deposit(int n, double L, long np, const double* x, const double* y, const double* z,
                  const double* m, double mscalar, const int* cell_start, double* rho)
@@ -181,6 +184,7 @@ void orc_deposit(int n, double L, long np, const double* x, const double* y, con
     const double dx = L / n;
     const double dxi = (double)n / L;
     const double inv_vol = 1.0 / (dx * dx * dx);
+    const double scale = m ? inv_vol : mscalar * inv_vol;
     // per-key partial sums: part[K*8 + corner], corner = cx + 2*cy + 4*cz where
     // cx = 0 is the cell i-1 (weight 1-f) and cx = 1 the cell i (weight f)
     std::vector<double> part(nc * 8);
@@ -195,11 +199,13 @@ void orc_deposit(int n, double L, long np, const double* x, const double* y, con
             const double sx[2] = {1.0 - fx, fx};
             const double sy[2] = {1.0 - fy, fy};
             const double sz[2] = {1.0 - fz, fz};
-            const double mq = m ? m[q] : mscalar;
             for (int cz = 0; cz < 2; ++cz)
                 for (int cy = 0; cy < 2; ++cy)
-                    for (int cx = 0; cx < 2; ++cx)
-                        s[cx + 2 * cy + 4 * cz] = s[cx + 2 * cy + 4 * cz] + ((sx[cx] * sy[cy]) * sz[cz]) * mq;
+                    for (int cx = 0; cx < 2; ++cx) {
+                        const double w = (sx[cx] * sy[cy]) * sz[cz];
+                        double& a = s[cx + 2 * cy + 4 * cz];
+                        a = m ? std::fma(w, m[q], a) : a + w;
+                    }
         }
         for (int c = 0; c < 8; ++c) part[K * 8 + c] = s[c];
     }
@@ -216,7 +222,7 @@ void orc_deposit(int n, double L, long np, const double* x, const double* y, con
                             int corner = (1 - di) + 2 * (1 - dj) + 4 * (1 - dk);
                             acc = acc + part[K * 8 + corner];
                         }
-                rho[cidx(i, j, k, n)] = acc * inv_vol;
+                rho[cidx(i, j, k, n)] = acc * scale;
             }
 }
 
@@ -279,9 +285,8 @@ namespace {
 
 struct Level {
     int n;
-    double h2;   // h*h
-    double ih2;  // 1/(h*h)
-    std::vector<double> phi, rhs;
+    std::vector<double> phi;
+    std::vector<double> beta;   // right-hand side in smoother units: h^2 rhs / 6
 };
 
 inline double nbr_sum(const double* p, int i, int j, int k, int n)
@@ -299,30 +304,31 @@ inline double nbr_sum(const double* p, int i, int j, int k, int n)
 
 const double kSixth = 1.0 / 6.0;
 
-// one red-black sweep: red cells ((i+j+k) even) then black
+// one red-black sweep: red cells ((i+j+k) even) then black;
+// phi = s/6 - beta with s the sum of the 6 neighbours (one fused multiply-add)
 void gsrb(Level& lv)
 {
     const int n = lv.n;
     double* p = lv.phi.data();
-    const double* r = lv.rhs.data();
+    const double* b = lv.beta.data();
     for (int color = 0; color < 2; ++color) {
 #pragma omp parallel for schedule(static)
         for (int k = 0; k < n; ++k)
             for (int j = 0; j < n; ++j)
                 for (int i = (j + k + color) & 1; i < n; i += 2) {
                     const double s = nbr_sum(p, i, j, k, n);
-                    p[cidx(i, j, k, n)] = (s - lv.h2 * r[cidx(i, j, k, n)]) * kSixth;
+                    p[cidx(i, j, k, n)] = std::fma(s, kSixth, -b[cidx(i, j, k, n)]);
                 }
     }
 }
 
+// residual in smoother units: beta - (s/6 - phi)  ( = h^2/6 (rhs - lap phi) )
 inline double resid_at(const Level& lv, int i, int j, int k)
 {
     const int n = lv.n;
     const double* p = lv.phi.data();
     const double s = nbr_sum(p, i, j, k, n);
-    const double c = p[cidx(i, j, k, n)];
-    return lv.rhs[cidx(i, j, k, n)] - (s - 6.0 * c) * lv.ih2;
+    return lv.beta[cidx(i, j, k, n)] - std::fma(s, kSixth, -p[cidx(i, j, k, n)]);
 }
 
 double resid_norm(const Level& lv)
@@ -350,7 +356,8 @@ double inf_norm(const double* f, long nc)
     return mx;
 }
 
-// coarse rhs = average of the 8 fine residuals, summed in (dk,dj,di) order
+// coarse beta = 1/2 of the sum of the 8 fine residuals (summed dk, dj, di):
+// the 8-cell average of rhs - lap phi, rescaled by h_c^2/6 = 4 h_f^2/6
 void restrict_resid(const Level& f, Level& c)
 {
     const int nc = c.n;
@@ -363,16 +370,19 @@ void restrict_resid(const Level& f, Level& c)
                     for (int dj = 0; dj < 2; ++dj)
                         for (int di = 0; di < 2; ++di)
                             s = s + resid_at(f, 2 * I + di, 2 * J + dj, 2 * K + dk);
-                c.rhs[cidx(I, J, K, nc)] = s * 0.125;
+                c.beta[cidx(I, J, K, nc)] = s * 0.5;
             }
 }
 
-// trilinear cell-centred prolongation of the coarse correction, added to phi
+// trilinear cell-centred prolongation weights (3/4, 1/4 per axis; exact in binary),
+// indexed t + 2a + 4b with t, a, b selecting (parent, neighbour) along x, y, z
+const double kProlongW[8] = {0.421875, 0.140625, 0.140625, 0.046875,
+                             0.140625, 0.046875, 0.046875, 0.015625};
+
 void prolong_add(const Level& c, Level& f)
 {
     const int n = f.n, nc = c.n;
     const double* e = c.phi.data();
-    static const double w[2] = {0.75, 0.25};
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < n; ++k)
         for (int j = 0; j < n; ++j)
@@ -386,7 +396,7 @@ void prolong_add(const Level& c, Level& f)
                 for (int b = 0; b < 2; ++b)
                     for (int a = 0; a < 2; ++a)
                         for (int t = 0; t < 2; ++t)
-                            s = s + ((w[t] * w[a]) * w[b]) * e[cidx(Is[t], Js[a], Ks[b], nc)];
+                            s = std::fma(kProlongW[t + 2 * a + 4 * b], e[cidx(Is[t], Js[a], Ks[b], nc)], s);
                 f.phi[cidx(i, j, k, n)] = f.phi[cidx(i, j, k, n)] + s;
             }
 }
@@ -396,8 +406,9 @@ void prolong_add(const Level& c, Level& f)
 extern "C" {
 
 // Green's function of the periodic 7-point Laplacian on an nb^3 grid with
-// spacing h, projected off the constant mode:
-// G(d) = (1/nb^3) sum_{kappa != 0} cos(2 pi kappa.d / nb) / lambda(kappa),
+// spacing h, projected off the constant mode, in smoother units (applied to
+// beta = h^2 rhs / 6):
+// G(d) = (6/h^2) (1/nb^3) sum_{kappa != 0} cos(2 pi kappa.d / nb) / lambda(kappa),
 // lambda = sum_d (2 cos(2 pi kappa_d / nb) - 2) / h^2.
 void orc_bottom_green(int nb, double h, double* G)
 {
@@ -411,6 +422,7 @@ void orc_bottom_green(int nb, double h, double* G)
                          + (2.0 * std::cos(twopi * kz / nb) - 2.0);
                 lam[cidx(kx, ky, kz, nb)] = l / (h * h);
             }
+    const double scale = 6.0 / (h * h);
     for (int dz = 0; dz < nb; ++dz)
         for (int dy = 0; dy < nb; ++dy)
             for (int dxx = 0; dxx < nb; ++dxx) {
@@ -422,7 +434,7 @@ void orc_bottom_green(int nb, double h, double* G)
                             const long ph = ((long)kx * dxx + (long)ky * dy + (long)kz * dz) % nb;
                             s += std::cos(twopi * (double)ph / nb) / lam[cidx(kx, ky, kz, nb)];
                         }
-                G[cidx(dxx, dy, dz, nb)] = s / (double)nc;
+                G[cidx(dxx, dy, dz, nb)] = (s / (double)nc) * scale;
             }
 }
 
@@ -430,19 +442,20 @@ void orc_bottom_green(int nb, double h, double* G)
 
 namespace {
 
+// exact coarsest solve: phi = G * beta (cyclic convolution, y in storage order)
 void bottom_solve(Level& lv, const std::vector<double>& G)
 {
     const int n = lv.n;
-    const long nc = (long)n * n * n;
     for (int k = 0; k < n; ++k)
         for (int j = 0; j < n; ++j)
             for (int i = 0; i < n; ++i) {
                 double s = 0.0;
-                for (long y = 0; y < nc; ++y) {
-                    const int yi = (int)(y % n), yj = (int)((y / n) % n), yk = (int)(y / ((long)n * n));
-                    const long d = cidx(wrapi(i - yi, n), wrapi(j - yj, n), wrapi(k - yk, n), n);
-                    s = s + G[d] * lv.rhs[y];
-                }
+                for (int yk = 0; yk < n; ++yk)
+                    for (int yj = 0; yj < n; ++yj)
+                        for (int yi = 0; yi < n; ++yi) {
+                            const long d = cidx(wrapi(i - yi, n), wrapi(j - yj, n), wrapi(k - yk, n), n);
+                            s = std::fma(G[d], lv.beta[cidx(yi, yj, yk, n)], s);
+                        }
                 lv.phi[cidx(i, j, k, n)] = s;
             }
 }
@@ -460,11 +473,8 @@ bool build_hierarchy(int n, double L, Hierarchy& H)
     for (int nl = n;; nl /= 2) {
         Level l;
         l.n = nl;
-        const double h = L / nl;
-        l.h2 = h * h;
-        l.ih2 = 1.0 / (h * h);
         l.phi.assign((long)nl * nl * nl, 0.0);
-        l.rhs.assign((long)nl * nl * nl, 0.0);
+        l.beta.assign((long)nl * nl * nl, 0.0);
         H.lv.push_back(std::move(l));
         if (nl == m) break;
     }
@@ -498,8 +508,18 @@ int orc_mg_levels(int n)
     return (m > 8 || n < 2) ? 0 : L;
 }
 
+// Scale factor from rhs to smoother units on an n^3 grid of side L: (h*h)*(1/6).
+double orc_beta_scale(int n, double L)
+{
+    const double h = L / n;
+    return (h * h) * kSixth;
+}
+
 // Solve lap(phi) = rhs (periodic, 7-point) by V-cycles from the initial guess in
-// phi.  Returns 0 when converged, 4 when max_cycles was reached, 1 on bad n.
+// phi.  The convergence test is done in smoother units,
+// ||r_beta||_inf <= rel_tol * max(||beta||_inf, ||r_beta0||_inf); the norms are
+// reported in rhs units (divided by the scale).  Returns 0 when converged, 4 when
+// max_cycles was reached, 1 on bad n.
 int orc_mg_solve(int n, double L, const double* rhs, double* phi, double rel_tol, int max_cycles,
                  int nu1, int nu2, int* ncycles, double* resnorm0, double* resnorm)
 {
@@ -507,9 +527,11 @@ int orc_mg_solve(int n, double L, const double* rhs, double* phi, double rel_tol
     if (!build_hierarchy(n, L, H)) return 1;
     const long nc = (long)n * n * n;
     Level& f = H.lv[0];
-    std::memcpy(f.rhs.data(), rhs, sizeof(double) * nc);
+    const double k0 = orc_beta_scale(n, L);
+    const double inv_k0 = 1.0 / k0;
+    for (long c = 0; c < nc; ++c) f.beta[c] = rhs[c] * k0;
     std::memcpy(f.phi.data(), phi, sizeof(double) * nc);
-    const double bnorm = inf_norm(rhs, nc);
+    const double bnorm = inf_norm(f.beta.data(), nc);
     const double r0 = resid_norm(f);
     const double target = rel_tol * std::max(bnorm, r0);
     double r = r0;
@@ -525,14 +547,15 @@ int orc_mg_solve(int n, double L, const double* rhs, double* phi, double rel_tol
     }
     std::memcpy(phi, f.phi.data(), sizeof(double) * nc);
     if (ncycles) *ncycles = it;
-    if (resnorm0) *resnorm0 = r0;
-    if (resnorm) *resnorm = r;
+    if (resnorm0) *resnorm0 = r0 * inv_k0;
+    if (resnorm) *resnorm = r * inv_k0;
     return status;
 }
 
 // Cell-centred gravity vector g = average of the two face gradients
-// (Gravity.cpp:817-850): g_d(c) = 0.5*((phi_c - phi_{c-e_d})*dxi + (phi_{c+e_d} - phi_c)*dxi).
-// g holds the three components one after another (component-major).
+// (Gravity.cpp:817-850): g_d(c) = 0.5*((phi_c - phi_{c-e_d})*dxi + (phi_{c+e_d} - phi_c)*dxi),
+// the second product fused with the sum.  g holds the three components one
+// after another (component-major).
 void orc_grav_vector(int n, double L, const double* phi, double* g)
 {
     const long nc = (long)n * n * n;
@@ -546,14 +569,17 @@ void orc_grav_vector(int n, double L, const double* phi, double* g)
                 const long xm = cidx(wrapi(i - 1, n), j, k, n), xp = cidx(wrapi(i + 1, n), j, k, n);
                 const long ym = cidx(i, wrapi(j - 1, n), k, n), yp = cidx(i, wrapi(j + 1, n), k, n);
                 const long zm = cidx(i, j, wrapi(k - 1, n), n), zp = cidx(i, j, wrapi(k + 1, n), n);
-                g[c] = 0.5 * ((pc - phi[xm]) * dxi + (phi[xp] - pc) * dxi);
-                g[nc + c] = 0.5 * ((pc - phi[ym]) * dxi + (phi[yp] - pc) * dxi);
-                g[2 * nc + c] = 0.5 * ((pc - phi[zm]) * dxi + (phi[zp] - pc) * dxi);
+                g[c] = 0.5 * std::fma(phi[xp] - pc, dxi, (pc - phi[xm]) * dxi);
+                g[nc + c] = 0.5 * std::fma(phi[yp] - pc, dxi, (pc - phi[ym]) * dxi);
+                g[2 * nc + c] = 0.5 * std::fma(phi[zp] - pc, dxi, (pc - phi[zm]) * dxi);
             }
 }
 
 // update_dm_particle_single (DarkMatterParticleContainer.cpp:250-306) over all
-// particles, with the acceleration field g (component-major, periodic).
+// particles, with the acceleration field g (component-major, periodic):
+// l = x*dxi + 1/2 (fused), i = floor(l), weights w = (sx*sy)*sz of the 8 cells
+// (i-ii, j-jj, k-kk) in the order kk, jj, ii; val_d = sum w*g_d (fused);
+// v = (a_prev*v + dt/2*val) / a_cur (the first product fused); x += dt/a_cur*v (fused).
 void orc_move(int n, double L, long np, double* x, double* y, double* z, double* vx, double* vy,
               double* vz, const double* g, double dt, double a_prev, double a_cur, int do_move)
 {
@@ -564,32 +590,35 @@ void orc_move(int n, double L, long np, double* x, double* y, double* z, double*
     const double dt_a_cur_inv = dt * a_cur_inv;
 #pragma omp parallel for schedule(static)
     for (long q = 0; q < np; ++q) {
-        const double lx = x[q] * dxi + 0.5;
-        const double ly = y[q] * dxi + 0.5;
-        const double lz = z[q] * dxi + 0.5;
-        const int i = (int)std::floor(lx);
-        const int j = (int)std::floor(ly);
-        const int k = (int)std::floor(lz);
-        const double xint = lx - i, yint = ly - j, zint = lz - k;
+        const double lx = std::fma(x[q], dxi, 0.5);
+        const double ly = std::fma(y[q], dxi, 0.5);
+        const double lz = std::fma(z[q], dxi, 0.5);
+        const double fi = std::floor(lx), fj = std::floor(ly), fk = std::floor(lz);
+        const int i = (int)fi, j = (int)fj, k = (int)fk;
+        const double xint = lx - fi, yint = ly - fj, zint = lz - fk;
         const double sx[2] = {1.0 - xint, xint};
         const double sy[2] = {1.0 - yint, yint};
         const double sz[2] = {1.0 - zint, zint};
+        double w[8];
+        long cells[8];
+        for (int kk = 0; kk <= 1; ++kk)
+            for (int jj = 0; jj <= 1; ++jj)
+                for (int ii = 0; ii <= 1; ++ii) {
+                    const int t = ii + 2 * jj + 4 * kk;
+                    w[t] = (sx[1 - ii] * sy[1 - jj]) * sz[1 - kk];
+                    cells[t] = cidx(wrapi(i - ii, n), wrapi(j - jj, n), wrapi(k - kk, n), n);
+                }
         double* v[3] = {vx + q, vy + q, vz + q};
         for (int d = 0; d < 3; ++d) {
             double val = 0.0;
-            for (int kk = 0; kk <= 1; ++kk)
-                for (int jj = 0; jj <= 1; ++jj)
-                    for (int ii = 0; ii <= 1; ++ii) {
-                        const long c = cidx(wrapi(i - ii, n), wrapi(j - jj, n), wrapi(k - kk, n), n);
-                        val = val + ((sx[std::abs(ii - 1)] * sy[std::abs(jj - 1)]) * sz[std::abs(kk - 1)]) * g[d * nc + c];
-                    }
-            double u = a_prev * *v[d] + half_dt * val;
+            for (int t = 0; t < 8; ++t) val = std::fma(w[t], g[d * nc + cells[t]], val);
+            const double u = std::fma(a_prev, *v[d], half_dt * val);
             *v[d] = u * a_cur_inv;
         }
         if (do_move == 1) {
-            x[q] = x[q] + dt_a_cur_inv * vx[q];
-            y[q] = y[q] + dt_a_cur_inv * vy[q];
-            z[q] = z[q] + dt_a_cur_inv * vz[q];
+            x[q] = std::fma(dt_a_cur_inv, vx[q], x[q]);
+            y[q] = std::fma(dt_a_cur_inv, vy[q], y[q]);
+            z[q] = std::fma(dt_a_cur_inv, vz[q], z[q]);
         }
     }
 }

@@ -60,6 +60,7 @@ typedef struct nyxpm_params {
     int max_vcycles;        /* V-cycle limit per solve */
     int nu1, nu2;           /* red-black Gauss-Seidel sweeps before / after the coarse correction */
     int verbose;
+    int mixed_inner_vcycles;/* NYXPM_MIXED: FP32 V-cycles per FP64 defect-correction iteration */
 } nyxpm_params;
 
 typedef struct nyxpm_ctx nyxpm_ctx;

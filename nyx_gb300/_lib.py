@@ -46,6 +46,7 @@ class Params(C.Structure):
         ("nu1", C.c_int),
         ("nu2", C.c_int),
         ("verbose", C.c_int),
+        ("mixed_inner_vcycles", C.c_int),
     ]
 
 

@@ -71,7 +71,7 @@ nyxpm_status dalloc(Ctx& c, Box& b, T** p, size_t count)
 int bottom_edge(int n)
 {
     int m = n;
-    while (m % 2 == 0 && m > kMaxBottom) m /= 2;
+    while (m % 2 == 0 && m > kCoarsenAbove) m /= 2;
     return m;
 }
 
@@ -128,11 +128,13 @@ nyxpm_status do_deposit(Ctx& c, Box& b)
 nyxpm_status do_solve(Ctx& c, Box& b, double a, int zero_guess, nyxpm_solve_info* info)
 {
     nyxpm_status st;
-    if ((st = launch_make_rhs(c, b, a)) != NYXPM_OK) return st;
+    const bool mixed = b.prec == NYXPM_MIXED;
+    if ((st = mixed ? mixed_make_rhs(c, b, a) : launch_make_rhs(c, b, a)) != NYXPM_OK) return st;
     if (zero_guess && (st = launch_zero_phi(c, b)) != NYXPM_OK) return st;
-    nyxpm_status solved = b.prec == NYXPM_MIXED ? mixed_solve(c, b, info) : mg_solve(c, b, info);
+    nyxpm_status solved = mixed ? mixed_solve(c, b, info) : mg_solve(c, b, info);
     if (solved != NYXPM_OK && solved != NYXPM_NOT_CONVERGED) return solved;
-    if ((st = launch_grav_vector(c, b)) != NYXPM_OK) return st;
+    // the mixed solve leaves its FP32 gravity vector in g32 itself
+    if (!mixed && (st = launch_grav_vector(c, b)) != NYXPM_OK) return st;
     return solved;
 }
 
@@ -187,13 +189,16 @@ void nyxpm_default_params(nyxpm_params* p)
     p->nu1 = 2;
     p->nu2 = 2;
     p->verbose = 0;
+    p->mixed_inner_vcycles = 2;
 }
 
 nyxpm_status nyxpm_create(const nyxpm_params* p, nyxpm_ctx** out)
 {
     if (!p || !out) return NYXPM_INVALID_ARG;
     *out = nullptr;
-    if (p->nu1 < 0 || p->nu2 < 0 || p->max_vcycles < 1 || !(p->rel_tol > 0)) return NYXPM_INVALID_ARG;
+    if (p->nu1 < 0 || p->nu2 < 0 || p->max_vcycles < 1 || !(p->rel_tol > 0) ||
+        p->mixed_inner_vcycles < 1)
+        return NYXPM_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -250,10 +255,10 @@ size_t nyxpm_box_bytes(int n, int64_t np, nyxpm_precision prec)
     if (prec == NYXPM_MIXED) {
         // cell + 3 offsets + 3 vel + mass + id, double-buffered; key, perm; staging
         per_particle = 2.0 * (4 + 12 + 12 + 4 + 4) + 8 + 56;
-        per_cell = 4 + 4 + 4 + 8 + 24 + 16.0 * 8 / 7 + 8.0 * 8 / 7 + 8;
+        per_cell = 4 + 4 + 4 + 8 + 24 + 8 + 12 + 16.0 * 8 / 7 + 8.0 * 8 / 7;
     } else {
         per_particle = 2.0 * (7 * 8 + 4) + 8 + 56;
-        per_cell = 4 + 4 + 8 + 24 + 16.0 * 8 / 7;
+        per_cell = 4 + 4 + 8 + 24 + 8 + 16.0 * 8 / 7;
     }
     return (size_t)(per_particle * (double)np + per_cell * nc + 8.0 * n * n + (1 << 20));
 }
@@ -302,7 +307,7 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
         ALLOC(b->cell2, np); ALLOC(b->ox2, np); ALLOC(b->oy2, np); ALLOC(b->oz2, np);
         ALLOC(b->fvx2, np); ALLOC(b->fvy2, np); ALLOC(b->fvz2, np); ALLOC(b->fm2, np); ALLOC(b->id2, np);
         ALLOC(b->frho, nc);
-        ALLOC(b->resid, nc);
+        ALLOC(b->g32, 3 * nc);
     }
     ALLOC(b->key, np);
     ALLOC(b->perm, np);
@@ -348,12 +353,14 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
     }
     b->nb = nbot;
     ALLOC(b->G, (size_t)nbot * nbot * nbot);
+    ALLOC(b->Gf, (size_t)nbot * nbot * nbot);
 #undef ALLOC
-    {
-        std::vector<double> G((size_t)nbot * nbot * nbot);
-        bottom_green(nbot, L / nbot, G.data());
-        cudaMemcpyAsync(b->G, G.data(), sizeof(double) * G.size(), cudaMemcpyHostToDevice, c->stream);
-    }
+    std::vector<double> G((size_t)nbot * nbot * nbot);
+    std::vector<float> Gf(G.size());
+    bottom_green(nbot, L / nbot, G.data());
+    for (size_t t = 0; t < G.size(); ++t) Gf[t] = (float)G[t];
+    cudaMemcpyAsync(b->G, G.data(), sizeof(double) * G.size(), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(b->Gf, Gf.data(), sizeof(float) * Gf.size(), cudaMemcpyHostToDevice, c->stream);
     cudaMemsetAsync(b->cell_count, 0, sizeof(int) * nc, c->stream);
     for (const Level& l : b->levels) {
         const size_t cnt = (size_t)l.n * l.n * l.n;
@@ -473,6 +480,7 @@ nyxpm_status nyxpm_deposit(nyxpm_ctx* c, nyxpm_box* b, double* rho_out)
     TRY(do_deposit(*c, *b));
     if (rho_out) {
         const size_t nc = (size_t)b->n * b->n * b->n;
+        if (b->prec == NYXPM_MIXED) TRY(mixed_rho_to_double(*c, *b));
         cudaMemcpyAsync(rho_out, b->rho, sizeof(double) * nc, cudaMemcpyDeviceToHost, c->stream);
         TRY(check_launch(*c, "rho copy"));
         return nyxpm_synchronize(c);
@@ -508,6 +516,7 @@ nyxpm_status nyxpm_set_phi(nyxpm_ctx* c, nyxpm_box* b, const double* phi)
     TRY(check_launch(*c, "phi copy"));
     TRY(launch_phi_from_natural(*c, *b, b->nat));
     TRY(launch_grav_vector(*c, *b));
+    if (b->prec == NYXPM_MIXED) TRY(mixed_grav32(*c, *b));
     b->have_phi = 1;
     return nyxpm_synchronize(c);
 }
@@ -516,6 +525,7 @@ nyxpm_status nyxpm_grav_vector(nyxpm_ctx* c, nyxpm_box* b, double* g_out)
 {
     CHECK_BOX(c, b);
     if (!b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field: solve or set phi first");
+    if (b->prec == NYXPM_MIXED) TRY(launch_grav_vector(*c, *b));
     if (g_out) {
         const size_t nc = (size_t)b->n * b->n * b->n;
         cudaMemcpyAsync(g_out, b->g, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream);

@@ -22,7 +22,47 @@
 
 namespace nyxpm {
 
-constexpr int kMaxBottom = 8;          // coarsest grid edge solved exactly
+constexpr int kMaxBottom = 8;          // largest coarsest-grid edge (solved exactly)
+constexpr int kCoarsenAbove = 4;       // levels halve while the edge is even and above this
+
+// |v| as ordered bits: for non-negative doubles the bit patterns order like the
+// values and a NaN orders above every number, so max reductions run on the
+// integer pipe (FP64 compares would take FP64 issue slots)
+__host__ __device__ inline unsigned long long absbits(double v)
+{
+#ifdef __CUDA_ARCH__
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+#else
+    unsigned long long u;
+    __builtin_memcpy(&u, &v, sizeof(u));
+    return u & 0x7fffffffffffffffULL;
+#endif
+}
+
+// block max of bits into *out (blocks are whole warps)
+__device__ inline void block_umax_store(unsigned long long v, unsigned long long* out)
+{
+    __shared__ unsigned long long sm[32];
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, v, off);
+        v = o > v ? o : v;
+    }
+    const int lane = tid & 31, w = tid >> 5;
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (nthreads >> 5) ? sm[lane] : 0ULL;
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            const unsigned long long o = __shfl_down_sync(0xffffffffu, v, off);
+            v = o > v ? o : v;
+        }
+        if (lane == 0) atomicMax(out, v);
+    }
+}
 
 // One multigrid level.  The right-hand side is stored in smoother units,
 // beta = h^2 rhs / 6, so a Gauss-Seidel update is phi = s/6 - beta (s = sum of
@@ -147,7 +187,7 @@ struct Box {
     int* id2 = nullptr;
 
     // particles (mixed form): cell-relative FP32
-    int* cell = nullptr;               // linear cell of floor(x/dx)
+    int* cell = nullptr;               // cell of floor(x/dx), packed i | j << 10 | k << 20
     float *ox = nullptr, *oy = nullptr, *oz = nullptr;   // offset within the cell, [0,1)
     float *fvx = nullptr, *fvy = nullptr, *fvz = nullptr;
     float* fm = nullptr;
@@ -175,10 +215,12 @@ struct Box {
     double* scal = nullptr;            // [0] mean
     unsigned long long* norms = nullptr;   // [0] ||rhs||inf, [1] ||r||inf, [2] bad uploads
     unsigned long long* h_norms = nullptr; // pinned host mirror
-    double* G = nullptr;               // bottom Green's function
+    double* G = nullptr;               // bottom Green's function (smoother units)
+    float* Gf = nullptr;               // the same in FP32 (mixed inner V-cycles)
+    float* g32 = nullptr;              // mixed: 3 n^3 FP32 gravity vector for the kicks
+    double mscalar32_scale = 0;        // mixed: m / dx^3 applied to the FP32 deposit
     int nb = 0;
     std::vector<Level> levels;
-    double* resid = nullptr;           // mixed: FP64 outer residual scratch (n^3, natural)
 
     // host<->device staging: AoS pos (3 np), vel (3 np), mass (np) doubles
     double* staging = nullptr;
@@ -234,9 +276,14 @@ nyxpm_status mixed_deposit(Ctx& c, Box& b);
 nyxpm_status mixed_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move);
 nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info);
 
+nyxpm_status mixed_make_rhs(Ctx& c, Box& b, double a);
+nyxpm_status mixed_grav32(Ctx& c, Box& b);  // FP32 gravity vector of the FP64 phi
+nyxpm_status mixed_rho_to_double(Ctx& c, Box& b);
+
 // host-side helpers shared by the forms
-nyxpm_status scan_counts(Ctx& c, Box& b);   // cell_count -> cell_start
-nyxpm_status fix_segments(Ctx& c, Box& b);  // deterministic order inside each key segment
+nyxpm_status scan_counts(Ctx& c, Box& b);     // cell_count -> cell_start
+nyxpm_status fix_segments(Ctx& c, Box& b);    // deterministic order inside each key segment
+nyxpm_status sort_from_keys(Ctx& c, Box& b);  // key + cell_count -> perm (scan, scatter, fix)
 
 }  // namespace nyxpm
 

@@ -1,20 +1,881 @@
-// Mixed-precision form of the PM step (FP32 cell-relative particles, FP32
-// deposit and V-cycles inside FP64 defect correction).
+// Mixed-precision form of the PM step.
+//
+// Particles are stored cell-relative: the cell of floor(x/dx) packed as
+// i | j << 10 | k << 20 and the offset inside it as three FP32 values in [0, 1),
+// so a position keeps 24 bits relative to its cell anywhere in the box.
+// Velocities are FP32.  The deposit and the multigrid V-cycles run in FP32; the
+// solution phi, the right-hand side and the outer residual stay FP64 and the
+// FP32 V-cycles are used as the inner solver of an FP64 defect correction
+// (r = rhs - L phi in FP64; L e = r by FP32 V-cycles; phi += e in FP64) until
+// the FP64 residual meets the same relative tolerance as the FP64 form.  The
+// global mean density is a compensated FP64 sum; a(t) stays FP64 on the host.
+//
+// FP32 arithmetic is compiled with multiply-add contraction (the default): this
+// form is checked against the FP64 oracle by a stated tolerance, not bitwise.
 #include "pm_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
 
 namespace nyxpm {
 
-static nyxpm_status not_built(Ctx& c)
+namespace {
+
+constexpr int kThreads = 256;
+constexpr float kSixthF = 1.0f / 6.0f;
+constexpr double kSixth = 1.0 / 6.0;
+
+__constant__ float kProlongWF[8] = {0.421875f, 0.140625f, 0.140625f, 0.046875f,
+                                    0.140625f, 0.046875f, 0.046875f, 0.015625f};
+
+inline unsigned blocks_for(long long n, int t = kThreads)
 {
-    c.err = "mixed-precision form not available";
-    return NYXPM_INVALID_ARG;
+    long long b = (n + t - 1) / t;
+    return (unsigned)(b < 1 ? 1 : b);
 }
 
-nyxpm_status mixed_unpack(Ctx& c, Box&, const double*, const double*, const double*) { return not_built(c); }
-nyxpm_status mixed_pack(Ctx& c, Box&, double*, double*) { return not_built(c); }
-nyxpm_status mixed_sort(Ctx& c, Box&) { return not_built(c); }
-nyxpm_status mixed_deposit(Ctx& c, Box&) { return not_built(c); }
-nyxpm_status mixed_kick(Ctx& c, Box&, double, double, double, int) { return not_built(c); }
-nyxpm_status mixed_solve(Ctx& c, Box&, nyxpm_solve_info*) { return not_built(c); }
+__device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+__device__ __forceinline__ int pack_cell(int i, int j, int k) { return i | (j << 10) | (k << 20); }
+__device__ __forceinline__ int cell_i(int c) { return c & 1023; }
+__device__ __forceinline__ int cell_j(int c) { return (c >> 10) & 1023; }
+__device__ __forceinline__ int cell_k(int c) { return (c >> 20) & 1023; }
+
+// split x = (i + o) dx with i = floor(x/dx) wrapped, o in [0, 1)
+__device__ __forceinline__ void to_cell(double x, double dxi, int n, int* i, float* o)
+{
+    const double l = x * dxi;
+    double fl = floor(l);
+    float f = (float)(l - fl);
+    if (f >= 1.0f) {  // rounding up to 1 moves the particle to the next cell's origin
+        f = 0.0f;
+        fl += 1.0;
+    }
+    *i = wrapi((int)fl, n);
+    *o = f;
+}
+
+// deposit key along one axis and the CIC fraction: floor(o + 1/2) relative to the cell
+__device__ __forceinline__ int key_frac(int ci, float o, int n, float* f)
+{
+    if (o >= 0.5f) {
+        *f = o - 0.5f;
+        return ci + 1 == n ? 0 : ci + 1;
+    }
+    *f = o + 0.5f;
+    return ci;
+}
+
+// ---------------------------------------------------------------------------
+// upload / download
+// ---------------------------------------------------------------------------
+__global__ void k_mx_unpack(long long np, int n, double dxi, const double* __restrict__ pos,
+                            const double* __restrict__ vel, const double* __restrict__ mass,
+                            int* cell, float* ox, float* oy, float* oz, float* vx, float* vy,
+                            float* vz, float* m, int* id, unsigned long long* bad)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) ok = ok && isfinite(pos[3 * q + d]) && isfinite(vel[3 * q + d]);
+    if (!ok) {
+        atomicAdd(bad, 1ULL);
+        cell[q] = 0;
+        ox[q] = oy[q] = oz[q] = 0.f;
+        vx[q] = vy[q] = vz[q] = 0.f;
+        id[q] = (int)q;
+        return;
+    }
+    int i, j, k;
+    float a, b, c;
+    to_cell(pos[3 * q], dxi, n, &i, &a);
+    to_cell(pos[3 * q + 1], dxi, n, &j, &b);
+    to_cell(pos[3 * q + 2], dxi, n, &k, &c);
+    cell[q] = pack_cell(i, j, k);
+    ox[q] = a;
+    oy[q] = b;
+    oz[q] = c;
+    vx[q] = (float)vel[3 * q];
+    vy[q] = (float)vel[3 * q + 1];
+    vz[q] = (float)vel[3 * q + 2];
+    if (m) m[q] = (float)mass[q];
+    id[q] = (int)q;
+}
+
+__global__ void k_mx_pack(long long np, double dx, const int* __restrict__ cell,
+                          const float* __restrict__ ox, const float* __restrict__ oy,
+                          const float* __restrict__ oz, const float* __restrict__ vx,
+                          const float* __restrict__ vy, const float* __restrict__ vz,
+                          const int* __restrict__ id, double* pos, double* vel)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const int c = cell[q];
+    const long long o = 3LL * id[q];
+    pos[o] = ((double)cell_i(c) + (double)ox[q]) * dx;
+    pos[o + 1] = ((double)cell_j(c) + (double)oy[q]) * dx;
+    pos[o + 2] = ((double)cell_k(c) + (double)oz[q]) * dx;
+    vel[o] = vx[q];
+    vel[o + 1] = vy[q];
+    vel[o + 2] = vz[q];
+}
+
+// ---------------------------------------------------------------------------
+// sort
+// ---------------------------------------------------------------------------
+__global__ void k_mx_keys(long long np, int n, const int* __restrict__ cell,
+                          const float* __restrict__ ox, const float* __restrict__ oy,
+                          const float* __restrict__ oz, int* key, int* count)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const int c = cell[q];
+    float f;
+    const int i = key_frac(cell_i(c), ox[q], n, &f);
+    const int j = key_frac(cell_j(c), oy[q], n, &f);
+    const int k = key_frac(cell_k(c), oz[q], n, &f);
+    const int K = (int)cidx(i, j, k, n);
+    key[q] = K;
+    atomicAdd(count + K, 1);
+}
+
+__global__ void k_mx_gather(long long np, const int* __restrict__ perm, const int* __restrict__ cell,
+                            const float* __restrict__ ox, const float* __restrict__ oy,
+                            const float* __restrict__ oz, const float* __restrict__ vx,
+                            const float* __restrict__ vy, const float* __restrict__ vz,
+                            const float* __restrict__ m, const int* __restrict__ id, int* cell2,
+                            float* ox2, float* oy2, float* oz2, float* vx2, float* vy2, float* vz2,
+                            float* m2, int* id2)
+{
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= np) return;
+    const int q = perm[s];
+    cell2[s] = cell[q];
+    ox2[s] = ox[q];
+    oy2[s] = oy[q];
+    oz2[s] = oz[q];
+    vx2[s] = vx[q];
+    vy2[s] = vy[q];
+    vz2[s] = vz[q];
+    if (m) m2[s] = m[q];
+    id2[s] = id[q];
+}
+
+// ---------------------------------------------------------------------------
+// FP32 deposit (same tiling as the FP64 form: per-key partials in shared
+// memory, cells add their 8 key partials in a fixed order)
+// ---------------------------------------------------------------------------
+constexpr int kTx = 8, kTy = 8, kTz = 8;
+constexpr int kKx = kTx + 1, kKy = kTy + 1, kKz = kTz + 1;
+constexpr int kNKeys = kKx * kKy * kKz;
+
+__global__ void __launch_bounds__(256) k_mx_deposit(int n, float scale, const int* __restrict__ cell,
+                                                    const float* __restrict__ ox,
+                                                    const float* __restrict__ oy,
+                                                    const float* __restrict__ oz,
+                                                    const float* __restrict__ m,
+                                                    const int* __restrict__ start, float* rho)
+{
+    __shared__ float part[kNKeys * 8];
+    const int i0 = blockIdx.x * kTx, j0 = blockIdx.y * kTy, k0 = blockIdx.z * kTz;
+    for (int kl = threadIdx.x; kl < kNKeys; kl += blockDim.x) {
+        const int ki = kl % kKx, kj = (kl / kKx) % kKy, kk = kl / (kKx * kKy);
+        const long long K = cidx(wrapi(i0 + ki, n), wrapi(j0 + kj, n), wrapi(k0 + kk, n), n);
+        float s[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s[c] = 0.f;
+        const int e = start[K + 1];
+        for (int q = start[K]; q < e; ++q) {
+            const int c = cell[q];
+            float fx, fy, fz;
+            key_frac(cell_i(c), ox[q], n, &fx);
+            key_frac(cell_j(c), oy[q], n, &fy);
+            key_frac(cell_k(c), oz[q], n, &fz);
+            const float sx[2] = {1.f - fx, fx};
+            const float sy[2] = {1.f - fy, fy};
+            const float sz[2] = {1.f - fz, fz};
+            const float mq = m ? m[q] : 1.f;
+#pragma unroll
+            for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+                for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                    for (int cx = 0; cx < 2; ++cx)
+                        s[cx + 2 * cy + 4 * cz] += (sx[cx] * sy[cy]) * sz[cz] * mq;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
+    }
+    __syncthreads();
+    for (int cl = threadIdx.x; cl < kTx * kTy * kTz; cl += blockDim.x) {
+        const int ci = cl % kTx, cj = (cl / kTx) % kTy, ck = cl / (kTx * kTy);
+        const int i = i0 + ci, j = j0 + cj, k = k0 + ck;
+        if (i >= n || j >= n || k >= n) continue;
+        float acc = 0.f;
+#pragma unroll
+        for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+            for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+                for (int di = 0; di < 2; ++di) {
+                    const int kl = (ci + di) + kKx * ((cj + dj) + kKy * (ck + dk));
+                    acc += part[kl * 8 + (1 - di) + 2 * (1 - dj) + 4 * (1 - dk)];
+                }
+        rho[cidx(i, j, k, n)] = acc * scale;
+    }
+}
+
+__global__ void k_f2d(long long cnt, const float* __restrict__ a, double* b)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < cnt) b[t] = a[t];
+}
+
+// ---------------------------------------------------------------------------
+// compensated FP64 mean of (rho - mass_offset) and the FP64 right-hand side
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void kahan_add(double& s, double& c, double v)
+{
+    const double y = v - c;
+    const double t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// one warp per plane row: compensated lane sums, then the compensated totals of the lanes
+__global__ void k_mx_rowsum(int n, const float* __restrict__ rho, double mo, double* rows)
+{
+    const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= (long long)n * n) return;
+    const float* r = rho + row * n;
+    double s = 0.0, c = 0.0;
+    for (int i = lane; i < n; i += 32) kahan_add(s, c, (double)r[i] - mo);
+    s -= c;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const double t = __shfl_down_sync(0xffffffffu, s, off);
+        if (lane < off) s = s + t;
+    }
+    if (lane == 0) rows[row] = s;
+}
+
+__global__ void k_mx_mean(int n, double dx, double L, const double* __restrict__ rows, double* scal)
+{
+    // one block: compensated sum of the n^2 row sums
+    __shared__ double ss[32];
+    double s = 0.0, c = 0.0;
+    for (long long r = threadIdx.x; r < (long long)n * n; r += blockDim.x) kahan_add(s, c, rows[r]);
+    s -= c;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) ss[w] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0, tc = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) kahan_add(t, tc, ss[q]);
+        t -= tc;
+        scal[0] = (t * (dx * dx * dx)) / (L * L * L);
+    }
+}
+
+__global__ void k_mx_make_beta(int n, int split, const float* __restrict__ rho, double mo,
+                               const double* __restrict__ scal, double ggrav, double ainv, double k0,
+                               double* beta_r, double* beta_b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n || j >= n) return;
+    const double v = (double)rho[cidx(i, j, k, n)];
+    *lv_ptr<double>(beta_r, beta_b, n, split, i, j, k) = ((((v - mo) - scal[0]) * ggrav) * ainv) * k0;
+}
+
+// ---------------------------------------------------------------------------
+// norms (max over |v| bits on the integer pipe)
+// ---------------------------------------------------------------------------
+__global__ void k_mx_absmax(long long cnt, const double* __restrict__ a, unsigned long long* out)
+{
+    unsigned long long v = 0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < cnt;
+         t += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long u = absbits(a[t]);
+        v = u > v ? u : v;
+    }
+    block_umax_store(v, out);
+}
+
+// ---------------------------------------------------------------------------
+// outer FP64 residual -> FP32 inner right-hand side (+ its max norm)
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T nbr_sum_split(const T* other, int n, int half, int ih, int j, int k,
+                                           int q)
+{
+    const int ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
+    const int ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    const long long row = (long long)j + (long long)n * k;
+    T s = other[row * half + ihm] + other[row * half + ihp];
+    s = s + other[((long long)jm + (long long)n * k) * half + ih];
+    s = s + other[((long long)jp + (long long)n * k) * half + ih];
+    s = s + other[((long long)j + (long long)n * km) * half + ih];
+    s = s + other[((long long)j + (long long)n * kp) * half + ih];
+    return s;
+}
+
+// residual of both colours of a split level 0: r = beta - (s/6 - phi), one thread per (ih, j, k)
+__global__ void k_mx_resid(int n, const double* __restrict__ phi_r, const double* __restrict__ phi_b,
+                           const double* __restrict__ beta_r, const double* __restrict__ beta_b,
+                           float* r_r, float* r_b, unsigned long long* norm)
+{
+    const int half = n >> 1;
+    const int ih = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    unsigned long long v = 0;
+    if (ih < half && j < n) {
+        const long long t = ((long long)j + (long long)n * k) * half + ih;
+#pragma unroll
+        for (int color = 0; color < 2; ++color) {
+            const int q = (j + k + color) & 1;
+            const double* other = color ? phi_r : phi_b;
+            const double* mine = color ? phi_b : phi_r;
+            const double* beta = color ? beta_b : beta_r;
+            const double s = nbr_sum_split<double>(other, n, half, ih, j, k, q);
+            const double r = beta[t] - fma(s, kSixth, -mine[t]);
+            (color ? r_b : r_r)[t] = (float)r;
+            const unsigned long long u = absbits(r);
+            v = u > v ? u : v;
+        }
+    }
+    block_umax_store(v, norm);
+}
+
+// the same for a natural-layout level 0 (n <= 8)
+__global__ void k_mx_resid_nat(int n, const double* __restrict__ phi, const double* __restrict__ beta,
+                               float* r, unsigned long long* norm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    unsigned long long v = 0;
+    if (i < n && j < n) {
+        const int im = wrap1(i - 1, n), ip = wrap1(i + 1, n), jm = wrap1(j - 1, n), jp = wrap1(j + 1, n);
+        const int km = wrap1(k - 1, n), kp = wrap1(k + 1, n);
+        double s = phi[cidx(im, j, k, n)] + phi[cidx(ip, j, k, n)];
+        s = s + phi[cidx(i, jm, k, n)];
+        s = s + phi[cidx(i, jp, k, n)];
+        s = s + phi[cidx(i, j, km, n)];
+        s = s + phi[cidx(i, j, kp, n)];
+        const long long c = cidx(i, j, k, n);
+        const double rr = beta[c] - fma(s, kSixth, -phi[c]);
+        r[c] = (float)rr;
+        v = absbits(rr);
+    }
+    block_umax_store(v, norm);
+}
+
+// phi += e (FP64 update with the FP32 correction)
+__global__ void k_mx_update(long long cnt, double* phi, const float* __restrict__ e)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < cnt) phi[t] = phi[t] + (double)e[t];
+}
+
+// ---------------------------------------------------------------------------
+// FP32 V-cycle kernels (smoother units, same structure as the FP64 form)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_gsrb_f(int n, int color, float* __restrict__ mine,
+                                                const float* __restrict__ other,
+                                                const float* __restrict__ beta)
+{
+    const int half = n >> 1;
+    const int ih = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (ih >= half || j >= n) return;
+    const int q = (j + k + color) & 1;
+    const long long t = ((long long)j + (long long)n * k) * half + ih;
+    const float s = nbr_sum_split<float>(other, n, half, ih, j, k, q);
+    mine[t] = fmaf(s, kSixthF, -beta[t]);
+}
+
+__device__ __forceinline__ float resid_f(const LevelViewF& L, int i, int j, int k)
+{
+    const int n = L.n;
+    const int im = i == 0 ? n - 1 : i - 1, ip = i == n - 1 ? 0 : i + 1;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    float s = *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, im, j, k) +
+              *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, ip, j, k);
+    s += *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, jm, k);
+    s += *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, jp, k);
+    s += *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, j, km);
+    s += *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, j, kp);
+    const float c = *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, j, k);
+    return *lv_ptr<float>(L.beta_r, L.beta_b, n, L.split, i, j, k) - fmaf(s, kSixthF, -c);
+}
+
+__global__ void k_restrict_f(LevelViewF F, LevelViewF Cv)
+{
+    const int nc = Cv.n;
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z;
+    if (I >= nc || J >= nc) return;
+    float s = 0.f;
+#pragma unroll
+    for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+            for (int di = 0; di < 2; ++di) s += resid_f(F, 2 * I + di, 2 * J + dj, 2 * K + dk);
+    *lv_ptr<float>(Cv.beta_r, Cv.beta_b, nc, Cv.split, I, J, K) = s * 0.5f;
+    *lv_ptr<float>(Cv.phi_r, Cv.phi_b, nc, Cv.split, I, J, K) = 0.f;
+}
+
+__global__ void k_prolong_f(LevelViewF Cv, LevelViewF F)
+{
+    const int n = F.n, nc = Cv.n, half = n >> 1;
+    const int ih = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (ih >= half || j >= n) return;
+    const int J = j >> 1, K = k >> 1;
+    const int Js[2] = {J, wrap1((j & 1) ? J + 1 : J - 1, nc)};
+    const int Ks[2] = {K, wrap1((k & 1) ? K + 1 : K - 1, nc)};
+    const long long t = ((long long)j + (long long)n * k) * half + ih;
+#pragma unroll
+    for (int odd = 0; odd < 2; ++odd) {
+        const int i = 2 * ih + odd;
+        const int Is[2] = {ih, wrap1(odd ? ih + 1 : ih - 1, nc)};
+        float s = 0.f;
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int tt = 0; tt < 2; ++tt)
+                    s = fmaf(kProlongWF[tt + 2 * a + 4 * b],
+                             *lv_ptr<const float>(Cv.phi_r, Cv.phi_b, nc, Cv.split, Is[tt], Js[a], Ks[b]), s);
+        float* p = (((i + j + k) & 1) ? F.phi_b : F.phi_r) + t;
+        *p += s;
+    }
+}
+
+__global__ void k_bottom_f(int nb, const float* __restrict__ G, const float* __restrict__ beta, float* phi)
+{
+    __shared__ float r[kMaxBottom * kMaxBottom * kMaxBottom];
+    __shared__ float g[kMaxBottom * kMaxBottom * kMaxBottom];
+    const int nc = nb * nb * nb;
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) {
+        r[t] = beta[t];
+        g[t] = G[t];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const int i = c % nb, j = (c / nb) % nb, k = c / (nb * nb);
+        float s = 0.f;
+        int y = 0;
+        for (int yk = 0; yk < nb; ++yk) {
+            const int dk = wrap1(k - yk, nb) * nb * nb;
+            for (int yj = 0; yj < nb; ++yj) {
+                const int djk = dk + wrap1(j - yj, nb) * nb;
+                for (int yi = 0; yi < nb; ++yi, ++y) s = fmaf(g[djk + wrap1(i - yi, nb)], r[y], s);
+            }
+        }
+        phi[c] = s;
+    }
+}
+
+// FP32 gravity vector from the FP64 phi: the difference in FP64, the scaling in FP32
+// (component-major, 3 n^3)
+__global__ void k_mx_grav(LevelView L, float half_dxi, float* g)
+{
+    const int n = L.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n || j >= n) return;
+    const long long nc = (long long)n * n * n;
+    const long long c = cidx(i, j, k, n);
+    auto P = [&](int a, int b, int d) {
+        return *lv_ptr<const double>(L.phi_r, L.phi_b, n, L.split, a, b, d);
+    };
+    const int im = i == 0 ? n - 1 : i - 1, ip = i == n - 1 ? 0 : i + 1;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    g[c] = (float)(P(ip, j, k) - P(im, j, k)) * half_dxi;
+    g[nc + c] = (float)(P(i, jp, k) - P(i, jm, k)) * half_dxi;
+    g[2 * nc + c] = (float)(P(i, j, kp) - P(i, j, km)) * half_dxi;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 CIC interpolation + kick (+ drift in cell units with re-binning)
+// ---------------------------------------------------------------------------
+struct MxKickArgs {
+    int n;
+    const float* g;
+    float half_dt, a_prev, a_cur_inv, drift;  // drift = dt / a_cur / dx (cell units)
+    int do_move;
+};
+
+__global__ void __launch_bounds__(256) k_mx_kick(long long np, MxKickArgs A, int* cell, float* ox,
+                                                 float* oy, float* oz, float* vx, float* vy, float* vz)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const int n = A.n;
+    const long long nc = (long long)n * n * n;
+    const int c = cell[q];
+    int ci = cell_i(c), cj = cell_j(c), ck = cell_k(c);
+    float o[3] = {ox[q], oy[q], oz[q]};
+    float fx, fy, fz;
+    const int i = key_frac(ci, o[0], n, &fx);
+    const int j = key_frac(cj, o[1], n, &fy);
+    const int k = key_frac(ck, o[2], n, &fz);
+    const float sx[2] = {1.f - fx, fx};
+    const float sy[2] = {1.f - fy, fy};
+    const float sz[2] = {1.f - fz, fz};
+    float w[8];
+    long long cc[8];
+#pragma unroll
+    for (int kk = 0; kk <= 1; ++kk)
+#pragma unroll
+        for (int jj = 0; jj <= 1; ++jj)
+#pragma unroll
+            for (int ii = 0; ii <= 1; ++ii) {
+                const int t = ii + 2 * jj + 4 * kk;
+                w[t] = (sx[1 - ii] * sy[1 - jj]) * sz[1 - kk];
+                cc[t] = cidx(wrap1(i - ii, n), wrap1(j - jj, n), wrap1(k - kk, n), n);
+            }
+    float v[3] = {vx[q], vy[q], vz[q]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float* gd = A.g + d * nc;
+        float val = 0.f;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) val = fmaf(w[t], __ldg(gd + cc[t]), val);
+        v[d] = fmaf(A.a_prev, v[d], A.half_dt * val) * A.a_cur_inv;
+    }
+    vx[q] = v[0];
+    vy[q] = v[1];
+    vz[q] = v[2];
+    if (A.do_move) {
+        int ic[3] = {ci, cj, ck};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            float p = fmaf(A.drift, v[d], o[d]);
+            const float fl = floorf(p);
+            p -= fl;
+            if (p >= 1.f) p = 0.f;  // -tiny + 1 rounding up
+            int idx = ic[d] + (int)fl;
+            idx %= n;
+            if (idx < 0) idx += n;
+            ic[d] = idx;
+            o[d] = p;
+        }
+        cell[q] = pack_cell(ic[0], ic[1], ic[2]);
+        ox[q] = o[0];
+        oy[q] = o[1];
+        oz[q] = o[2];
+    }
+}
+
+inline unsigned norm_blocks(Ctx& c, long long cnt)
+{
+    long long b = (cnt + kThreads - 1) / kThreads;
+    long long cap = (long long)c.sm_count * 8;
+    return (unsigned)std::max<long long>(1, std::min(b, cap));
+}
+
+double read_norm(Box& b, int slot)
+{
+    double v;
+    std::memcpy(&v, &b.h_norms[slot], sizeof(v));
+    return v;
+}
+
+nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine)
+{
+    const long long half_cells = (long long)l.n * l.n * l.n / 2;
+    const Geo g = geo3(l.n / 2, l.n, l.n);
+    for (int color = 0; color < 2; ++color) {
+        prof_begin(c);
+        k_gsrb_f<<<g.grid, g.block, 0, c.stream>>>(l.n, color, color ? l.fphi_b : l.fphi_r,
+                                                  color ? l.fphi_r : l.fphi_b,
+                                                  color ? l.fbeta_b : l.fbeta_r);
+        prof_end(c, NYXPM_ST_SMOOTH, 12.0 * half_cells, fine);
+    }
+    return check_launch(c, "gsrb f32");
+}
+
+nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li)
+{
+    nyxpm_status st;
+    const Level& f = b.levels[li];
+    if (li + 1 == b.levels.size()) {
+        prof_begin(c);
+        k_bottom_f<<<1, 512, 0, c.stream>>>(b.nb, b.Gf, f.fbeta_r, f.fphi_r);
+        prof_end(c, NYXPM_ST_BOTTOM, 8.0 * f.n * f.n * f.n);
+        return check_launch(c, "bottom f32");
+    }
+    for (int s = 0; s < c.p.nu1; ++s)
+        if ((st = gsrb_sweep_f(c, f, li == 0)) != NYXPM_OK) return st;
+    const Level& cl = b.levels[li + 1];
+    const long long ncc = (long long)cl.n * cl.n * cl.n;
+    const long long ncf = (long long)f.n * f.n * f.n;
+    {
+        const Geo g = geo3(cl.n, cl.n, cl.n);
+        prof_begin(c);
+        k_restrict_f<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+        prof_end(c, NYXPM_ST_RESTRICT, 8.0 * ncf + 8.0 * ncc);
+    }
+    if ((st = check_launch(c, "restrict f32")) != NYXPM_OK) return st;
+    if ((st = vcycle_f(c, b, li + 1)) != NYXPM_OK) return st;
+    {
+        const Geo g = geo3(f.n / 2, f.n, f.n);
+        prof_begin(c);
+        k_prolong_f<<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+        prof_end(c, NYXPM_ST_PROLONG, 8.0 * ncf + 4.0 * ncc);
+    }
+    if ((st = check_launch(c, "prolong f32")) != NYXPM_OK) return st;
+    for (int s = 0; s < c.p.nu2; ++s)
+        if ((st = gsrb_sweep_f(c, f, li == 0)) != NYXPM_OK) return st;
+    return NYXPM_OK;
+}
+
+// FP64 residual of level 0 into the FP32 inner right-hand side, its norm into norms[1]
+nyxpm_status launch_mx_resid(Ctx& c, Box& b)
+{
+    const Level& l = b.levels[0];
+    const long long nc = (long long)l.n * l.n * l.n;
+    prof_begin(c);
+    cudaMemsetAsync(b.norms + 1, 0, sizeof(unsigned long long), c.stream);
+    if (l.split) {
+        const Geo g = geo3(l.n / 2, l.n, l.n);
+        k_mx_resid<<<g.grid, g.block, 0, c.stream>>>(l.n, l.phi_r, l.phi_b, l.beta_r, l.beta_b,
+                                                     l.fbeta_r, l.fbeta_b, b.norms + 1);
+    } else {
+        const Geo g = geo3(l.n, l.n, l.n);
+        k_mx_resid_nat<<<g.grid, g.block, 0, c.stream>>>(l.n, l.phi_r, l.beta_r, l.fbeta_r,
+                                                         b.norms + 1);
+    }
+    prof_end(c, NYXPM_ST_NORM, 20.0 * nc);
+    return check_launch(c, "mixed residual");
+}
+
+nyxpm_status launch_mx_update(Ctx& c, Box& b)
+{
+    const Level& l = b.levels[0];
+    const long long nc = (long long)l.n * l.n * l.n;
+    prof_begin(c);
+    if (l.split) {
+        k_mx_update<<<blocks_for(nc / 2), kThreads, 0, c.stream>>>(nc / 2, l.phi_r, l.fphi_r);
+        k_mx_update<<<blocks_for(nc / 2), kThreads, 0, c.stream>>>(nc / 2, l.phi_b, l.fphi_b);
+        c.launches += 1;
+    } else {
+        k_mx_update<<<blocks_for(nc), kThreads, 0, c.stream>>>(nc, l.phi_r, l.fphi_r);
+    }
+    prof_end(c, NYXPM_ST_PROLONG, 20.0 * nc);
+    return check_launch(c, "mixed update");
+}
+
+}  // namespace
+
+nyxpm_status mixed_unpack(Ctx& c, Box& b, const double* d_pos, const double* d_vel,
+                          const double* d_mass)
+{
+    prof_begin(c);
+    k_mx_unpack<<<blocks_for(b.np), kThreads, 0, c.stream>>>(
+        b.np, b.n, b.dxi, d_pos, d_vel, d_mass, b.cell, b.ox, b.oy, b.oz, b.fvx, b.fvy, b.fvz,
+        d_mass ? b.fm : nullptr, b.id, b.norms + 2);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "mixed unpack");
+}
+
+nyxpm_status mixed_pack(Ctx& c, Box& b, double* d_pos, double* d_vel)
+{
+    prof_begin(c);
+    k_mx_pack<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.dx, b.cell, b.ox, b.oy, b.oz,
+                                                            b.fvx, b.fvy, b.fvz, b.id, d_pos, d_vel);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "mixed pack");
+}
+
+nyxpm_status mixed_sort(Ctx& c, Box& b)
+{
+    nyxpm_status st;
+    cudaMemsetAsync(b.cell_count, 0, sizeof(int) * (size_t)b.n * b.n * b.n, c.stream);
+    prof_begin(c);
+    k_mx_keys<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.n, b.cell, b.ox, b.oy, b.oz,
+                                                            b.key, b.cell_count);
+    prof_end(c, NYXPM_ST_KEYS, 20.0 * b.np);
+    if ((st = check_launch(c, "mixed keys")) != NYXPM_OK) return st;
+    if ((st = sort_from_keys(c, b)) != NYXPM_OK) return st;
+    const bool pm = !b.uniform_mass;
+    prof_begin(c);
+    k_mx_gather<<<blocks_for(b.np), kThreads, 0, c.stream>>>(
+        b.np, b.perm, b.cell, b.ox, b.oy, b.oz, b.fvx, b.fvy, b.fvz, pm ? b.fm : nullptr, b.id,
+        b.cell2, b.ox2, b.oy2, b.oz2, b.fvx2, b.fvy2, b.fvz2, pm ? b.fm2 : nullptr, b.id2);
+    prof_end(c, NYXPM_ST_GATHER, (pm ? 76.0 : 68.0) * b.np);
+    if ((st = check_launch(c, "mixed gather")) != NYXPM_OK) return st;
+    std::swap(b.cell, b.cell2);
+    std::swap(b.ox, b.ox2);
+    std::swap(b.oy, b.oy2);
+    std::swap(b.oz, b.oz2);
+    std::swap(b.fvx, b.fvx2);
+    std::swap(b.fvy, b.fvy2);
+    std::swap(b.fvz, b.fvz2);
+    std::swap(b.fm, b.fm2);
+    std::swap(b.id, b.id2);
+    b.sorted = 1;
+    return NYXPM_OK;
+}
+
+nyxpm_status mixed_deposit(Ctx& c, Box& b)
+{
+    const int n = b.n;
+    dim3 grid((n + kTx - 1) / kTx, (n + kTy - 1) / kTy, (n + kTz - 1) / kTz);
+    const double dx = b.L / n;
+    const double inv_vol = 1.0 / (dx * dx * dx);
+    const float scale = (float)(b.uniform_mass ? b.mscalar * inv_vol : inv_vol);
+    const double nc = (double)n * n * n;
+    prof_begin(c);
+    k_mx_deposit<<<grid, 256, 0, c.stream>>>(n, scale, b.cell, b.ox, b.oy, b.oz,
+                                             b.uniform_mass ? nullptr : b.fm, b.cell_start, b.frho);
+    prof_end(c, NYXPM_ST_DEPOSIT, (b.uniform_mass ? 16.0 : 20.0) * b.np + 8.0 * nc);
+    return check_launch(c, "mixed deposit");
+}
+
+nyxpm_status mixed_rho_to_double(Ctx& c, Box& b)
+{
+    const long long nc = (long long)b.n * b.n * b.n;
+    k_f2d<<<blocks_for(nc), kThreads, 0, c.stream>>>(nc, b.frho, b.rho);
+    c.launches += 1;
+    return check_launch(c, "rho to double");
+}
+
+nyxpm_status mixed_make_rhs(Ctx& c, Box& b, double a)
+{
+    const int n = b.n;
+    const long long nc = (long long)n * n * n;
+    const Level& l0 = b.levels[0];
+    const double dx = b.L / n;
+    const Geo g = geo3(n, n, n);
+    prof_begin(c);
+    k_mx_rowsum<<<blocks_for((long long)n * n * 32), kThreads, 0, c.stream>>>(n, b.frho,
+                                                                             b.mass_offset, b.rows);
+    k_mx_mean<<<1, 1024, 0, c.stream>>>(n, dx, b.L, b.rows, b.scal);
+    k_mx_make_beta<<<g.grid, g.block, 0, c.stream>>>(n, l0.split, b.frho, b.mass_offset, b.scal,
+                                                     -4.0 * M_PI * c.p.gconst, 1.0 / a,
+                                                     beta_scale(b), l0.beta_r, l0.beta_b);
+    prof_end(c, NYXPM_ST_RHS, 20.0 * nc);
+    c.launches += 2;
+    return check_launch(c, "mixed rhs");
+}
+
+nyxpm_status mixed_grav32(Ctx& c, Box& b)
+{
+    const long long nc = (long long)b.n * b.n * b.n;
+    const Geo g = geo3(b.n, b.n, b.n);
+    prof_begin(c);
+    k_mx_grav<<<g.grid, g.block, 0, c.stream>>>(view(b.levels[0]), (float)(0.5 * b.dxi), b.g32);
+    prof_end(c, NYXPM_ST_KICK, 20.0 * nc);
+    return check_launch(c, "mixed grav");
+}
+
+nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
+{
+    nyxpm_status st;
+    const Level& l0 = b.levels[0];
+    const long long nc = (long long)l0.n * l0.n * l0.n;
+    prof_begin(c);
+    cudaMemsetAsync(b.norms, 0, sizeof(unsigned long long), c.stream);
+    if (l0.split) {
+        k_mx_absmax<<<norm_blocks(c, nc / 2), kThreads, 0, c.stream>>>(nc / 2, l0.beta_r, b.norms);
+        k_mx_absmax<<<norm_blocks(c, nc / 2), kThreads, 0, c.stream>>>(nc / 2, l0.beta_b, b.norms);
+        c.launches += 1;
+    } else {
+        k_mx_absmax<<<norm_blocks(c, nc), kThreads, 0, c.stream>>>(nc, l0.beta_r, b.norms);
+    }
+    prof_end(c, NYXPM_ST_NORM, 8.0 * nc);
+    if ((st = check_launch(c, "mixed rhs norm")) != NYXPM_OK) return st;
+    if ((st = launch_mx_resid(c, b)) != NYXPM_OK) return st;
+    cudaMemcpyAsync(b.h_norms, b.norms, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                    c.stream);
+    if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "mixed sync");
+    const double bnorm = read_norm(b, 0);
+    const double r0 = read_norm(b, 1);
+    const double target = c.p.rel_tol * std::max(bnorm, r0);
+    double r = r0;
+    int it = 0, inner = 0;
+    nyxpm_status result = NYXPM_OK;
+    const size_t half_bytes = (size_t)nc / 2 * sizeof(float);
+    if (!(r0 <= target)) {
+        for (it = 1; it <= c.p.max_vcycles; ++it) {
+            // inner FP32 solve of L e = r from e = 0
+            if (l0.split) {
+                cudaMemsetAsync(l0.fphi_r, 0, half_bytes, c.stream);
+                cudaMemsetAsync(l0.fphi_b, 0, half_bytes, c.stream);
+            } else {
+                cudaMemsetAsync(l0.fphi_r, 0, (size_t)nc * sizeof(float), c.stream);
+            }
+            for (int v = 0; v < c.p.mixed_inner_vcycles; ++v, ++inner)
+                if ((st = vcycle_f(c, b, 0)) != NYXPM_OK) return st;
+            if ((st = launch_mx_update(c, b)) != NYXPM_OK) return st;
+            if ((st = launch_mx_resid(c, b)) != NYXPM_OK) return st;
+            cudaMemcpyAsync(b.h_norms + 1, b.norms + 1, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, c.stream);
+            if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "mixed sync");
+            r = read_norm(b, 1);
+            if (r != r) {
+                c.err = "mixed defect correction residual is NaN";
+                return NYXPM_NOT_CONVERGED;
+            }
+            if (r <= target) break;
+        }
+        if (it > c.p.max_vcycles) {
+            it = c.p.max_vcycles;
+            result = NYXPM_NOT_CONVERGED;
+            c.err = "defect correction reached max_vcycles above tolerance";
+        }
+    }
+    b.have_phi = 1;
+    if ((st = mixed_grav32(c, b)) != NYXPM_OK) return st;
+    if (info) {
+        const double inv_k0 = 1.0 / beta_scale(b);
+        info->vcycles = it;
+        info->inner_vcycles = inner;
+        info->resnorm0 = r0 * inv_k0;
+        info->resnorm = r * inv_k0;
+        info->bnorm = bnorm * inv_k0;
+    }
+    return result;
+}
+
+nyxpm_status mixed_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move)
+{
+    MxKickArgs A;
+    A.n = b.n;
+    A.g = b.g32;
+    A.half_dt = (float)(0.5 * dt);
+    A.a_prev = (float)a_prev;
+    A.a_cur_inv = (float)(1.0 / a_cur);
+    A.drift = (float)(dt / a_cur * b.dxi);
+    A.do_move = do_move;
+    prof_begin(c);
+    k_mx_kick<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, A, b.cell, b.ox, b.oy, b.oz, b.fvx,
+                                                            b.fvy, b.fvz);
+    const double nc = (double)b.n * b.n * b.n;
+    prof_end(c, NYXPM_ST_KICK, (do_move ? 56.0 : 40.0) * b.np + 12.0 * nc);
+    if (do_move) b.sorted = 0;
+    return check_launch(c, "mixed kick");
+}
 
 }  // namespace nyxpm

@@ -90,37 +90,15 @@ __global__ void k_make_beta(int n, int split, const double* __restrict__ rho, do
 // ---------------------------------------------------------------------------
 // norms (max is order independent; non-negative doubles compare as their bits)
 // ---------------------------------------------------------------------------
-// max that keeps a NaN (so a diverged solve is seen by the host)
-__device__ __forceinline__ double nanmax(double a, double b)
-{
-    return (a != a) ? a : ((b != b) ? b : (a > b ? a : b));
-}
-
-__device__ __forceinline__ void block_max_store(double v, unsigned long long* out)
-{
-    __shared__ double sm[32];
-    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, off));
-    const int lane = tid & 31, w = tid >> 5;
-    if (lane == 0) sm[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        v = lane < (nthreads >> 5) ? sm[lane] : 0.0;
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) v = nanmax(v, __shfl_down_sync(0xffffffffu, v, off));
-        if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
-    }
-}
-
 __global__ void k_absmax(long long cnt, const double* __restrict__ a, unsigned long long* out)
 {
-    double v = 0.0;
+    unsigned long long v = 0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < cnt;
-         t += (long long)gridDim.x * blockDim.x)
-        v = nanmax(v, fabs(a[t]));
-    block_max_store(v, out);
+         t += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long u = absbits(a[t]);
+        v = u > v ? u : v;
+    }
+    block_umax_store(v, out);
 }
 
 // neighbour sum in the oracle's order: x-, x+, y-, y+, z-, z+
@@ -155,12 +133,40 @@ __global__ void k_resnorm_split(LevelView L, unsigned long long* out)
     const int ih = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
-    double v = 0.0;
+    unsigned long long v = 0;
     if (ih < half && j < L.n) {
-        v = nanmax(v, fabs(resid_at(L, 2 * ih, j, k)));
-        v = nanmax(v, fabs(resid_at(L, 2 * ih + 1, j, k)));
+        const unsigned long long a = absbits(resid_at(L, 2 * ih, j, k));
+        const unsigned long long b = absbits(resid_at(L, 2 * ih + 1, j, k));
+        v = a > b ? a : b;
     }
-    block_max_store(v, out);
+    block_umax_store(v, out);
+}
+
+// the same over the red cells only: one thread per red cell of the split level
+__global__ void k_resnorm_red(int n, const double* __restrict__ phi_r, const double* __restrict__ phi_b,
+                              const double* __restrict__ beta_r, unsigned long long* out)
+{
+    const int half = n >> 1;
+    const int ih = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    unsigned long long v = 0;
+    if (ih < half && j < n) {
+        const int q = (j + k) & 1;  // the red cell of this pair is i = 2*ih + q
+        const int ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
+        const int ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
+        const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        const long long row = (long long)j + (long long)n * k;
+        const long long t = row * half + ih;
+        double s = phi_b[row * half + ihm] + phi_b[row * half + ihp];
+        s = s + phi_b[((long long)jm + (long long)n * k) * half + ih];
+        s = s + phi_b[((long long)jp + (long long)n * k) * half + ih];
+        s = s + phi_b[((long long)j + (long long)n * km) * half + ih];
+        s = s + phi_b[((long long)j + (long long)n * kp) * half + ih];
+        v = absbits(beta_r[t] - fma(s, kSixth, -phi_r[t]));
+    }
+    block_umax_store(v, out);
 }
 
 __global__ void k_resnorm_nat(LevelView L, unsigned long long* out)
@@ -168,9 +174,9 @@ __global__ void k_resnorm_nat(LevelView L, unsigned long long* out)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
-    double v = 0.0;
-    if (i < L.n && j < L.n) v = fabs(resid_at(L, i, j, k));
-    block_max_store(v, out);
+    unsigned long long v = 0;
+    if (i < L.n && j < L.n) v = absbits(resid_at(L, i, j, k));
+    block_umax_store(v, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -380,21 +386,25 @@ nyxpm_status vcycle(Ctx& c, Box& b, size_t li)
     return NYXPM_OK;
 }
 
-// launch ||r_beta||_inf of level 0 into norms[slot]
-nyxpm_status launch_resnorm(Ctx& c, Box& b, int slot)
+// launch ||r_beta||_inf of level 0 into norms[slot]: all cells, or the red
+// cells only after a cycle that ended with a black half sweep
+nyxpm_status launch_resnorm(Ctx& c, Box& b, int slot, int red_only)
 {
     const Level& l = b.levels[0];
     const long long nc = (long long)l.n * l.n * l.n;
     prof_begin(c);
     cudaMemsetAsync(b.norms + slot, 0, sizeof(unsigned long long), c.stream);
-    if (l.split) {
+    if (l.split && red_only) {
+        const Geo g = geo3(l.n / 2, l.n, l.n);
+        k_resnorm_red<<<g.grid, g.block, 0, c.stream>>>(l.n, l.phi_r, l.phi_b, l.beta_r, b.norms + slot);
+    } else if (l.split) {
         const Geo g = geo3(l.n / 2, l.n, l.n);
         k_resnorm_split<<<g.grid, g.block, 0, c.stream>>>(view(l), b.norms + slot);
     } else {
         const Geo g = geo3(l.n, l.n, l.n);
         k_resnorm_nat<<<g.grid, g.block, 0, c.stream>>>(view(l), b.norms + slot);
     }
-    prof_end(c, NYXPM_ST_NORM, 16.0 * nc);
+    prof_end(c, NYXPM_ST_NORM, (red_only ? 12.0 : 16.0) * nc);
     return check_launch(c, "resnorm");
 }
 
@@ -463,7 +473,7 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
     }
     prof_end(c, NYXPM_ST_NORM, 8.0 * nc);
     if ((st = check_launch(c, "rhs norm")) != NYXPM_OK) return st;
-    if ((st = launch_resnorm(c, b, 1)) != NYXPM_OK) return st;
+    if ((st = launch_resnorm(c, b, 1, 0)) != NYXPM_OK) return st;
     cudaMemcpyAsync(b.h_norms, b.norms, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                     c.stream);
     if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "solve sync");
@@ -473,10 +483,11 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
     double r = r0;
     int it = 0;
     nyxpm_status result = NYXPM_OK;
+    const int red_only = (c.p.nu2 > 0 && b.levels.size() > 1) ? 1 : 0;
     if (!(r0 <= target)) {
         for (it = 1; it <= c.p.max_vcycles; ++it) {
             if ((st = vcycle(c, b, 0)) != NYXPM_OK) return st;
-            if ((st = launch_resnorm(c, b, 1)) != NYXPM_OK) return st;
+            if ((st = launch_resnorm(c, b, 1, red_only)) != NYXPM_OK) return st;
             cudaMemcpyAsync(b.h_norms + 1, b.norms + 1, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, c.stream);
             if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "solve sync");

@@ -498,6 +498,18 @@ nyxpm_status fix_segments(Ctx& c, Box& b)
     return check_launch(c, "fix segments");
 }
 
+nyxpm_status sort_from_keys(Ctx& c, Box& b)
+{
+    nyxpm_status st;
+    if ((st = scan_counts(c, b)) != NYXPM_OK) return st;
+    prof_begin(c);
+    k_scatter<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.key, b.cell_start, b.cell_count,
+                                                            b.perm);
+    prof_end(c, NYXPM_ST_SCATTER, 12.0 * b.np);
+    if ((st = check_launch(c, "scatter")) != NYXPM_OK) return st;
+    return fix_segments(c, b);
+}
+
 nyxpm_status launch_sort(Ctx& c, Box& b)
 {
     nyxpm_status st;
@@ -508,13 +520,7 @@ nyxpm_status launch_sort(Ctx& c, Box& b)
                                                          b.cell_count);
     prof_end(c, NYXPM_ST_KEYS, 32.0 * b.np);
     if ((st = check_launch(c, "keys")) != NYXPM_OK) return st;
-    if ((st = scan_counts(c, b)) != NYXPM_OK) return st;
-    prof_begin(c);
-    k_scatter<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.key, b.cell_start, b.cell_count,
-                                                            b.perm);
-    prof_end(c, NYXPM_ST_SCATTER, 12.0 * b.np);
-    if ((st = check_launch(c, "scatter")) != NYXPM_OK) return st;
-    if ((st = fix_segments(c, b)) != NYXPM_OK) return st;
+    if ((st = sort_from_keys(c, b)) != NYXPM_OK) return st;
     const int nvals = b.uniform_mass ? 6 : 7;
     prof_begin(c);
     k_gather<<<blocks_for(b.np), kThreads, 0, c.stream>>>(

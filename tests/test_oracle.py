@@ -115,7 +115,7 @@ def test_multigrid_odd_bottom_and_small_grids():
         assert st == 0, n
         assert r <= 1e-11 * max(np.abs(rhs).max(), r0) * (1 + 1e-12), n
     assert O.mg_levels(9) == 0 and O.mg_levels(18) == 0 and O.mg_levels(20) == 3
-    assert O.mg_levels(256) == 6 and O.mg_levels(48) == 4
+    assert O.mg_levels(256) == 7 and O.mg_levels(48) == 5
 
 
 def test_two_particle_attraction_sign():

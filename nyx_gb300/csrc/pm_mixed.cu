@@ -571,9 +571,12 @@ __global__ void __launch_bounds__(256) k_mx_kick(long long np, MxKickArgs A, int
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             float p = fmaf(A.drift, v[d], o[d]);
-            const float fl = floorf(p);
+            float fl = floorf(p);
             p -= fl;
-            if (p >= 1.f) p = 0.f;  // -tiny + 1 rounding up
+            if (p >= 1.f) {  // -tiny + 1 rounded up to 1: the particle sits at the next cell's origin
+                p = 0.f;
+                fl += 1.f;
+            }
             int idx = ic[d] + (int)fl;
             idx %= n;
             if (idx < 0) idx += n;

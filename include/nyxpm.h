@@ -184,6 +184,60 @@ double nyxpm_integrate_a(const nyxpm_params* p, double a_old, double dt);
 /* Nyx::integrate_comoving_a_to_a, comoving.cpp:74-130 (dt_window = search window). */
 double nyxpm_dt_for_da(const nyxpm_params* p, double a_old, double a_value, double dt_window);
 
+/* ---- ensembles and serving ------------------------------------------------------ */
+
+/* An ensemble holds many independent periodic boxes of uneven sizes in the
+ * mixed-precision form and advances them together: every stage of a step is one
+ * persistent launch over a work list spanning all boxes, and the step is
+ * replayed from captured CUDA graphs.  Box memory comes from a device arena of
+ * a fixed byte budget allocated at creation, so boxes can be added and removed
+ * between steps (continuous batching) without further device allocation.  No
+ * counterpart in the reference: Nyx runs one simulation per process. */
+typedef struct nyxpm_ensemble nyxpm_ensemble;
+
+/* Shapes chosen by the autotuner (nyx_gb300/autotune.py). */
+typedef struct nyxpm_tuning {
+    int deposit_tile;       /* 0: 8x8x8 cells, 1: 8x8x4, 2: 16x8x4 */
+    int smooth_rows;        /* plane rows per multigrid work item: 1, 2, 4 or 8 */
+    int inner_vcycles;      /* FP32 V-cycles per FP64 defect-correction iteration */
+    int max_outer;          /* defect-correction iterations inside the step graph */
+} nyxpm_tuning;
+
+typedef struct nyxpm_ensemble_info {
+    int boxes;              /* boxes stepped */
+    int max_outer_used;     /* most defect-correction iterations any box needed */
+    int max_inner_used;     /* most FP32 V-cycles any box ran */
+    int fallback_iters;     /* iterations run after the graph for boxes still above tolerance */
+    int launches;           /* kernels launched by the step (graph nodes included) */
+    int pad;
+    double ms;              /* device time of the step (CUDA events) */
+} nyxpm_ensemble_info;
+
+nyxpm_status nyxpm_ensemble_create(nyxpm_ctx* ctx, size_t arena_bytes, nyxpm_ensemble** out);
+nyxpm_status nyxpm_ensemble_destroy(nyxpm_ctx* ctx, nyxpm_ensemble* ens);
+/* Device bytes one box of this shape takes from the arena. */
+size_t nyxpm_ensemble_box_bytes(int n, int64_t np);
+size_t nyxpm_ensemble_arena_used(const nyxpm_ensemble* ens);
+/* Add a box (n >= 16, m * 2^k with m <= 8); NYXPM_OOM when the arena budget is exhausted. */
+nyxpm_status nyxpm_ensemble_add(nyxpm_ctx* ctx, nyxpm_ensemble* ens, int n, double L, int64_t np,
+                                int* slot);
+nyxpm_status nyxpm_ensemble_remove(nyxpm_ctx* ctx, nyxpm_ensemble* ens, int slot);
+/* Particles in (np x 3 positions and velocities, uniform mass); the box gets its
+ * initial field at the a_old of its first step. */
+nyxpm_status nyxpm_ensemble_upload(nyxpm_ctx* ctx, nyxpm_ensemble* ens, int slot, const double* pos,
+                                   const double* vel, double mass);
+nyxpm_status nyxpm_ensemble_download(nyxpm_ctx* ctx, nyxpm_ensemble* ens, int slot, double* pos,
+                                     double* vel);
+nyxpm_status nyxpm_ensemble_get_phi(nyxpm_ctx* ctx, nyxpm_ensemble* ens, int slot, double* phi);
+/* The FP32 gravity vector the kicks use, widened to FP64 (3 n^3, component-major). */
+nyxpm_status nyxpm_ensemble_grav_vector(nyxpm_ctx* ctx, nyxpm_ensemble* ens, int slot, double* g_out);
+nyxpm_status nyxpm_ensemble_set_tuning(nyxpm_ctx* ctx, nyxpm_ensemble* ens, const nyxpm_tuning* t);
+nyxpm_status nyxpm_ensemble_get_tuning(nyxpm_ctx* ctx, nyxpm_ensemble* ens, nyxpm_tuning* t);
+/* One PM step (old-time field reused: kick-drift, deposit, solve, kick) of every
+ * slot with a_old[slot] > 0; arrays are indexed by slot; other slots idle. */
+nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* ctx, nyxpm_ensemble* ens, const double* a_old,
+                                 const double* a_new, const double* dt, nyxpm_ensemble_info* info);
+
 /* ---- measurement ------------------------------------------------------------- */
 
 #define NYXPM_NUM_STAGES 12

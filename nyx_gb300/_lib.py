@@ -30,6 +30,11 @@ EXPORTS = [
     "nyxpm_get_phi", "nyxpm_set_phi", "nyxpm_grav_vector", "nyxpm_kick_drift", "nyxpm_kick",
     "nyxpm_step", "nyxpm_init_field", "nyxpm_integrate_a", "nyxpm_dt_for_da",
     "nyxpm_set_profiling", "nyxpm_get_profile", "nyxpm_launch_count",
+    "nyxpm_ensemble_create", "nyxpm_ensemble_destroy", "nyxpm_ensemble_box_bytes",
+    "nyxpm_ensemble_arena_used", "nyxpm_ensemble_add", "nyxpm_ensemble_remove",
+    "nyxpm_ensemble_upload", "nyxpm_ensemble_download", "nyxpm_ensemble_get_phi",
+    "nyxpm_ensemble_grav_vector", "nyxpm_ensemble_set_tuning", "nyxpm_ensemble_get_tuning",
+    "nyxpm_ensemble_step",
 ]
 
 
@@ -76,6 +81,23 @@ class Profile(C.Structure):
         ("fine_smooth_ms", C.c_double),
         ("fine_smooth_bytes", C.c_double),
     ]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("deposit_tile", C.c_int), ("smooth_rows", C.c_int), ("inner_vcycles", C.c_int),
+                ("max_outer", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class EnsembleInfo(C.Structure):
+    _fields_ = [("boxes", C.c_int), ("max_outer_used", C.c_int), ("max_inner_used", C.c_int),
+                ("fallback_iters", C.c_int), ("launches", C.c_int), ("pad", C.c_int),
+                ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
 
 
 _lib = None
@@ -131,5 +153,21 @@ def load(path: str | None = None):
     L.nyxpm_get_profile.argtypes = [vp, C.POINTER(Profile), C.c_int]
     L.nyxpm_launch_count.argtypes = [vp]
     L.nyxpm_launch_count.restype = i64
+    dp = C.POINTER(C.c_double)
+    L.nyxpm_ensemble_create.argtypes = [vp, C.c_size_t, C.POINTER(vp)]
+    L.nyxpm_ensemble_destroy.argtypes = [vp, vp]
+    L.nyxpm_ensemble_box_bytes.argtypes = [C.c_int, i64]
+    L.nyxpm_ensemble_box_bytes.restype = C.c_size_t
+    L.nyxpm_ensemble_arena_used.argtypes = [vp]
+    L.nyxpm_ensemble_arena_used.restype = C.c_size_t
+    L.nyxpm_ensemble_add.argtypes = [vp, vp, C.c_int, d, i64, C.POINTER(C.c_int)]
+    L.nyxpm_ensemble_remove.argtypes = [vp, vp, C.c_int]
+    L.nyxpm_ensemble_upload.argtypes = [vp, vp, C.c_int, vp, vp, d]
+    L.nyxpm_ensemble_download.argtypes = [vp, vp, C.c_int, vp, vp]
+    L.nyxpm_ensemble_get_phi.argtypes = [vp, vp, C.c_int, vp]
+    L.nyxpm_ensemble_grav_vector.argtypes = [vp, vp, C.c_int, vp]
+    L.nyxpm_ensemble_set_tuning.argtypes = [vp, vp, C.POINTER(Tuning)]
+    L.nyxpm_ensemble_get_tuning.argtypes = [vp, vp, C.POINTER(Tuning)]
+    L.nyxpm_ensemble_step.argtypes = [vp, vp, dp, dp, dp, C.POINTER(EnsembleInfo)]
     _lib = L
     return L

@@ -28,6 +28,7 @@ UNITS = {
     "pm_particles.cu": ["--fmad=false"],
     "pm_multigrid.cu": ["--fmad=false"],
     "pm_mixed.cu": [],
+    "pm_ensemble.cu": [],
 }
 
 

@@ -62,6 +62,7 @@ __device__ inline void block_umax_store(unsigned long long v, unsigned long long
         }
         if (lane == 0) atomicMax(out, v);
     }
+    __syncthreads();  // sm may be reused by the caller's next loop iteration
 }
 
 // One multigrid level.  The right-hand side is stored in smoother units,

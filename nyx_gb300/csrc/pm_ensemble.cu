@@ -1,0 +1,1801 @@
+// Batched ensemble of independent periodic PM boxes of uneven sizes, all in the
+// mixed-precision form, advanced together: every stage of a step is ONE
+// persistent launch over a work list that spans all boxes (particle chunks,
+// plane rows of every multigrid level, deposit tiles, per-box items), and the
+// step is captured in CUDA graphs and replayed.
+//
+// What a kernel needs about a box comes from two device arrays: a descriptor
+// (sizes and array pointers; written by the host, read-only on the device) and
+// a state record (current particle buffer, activity, step scalars, convergence;
+// owned by the device).  The graphs therefore replay without host updates; the
+// per-box step scalars are copied in from a pinned host buffer by the graph
+// itself.  Box storage comes from a device arena (one cudaMalloc at creation,
+// first-fit sub-allocation), so boxes join and leave without cudaMalloc.
+//
+// The arithmetic per box is that of the single-box mixed form (FP32
+// cell-relative particles, FP32 deposit and V-cycles, FP64 defect correction to
+// the context's relative tolerance, compensated FP64 mean, FP64 a(t) on the
+// host).  Convergence is per box: the solve graph runs max_outer
+// defect-correction iterations, a box that has met its tolerance skips the rest,
+// and boxes still above tolerance get further iterations before the gravity +
+// kick graph runs.
+#include "pm_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+namespace nyxpm {
+
+namespace {
+
+constexpr int kMaxLev = 9;
+constexpr int kPT = 256;             // particles per particle work item
+constexpr int kScanT = 512, kScanIPT = 8, kScanTile = kScanT * kScanIPT;
+constexpr float kSixthF = 1.0f / 6.0f;
+constexpr double kSixth = 1.0 / 6.0;
+
+__constant__ float kProlongWE[8] = {0.421875f, 0.140625f, 0.140625f, 0.046875f,
+                                    0.140625f, 0.046875f, 0.046875f, 0.015625f};
+
+struct ELevel {
+    int n, split;
+    float* phi_r;
+    float* phi_b;
+    float* beta_r;
+    float* beta_b;
+};
+
+// per-box descriptor: written by the host, read-only on the device
+struct EDesc {
+    int n, nlev, nb, used;
+    long long np;
+    double L, dx, dxi, mass_offset, mscalar, beta_scale;
+    // particle arrays: buffer 0 and buffer 1 (the sort gathers from one into the other)
+    int *cell0, *id0, *cell1, *id1;
+    float *ox0, *oy0, *oz0, *vx0, *vy0, *vz0;
+    float *ox1, *oy1, *oz1, *vx1, *vy1, *vz1;
+    int *key, *perm, *cell_count, *cell_start, *tile_sums, *long_list, *long_count;
+    float *frho, *g32;
+    double *rows, *scal;              // scal[0] mean
+    double *phi_r, *phi_b, *beta_r, *beta_b;   // level-0 FP64, split layout
+    float* Gf;
+    unsigned long long* norms;        // [0] ||beta||, [1] ||r||, [2] bad uploads
+    ELevel lv[kMaxLev];
+};
+
+// per-box state owned by the device (the host reads it, or resets it for a new box)
+struct EState {
+    int parity;                       // which particle buffer is current
+    int active;                       // takes part in the current pass
+    int solve_active;                 // still iterating in the current solve
+    int outer, inner;                 // defect-correction / FP32 V-cycle counts of the last solve
+    int pad;
+    double target;                    // convergence target of the current solve (smoother units)
+    double a_old, a_new, dt;
+};
+
+// step scalars written by the host each step (pinned) and copied in by the graph
+struct EStep {
+    double a_old, a_new, dt;
+    int active;
+    int pad;
+};
+
+struct Item {
+    int box, a, b, c;
+};
+
+// current particle arrays of a box
+struct PArr {
+    int* cell;
+    int* id;
+    float *ox, *oy, *oz, *vx, *vy, *vz;
+};
+
+__device__ __forceinline__ PArr parr(const EDesc& d, int parity)
+{
+    if (parity) return PArr{d.cell1, d.id1, d.ox1, d.oy1, d.oz1, d.vx1, d.vy1, d.vz1};
+    return PArr{d.cell0, d.id0, d.ox0, d.oy0, d.oz0, d.vx0, d.vy0, d.vz0};
+}
+
+__device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+__device__ __forceinline__ int pack_cell(int i, int j, int k) { return i | (j << 10) | (k << 20); }
+__device__ __forceinline__ int cell_i(int c) { return c & 1023; }
+__device__ __forceinline__ int cell_j(int c) { return (c >> 10) & 1023; }
+__device__ __forceinline__ int cell_k(int c) { return (c >> 20) & 1023; }
+
+__device__ __forceinline__ int key_frac(int ci, float o, int n, float* f)
+{
+    if (o >= 0.5f) {
+        *f = o - 0.5f;
+        return ci + 1 == n ? 0 : ci + 1;
+    }
+    *f = o + 0.5f;
+    return ci;
+}
+
+__device__ __forceinline__ void to_cell(double x, double dxi, int n, int* i, float* o)
+{
+    const double l = x * dxi;
+    double fl = floor(l);
+    float f = (float)(l - fl);
+    if (f >= 1.0f) {
+        f = 0.0f;
+        fl += 1.0;
+    }
+    *i = wrapi((int)fl, n);
+    *o = f;
+}
+
+// ---------------------------------------------------------------------------
+// step scalars
+// ---------------------------------------------------------------------------
+__global__ void e_load_step(int nbox, const EStep* __restrict__ st, EState* S)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbox) return;
+    S[b].a_old = st[b].a_old;
+    S[b].a_new = st[b].a_new;
+    S[b].dt = st[b].dt;
+    S[b].active = st[b].active;
+}
+
+// ---------------------------------------------------------------------------
+// particle stages: item = (box, chunk of kPT particles)
+// ---------------------------------------------------------------------------
+// phase 0: kick-drift (a_old -> a_half, move); phase 1: kick (a_half -> a_new)
+__global__ void __launch_bounds__(kPT) e_kick(const Item* __restrict__ items, int nitems,
+                                               const EDesc* __restrict__ D, const EState* __restrict__ S,
+                                               int phase)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!st.active) continue;
+        const EDesc& d = D[it.box];
+        const long long q = (long long)it.a * kPT + threadIdx.x;
+        if (q >= d.np) continue;
+        const PArr P = parr(d, st.parity);
+        const int n = d.n;
+        const long long nc = (long long)n * n * n;
+        const double a_half = 0.5 * (st.a_old + st.a_new);
+        const float a_prev = (float)(phase == 0 ? st.a_old : a_half);
+        const double a_cur = phase == 0 ? a_half : st.a_new;
+        const float a_cur_inv = (float)(1.0 / a_cur);
+        const float half_dt = (float)(0.5 * st.dt);
+        const float drift = (float)(st.dt / a_cur * d.dxi);
+        const int c = P.cell[q];
+        const int ci = cell_i(c), cj = cell_j(c), ck = cell_k(c);
+        float o[3] = {P.ox[q], P.oy[q], P.oz[q]};
+        float fx, fy, fz;
+        const int i = key_frac(ci, o[0], n, &fx);
+        const int j = key_frac(cj, o[1], n, &fy);
+        const int k = key_frac(ck, o[2], n, &fz);
+        const float sx[2] = {1.f - fx, fx};
+        const float sy[2] = {1.f - fy, fy};
+        const float sz[2] = {1.f - fz, fz};
+        float wgt[8];
+        long long cc[8];
+#pragma unroll
+        for (int kk = 0; kk <= 1; ++kk)
+#pragma unroll
+            for (int jj = 0; jj <= 1; ++jj)
+#pragma unroll
+                for (int ii = 0; ii <= 1; ++ii) {
+                    const int t = ii + 2 * jj + 4 * kk;
+                    wgt[t] = (sx[1 - ii] * sy[1 - jj]) * sz[1 - kk];
+                    cc[t] = cidx(wrap1(i - ii, n), wrap1(j - jj, n), wrap1(k - kk, n), n);
+                }
+        float v[3] = {P.vx[q], P.vy[q], P.vz[q]};
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd) {
+            const float* gd = d.g32 + dd * nc;
+            float val = 0.f;
+#pragma unroll
+            for (int t = 0; t < 8; ++t) val = fmaf(wgt[t], __ldg(gd + cc[t]), val);
+            v[dd] = fmaf(a_prev, v[dd], half_dt * val) * a_cur_inv;
+        }
+        P.vx[q] = v[0];
+        P.vy[q] = v[1];
+        P.vz[q] = v[2];
+        if (phase == 0) {
+            int ic[3] = {ci, cj, ck};
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd) {
+                float p = fmaf(drift, v[dd], o[dd]);
+                float fl = floorf(p);
+                p -= fl;
+                if (p >= 1.f) {  // -tiny + 1 rounded up to 1: the next cell's origin
+                    p = 0.f;
+                    fl += 1.f;
+                }
+                int idx = (ic[dd] + (int)fl) % n;
+                if (idx < 0) idx += n;
+                ic[dd] = idx;
+                o[dd] = p;
+            }
+            P.cell[q] = pack_cell(ic[0], ic[1], ic[2]);
+            P.ox[q] = o[0];
+            P.oy[q] = o[1];
+            P.oz[q] = o[2];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kPT) e_keys(const Item* __restrict__ items, int nitems,
+                                               const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!st.active) continue;
+        const EDesc& d = D[it.box];
+        const long long q = (long long)it.a * kPT + threadIdx.x;
+        if (q >= d.np) continue;
+        const PArr P = parr(d, st.parity);
+        const int c = P.cell[q];
+        float f;
+        const int i = key_frac(cell_i(c), P.ox[q], d.n, &f);
+        const int j = key_frac(cell_j(c), P.oy[q], d.n, &f);
+        const int k = key_frac(cell_k(c), P.oz[q], d.n, &f);
+        const int K = (int)cidx(i, j, k, d.n);
+        d.key[q] = K;
+        atomicAdd(d.cell_count + K, 1);
+    }
+}
+
+__global__ void __launch_bounds__(kPT) e_scatter(const Item* __restrict__ items, int nitems,
+                                                  const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        if (!S[it.box].active) continue;
+        const EDesc& d = D[it.box];
+        const long long q = (long long)it.a * kPT + threadIdx.x;
+        if (q >= d.np) continue;
+        const int K = d.key[q];
+        d.perm[d.cell_start[K] + atomicSub(d.cell_count + K, 1) - 1] = (int)q;
+    }
+}
+
+__global__ void __launch_bounds__(kPT) e_gather(const Item* __restrict__ items, int nitems,
+                                                 const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!st.active) continue;
+        const EDesc& d = D[it.box];
+        const long long s = (long long)it.a * kPT + threadIdx.x;
+        if (s >= d.np) continue;
+        const PArr A = parr(d, st.parity), B = parr(d, st.parity ^ 1);
+        const int q = d.perm[s];
+        B.cell[s] = A.cell[q];
+        B.ox[s] = A.ox[q];
+        B.oy[s] = A.oy[q];
+        B.oz[s] = A.oz[q];
+        B.vx[s] = A.vx[q];
+        B.vy[s] = A.vy[q];
+        B.vz[s] = A.vz[q];
+        B.id[s] = A.id[q];
+    }
+}
+
+// flip the current particle buffer of every active box (after the gather)
+__global__ void e_flip(int nbox, EState* S)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbox || !S[b].active) return;
+    S[b].parity ^= 1;
+}
+
+// ---------------------------------------------------------------------------
+// per-box segmented scan of the key counts: item = (box, tile of 4096 keys)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int warp_incl_scan(int v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+__device__ int block_excl_scan(int v, int* total)
+{
+    __shared__ int ws[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int inc = warp_incl_scan(v);
+    if (lane == 31) ws[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        int s = lane < nw ? ws[lane] : 0;
+        s = warp_incl_scan(s);
+        ws[lane] = s;
+    }
+    __syncthreads();
+    const int before = (w > 0 ? ws[w - 1] : 0) + inc - v;
+    *total = ws[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(kScanT) e_scan_reduce(const Item* __restrict__ items, int nitems,
+                                                        const EDesc* __restrict__ D,
+                                                        const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        if (!S[it.box].active) continue;  // uniform across the block
+        const EDesc& d = D[it.box];
+        const int nc = d.n * d.n * d.n;
+        const long long base = (long long)it.a * kScanTile + (long long)threadIdx.x * kScanIPT;
+        int s = 0;
+#pragma unroll
+        for (int t = 0; t < kScanIPT; ++t)
+            if (base + t < nc) s += d.cell_count[base + t];
+        int total;
+        block_excl_scan(s, &total);
+        if (threadIdx.x == 0) d.tile_sums[it.a] = total;
+    }
+}
+
+__global__ void e_scan_top(int nbox, const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    const int b = blockIdx.x;
+    if (b >= nbox || !S[b].active) return;
+    const EDesc& d = D[b];
+    const int nc = d.n * d.n * d.n;
+    const int ntiles = (nc + kScanTile - 1) / kScanTile;
+    int carry = 0;
+    for (int b0 = 0; b0 < ntiles; b0 += blockDim.x) {
+        const int i = b0 + threadIdx.x;
+        const int v = i < ntiles ? d.tile_sums[i] : 0;
+        int total;
+        const int ex = block_excl_scan(v, &total);
+        if (i < ntiles) d.tile_sums[i] = carry + ex;
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(kScanT) e_scan_down(const Item* __restrict__ items, int nitems,
+                                                      const EDesc* __restrict__ D,
+                                                      const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        if (!S[it.box].active) continue;
+        const EDesc& d = D[it.box];
+        const int nc = d.n * d.n * d.n;
+        const long long base = (long long)it.a * kScanTile + (long long)threadIdx.x * kScanIPT;
+        int v[kScanIPT];
+        int s = 0;
+#pragma unroll
+        for (int t = 0; t < kScanIPT; ++t) {
+            v[t] = base + t < nc ? d.cell_count[base + t] : 0;
+            s += v[t];
+        }
+        int total;
+        int run = block_excl_scan(s, &total) + d.tile_sums[it.a];
+#pragma unroll
+        for (int t = 0; t < kScanIPT; ++t) {
+            if (base + t < nc) d.cell_start[base + t] = run;
+            run += v[t];
+        }
+        if (base < nc && base + kScanIPT >= nc) d.cell_start[nc] = run;
+    }
+}
+
+// deterministic order inside each key segment: item = (box, chunk of 256 keys)
+__global__ void __launch_bounds__(256) e_fix_short(const Item* __restrict__ items, int nitems,
+                                                    const EDesc* __restrict__ D,
+                                                    const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        if (!S[it.box].active) continue;
+        const EDesc& d = D[it.box];
+        const int K = it.a * 256 + threadIdx.x;
+        if (K >= d.n * d.n * d.n) continue;
+        const int s = d.cell_start[K], len = d.cell_start[K + 1] - s;
+        if (len <= 1) continue;
+        if (len > 32) {
+            d.long_list[atomicAdd(d.long_count, 1)] = K;
+            continue;
+        }
+        int v[32];
+#pragma unroll
+        for (int t = 0; t < 32; ++t)
+            if (t < len) v[t] = d.perm[s + t];
+        for (int a = 1; a < len; ++a) {
+            int cur = v[a];
+            int bb = a - 1;
+            while (bb >= 0 && v[bb] > cur) {
+                v[bb + 1] = v[bb];
+                --bb;
+            }
+            v[bb + 1] = cur;
+        }
+#pragma unroll
+        for (int t = 0; t < 32; ++t)
+            if (t < len) d.perm[s + t] = v[t];
+    }
+}
+
+constexpr int kLongSmem = 12288;
+
+__global__ void e_fix_long(int nbox, const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    __shared__ int sv[kLongSmem];
+    for (int b = 0; b < nbox; ++b) {
+        if (!S[b].active) continue;
+        const EDesc& d = D[b];
+        const int total = *d.long_count;
+        for (int li = blockIdx.x; li < total; li += gridDim.x) {
+            const int K = d.long_list[li];
+            const int s = d.cell_start[K], len = d.cell_start[K + 1] - s;
+            const bool in_smem = len <= kLongSmem;
+            __syncthreads();
+            if (in_smem)
+                for (int t = threadIdx.x; t < len; t += blockDim.x) sv[t] = d.perm[s + t];
+            __syncthreads();
+            for (int t = threadIdx.x; t < len; t += blockDim.x) {
+                const int v = in_smem ? sv[t] : d.perm[s + t];
+                int rank = 0;
+                if (in_smem) {
+                    for (int u = 0; u < len; ++u) rank += sv[u] < v;
+                } else {
+                    for (int u = 0; u < len; ++u) rank += d.perm[s + u] < v;
+                }
+                d.key[s + rank] = v;
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < len; t += blockDim.x) d.perm[s + t] = d.key[s + t];
+        }
+    }
+}
+
+__global__ void e_sort_reset(int nbox, const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbox || !S[b].active) return;
+    *D[b].long_count = 0;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 deposit: item = (box, tile); tile shape from the template
+// ---------------------------------------------------------------------------
+template <int TX, int TY, int TZ>
+__global__ void __launch_bounds__(256) e_deposit(const Item* __restrict__ items, int nitems,
+                                                 const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    constexpr int KX = TX + 1, KY = TY + 1, KZ = TZ + 1, NK = KX * KY * KZ;
+    __shared__ float part[NK * 8];
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!st.active) continue;
+        const EDesc& d = D[it.box];
+        const PArr P = parr(d, st.parity);
+        const int n = d.n;
+        const int i0 = it.a * TX, j0 = it.b * TY, k0 = it.c * TZ;
+        __syncthreads();
+        for (int kl = threadIdx.x; kl < NK; kl += blockDim.x) {
+            const int ki = kl % KX, kj = (kl / KX) % KY, kk = kl / (KX * KY);
+            const long long K = cidx(wrapi(i0 + ki, n), wrapi(j0 + kj, n), wrapi(k0 + kk, n), n);
+            float s[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) s[c] = 0.f;
+            const int e = d.cell_start[K + 1];
+            for (int q = d.cell_start[K]; q < e; ++q) {
+                const int c = P.cell[q];
+                float fx, fy, fz;
+                key_frac(cell_i(c), P.ox[q], n, &fx);
+                key_frac(cell_j(c), P.oy[q], n, &fy);
+                key_frac(cell_k(c), P.oz[q], n, &fz);
+                const float sx[2] = {1.f - fx, fx};
+                const float sy[2] = {1.f - fy, fy};
+                const float sz[2] = {1.f - fz, fz};
+#pragma unroll
+                for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+                    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                        for (int cx = 0; cx < 2; ++cx) s[cx + 2 * cy + 4 * cz] += (sx[cx] * sy[cy]) * sz[cz];
+            }
+#pragma unroll
+            for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
+        }
+        __syncthreads();
+        const float scale = (float)(d.mscalar / (d.dx * d.dx * d.dx));
+        for (int cl = threadIdx.x; cl < TX * TY * TZ; cl += blockDim.x) {
+            const int ci = cl % TX, cj = (cl / TX) % TY, ck = cl / (TX * TY);
+            const int i = i0 + ci, j = j0 + cj, k = k0 + ck;
+            if (i >= n || j >= n || k >= n) continue;
+            float acc = 0.f;
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+                for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+                    for (int di = 0; di < 2; ++di) {
+                        const int kl = (ci + di) + KX * ((cj + dj) + KY * (ck + dk));
+                        acc += part[kl * 8 + (1 - di) + 2 * (1 - dj) + 4 * (1 - dk)];
+                    }
+            d.frho[cidx(i, j, k, n)] = acc * scale;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// RHS: item = (box, 8 rows); warp per row, compensated FP64 lane sums
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void kahan_add(double& s, double& c, double v)
+{
+    const double y = v - c;
+    const double t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+__global__ void __launch_bounds__(256) e_rowsum(const Item* __restrict__ items, int nitems,
+                                                const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    const int lane = threadIdx.x & 31, wr = threadIdx.x >> 5;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        if (!S[it.box].active) continue;
+        const EDesc& d = D[it.box];
+        const int n = d.n;
+        const long long row = (long long)it.a * 8 + wr;
+        if (row >= (long long)n * n) continue;
+        const float* r = d.frho + row * n;
+        double s = 0.0, c = 0.0;
+        for (int i = lane; i < n; i += 32) kahan_add(s, c, (double)r[i] - d.mass_offset);
+        s -= c;
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+        if (lane == 0) d.rows[row] = s;
+    }
+}
+
+// per-box mean (one block per box); also opens the solve of every active box
+__global__ void e_mean(int nbox, const EDesc* __restrict__ D, EState* S)
+{
+    __shared__ double ss[32];
+    const int b = blockIdx.x;
+    if (b >= nbox || !S[b].active) return;
+    const EDesc& d = D[b];
+    const long long nr = (long long)d.n * d.n;
+    double s = 0.0, c = 0.0;
+    for (long long r = threadIdx.x; r < nr; r += blockDim.x) kahan_add(s, c, d.rows[r]);
+    s -= c;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) ss[w] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0, tc = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) kahan_add(t, tc, ss[q]);
+        t -= tc;
+        d.scal[0] = (t * (d.dx * d.dx * d.dx)) / (d.L * d.L * d.L);
+        d.norms[0] = 0ULL;
+        d.norms[1] = 0ULL;
+        S[b].solve_active = 1;
+    }
+}
+
+// beta (FP64, split) from the FP32 density; |beta| max into norms[0].
+// item = (box, level 0, plane k, first row j0), block (32, R)
+__global__ void __launch_bounds__(256) e_make_beta(const Item* __restrict__ items, int nitems,
+                                                   const EDesc* __restrict__ D,
+                                                   const EState* __restrict__ S, double ggrav)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!st.active) continue;  // uniform across the block
+        const EDesc& d = D[it.box];
+        unsigned long long vmax = 0;
+        const int n = d.n, half = n >> 1, k = it.b;
+        const int j = it.c + threadIdx.y;
+        if (j < n) {
+            const double mean = d.scal[0];
+            const double ainv = 1.0 / st.a_new;
+            for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
+                const long long t = ((long long)j + (long long)n * k) * half + ih;
+#pragma unroll
+                for (int odd = 0; odd < 2; ++odd) {
+                    const int i = 2 * ih + odd;
+                    const double v = (double)d.frho[cidx(i, j, k, n)];
+                    const double bt = ((((v - d.mass_offset) - mean) * ggrav) * ainv) * d.beta_scale;
+                    (((i + j + k) & 1) ? d.beta_b : d.beta_r)[t] = bt;
+                    const unsigned long long u = absbits(bt);
+                    vmax = u > vmax ? u : vmax;
+                }
+            }
+        }
+        block_umax_store(vmax, d.norms + 0);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T nbr_sum_split(const T* other, int n, int half, int ih, int j, int k, int q)
+{
+    const int ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
+    const int ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    const long long row = (long long)j + (long long)n * k;
+    T s = other[row * half + ihm] + other[row * half + ihp];
+    s = s + other[((long long)jm + (long long)n * k) * half + ih];
+    s = s + other[((long long)jp + (long long)n * k) * half + ih];
+    s = s + other[((long long)j + (long long)n * km) * half + ih];
+    s = s + other[((long long)j + (long long)n * kp) * half + ih];
+    return s;
+}
+
+// FP64 residual of level 0 -> FP32 inner rhs (level-0 FP32 beta) with e = 0;
+// max |r| into norms[1]; boxes still iterating
+__global__ void __launch_bounds__(256) e_resid(const Item* __restrict__ items, int nitems,
+                                               const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        unsigned long long vmax = 0;
+        const int n = d.n, half = n >> 1, k = it.b;
+        const int j = it.c + threadIdx.y;
+        if (j < n) {
+            for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
+                const long long t = ((long long)j + (long long)n * k) * half + ih;
+#pragma unroll
+                for (int color = 0; color < 2; ++color) {
+                    const int q = (j + k + color) & 1;
+                    const double* other = color ? d.phi_r : d.phi_b;
+                    const double* mine = color ? d.phi_b : d.phi_r;
+                    const double* beta = color ? d.beta_b : d.beta_r;
+                    const double s = nbr_sum_split<double>(other, n, half, ih, j, k, q);
+                    const double r = beta[t] - fma(s, kSixth, -mine[t]);
+                    (color ? d.lv[0].beta_b : d.lv[0].beta_r)[t] = (float)r;
+                    (color ? d.lv[0].phi_b : d.lv[0].phi_r)[t] = 0.f;
+                    const unsigned long long u = absbits(r);
+                    vmax = u > vmax ? u : vmax;
+                }
+            }
+        }
+        block_umax_store(vmax, d.norms + 1);
+    }
+}
+
+// per-box convergence after a residual pass.  first = 1: set the target from
+// ||beta|| and ||r0|| and start iterating if above it
+__global__ void e_flags(int nbox, const EDesc* __restrict__ D, EState* S, double rel_tol, int first)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbox) return;
+    EState& st = S[b];
+    if (!st.active) return;
+    const EDesc& d = D[b];
+    if (!first && !st.solve_active) return;
+    double r;
+    {
+        const unsigned long long u = d.norms[1];
+        memcpy(&r, &u, sizeof(r));
+    }
+    if (first) {
+        double bn;
+        const unsigned long long u = d.norms[0];
+        memcpy(&bn, &u, sizeof(bn));
+        st.target = rel_tol * (bn > r ? bn : r);
+        st.outer = 0;
+        st.inner = 0;
+        st.solve_active = (r <= st.target) ? 0 : 1;
+    } else {
+        st.outer += 1;
+        if (r <= st.target) st.solve_active = 0;
+    }
+    d.norms[1] = 0ULL;
+}
+
+__global__ void e_count_inner(int nbox, EState* S, int cycles)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbox) return;
+    if (S[b].active && S[b].solve_active) S[b].inner += cycles;
+}
+
+// phi += e on level 0 (split), boxes still iterating
+__global__ void __launch_bounds__(256) e_update(const Item* __restrict__ items, int nitems,
+                                                const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        const int n = d.n, half = n >> 1, k = it.b;
+        const int j = it.c + threadIdx.y;
+        if (j >= n) continue;
+        for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
+            const long long t = ((long long)j + (long long)n * k) * half + ih;
+            d.phi_r[t] = d.phi_r[t] + (double)d.lv[0].phi_r[t];
+            d.phi_b[t] = d.phi_b[t] + (double)d.lv[0].phi_b[t];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 V-cycle kernels over level rows
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) e_gsrb(const Item* __restrict__ items, int nitems,
+                                              const EDesc* __restrict__ D, const EState* __restrict__ S,
+                                              int color)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        const ELevel& L = d.lv[it.a];
+        const int n = L.n, half = n >> 1, k = it.b;
+        const int j = it.c + threadIdx.y;
+        if (j >= n) continue;
+        float* mine = color ? L.phi_b : L.phi_r;
+        const float* other = color ? L.phi_r : L.phi_b;
+        const float* beta = color ? L.beta_b : L.beta_r;
+        const int q = (j + k + color) & 1;
+        for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
+            const long long t = ((long long)j + (long long)n * k) * half + ih;
+            const float s = nbr_sum_split<float>(other, n, half, ih, j, k, q);
+            mine[t] = fmaf(s, kSixthF, -beta[t]);
+        }
+    }
+}
+
+__device__ __forceinline__ float resid_f(const ELevel& L, int i, int j, int k)
+{
+    const int n = L.n;
+    const int im = i == 0 ? n - 1 : i - 1, ip = i == n - 1 ? 0 : i + 1;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    float s = *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, im, j, k) +
+              *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, ip, j, k);
+    s += *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, jm, k);
+    s += *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, jp, k);
+    s += *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, j, km);
+    s += *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, j, kp);
+    const float c = *lv_ptr<float>(L.phi_r, L.phi_b, n, L.split, i, j, k);
+    return *lv_ptr<float>(L.beta_r, L.beta_b, n, L.split, i, j, k) - fmaf(s, kSixthF, -c);
+}
+
+// item level = the coarse level; rows of the coarse level (natural coordinates)
+__global__ void __launch_bounds__(256) e_restrict(const Item* __restrict__ items, int nitems,
+                                                  const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        const ELevel& F = d.lv[it.a - 1];
+        const ELevel& C = d.lv[it.a];
+        const int nc = C.n, K = it.b;
+        const int J = it.c + threadIdx.y;
+        if (J >= nc) continue;
+        for (int I = threadIdx.x; I < nc; I += blockDim.x) {
+            float s = 0.f;
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+                for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+                    for (int di = 0; di < 2; ++di) s += resid_f(F, 2 * I + di, 2 * J + dj, 2 * K + dk);
+            *lv_ptr<float>(C.beta_r, C.beta_b, nc, C.split, I, J, K) = s * 0.5f;
+            *lv_ptr<float>(C.phi_r, C.phi_b, nc, C.split, I, J, K) = 0.f;
+        }
+    }
+}
+
+// item level = the fine level (split); rows of the fine level
+__global__ void __launch_bounds__(256) e_prolong(const Item* __restrict__ items, int nitems,
+                                                 const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        const ELevel& F = d.lv[it.a];
+        const ELevel& C = d.lv[it.a + 1];
+        const int n = F.n, nc = C.n, half = n >> 1, k = it.b;
+        const int j = it.c + threadIdx.y;
+        if (j >= n) continue;
+        const int J = j >> 1, K = k >> 1;
+        const int Js[2] = {J, wrap1((j & 1) ? J + 1 : J - 1, nc)};
+        const int Ks[2] = {K, wrap1((k & 1) ? K + 1 : K - 1, nc)};
+        for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
+            const long long t = ((long long)j + (long long)n * k) * half + ih;
+#pragma unroll
+            for (int odd = 0; odd < 2; ++odd) {
+                const int i = 2 * ih + odd;
+                const int Is[2] = {ih, wrap1(odd ? ih + 1 : ih - 1, nc)};
+                float s = 0.f;
+#pragma unroll
+                for (int b = 0; b < 2; ++b)
+#pragma unroll
+                    for (int a = 0; a < 2; ++a)
+#pragma unroll
+                        for (int tt = 0; tt < 2; ++tt)
+                            s = fmaf(kProlongWE[tt + 2 * a + 4 * b],
+                                     *lv_ptr<const float>(C.phi_r, C.phi_b, nc, C.split, Is[tt], Js[a], Ks[b]), s);
+                float* p = (((i + j + k) & 1) ? F.phi_b : F.phi_r) + t;
+                *p += s;
+            }
+        }
+    }
+}
+
+// exact coarsest solve of every iterating box: one block per box
+__global__ void e_bottom(int nbox, const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    __shared__ float r[kMaxBottom * kMaxBottom * kMaxBottom];
+    __shared__ float g[kMaxBottom * kMaxBottom * kMaxBottom];
+    const int b = blockIdx.x;
+    if (b >= nbox) return;
+    if (!(S[b].active && S[b].solve_active)) return;
+    const EDesc& d = D[b];
+    const ELevel& L = d.lv[d.nlev - 1];
+    const int nb = L.n, nc = nb * nb * nb;
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) {
+        r[t] = L.beta_r[t];
+        g[t] = d.Gf[t];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const int i = c % nb, j = (c / nb) % nb, k = c / (nb * nb);
+        float s = 0.f;
+        int y = 0;
+        for (int yk = 0; yk < nb; ++yk) {
+            const int dk = wrap1(k - yk, nb) * nb * nb;
+            for (int yj = 0; yj < nb; ++yj) {
+                const int djk = dk + wrap1(j - yj, nb) * nb;
+                for (int yi = 0; yi < nb; ++yi, ++y) s = fmaf(g[djk + wrap1(i - yi, nb)], r[y], s);
+            }
+        }
+        L.phi_r[c] = s;
+    }
+}
+
+// FP32 gravity vector from the FP64 phi (level-0 rows, natural coordinates)
+__global__ void __launch_bounds__(256) e_grav(const Item* __restrict__ items, int nitems,
+                                              const EDesc* __restrict__ D, const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        if (!S[it.box].active) continue;
+        const EDesc& d = D[it.box];
+        const int n = d.n, k = it.b;
+        const int j = it.c + threadIdx.y;
+        if (j >= n) continue;
+        const long long nc = (long long)n * n * n;
+        const float hdxi = (float)(0.5 * d.dxi);
+        const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int im = i == 0 ? n - 1 : i - 1, ip = i == n - 1 ? 0 : i + 1;
+            auto P = [&](int a, int b2, int c2) {
+                return *lv_ptr<const double>(d.phi_r, d.phi_b, n, 1, a, b2, c2);
+            };
+            const long long c = cidx(i, j, k, n);
+            d.g32[c] = (float)(P(ip, j, k) - P(im, j, k)) * hdxi;
+            d.g32[nc + c] = (float)(P(i, jp, k) - P(i, jm, k)) * hdxi;
+            d.g32[2 * nc + c] = (float)(P(i, j, kp) - P(i, j, km)) * hdxi;
+        }
+    }
+}
+
+__global__ void e_phi_to_natural(int n, const double* __restrict__ pr, const double* __restrict__ pb,
+                                 double* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n || j >= n) return;
+    out[cidx(i, j, k, n)] = *lv_ptr<const double>(pr, pb, n, 1, i, j, k);
+}
+
+__global__ void e_g32_to_double(long long cnt, const float* __restrict__ a, double* b)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < cnt) b[t] = a[t];
+}
+
+// ---------------------------------------------------------------------------
+// device arena: first-fit sub-allocator over one cudaMalloc (256-byte granules)
+// ---------------------------------------------------------------------------
+class Arena {
+public:
+    void* base = nullptr;
+    size_t bytes = 0;
+    std::map<size_t, size_t> free_;   // offset -> size
+    std::map<size_t, size_t> used_;   // offset -> size
+
+    bool init(size_t b)
+    {
+        bytes = (b + 255) & ~size_t(255);
+        if (bytes == 0 || cudaMalloc(&base, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            base = nullptr;
+            return false;
+        }
+        free_[0] = bytes;
+        return true;
+    }
+    void* alloc(size_t b)
+    {
+        b = (b + 255) & ~size_t(255);
+        if (b == 0) b = 256;
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= b) {
+                const size_t off = it->first, sz = it->second;
+                free_.erase(it);
+                if (sz > b) free_[off + b] = sz - b;
+                used_[off] = b;
+                return static_cast<char*>(base) + off;
+            }
+        }
+        return nullptr;
+    }
+    void release(void* p)
+    {
+        if (!p) return;
+        const size_t off = static_cast<char*>(p) - static_cast<char*>(base);
+        auto u = used_.find(off);
+        if (u == used_.end()) return;
+        size_t sz = u->second, o = off;
+        used_.erase(u);
+        auto nx = free_.lower_bound(o);
+        if (nx != free_.end() && o + sz == nx->first) {
+            sz += nx->second;
+            free_.erase(nx);
+        }
+        auto pv = free_.lower_bound(o);
+        if (pv != free_.begin()) {
+            --pv;
+            if (pv->first + pv->second == o) {
+                o = pv->first;
+                sz += pv->second;
+                free_.erase(pv);
+            }
+        }
+        free_[o] = sz;
+    }
+    size_t used_bytes() const
+    {
+        size_t s = 0;
+        for (auto& kv : used_) s += kv.second;
+        return s;
+    }
+    void destroy()
+    {
+        if (base) cudaFree(base);
+        base = nullptr;
+    }
+};
+
+int ens_bottom_edge(int n)
+{
+    int m = n;
+    while (m % 2 == 0 && m > kCoarsenAbove) m /= 2;
+    return m;
+}
+
+int ens_levels(int n)
+{
+    int L = 1, m = n;
+    while (m % 2 == 0 && m > kCoarsenAbove) {
+        m /= 2;
+        ++L;
+    }
+    return L;
+}
+
+}  // namespace
+
+struct EnsSlot {
+    int used = 0;
+    int uploaded = 0;
+    int init_pending = 0;
+    int fresh = 1;                    // device state not yet reset
+    std::vector<void*> blocks;
+    EDesc desc{};
+};
+
+}  // namespace nyxpm
+
+struct nyxpm_ensemble {
+    nyxpm::Arena arena;
+    std::vector<nyxpm::EnsSlot> slots;
+    int dirty = 1;                    // membership or tuning changed: tables and graphs stale
+    struct Range {
+        int off = 0, cnt = 0;
+    };
+    nyxpm::Item* d_items = nullptr;
+    size_t items_cap = 0;
+    Range r_part, r_scan, r_keys, r_tile, r_rows_rho;
+    Range r_rows_split[nyxpm::kMaxLev];   // rows of split levels (compact extent)
+    Range r_rows_nat[nyxpm::kMaxLev];     // rows of levels >= 1 (natural coordinates)
+    nyxpm::EDesc* d_desc = nullptr;
+    nyxpm::EState* d_state = nullptr;
+    nyxpm::EStep* d_step = nullptr;
+    nyxpm::EStep* h_step = nullptr;       // pinned, the step graph's source
+    nyxpm::EStep* h_init = nullptr;       // pinned, the init pass's source
+    nyxpm::EState* h_state = nullptr;     // pinned, state read back
+    unsigned long long* h_scratch = nullptr;  // pinned
+    int cap = 0;
+    int max_lev = 0;
+    nyxpm_tuning tune{};
+    cudaGraphExec_t exec_solve = nullptr, exec_finish = nullptr;
+    int sm = 0;
+    int64_t graph_launches_solve = 0, graph_launches_finish = 0;
+};
+
+using namespace nyxpm;
+
+namespace {
+
+nyxpm_status efail(nyxpm_ctx* c, nyxpm_status st, const char* msg)
+{
+    if (c) c->err = msg;
+    return st;
+}
+
+nyxpm_status echeck(nyxpm_ctx* c, const char* what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) return NYXPM_OK;
+    c->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return NYXPM_CUDA_ERROR;
+}
+
+#define ETRY(expr)                                                                           \
+    do {                                                                                     \
+        nyxpm_status _st = (expr);                                                           \
+        if (_st != NYXPM_OK) return _st;                                                     \
+    } while (0)
+
+unsigned pgrid(nyxpm_ensemble* E, int nitems, int per_sm = 8)
+{
+    const int cap = E->sm * per_sm;
+    return (unsigned)std::max(1, std::min(nitems, cap));
+}
+
+void invalidate_graphs(nyxpm_ensemble* E)
+{
+    if (E->exec_solve) cudaGraphExecDestroy(E->exec_solve);
+    if (E->exec_finish) cudaGraphExecDestroy(E->exec_finish);
+    E->exec_solve = E->exec_finish = nullptr;
+}
+
+bool slot_ok(nyxpm_ensemble* E, int slot)
+{
+    return slot >= 0 && slot < (int)E->slots.size() && E->slots[slot].used;
+}
+
+// rebuild work tables and push descriptors after a membership or tuning change
+nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
+{
+    std::vector<Item> items;
+    const int nbox = (int)E->slots.size();
+    const int R = E->tune.smooth_rows;
+    E->max_lev = 0;
+    for (auto& s : E->slots)
+        if (s.used) E->max_lev = std::max(E->max_lev, s.desc.nlev);
+    auto begin = [&](nyxpm_ensemble::Range& r) { r.off = (int)items.size(); };
+    auto end = [&](nyxpm_ensemble::Range& r) { r.cnt = (int)items.size() - r.off; };
+    begin(E->r_part);
+    for (int b = 0; b < nbox; ++b) {
+        const EnsSlot& s = E->slots[b];
+        if (!s.used) continue;
+        for (long long ch = 0; ch < (s.desc.np + kPT - 1) / kPT; ++ch) items.push_back(Item{b, (int)ch, 0, 0});
+    }
+    end(E->r_part);
+    begin(E->r_scan);
+    for (int b = 0; b < nbox; ++b) {
+        const EnsSlot& s = E->slots[b];
+        if (!s.used) continue;
+        const long long nc = (long long)s.desc.n * s.desc.n * s.desc.n;
+        for (long long t = 0; t < (nc + kScanTile - 1) / kScanTile; ++t) items.push_back(Item{b, (int)t, 0, 0});
+    }
+    end(E->r_scan);
+    begin(E->r_keys);
+    for (int b = 0; b < nbox; ++b) {
+        const EnsSlot& s = E->slots[b];
+        if (!s.used) continue;
+        const long long nc = (long long)s.desc.n * s.desc.n * s.desc.n;
+        for (long long t = 0; t < (nc + 255) / 256; ++t) items.push_back(Item{b, (int)t, 0, 0});
+    }
+    end(E->r_keys);
+    int TX = 8, TY = 8, TZ = 8;
+    if (E->tune.deposit_tile == 1) TZ = 4;
+    if (E->tune.deposit_tile == 2) {
+        TX = 16;
+        TZ = 4;
+    }
+    begin(E->r_tile);
+    for (int b = 0; b < nbox; ++b) {
+        const EnsSlot& s = E->slots[b];
+        if (!s.used) continue;
+        const int n = s.desc.n;
+        for (int tk = 0; tk < (n + TZ - 1) / TZ; ++tk)
+            for (int tj = 0; tj < (n + TY - 1) / TY; ++tj)
+                for (int ti = 0; ti < (n + TX - 1) / TX; ++ti) items.push_back(Item{b, ti, tj, tk});
+    }
+    end(E->r_tile);
+    begin(E->r_rows_rho);
+    for (int b = 0; b < nbox; ++b) {
+        const EnsSlot& s = E->slots[b];
+        if (!s.used) continue;
+        const long long nr = (long long)s.desc.n * s.desc.n;
+        for (long long t = 0; t < (nr + 7) / 8; ++t) items.push_back(Item{b, (int)t, 0, 0});
+    }
+    end(E->r_rows_rho);
+    for (int l = 0; l < kMaxLev; ++l) {
+        begin(E->r_rows_split[l]);
+        for (int b = 0; b < nbox; ++b) {
+            const EnsSlot& s = E->slots[b];
+            if (!s.used || l >= s.desc.nlev - 1) continue;
+            const int nl = s.desc.lv[l].n;
+            for (int k = 0; k < nl; ++k)
+                for (int j0 = 0; j0 < nl; j0 += R) items.push_back(Item{b, l, k, j0});
+        }
+        end(E->r_rows_split[l]);
+        begin(E->r_rows_nat[l]);
+        for (int b = 0; b < nbox; ++b) {
+            const EnsSlot& s = E->slots[b];
+            if (!s.used || l == 0 || l >= s.desc.nlev) continue;
+            const int nl = s.desc.lv[l].n;
+            for (int k = 0; k < nl; ++k)
+                for (int j0 = 0; j0 < nl; j0 += R) items.push_back(Item{b, l, k, j0});
+        }
+        end(E->r_rows_nat[l]);
+    }
+    if (items.empty()) items.push_back(Item{0, 0, 0, 0});
+    if (items.size() > E->items_cap) {
+        if (E->d_items) cudaFree(E->d_items);
+        E->items_cap = items.size() + items.size() / 4 + 1024;
+        if (cudaMalloc(&E->d_items, E->items_cap * sizeof(Item)) != cudaSuccess) {
+            cudaGetLastError();
+            E->d_items = nullptr;
+            E->items_cap = 0;
+            return efail(c, NYXPM_OOM, "ensemble work tables");
+        }
+    }
+    if (nbox > E->cap) {
+        // grow the descriptor / state arrays, keeping the device state of existing boxes
+        const int ncap = nbox + 16;
+        EDesc* nd = nullptr;
+        EState* ns = nullptr;
+        EStep* nst = nullptr;
+        EStep *hs = nullptr, *hi = nullptr;
+        EState* hst = nullptr;
+        if (cudaMalloc(&nd, ncap * sizeof(EDesc)) != cudaSuccess ||
+            cudaMalloc(&ns, ncap * sizeof(EState)) != cudaSuccess ||
+            cudaMalloc(&nst, ncap * sizeof(EStep)) != cudaSuccess ||
+            cudaMallocHost(&hs, ncap * sizeof(EStep)) != cudaSuccess ||
+            cudaMallocHost(&hi, ncap * sizeof(EStep)) != cudaSuccess ||
+            cudaMallocHost(&hst, ncap * sizeof(EState)) != cudaSuccess) {
+            cudaGetLastError();
+            return efail(c, NYXPM_OOM, "ensemble descriptors");
+        }
+        cudaMemsetAsync(ns, 0, ncap * sizeof(EState), c->stream);
+        if (E->d_state && E->cap > 0)
+            cudaMemcpyAsync(ns, E->d_state, E->cap * sizeof(EState), cudaMemcpyDeviceToDevice, c->stream);
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) return echeck(c, "ensemble grow");
+        if (E->d_desc) cudaFree(E->d_desc);
+        if (E->d_state) cudaFree(E->d_state);
+        if (E->d_step) cudaFree(E->d_step);
+        if (E->h_step) cudaFreeHost(E->h_step);
+        if (E->h_init) cudaFreeHost(E->h_init);
+        if (E->h_state) cudaFreeHost(E->h_state);
+        E->d_desc = nd;
+        E->d_state = ns;
+        E->d_step = nst;
+        E->h_step = hs;
+        E->h_init = hi;
+        E->h_state = hst;
+        std::memset(E->h_step, 0, ncap * sizeof(EStep));
+        std::memset(E->h_init, 0, ncap * sizeof(EStep));
+        E->cap = ncap;
+    }
+    std::vector<EDesc> descs(nbox);
+    for (int b = 0; b < nbox; ++b) {
+        descs[b] = E->slots[b].desc;
+        descs[b].used = E->slots[b].used;
+        if (E->slots[b].used && E->slots[b].fresh) {
+            cudaMemsetAsync(E->d_state + b, 0, sizeof(EState), c->stream);
+            E->slots[b].fresh = 0;
+        }
+    }
+    cudaMemcpyAsync(E->d_items, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(E->d_desc, descs.data(), nbox * sizeof(EDesc), cudaMemcpyHostToDevice, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return echeck(c, "ensemble rebuild");
+    invalidate_graphs(E);
+    E->dirty = 0;
+    return NYXPM_OK;
+}
+
+nyxpm_status pull_state(nyxpm_ctx* c, nyxpm_ensemble* E)
+{
+    const int nbox = (int)E->slots.size();
+    if (!E->d_state || nbox == 0) return NYXPM_OK;
+    cudaMemcpyAsync(E->h_state, E->d_state, nbox * sizeof(EState), cudaMemcpyDeviceToHost, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return echeck(c, "ensemble state");
+    return NYXPM_OK;
+}
+
+// sort + deposit + RHS + first residual + targets of the active boxes
+void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
+{
+    cudaStream_t s = c->stream;
+    const int nbox = (int)E->slots.size();
+    const Item* it = E->d_items;
+    const EDesc* D = E->d_desc;
+    EState* S = E->d_state;
+    const unsigned bb = (unsigned)((nbox + 127) / 128);
+    e_sort_reset<<<bb, 128, 0, s>>>(nbox, D, S);
+    e_keys<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S);
+    e_scan_reduce<<<pgrid(E, E->r_scan.cnt), kScanT, 0, s>>>(it + E->r_scan.off, E->r_scan.cnt, D, S);
+    e_scan_top<<<nbox, 1024, 0, s>>>(nbox, D, S);
+    e_scan_down<<<pgrid(E, E->r_scan.cnt), kScanT, 0, s>>>(it + E->r_scan.off, E->r_scan.cnt, D, S);
+    e_scatter<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S);
+    e_fix_short<<<pgrid(E, E->r_keys.cnt), 256, 0, s>>>(it + E->r_keys.off, E->r_keys.cnt, D, S);
+    e_fix_long<<<E->sm * 2, 512, 0, s>>>(nbox, D, S);
+    e_gather<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S);
+    e_flip<<<bb, 128, 0, s>>>(nbox, S);
+    const unsigned gt = pgrid(E, E->r_tile.cnt, 4);
+    if (E->tune.deposit_tile == 1)
+        e_deposit<8, 8, 4><<<gt, 256, 0, s>>>(it + E->r_tile.off, E->r_tile.cnt, D, S);
+    else if (E->tune.deposit_tile == 2)
+        e_deposit<16, 8, 4><<<gt, 256, 0, s>>>(it + E->r_tile.off, E->r_tile.cnt, D, S);
+    else
+        e_deposit<8, 8, 8><<<gt, 256, 0, s>>>(it + E->r_tile.off, E->r_tile.cnt, D, S);
+    e_rowsum<<<pgrid(E, E->r_rows_rho.cnt), 256, 0, s>>>(it + E->r_rows_rho.off, E->r_rows_rho.cnt, D, S);
+    e_mean<<<nbox, 512, 0, s>>>(nbox, D, S);
+    const dim3 rb(32, E->tune.smooth_rows);
+    const double ggrav = -4.0 * M_PI * c->p.gconst;
+    const auto& r0 = E->r_rows_split[0];
+    e_make_beta<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, ggrav);
+    e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+    e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 1);
+    c->launches += 16;
+}
+
+// `outer` defect-correction iterations (boxes that converged skip them)
+void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer)
+{
+    cudaStream_t s = c->stream;
+    const int nbox = (int)E->slots.size();
+    const Item* it = E->d_items;
+    const EDesc* D = E->d_desc;
+    EState* S = E->d_state;
+    const unsigned bb = (unsigned)((nbox + 127) / 128);
+    const dim3 rb(32, E->tune.smooth_rows);
+    for (int o = 0; o < outer; ++o) {
+        for (int v = 0; v < E->tune.inner_vcycles; ++v) {
+            for (int l = 0; l < E->max_lev - 1; ++l) {
+                const auto& rs = E->r_rows_split[l];
+                if (rs.cnt == 0) continue;
+                for (int sw = 0; sw < c->p.nu1; ++sw)
+                    for (int color = 0; color < 2; ++color)
+                        e_gsrb<<<pgrid(E, rs.cnt), rb, 0, s>>>(it + rs.off, rs.cnt, D, S, color);
+                const auto& rn = E->r_rows_nat[l + 1];
+                e_restrict<<<pgrid(E, rn.cnt), rb, 0, s>>>(it + rn.off, rn.cnt, D, S);
+                c->launches += 2 * c->p.nu1 + 1;
+            }
+            e_bottom<<<nbox, 128, 0, s>>>(nbox, D, S);
+            c->launches += 1;
+            for (int l = E->max_lev - 2; l >= 0; --l) {
+                const auto& rs = E->r_rows_split[l];
+                if (rs.cnt == 0) continue;
+                e_prolong<<<pgrid(E, rs.cnt), rb, 0, s>>>(it + rs.off, rs.cnt, D, S);
+                for (int sw = 0; sw < c->p.nu2; ++sw)
+                    for (int color = 0; color < 2; ++color)
+                        e_gsrb<<<pgrid(E, rs.cnt), rb, 0, s>>>(it + rs.off, rs.cnt, D, S, color);
+                c->launches += 2 * c->p.nu2 + 1;
+            }
+        }
+        const auto& r0 = E->r_rows_split[0];
+        e_count_inner<<<bb, 128, 0, s>>>(nbox, S, E->tune.inner_vcycles);
+        e_update<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+        e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+        e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 0);
+        c->launches += 4;
+    }
+}
+
+void enqueue_grav(nyxpm_ctx* c, nyxpm_ensemble* E)
+{
+    const dim3 rb(32, E->tune.smooth_rows);
+    const auto& r0 = E->r_rows_split[0];
+    e_grav<<<pgrid(E, r0.cnt), rb, 0, c->stream>>>(E->d_items + r0.off, r0.cnt, E->d_desc, E->d_state);
+    c->launches += 1;
+}
+
+void enqueue_kick(nyxpm_ctx* c, nyxpm_ensemble* E, int phase)
+{
+    e_kick<<<pgrid(E, E->r_part.cnt), kPT, 0, c->stream>>>(E->d_items + E->r_part.off, E->r_part.cnt,
+                                                            E->d_desc, E->d_state, phase);
+    c->launches += 1;
+}
+
+void enqueue_load(nyxpm_ctx* c, nyxpm_ensemble* E, const EStep* host_src)
+{
+    const int nbox = (int)E->slots.size();
+    cudaMemcpyAsync(E->d_step, host_src, nbox * sizeof(EStep), cudaMemcpyHostToDevice, c->stream);
+    e_load_step<<<(nbox + 127) / 128, 128, 0, c->stream>>>(nbox, E->d_step, E->d_state);
+    c->launches += 1;
+}
+
+// iterate eagerly until every active box has converged
+nyxpm_status finish_unconverged(nyxpm_ctx* c, nyxpm_ensemble* E, int* extra)
+{
+    *extra = 0;
+    const int nbox = (int)E->slots.size();
+    for (int guard = 0; guard <= c->p.max_vcycles; ++guard) {
+        ETRY(pull_state(c, E));
+        bool any = false;
+        for (int b = 0; b < nbox; ++b)
+            if (E->slots[b].used && E->h_state[b].active && E->h_state[b].solve_active) any = true;
+        if (!any) return NYXPM_OK;
+        if (guard == c->p.max_vcycles) break;
+        enqueue_iterations(c, E, 1);
+        ETRY(echeck(c, "ensemble iterations"));
+        *extra += 1;
+    }
+    return efail(c, NYXPM_NOT_CONVERGED, "ensemble: a box did not converge");
+}
+
+nyxpm_status capture(nyxpm_ctx* c, nyxpm_ensemble* E, cudaGraphExec_t* exec, int which)
+{
+    cudaGraph_t g = nullptr;
+    const int64_t l0 = c->launches;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return echeck(c, "ensemble capture begin");
+    if (which == 0) {
+        enqueue_load(c, E, E->h_step);
+        enqueue_kick(c, E, 0);
+        enqueue_solve_head(c, E);
+        enqueue_iterations(c, E, E->tune.max_outer);
+    } else {
+        enqueue_grav(c, E);
+        enqueue_kick(c, E, 1);
+    }
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (ce != cudaSuccess) return echeck(c, "ensemble capture end");
+    if (cudaGraphInstantiate(exec, g, 0) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return echeck(c, "ensemble graph instantiate");
+    }
+    cudaGraphDestroy(g);
+    const int64_t n = c->launches - l0;
+    c->launches = l0;
+    if (which == 0) E->graph_launches_solve = n;
+    else E->graph_launches_finish = n;
+    return NYXPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t nyxpm_ensemble_box_bytes(int n, int64_t np)
+{
+    const double nc = (double)n * n * n;
+    // particles: 2 x (cell, id, 3 offsets, 3 velocities) + key + perm + staging for upload
+    // cells: count, start, FP32 rho, FP32 g (3), FP64 phi + beta, FP32 levels (phi + beta, 8/7)
+    return (size_t)(np * (2.0 * 32 + 8) + nc * (4 + 4 + 4 + 12 + 16 + 16 + 8.0 * 8 / 7) + 8.0 * n * n +
+                    4.0 * (np / 32 + 2) + 256.0 * 64 + 4.0 * nc / 4096);
+}
+
+nyxpm_status nyxpm_ensemble_create(nyxpm_ctx* c, size_t arena_bytes, nyxpm_ensemble** out)
+{
+    if (!c || !out) return NYXPM_INVALID_ARG;
+    *out = nullptr;
+    cudaSetDevice(c->p.device);
+    nyxpm_ensemble* E = new (std::nothrow) nyxpm_ensemble();
+    if (!E) return NYXPM_OOM;
+    if (!E->arena.init(arena_bytes)) {
+        delete E;
+        return efail(c, NYXPM_OOM, "ensemble arena (memory budget) could not be allocated");
+    }
+    if (cudaMallocHost(&E->h_scratch, 64) != cudaSuccess) {
+        cudaGetLastError();
+        E->arena.destroy();
+        delete E;
+        return efail(c, NYXPM_OOM, "ensemble pinned scratch");
+    }
+    E->tune.deposit_tile = 0;
+    E->tune.smooth_rows = 8;
+    E->tune.inner_vcycles = c->p.mixed_inner_vcycles;
+    E->tune.max_outer = 6;
+    E->sm = c->sm_count;
+    *out = E;
+    return NYXPM_OK;
+}
+
+nyxpm_status nyxpm_ensemble_destroy(nyxpm_ctx* c, nyxpm_ensemble* E)
+{
+    if (!c || !E) return NYXPM_INVALID_ARG;
+    cudaStreamSynchronize(c->stream);
+    invalidate_graphs(E);
+    if (E->d_items) cudaFree(E->d_items);
+    if (E->d_desc) cudaFree(E->d_desc);
+    if (E->d_state) cudaFree(E->d_state);
+    if (E->d_step) cudaFree(E->d_step);
+    if (E->h_step) cudaFreeHost(E->h_step);
+    if (E->h_init) cudaFreeHost(E->h_init);
+    if (E->h_state) cudaFreeHost(E->h_state);
+    if (E->h_scratch) cudaFreeHost(E->h_scratch);
+    E->arena.destroy();
+    delete E;
+    return NYXPM_OK;
+}
+
+nyxpm_status nyxpm_ensemble_add(nyxpm_ctx* c, nyxpm_ensemble* E, int n, double L, int64_t np, int* slot)
+{
+    if (!c || !E || !slot) return NYXPM_INVALID_ARG;
+    if (n < 16 || n > 1024 || ens_bottom_edge(n) > kMaxBottom)
+        return efail(c, NYXPM_INVALID_ARG, "ensemble boxes need n >= 16 of the form m*2^k, m <= 8");
+    if (!(L > 0) || np < 1 || np > 0x7fffffffLL) return efail(c, NYXPM_INVALID_ARG, "bad L / np");
+    if (ens_levels(n) > kMaxLev) return efail(c, NYXPM_INVALID_ARG, "too many levels");
+    int b = -1;
+    for (int i = 0; i < (int)E->slots.size(); ++i)
+        if (!E->slots[i].used) {
+            b = i;
+            break;
+        }
+    if (b < 0) {
+        b = (int)E->slots.size();
+        E->slots.emplace_back();
+    }
+    EnsSlot& s = E->slots[b];
+    s = EnsSlot();
+    const size_t nc = (size_t)n * n * n;
+    bool ok = true;
+    auto A = [&](size_t bytes) -> void* {
+        void* p = E->arena.alloc(bytes);
+        if (!p) ok = false;
+        else s.blocks.push_back(p);
+        return p;
+    };
+    EDesc& d = s.desc;
+    std::memset(&d, 0, sizeof(d));
+    d.n = n;
+    d.nlev = ens_levels(n);
+    d.nb = ens_bottom_edge(n);
+    d.np = np;
+    d.L = L;
+    d.dx = L / n;
+    d.dxi = (double)n / L;
+    {
+        const double h = L / n;
+        d.beta_scale = (h * h) * kSixth;
+    }
+    d.cell0 = (int*)A(4 * np); d.id0 = (int*)A(4 * np); d.cell1 = (int*)A(4 * np); d.id1 = (int*)A(4 * np);
+    d.ox0 = (float*)A(4 * np); d.oy0 = (float*)A(4 * np); d.oz0 = (float*)A(4 * np);
+    d.vx0 = (float*)A(4 * np); d.vy0 = (float*)A(4 * np); d.vz0 = (float*)A(4 * np);
+    d.ox1 = (float*)A(4 * np); d.oy1 = (float*)A(4 * np); d.oz1 = (float*)A(4 * np);
+    d.vx1 = (float*)A(4 * np); d.vy1 = (float*)A(4 * np); d.vz1 = (float*)A(4 * np);
+    d.key = (int*)A(4 * np); d.perm = (int*)A(4 * np);
+    d.cell_count = (int*)A(4 * nc);
+    d.cell_start = (int*)A(4 * (nc + 1));
+    d.tile_sums = (int*)A(4 * ((nc + kScanTile - 1) / kScanTile + 1));
+    d.long_list = (int*)A(4 * (np / 32 + 2));
+    d.long_count = (int*)A(256);
+    d.frho = (float*)A(4 * nc);
+    d.g32 = (float*)A(12 * nc);
+    d.rows = (double*)A(8 * (size_t)n * n);
+    d.scal = (double*)A(256);
+    d.norms = (unsigned long long*)A(256);
+    d.phi_r = (double*)A(8 * nc / 2); d.phi_b = (double*)A(8 * nc / 2);
+    d.beta_r = (double*)A(8 * nc / 2); d.beta_b = (double*)A(8 * nc / 2);
+    for (int l = 0, nl = n; l < d.nlev; ++l, nl /= 2) {
+        ELevel& lv = d.lv[l];
+        lv.n = nl;
+        lv.split = (l < d.nlev - 1) ? 1 : 0;
+        const size_t cnt = (size_t)nl * nl * nl;
+        if (lv.split) {
+            lv.phi_r = (float*)A(4 * cnt / 2); lv.phi_b = (float*)A(4 * cnt / 2);
+            lv.beta_r = (float*)A(4 * cnt / 2); lv.beta_b = (float*)A(4 * cnt / 2);
+        } else {
+            lv.phi_r = (float*)A(4 * cnt); lv.beta_r = (float*)A(4 * cnt);
+        }
+    }
+    d.Gf = (float*)A(4 * (size_t)d.nb * d.nb * d.nb);
+    if (!ok) {
+        for (void* p : s.blocks) E->arena.release(p);
+        s = EnsSlot();
+        s.used = 0;
+        return efail(c, NYXPM_OOM, "ensemble arena exhausted (memory budget)");
+    }
+    {
+        const int nb = d.nb;
+        const long ncb = (long)nb * nb * nb;
+        std::vector<float> Gf(ncb);
+        const double h = L / nb, twopi = 2.0 * std::acos(-1.0);
+        std::vector<double> lam(ncb);
+        for (int kz = 0; kz < nb; ++kz)
+            for (int ky = 0; ky < nb; ++ky)
+                for (int kx = 0; kx < nb; ++kx)
+                    lam[kx + nb * (ky + (long)nb * kz)] =
+                        ((2.0 * std::cos(twopi * kx / nb) - 2.0) + (2.0 * std::cos(twopi * ky / nb) - 2.0) +
+                         (2.0 * std::cos(twopi * kz / nb) - 2.0)) / (h * h);
+        for (int dz = 0; dz < nb; ++dz)
+            for (int dy = 0; dy < nb; ++dy)
+                for (int dxx = 0; dxx < nb; ++dxx) {
+                    double acc = 0.0;
+                    for (int kz = 0; kz < nb; ++kz)
+                        for (int ky = 0; ky < nb; ++ky)
+                            for (int kx = 0; kx < nb; ++kx) {
+                                if (kx == 0 && ky == 0 && kz == 0) continue;
+                                const long ph = ((long)kx * dxx + (long)ky * dy + (long)kz * dz) % nb;
+                                acc += std::cos(twopi * (double)ph / nb) / lam[kx + nb * (ky + (long)nb * kz)];
+                            }
+                    Gf[dxx + nb * (dy + (long)nb * dz)] = (float)((acc / (double)ncb) * (6.0 / (h * h)));
+                }
+        cudaMemcpyAsync(d.Gf, Gf.data(), sizeof(float) * Gf.size(), cudaMemcpyHostToDevice, c->stream);
+        cudaMemsetAsync(d.cell_count, 0, 4 * nc, c->stream);
+        cudaMemsetAsync(d.phi_r, 0, 8 * nc / 2, c->stream);
+        cudaMemsetAsync(d.phi_b, 0, 8 * nc / 2, c->stream);
+        cudaMemsetAsync(d.long_count, 0, 4, c->stream);
+        cudaMemsetAsync(d.norms, 0, 32, c->stream);
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) return echeck(c, "ensemble add");
+    }
+    s.used = 1;
+    s.fresh = 1;
+    E->dirty = 1;
+    *slot = b;
+    return NYXPM_OK;
+}
+
+nyxpm_status nyxpm_ensemble_remove(nyxpm_ctx* c, nyxpm_ensemble* E, int slot)
+{
+    if (!c || !E || !slot_ok(E, slot)) return NYXPM_INVALID_ARG;
+    cudaStreamSynchronize(c->stream);
+    EnsSlot& s = E->slots[slot];
+    for (void* p : s.blocks) E->arena.release(p);
+    s = EnsSlot();
+    s.used = 0;
+    E->dirty = 1;
+    return NYXPM_OK;
+}
+
+size_t nyxpm_ensemble_arena_used(const nyxpm_ensemble* E) { return E ? E->arena.used_bytes() : 0; }
+
+// host-side split x = (i + o) dx, the arithmetic of to_cell() (this file is
+// compiled without host contraction)
+static void host_to_cell(double x, double dxi, int n, int* i, float* o)
+{
+    const double l = x * dxi;
+    double fl = std::floor(l);
+    float f = (float)(l - fl);
+    if (f >= 1.0f) {
+        f = 0.0f;
+        fl += 1.0;
+    }
+    *i = wrapi((int)fl, n);
+    *o = f;
+}
+
+nyxpm_status nyxpm_ensemble_upload(nyxpm_ctx* c, nyxpm_ensemble* E, int slot, const double* pos,
+                                   const double* vel, double mass)
+{
+    if (!c || !E || !slot_ok(E, slot) || !pos || !vel) return NYXPM_INVALID_ARG;
+    if (!(mass >= 0) || !std::isfinite(mass)) return efail(c, NYXPM_INVALID_ARG, "bad mass");
+    if (E->dirty) ETRY(rebuild(c, E));
+    EnsSlot& s = E->slots[slot];
+    EDesc& d = s.desc;
+    const long long np = d.np;
+    // convert on the host into the box's buffer-0 arrays: no device staging, so an
+    // upload never needs arena space beyond the box itself
+    std::vector<int> cell(np), id(np);
+    std::vector<float> f[6];
+    for (auto& a : f) a.resize(np);
+    for (long long q = 0; q < np; ++q) {
+        for (int k = 0; k < 3; ++k)
+            if (!std::isfinite(pos[3 * q + k]) || !std::isfinite(vel[3 * q + k])) {
+                s.uploaded = 0;
+                return efail(c, NYXPM_INVALID_ARG, "non-finite particle position or velocity");
+            }
+        int ii[3];
+        for (int k = 0; k < 3; ++k) host_to_cell(pos[3 * q + k], d.dxi, d.n, &ii[k], &f[k][q]);
+        cell[q] = ii[0] | (ii[1] << 10) | (ii[2] << 20);
+        for (int k = 0; k < 3; ++k) f[3 + k][q] = (float)vel[3 * q + k];
+        id[q] = (int)q;
+    }
+    float* dst[6] = {d.ox0, d.oy0, d.oz0, d.vx0, d.vy0, d.vz0};
+    cudaMemcpyAsync(d.cell0, cell.data(), 4 * np, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d.id0, id.data(), 4 * np, cudaMemcpyHostToDevice, c->stream);
+    for (int k = 0; k < 6; ++k) cudaMemcpyAsync(dst[k], f[k].data(), 4 * np, cudaMemcpyHostToDevice, c->stream);
+    cudaMemsetAsync(&E->d_state[slot].parity, 0, sizeof(int), c->stream);
+    d.mscalar = mass;
+    d.mass_offset = mass * (double)np / (d.L * d.L * d.L);
+    // the descriptor changed (mass): push it
+    cudaMemcpyAsync(E->d_desc + slot, &d, sizeof(EDesc), cudaMemcpyHostToDevice, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return echeck(c, "ensemble upload");
+    s.uploaded = 1;
+    s.init_pending = 1;
+    return NYXPM_OK;
+}
+
+nyxpm_status nyxpm_ensemble_download(nyxpm_ctx* c, nyxpm_ensemble* E, int slot, double* pos, double* vel)
+{
+    if (!c || !E || !slot_ok(E, slot) || !pos || !vel) return NYXPM_INVALID_ARG;
+    if (!E->slots[slot].uploaded) return efail(c, NYXPM_INVALID_ARG, "slot has no particles");
+    ETRY(pull_state(c, E));
+    const EDesc& d = E->slots[slot].desc;
+    const int par = E->h_state[slot].parity;
+    const long long np = d.np;
+    std::vector<int> cell(np), id(np);
+    std::vector<float> f[6];
+    for (auto& a : f) a.resize(np);
+    const float* src[6] = {par ? d.ox1 : d.ox0, par ? d.oy1 : d.oy0, par ? d.oz1 : d.oz0,
+                           par ? d.vx1 : d.vx0, par ? d.vy1 : d.vy0, par ? d.vz1 : d.vz0};
+    cudaMemcpyAsync(cell.data(), par ? d.cell1 : d.cell0, 4 * np, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(id.data(), par ? d.id1 : d.id0, 4 * np, cudaMemcpyDeviceToHost, c->stream);
+    for (int k = 0; k < 6; ++k) cudaMemcpyAsync(f[k].data(), src[k], 4 * np, cudaMemcpyDeviceToHost, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return echeck(c, "ensemble download");
+    for (long long q = 0; q < np; ++q) {
+        const long long o = 3LL * id[q];
+        if (id[q] < 0 || id[q] >= np) return efail(c, NYXPM_CUDA_ERROR, "corrupt particle id");
+        const int cc = cell[q];
+        const int ci[3] = {cc & 1023, (cc >> 10) & 1023, (cc >> 20) & 1023};
+        for (int k = 0; k < 3; ++k) {
+            pos[o + k] = ((double)ci[k] + (double)f[k][q]) * d.dx;
+            vel[o + k] = f[3 + k][q];
+        }
+    }
+    return NYXPM_OK;
+}
+
+nyxpm_status nyxpm_ensemble_get_phi(nyxpm_ctx* c, nyxpm_ensemble* E, int slot, double* phi)
+{
+    if (!c || !E || !slot_ok(E, slot) || !phi) return NYXPM_INVALID_ARG;
+    const EDesc& d = E->slots[slot].desc;
+    const size_t nc = (size_t)d.n * d.n * d.n;
+    void* tmp = E->arena.alloc(8 * nc);
+    if (!tmp) return efail(c, NYXPM_OOM, "ensemble phi staging");
+    const Geo g = geo3(d.n, d.n, d.n);
+    e_phi_to_natural<<<g.grid, g.block, 0, c->stream>>>(d.n, d.phi_r, d.phi_b, (double*)tmp);
+    cudaMemcpyAsync(phi, tmp, 8 * nc, cudaMemcpyDeviceToHost, c->stream);
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
+    E->arena.release(tmp);
+    return e == cudaSuccess ? NYXPM_OK : echeck(c, "ensemble get phi");
+}
+
+nyxpm_status nyxpm_ensemble_grav_vector(nyxpm_ctx* c, nyxpm_ensemble* E, int slot, double* g_out)
+{
+    if (!c || !E || !slot_ok(E, slot) || !g_out) return NYXPM_INVALID_ARG;
+    const EDesc& d = E->slots[slot].desc;
+    const long long cnt = 3LL * d.n * d.n * d.n;
+    void* tmp = E->arena.alloc(8 * cnt);
+    if (!tmp) return efail(c, NYXPM_OOM, "ensemble g staging");
+    e_g32_to_double<<<(unsigned)((cnt + 255) / 256), 256, 0, c->stream>>>(cnt, d.g32, (double*)tmp);
+    cudaMemcpyAsync(g_out, tmp, 8 * cnt, cudaMemcpyDeviceToHost, c->stream);
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
+    E->arena.release(tmp);
+    return e == cudaSuccess ? NYXPM_OK : echeck(c, "ensemble grav");
+}
+
+nyxpm_status nyxpm_ensemble_set_tuning(nyxpm_ctx* c, nyxpm_ensemble* E, const nyxpm_tuning* t)
+{
+    if (!c || !E || !t) return NYXPM_INVALID_ARG;
+    if (t->deposit_tile < 0 || t->deposit_tile > 2 ||
+        (t->smooth_rows != 1 && t->smooth_rows != 2 && t->smooth_rows != 4 && t->smooth_rows != 8) ||
+        t->inner_vcycles < 1 || t->inner_vcycles > 8 || t->max_outer < 1 || t->max_outer > 64)
+        return efail(c, NYXPM_INVALID_ARG, "bad tuning");
+    E->tune = *t;
+    E->dirty = 1;
+    return NYXPM_OK;
+}
+
+nyxpm_status nyxpm_ensemble_get_tuning(nyxpm_ctx* c, nyxpm_ensemble* E, nyxpm_tuning* t)
+{
+    if (!c || !E || !t) return NYXPM_INVALID_ARG;
+    *t = E->tune;
+    return NYXPM_OK;
+}
+
+nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* c, nyxpm_ensemble* E, const double* a_old,
+                                 const double* a_new, const double* dt, nyxpm_ensemble_info* info)
+{
+    if (!c || !E || !a_old || !a_new || !dt) return NYXPM_INVALID_ARG;
+    const int nbox = (int)E->slots.size();
+    if (info) std::memset(info, 0, sizeof(*info));
+    if (nbox == 0) return NYXPM_OK;
+    if (E->dirty) ETRY(rebuild(c, E));
+    const int64_t launches0 = c->launches;
+    cudaEvent_t ev0, ev1;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    cudaEventRecord(ev0, c->stream);
+    int extra = 0;
+    // initial fields of boxes uploaded since their last step (an eager pass with
+    // only those boxes active; the RHS of the init solve uses a_new = a_old)
+    bool any_init = false;
+    for (int b = 0; b < nbox; ++b) {
+        const EnsSlot& s = E->slots[b];
+        const bool init = s.used && s.uploaded && s.init_pending && a_old[b] > 0;
+        E->h_init[b].active = init ? 1 : 0;
+        E->h_init[b].a_old = a_old[b];
+        E->h_init[b].a_new = a_old[b];
+        E->h_init[b].dt = 0.0;
+        any_init = any_init || init;
+    }
+    if (any_init) {
+        enqueue_load(c, E, E->h_init);
+        enqueue_solve_head(c, E);
+        enqueue_iterations(c, E, E->tune.max_outer);
+        ETRY(echeck(c, "ensemble init"));
+        int more = 0;
+        ETRY(finish_unconverged(c, E, &more));
+        enqueue_grav(c, E);
+        for (int b = 0; b < nbox; ++b)
+            if (E->h_init[b].active) E->slots[b].init_pending = 0;
+        extra += more;
+    }
+    for (int b = 0; b < nbox; ++b) {
+        const EnsSlot& s = E->slots[b];
+        const bool on = s.used && s.uploaded && !s.init_pending && a_old[b] > 0;
+        E->h_step[b].active = on ? 1 : 0;
+        E->h_step[b].a_old = a_old[b];
+        E->h_step[b].a_new = a_new[b];
+        E->h_step[b].dt = dt[b];
+    }
+    if (!E->exec_solve) ETRY(capture(c, E, &E->exec_solve, 0));
+    if (!E->exec_finish) ETRY(capture(c, E, &E->exec_finish, 1));
+    if (cudaGraphLaunch(E->exec_solve, c->stream) != cudaSuccess) return echeck(c, "ensemble solve graph");
+    c->launches += E->graph_launches_solve;
+    int more = 0;
+    ETRY(finish_unconverged(c, E, &more));
+    extra += more;
+    if (cudaGraphLaunch(E->exec_finish, c->stream) != cudaSuccess) return echeck(c, "ensemble finish graph");
+    c->launches += E->graph_launches_finish;
+    cudaEventRecord(ev1, c->stream);
+    if (cudaEventSynchronize(ev1) != cudaSuccess) return echeck(c, "ensemble step");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    ETRY(pull_state(c, E));
+    if (info) {
+        int mx = 0, inner = 0, boxes = 0;
+        for (int b = 0; b < nbox; ++b)
+            if (E->slots[b].used && E->h_state[b].active) {
+                mx = std::max(mx, E->h_state[b].outer);
+                inner = std::max(inner, E->h_state[b].inner);
+                ++boxes;
+            }
+        info->boxes = boxes;
+        info->max_outer_used = mx;
+        info->max_inner_used = inner;
+        info->fallback_iters = extra;
+        info->launches = (int)(c->launches - launches0);
+        info->ms = ms;
+    }
+    return NYXPM_OK;
+}
+
+}  // extern "C"

@@ -103,3 +103,26 @@ def test_mixed_deposit_conserves_mass_and_is_deterministic(ctx):
     r2 = b.deposit()
     assert np.array_equal(r1, r2)
     assert r1.sum() * (1.0 / n) ** 3 == pytest.approx(ic.mass * len(ic.pos), rel=1e-5)
+
+
+def test_mixed_drift_rebinning_at_cell_origin(ctx):
+    """A particle at a cell origin drifting back by a sub-ulp distance stays at
+    (almost) the same position: its FP32 offset rounds up to 1 and must move it
+    to the next cell's origin, not one cell back."""
+    n, L = 16, 1.0
+    idx = np.arange(n)
+    Z, Y, X = np.meshgrid(idx, idx, idx, indexing="ij")
+    pos = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1) * (L / n)   # cell origins: offset 0
+    vel = np.zeros_like(pos)
+    b = Box(ctx, n, L, len(pos), precision="mixed")
+    mass = 1e9
+    a, dt = 0.5, 1e-6
+    # drift in cells = dt / a * v / dx = -1e-9
+    vel[:, 0] = -1e-9 * a * (L / n) / dt
+    b.upload(pos, vel, mass)
+    b.init_field(a)                        # uniform lattice: g = 0
+    assert np.abs(b.grav_vector()).max() < 1e-6 * mass
+    b.kick_drift(dt, a, a)
+    gpos, _ = b.download()
+    err = np.abs(min_image(gpos - pos, L)).max() / (L / n)
+    assert err < 1e-6, err

@@ -42,12 +42,18 @@ def parse():
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-requests", type=int, default=0,
+                    help="requests in the serving stream (0: as many as ~60 s at 80%% load, "
+                         "at most the configuration's 2000)")
+    ap.add_argument("--ensemble-boxes", type=int, default=256)
     ap.add_argument("--quick", action="store_true",
                     help="headline timing only (no reuse-field pass, e2e or CPU baseline); "
                          "the command the ncu captures run")
     a = ap.parse_args()
     if a.quick:
-        a.no_cpu_baseline = a.no_e2e = a.no_reuse = True
+        a.no_cpu_baseline = a.no_e2e = a.no_reuse = a.no_ensemble = a.no_serving = True
     else:
         a.no_reuse = False
     return a
@@ -225,6 +231,156 @@ def oracle_steps(ic, sched, n, max_seconds, pm=None):
         if secs >= max_seconds:
             break
     return done, secs, O.num_threads(), pm
+
+
+# ---------------------------------------------------------------------------
+# ensemble and serving forms
+# ---------------------------------------------------------------------------
+def _ic_worker(args):
+    from nyx_gb300.ics import zeldovich_ics
+    n, L, slope, seed, a, frac = args
+    ic = zeldovich_ics(n, L, slope, seed, a, rms_disp_cells=0.2, fraction=frac)
+    return ic.pos, ic.vel, ic.mass
+
+
+def make_ics(jobs):
+    """Seeded ICs for many boxes, generated by a spawn process pool (host FFTs)."""
+    import multiprocessing as mp
+    procs = max(1, min(len(jobs), (os.cpu_count() or 2) - 2))
+    with mp.get_context("spawn").Pool(procs) as pool:
+        return pool.map(_ic_worker, jobs, chunksize=1)
+
+
+def plain_step_ms(ctx, n, frac, cache):
+    """Device ms of one plain FP64 step (reference schedule) of an n^3 box, early a."""
+    key = (n, frac)
+    if key in cache:
+        return cache[key]
+    import torch
+    from nyx_gb300.ics import zeldovich_ics
+    from nyx_gb300.pm import Box
+    ic = zeldovich_ics(n, 1.0, -2.0, 99, A_START, fraction=frac)
+    box = Box(ctx, n, 1.0, len(ic.pos))
+    box.upload(ic.pos, ic.vel, ic.mass)
+    sched = ctx.step_schedule(A_START, A_START + 0.009 * 3, 3)
+    box.step(*sched[0])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for a0, a1, dt in sched[1:]:
+        box.step(a0, a1, dt)
+    torch.cuda.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0) / 2
+    box.close()
+    cache[key] = ms
+    return ms
+
+
+def run_ensemble_form(ctx, nboxes, steps=20):
+    """Batched ensemble: 256 boxes of {32..128}^3, particles = cells x {0.5, 1},
+    slopes in [-2.5, -1.5], a 0.02 -> 0.2 in 20 steps, mixed precision, one
+    persistent launch per stage, captured step graphs, autotuned shapes."""
+    import numpy as np
+    from nyx_gb300 import autotune
+    from nyx_gb300.ensemble import Ensemble, ensemble_workload
+    specs = ensemble_workload(nboxes, seed=4)
+    t0 = time.perf_counter()
+    ics = make_ics([(s.n, s.L, s.slope, s.seed, A_START, s.fraction) for s in specs])
+    t_ic = time.perf_counter() - t0
+    by_id = {id(s): ic for s, ic in zip(specs, ics)}
+    tune = autotune.tune(ctx, specs, cache_path=os.path.join(REPO, "nyx_gb300", "_tuning_cache.json"),
+                         ic_provider=lambda s: by_id[id(s)])
+    arena = int(sum(Ensemble.box_bytes(s.n, s.np) for s in specs) * 1.05) + (256 << 20)
+    ens = Ensemble(ctx, arena)
+    ens.set_tuning(**{k: tune[k] for k in ("deposit_tile", "smooth_rows", "inner_vcycles")})
+    slots = []
+    for s, (pos, vel, mass) in zip(specs, ics):
+        slot = ens.add(s.n, s.L, s.np)
+        ens.upload(slot, pos, vel, mass)
+        slots.append(slot)
+    sched = ctx.step_schedule(A_START, 0.2, steps)
+    total_ms, infos = 0.0, []
+    launches0 = ctx.launch_count()
+    for a0, a1, dt in sched:
+        info = ens.step({q: a0 for q in slots}, {q: a1 for q in slots}, {q: dt for q in slots})
+        total_ms += info["ms"]
+        infos.append(info)
+    launches = ctx.launch_count() - launches0
+    ens.close()
+    psteps = sum(s.np for s in specs) * steps
+    plain_cache = {}
+    plain_ms = sum(plain_step_ms(ctx, s.n, s.fraction, plain_cache) for s in specs) * steps
+    steady = [i["ms"] for i in infos[1:]]
+    return {
+        "boxes": nboxes, "steps": steps, "particles": int(sum(s.np for s in specs)),
+        "cells": int(sum(s.n ** 3 for s in specs)),
+        "size_mix": autotune.signature(specs),
+        "value": psteps / (total_ms / 1e3), "unit": UNIT,
+        "runs_per_s": nboxes / (total_ms / 1e3), "total_s": total_ms / 1e3,
+        "steady_ms_per_step": float(np.mean(steady)) if steady else None,
+        "first_step_ms_incl_initial_solve_and_capture": infos[0]["ms"],
+        "max_outer_iters": max(i["max_outer_used"] for i in infos),
+        "fallback_iters": sum(i["fallback_iters"] for i in infos),
+        "launches_per_step": launches / steps,
+        "tuning": {k: tune[k] for k in ("deposit_tile", "smooth_rows", "inner_vcycles")},
+        "tuning_cached": tune.get("cached", False),
+        "plain_fp64_one_at_a_time_s": plain_ms / 1e3,
+        "speedup_vs_plain_fp64": plain_ms / total_ms,
+        "ic_generation_s": t_ic,
+        "note": "plain FP64 time = sum over boxes of 20 x the measured per-step time of the "
+                "FP64 drop-in on a box of the same size (early-a ICs), one box at a time",
+    }
+
+
+def run_serving_form(ctx, nreq_arg, tuning=None, budget_gb=150.0):
+    """Serving: Poisson arrivals at ~80% of measured capacity, n in {32..192}^3
+    (weights 30/25/20/12/8/5 %), 10-40 steps, 150 GB HBM budget, continuous
+    batching; the same stream served one run at a time by the FP64 drop-in."""
+    import numpy as np
+    from nyx_gb300.serving import ContinuousBatchingServer, request_stream, serve_sequential, SIZES
+    # IC pool: 6 seeded ICs per size (distinct seeds and slopes); request r uses entry r mod 6
+    rng = np.random.default_rng(55)
+    jobs, keys = [], []
+    for n in SIZES:
+        for j in range(6):
+            jobs.append((n, 1.0, float(rng.uniform(-2.5, -1.5)), int(rng.integers(1, 2 ** 31 - 1)),
+                         0.02, 1.0))
+            keys.append((n, j))
+    pool = dict(zip(keys, make_ics(jobs)))
+
+    class IC:
+        def __init__(self, t):
+            self.pos, self.vel, self.mass = t
+
+    def provider(r):
+        return IC(pool[(r.n, r.rid % 6)])
+
+    budget = int(budget_gb * 1e9)
+    # capacity: a burst of requests all available at t = 0
+    burst = request_stream(200, 0.0, seed=6)
+    srv = ContinuousBatchingServer(ctx, budget, provider, tuning=tuning)
+    cap_stats = srv.serve(burst, realtime=False)
+    capacity = cap_stats.summary()["runs_per_s"]
+    rate = 0.8 * capacity
+    nreq = nreq_arg or int(min(2000, max(100, 60.0 * rate)))
+    reqs = request_stream(nreq, rate, seed=5)
+    st = srv.serve(reqs, realtime=True)
+    srv.close()
+    seq_n = min(len(reqs), 40)
+    seq = serve_sequential(ctx, reqs, provider, realtime=True, max_requests=seq_n)
+    s_sum, q_sum = st.summary(), seq.summary()
+    return {
+        "requests": nreq, "requests_in_config": 2000, "arrival_rate_per_s": rate,
+        "measured_capacity_runs_per_s": capacity, "budget_GB": budget_gb,
+        "runs_per_s": s_sum["runs_per_s"], "p50_latency_s": s_sum["p50_latency_s"],
+        "p99_latency_s": s_sum["p99_latency_s"], "max_concurrent_runs": s_sum["max_concurrent_runs"],
+        "peak_arena_GB": s_sum["peak_arena_GB"], "particle_steps_per_s": s_sum["particle_steps_per_s"],
+        "plain_fp64_one_at_a_time": {"requests": seq_n, "runs_per_s": q_sum["runs_per_s"],
+                                     "p50_latency_s": q_sum["p50_latency_s"],
+                                     "p99_latency_s": q_sum["p99_latency_s"]},
+        "speedup_runs_per_s": (s_sum["runs_per_s"] / q_sum["runs_per_s"]) if q_sum["runs_per_s"] else None,
+        "note": "ICs from a pool of 6 seeded ICs per size; the FP64 server takes the first "
+                f"{seq_n} requests of the same stream (its queue grows without bound at this rate)",
+    }
 
 
 def run_reference(args):
@@ -435,6 +591,14 @@ def run_ours(args):
                        "d2h_bytes_per_step": int(hpos.numel() * 8 + hvel.numel() * 8),
                        "ms_per_step": ms_e / K, "wall_ms_per_step": 1e3 * wall / K,
                        "api": "nyxpm_box_upload + nyxpm_step + nyxpm_box_download per step"}
+
+    # ---- batched ensemble and continuous-batching serving (rank 0, N = 1) ----
+    tuning = None
+    if rank == 0 and ws == 1 and not args.no_ensemble:
+        line["ensemble"] = run_ensemble_form(ctx, args.ensemble_boxes)
+        tuning = line["ensemble"]["tuning"]
+    if rank == 0 and ws == 1 and not args.no_serving:
+        line["serving"] = run_serving_form(ctx, args.serving_requests, tuning)
 
     # ---- CPU baseline: the oracle on a bounded sample, rank 0 at N=1 ----
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

@@ -56,8 +56,10 @@ def _sample(specs, max_boxes):
 
 
 def tune(ctx, specs, a_start=0.02, da=0.009, steps=2, max_boxes=48, cache_path=None,
-         ics=None, verbose=False):
-    """Return the best nyxpm_tuning values (dict) for this ensemble mix."""
+         ic_provider=None, verbose=False):
+    """Return the best nyxpm_tuning values (dict) for this ensemble mix.
+    ic_provider(spec) -> (pos, vel, mass) supplies the ICs of a sampled box
+    (default: generate them)."""
     key = f"{_gpu_name(ctx)}|{signature(specs)}"
     cache = {}
     if cache_path and os.path.exists(cache_path):
@@ -73,9 +75,13 @@ def tune(ctx, specs, a_start=0.02, da=0.009, steps=2, max_boxes=48, cache_path=N
     ens = Ensemble(ctx, arena)
     slots = []
     for s in sample:
-        ic = ics[id(s)] if ics and id(s) in ics else box_ics(s, a_start)
+        if ic_provider is not None:
+            pos, vel, mass = ic_provider(s)
+        else:
+            ic = box_ics(s, a_start)
+            pos, vel, mass = ic.pos, ic.vel, ic.mass
         slot = ens.add(s.n, s.L, s.np)
-        ens.upload(slot, ic.pos, ic.vel, ic.mass)
+        ens.upload(slot, pos, vel, mass)
         slots.append(slot)
     best = ens.tuning()
     a = [a_start]

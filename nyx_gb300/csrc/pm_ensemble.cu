@@ -118,19 +118,6 @@ __device__ __forceinline__ int key_frac(int ci, float o, int n, float* f)
     return ci;
 }
 
-__device__ __forceinline__ void to_cell(double x, double dxi, int n, int* i, float* o)
-{
-    const double l = x * dxi;
-    double fl = floor(l);
-    float f = (float)(l - fl);
-    if (f >= 1.0f) {
-        f = 0.0f;
-        fl += 1.0;
-    }
-    *i = wrapi((int)fl, n);
-    *o = f;
-}
-
 // ---------------------------------------------------------------------------
 // step scalars
 // ---------------------------------------------------------------------------

@@ -238,6 +238,29 @@ nyxpm_status nyxpm_ensemble_get_tuning(nyxpm_ctx* ctx, nyxpm_ensemble* ens, nyxp
 nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* ctx, nyxpm_ensemble* ens, const double* a_old,
                                  const double* a_new, const double* dt, nyxpm_ensemble_info* info);
 
+/* ---- allocation-free deposit ----------------------------------------------------- */
+
+/* The CIC mass density of np particles of equal mass that are already in device
+ * memory (positions as three device arrays x, y, z in [0, L) up to one cell
+ * outside), written to the caller's device array rho (n^3 doubles, x fastest),
+ * on `stream` (a cudaStream_t; NULL is the default stream).  No counterpart in
+ * the reference.  For callers that cannot allocate device memory themselves or
+ * let a library do it -- a host code whose device memory is owned by its own
+ * arena (an AMReX build reserves most of the GPU at start-up), where an extra
+ * cudaMalloc can fail or fragment that arena.  This call allocates nothing: the
+ * counting-sort scratch is a file-scope device array of about 10 MiB that every
+ * GPU loading this library holds until the process exits.  Limits: n <= 64 and
+ * np <= 262,144; larger problems return NYXPM_INVALID_ARG (use nyxpm_deposit).
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be ordered by the caller.  The
+ * result equals nyxpm_deposit's for the same particles in the same order, bit
+ * for bit.  errbuf (may be NULL) receives a message on failure. */
+nyxpm_status nyxpm_deposit_noalloc(const double* x, const double* y, const double* z, int64_t np,
+                                   double mass, int n, double L, double* rho, void* stream,
+                                   char* errbuf, size_t errlen);
+
 /* ---- measurement ------------------------------------------------------------- */
 
 #define NYXPM_NUM_STAGES 12

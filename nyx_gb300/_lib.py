@@ -34,7 +34,7 @@ EXPORTS = [
     "nyxpm_ensemble_arena_used", "nyxpm_ensemble_add", "nyxpm_ensemble_remove",
     "nyxpm_ensemble_upload", "nyxpm_ensemble_download", "nyxpm_ensemble_get_phi",
     "nyxpm_ensemble_grav_vector", "nyxpm_ensemble_set_tuning", "nyxpm_ensemble_get_tuning",
-    "nyxpm_ensemble_step",
+    "nyxpm_ensemble_step", "nyxpm_deposit_noalloc",
 ]
 
 
@@ -169,5 +169,7 @@ def load(path: str | None = None):
     L.nyxpm_ensemble_set_tuning.argtypes = [vp, vp, C.POINTER(Tuning)]
     L.nyxpm_ensemble_get_tuning.argtypes = [vp, vp, C.POINTER(Tuning)]
     L.nyxpm_ensemble_step.argtypes = [vp, vp, dp, dp, dp, C.POINTER(EnsembleInfo)]
+    L.nyxpm_deposit_noalloc.argtypes = [vp, vp, vp, i64, d, C.c_int, d, vp, vp, C.c_char_p,
+                                        C.c_size_t]
     _lib = L
     return L

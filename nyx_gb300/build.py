@@ -29,6 +29,7 @@ UNITS = {
     "pm_multigrid.cu": ["--fmad=false"],
     "pm_mixed.cu": [],
     "pm_ensemble.cu": [],
+    "pm_noalloc.cu": ["--fmad=false"],
 }
 
 

@@ -48,14 +48,35 @@ def parse():
                     help="requests in the serving stream (0: as many as ~60 s at 80%% load, "
                          "at most the configuration's 2000)")
     ap.add_argument("--ensemble-boxes", type=int, default=256)
+    ap.add_argument("--ensemble-only", action="store_true",
+                    help="run the batched-ensemble form alone and print its object (the command "
+                         "the ensemble's ncu captures run)")
+    ap.add_argument("--ensemble-steps", type=int, default=20)
+    ap.add_argument("--tuning", type=str, default="",
+                    help="deposit_tile,smooth_rows,inner_vcycles for the ensemble instead of "
+                         "the autotuner's choice")
     ap.add_argument("--quick", action="store_true",
                     help="headline timing only (no reuse-field pass, e2e or CPU baseline); "
                          "the command the ncu captures run")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="mixed-precision accuracy report instead of the timing line: 512^3 "
+                         "particles, P(k)~k^-2.5, 50 steps; relative L2 of rho, phi, g, x, v "
+                         "of the mixed form against the FP64 form at steps 1, 10 and 50")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
+                    help="with --quick: the form the headline box uses (profiling the mixed "
+                         "kernels); the default run always times FP64 first")
+    ap.add_argument("--fraction", type=float, default=1.0,
+                    help="with --quick: particles per cell (profiling the grid kernels of a "
+                         "larger grid within a few GB)")
+    ap.add_argument("--accuracy-n", type=int, default=512)
+    ap.add_argument("--accuracy-steps", type=str, default="1,10,50")
     a = ap.parse_args()
     if a.quick:
         a.no_cpu_baseline = a.no_e2e = a.no_reuse = a.no_ensemble = a.no_serving = True
     else:
         a.no_reuse = False
+        if a.precision != "fp64" or a.fraction != 1.0:
+            ap.error("--precision and --fraction apply to --quick runs only")
     return a
 
 
@@ -127,6 +148,20 @@ def allreduce_sum(ws, v, device=None):
     t = torch.tensor([v], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def whole_job_rate(ws, units, ms, device=None):
+    """Replicas: every rank timed its own units over the same barrier-bracketed
+    region; the job rate is all ranks' units over the slowest rank's time.
+    Returns (units per second, max ms)."""
+    ms_max = allreduce_max(ws, ms, device)
+    total = allreduce_sum(ws, float(units), device)
+    return total / (ms_max / 1e3), ms_max
+
+
+def replica_seed(rank):
+    """Each replica advances its own box: the workload's seed 2, shifted by rank."""
+    return 2 + rank
 
 
 # ---------------------------------------------------------------------------
@@ -275,7 +310,7 @@ def plain_step_ms(ctx, n, frac, cache):
     return ms
 
 
-def run_ensemble_form(ctx, nboxes, steps=20):
+def run_ensemble_form(ctx, nboxes, steps=20, fixed_tuning=None):
     """Batched ensemble: 256 boxes of {32..128}^3, particles = cells x {0.5, 1},
     slopes in [-2.5, -1.5], a 0.02 -> 0.2 in 20 steps, mixed precision, one
     persistent launch per stage, captured step graphs, autotuned shapes."""
@@ -287,8 +322,12 @@ def run_ensemble_form(ctx, nboxes, steps=20):
     ics = make_ics([(s.n, s.L, s.slope, s.seed, A_START, s.fraction) for s in specs])
     t_ic = time.perf_counter() - t0
     by_id = {id(s): ic for s, ic in zip(specs, ics)}
-    tune = autotune.tune(ctx, specs, cache_path=os.path.join(REPO, "nyx_gb300", "_tuning_cache.json"),
-                         ic_provider=lambda s: by_id[id(s)])
+    if fixed_tuning:
+        tune = dict(zip(("deposit_tile", "smooth_rows", "inner_vcycles"), fixed_tuning), cached=True)
+    else:
+        tune = autotune.tune(ctx, specs,
+                             cache_path=os.path.join(REPO, "nyx_gb300", "_tuning_cache.json"),
+                             ic_provider=lambda s: by_id[id(s)])
     arena = int(sum(Ensemble.box_bytes(s.n, s.np) for s in specs) * 1.05) + (256 << 20)
     ens = Ensemble(ctx, arena)
     ens.set_tuning(**{k: tune[k] for k in ("deposit_tile", "smooth_rows", "inner_vcycles")})
@@ -432,12 +471,13 @@ def run_ours(args):
 
     n = args.n
     W, K = args.warmup, args.steps
-    ic = zeldovich_ics(n, 1.0, -2.0, 2 + rank, A_START, rms_disp_cells=0.2)
+    ic = zeldovich_ics(n, 1.0, -2.0, replica_seed(rank), A_START, rms_disp_cells=0.2,
+                       fraction=args.fraction)
     npart = len(ic.pos)
     ctx = Context(device=local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     sched = schedule(ctx, W + K)
-    box = Box(ctx, n, 1.0, npart)
+    box = Box(ctx, n, 1.0, npart, precision=args.precision)
     box.upload(ic.pos, ic.vel, ic.mass)
 
     # ---- device-resident run: warm-up, then K timed steps ----
@@ -463,9 +503,7 @@ def run_ours(args):
     ms = e0.elapsed_time(e1)
     prof = ctx.profile(reset=True)
     ctx.set_profiling(False)
-    ms_max = allreduce_max(ws, ms, torch.device("cuda", local))
-    total_units = allreduce_sum(ws, float(npart) * K, torch.device("cuda", local))
-    value = total_units / (ms_max / 1e3)
+    value, ms_max = whole_job_rate(ws, float(npart) * K, ms, torch.device("cuda", local))
 
     # ---- roofline of the dominant kernel ----
     stages = prof["stages"]
@@ -479,8 +517,9 @@ def run_ours(args):
         fs = prof["fine_smooth"]
         per_launch = fs["bytes"] / fs["launches"]
         avg_ms = fs["ms"] / fs["launches"]
-        kname = "k_gsrb (finest-level red-black half sweep)"
-        tr = traffic.get("k_gsrb_fine")
+        kname = ("k_gsrb (finest-level red-black half sweep)" if args.precision == "fp64" else
+                 "k_gsrb_f (finest-level FP32 red-black half sweep)")
+        tr = traffic.get("k_gsrb_fine") if args.precision == "fp64" else None
     else:
         st = stages[dom]
         per_launch = st["bytes"] / max(st["launches"], 1)
@@ -498,13 +537,18 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "data": "synthetic",
+        "dtype": "f64" if args.precision == "fp64" else "f32 (inside FP64 defect correction)",
         "config": workload_config(n, W, K),
         "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
         "stages": stage_rows,
         "vcycles_per_step": {"old_mean": float(np.mean([v[0] for v in vcycles])),
                              "new_mean": float(np.mean([v[1] for v in vcycles]))},
     }
+
+    if args.precision != "fp64" or args.fraction != 1.0:
+        line["config"].update(precision=args.precision, fraction=args.fraction,
+                              n_particles=npart, note="profiling run, not the headline workload")
 
     # ---- same workload with the old-time field reused (1 deposit + 1 solve per step) ----
     if not args.no_reuse:
@@ -539,6 +583,24 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
         ms_m = allreduce_max(ws, e0.elapsed_time(e1), torch.device("cuda", local))
+        # per-stage CUDA-event times of three more steps (outside the timed region)
+        a_last = sched[W + K - 1][1]
+        da = (A_END - A_START) / NSTEPS_CFG
+        ctx.set_profiling(True)
+        ctx.profile(reset=True)
+        for a0, a1, dt in ctx.step_schedule(a_last, a_last + 3 * da, 3):
+            bm.step(a0, a1, dt, reuse_field=True)
+        mprof = ctx.profile(reset=True)
+        ctx.set_profiling(False)
+        mstages = {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                       "GB/s": round(v["bytes"] / (v["ms"] * 1e6), 1) if v["ms"] > 0 else None}
+                   for k, v in mprof["stages"].items() if v["launches"]}
+        mfs = mprof["fine_smooth"]
+        mfine = ({"kernel": "k_gsrb_f (finest-level FP32 red-black half sweep)",
+                  "launches": mfs["launches"], "avg_launch_ms": mfs["ms"] / mfs["launches"],
+                  "algorithmic_bytes_per_launch": mfs["bytes"] / mfs["launches"],
+                  "achieved_GBs": round(mfs["bytes"] / (mfs["ms"] * 1e6), 1)}
+                 if mfs["launches"] else None)
         # force error of one mixed step against one FP64 step from the same state
         pos_m, vel_m = bm.download()
         box.upload(pos_m, vel_m, ic.mass)
@@ -558,8 +620,10 @@ def run_ours(args):
             "force_rel_l2_vs_fp64": float(np.linalg.norm(gmx - g64) / np.linalg.norm(g64)),
             "vel_rel_l2_vs_fp64": float(np.linalg.norm(vmx - v64) / np.linalg.norm(v64)),
             "pos_err_cells_rms": float(np.sqrt(np.mean(dpos ** 2))) * n,
-            "note": "one step from the same state at the last timed a; the FP64 form equals the "
-                    "FP64 oracle bitwise in the parity tests"}
+            "stages": mstages, "fine_smooth": mfine,
+            "note": "errors: one step from the same state at the last timed a (the FP64 form "
+                    "equals the FP64 oracle bitwise in the parity tests); stages: CUDA events "
+                    "of 3 further steps outside the timed region"}
         bm.close()
 
     # ---- end to end through the C ABI with pinned host buffers ----
@@ -595,7 +659,9 @@ def run_ours(args):
     # ---- batched ensemble and continuous-batching serving (rank 0, N = 1) ----
     tuning = None
     if rank == 0 and ws == 1 and not args.no_ensemble:
-        line["ensemble"] = run_ensemble_form(ctx, args.ensemble_boxes)
+        line["ensemble"] = run_ensemble_form(
+            ctx, args.ensemble_boxes, args.ensemble_steps,
+            [int(v) for v in args.tuning.split(",")] if args.tuning else None)
         tuning = line["ensemble"]["tuning"]
     if rank == 0 and ws == 1 and not args.no_serving:
         line["serving"] = run_serving_form(ctx, args.serving_requests, tuning)
@@ -617,8 +683,113 @@ def run_ours(args):
     return 0
 
 
+def run_accuracy(args):
+    """Mixed-precision accuracy on the 512^3 configuration (P(k) ~ k^-2.5, seed 3,
+    a 0.02 -> 0.5 in 50 equal-da steps, reference schedule).  The comparison is the
+    FP64 form, which equals the FP64 oracle bit for bit in the parity tests (the
+    512^3 first step included).  Two measures at each reported step k:
+      * one step: both forms take step k from the same FP64 state (the FP64
+        run's state after step k-1) -- the error one mixed step adds;
+      * free running: both forms run from the ICs to step k on their own -- the
+        accumulated difference of two trajectories of a chaotic system.
+    Positions are compared as displacements from the unperturbed lattice
+    (minimum image), so the lattice offset does not hide the error."""
+    import numpy as np
+    import torch
+    from nyx_gb300 import _lib
+    _lib.load()
+    from nyx_gb300.ics import zeldovich_ics
+    from nyx_gb300.pm import Box, Context
+
+    n, L = args.accuracy_n, 1.0
+    report_at = sorted({int(s) for s in args.accuracy_steps.split(",")})
+    nsteps = max(report_at)
+    t0 = time.perf_counter()
+    ic = zeldovich_ics(n, L, -2.5, 3, A_START, rms_disp_cells=0.2)
+    t_ic = time.perf_counter() - t0
+    npart = len(ic.pos)
+    ctx = Context(device=0)
+    sched = ctx.step_schedule(A_START, A_END, NSTEPS_CFG)[:nsteps]
+
+    def rel(a, b):
+        return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+    def mr(f):
+        return f - f.mean()
+
+    def minimg(d):
+        return (d + 0.5 * L) % L - 0.5 * L
+
+    def compare(bm, bf):
+        rho_m, rho_f = bm.deposit(), bf.deposit()
+        out = {"rho": rel(rho_m, rho_f), "phi": rel(mr(bm.get_phi()), mr(bf.get_phi())),
+               "g": rel(bm.grav_vector(), bf.grav_vector())}
+        pm_, vm_ = bm.download()
+        pf_, vf_ = bf.download()
+        disp = minimg(pf_ - ic.lattice)
+        out["x"] = float(np.linalg.norm(minimg(pm_ - pf_)) / np.linalg.norm(disp))
+        out["v"] = rel(vm_, vf_)
+        out["x_err_cells_max"] = float(np.abs(minimg(pm_ - pf_)).max() * n / L)
+        return out
+
+    free_f = Box(ctx, n, L, npart)
+    free_m = Box(ctx, n, L, npart, precision="mixed")
+    one_f = Box(ctx, n, L, npart)
+    one_m = Box(ctx, n, L, npart, precision="mixed")
+    for b in (free_f, free_m):
+        b.upload(ic.pos, ic.vel, ic.mass)
+    rows = []
+    vcyc = []
+    for k, (a0, a1, dt) in enumerate(sched, start=1):
+        if k in report_at:
+            pos, vel = free_f.download()
+            for b in (one_f, one_m):
+                b.upload(pos, vel, ic.mass)
+            one_f.step(a0, a1, dt)
+            mi = one_m.step(a0, a1, dt)
+            row = {"step": k, "a": a1, "one_step": compare(one_m, one_f)}
+            row["mixed_outer_iters"] = mi["new_solve"]["vcycles"]
+            row["mixed_inner_vcycles"] = mi["new_solve"]["inner_vcycles"]
+        fi = free_f.step(a0, a1, dt)
+        free_m.step(a0, a1, dt)
+        vcyc.append(fi["new_solve"]["vcycles"])
+        if k in report_at:
+            row["free_running"] = compare(free_m, free_f)
+            row["fp64_vcycles"] = fi["new_solve"]["vcycles"]
+            rows.append(row)
+            print(json.dumps(row), file=sys.stderr, flush=True)
+    for b in (free_f, free_m, one_f, one_m):
+        b.close()
+    ctx.close()
+    line = {"report": "mixed-precision accuracy vs FP64", "n_grid": n, "n_particles": npart,
+            "workload": f"{n}^3 particles on a {n}^3 periodic grid, Zel'dovich ICs P(k)~k^-2.5 "
+                        f"seed 3, a {A_START}->{A_END} in {NSTEPS_CFG} equal-da steps, reference "
+                        f"schedule, MG rel tol 1e-10",
+            "target": "force (g) relative L2 <= 1e-6", "rows": rows,
+            "ic_seconds": t_ic, "seconds": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ensemble_only(args):
+    import torch
+    from nyx_gb300 import _lib
+    _lib.load()
+    from nyx_gb300.pm import Context
+    ctx = Context(device=0)
+    fixed = [int(v) for v in args.tuning.split(",")] if args.tuning else None
+    out = run_ensemble_form(ctx, args.ensemble_boxes, args.ensemble_steps, fixed)
+    ctx.close()
+    print(json.dumps({"ensemble": out}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.accuracy:
+        return run_accuracy(args)
+    if args.ensemble_only:
+        return run_ensemble_only(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

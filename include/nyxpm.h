@@ -184,6 +184,46 @@ double nyxpm_integrate_a(const nyxpm_params* p, double a_old, double dt);
 /* Nyx::integrate_comoving_a_to_a, comoving.cpp:74-130 (dt_window = search window). */
 double nyxpm_dt_for_da(const nyxpm_params* p, double a_old, double a_value, double dt_window);
 
+/* ---- time-step control ---------------------------------------------------------- */
+
+/* The inputs of Nyx's level-0 time-step choice (names of the reference's
+ * parameters; defaults from nyxpm_default_dt_params are the reference's). */
+typedef struct {
+    double cfl;                   /* particles.cfl (NyxParticles.cpp:152), 0.5 */
+    double change_max;            /* nyx.change_max (Nyx.cpp:83), 1.1; dt <= change_max * dt_old */
+    double relative_max_change_a; /* nyx.relative_max_change_a (comoving.cpp:10), 0.01 */
+    double absolute_max_change_a; /* nyx.absolute_max_change_a (comoving.cpp:11), -1 = off */
+    double final_a;               /* nyx.final_a (comoving.cpp:8), -1 = off */
+    double stop_time;             /* stop_time, -1 = off */
+    double dt_binpow;             /* nyx.dt_binpow (comoving.cpp:12), -1 = off */
+} nyxpm_dt_params;
+
+void nyxpm_default_dt_params(nyxpm_dt_params* dp);
+
+/* Particle time-step limit, replaces NyxParticleContainer::estTimestep
+ * (Source/Particle/NyxParticleContainer.H:329-465) as called from
+ * Nyx::particle_est_time_step (NyxParticles.cpp:1027-1067): the minimum over
+ * particles of cfl / max_d(|v_d| / (a dx)) and 1 / sqrt(|g| / dx), g the
+ * box's current gravity vector at the particle's cell.  *dt = 1e50 when no
+ * particle limits it, -1e50 when the box has no particles.  One GPU reduction;
+ * the box must hold a field (after a solve, a step or nyxpm_set_phi). */
+nyxpm_status nyxpm_est_time_step(nyxpm_ctx* ctx, nyxpm_box* box, double cfl, double a, double* dt);
+
+/* Nyx::comoving_est_time_step (Source/Driver/comoving.cpp:353-483) from scale
+ * factor a: limits estdt by how fast a may change (estdt_comoving_a and its
+ * helpers, :191-350).  Host FP64.  NYXPM_INVALID_ARG where the reference
+ * aborts (a > final_a, no convergence in 100 iterations). */
+nyxpm_status nyxpm_comoving_est_dt(const nyxpm_params* p, double a, double estdt,
+                                   const nyxpm_dt_params* dp, double* dt);
+
+/* Nyx::computeNewDt at level 0 without subcycling (Source/Driver/Nyx.cpp:1023-1208):
+ * est_time_step (particles, then the a-change limit; Nyx.cpp:912-1020), then
+ * dt <= change_max * dt_old (skipped when dt_old <= 0, the first step), then
+ * the stop_time clip; *a_new = a advanced by the chosen dt. */
+nyxpm_status nyxpm_compute_new_dt(nyxpm_ctx* ctx, nyxpm_box* box, const nyxpm_dt_params* dp,
+                                  double time, double a, double dt_old, double* dt_new,
+                                  double* a_new);
+
 /* ---- ensembles and serving ------------------------------------------------------ */
 
 /* An ensemble holds many independent periodic boxes of uneven sizes in the

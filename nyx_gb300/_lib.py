@@ -35,6 +35,8 @@ EXPORTS = [
     "nyxpm_ensemble_upload", "nyxpm_ensemble_download", "nyxpm_ensemble_get_phi",
     "nyxpm_ensemble_grav_vector", "nyxpm_ensemble_set_tuning", "nyxpm_ensemble_get_tuning",
     "nyxpm_ensemble_step", "nyxpm_deposit_noalloc",
+    "nyxpm_default_dt_params", "nyxpm_est_time_step", "nyxpm_comoving_est_dt",
+    "nyxpm_compute_new_dt",
 ]
 
 
@@ -52,6 +54,18 @@ class Params(C.Structure):
         ("nu2", C.c_int),
         ("verbose", C.c_int),
         ("mixed_inner_vcycles", C.c_int),
+    ]
+
+
+class DtParams(C.Structure):
+    _fields_ = [
+        ("cfl", C.c_double),
+        ("change_max", C.c_double),
+        ("relative_max_change_a", C.c_double),
+        ("absolute_max_change_a", C.c_double),
+        ("final_a", C.c_double),
+        ("stop_time", C.c_double),
+        ("dt_binpow", C.c_double),
     ]
 
 
@@ -149,6 +163,12 @@ def load(path: str | None = None):
     L.nyxpm_integrate_a.restype = d
     L.nyxpm_dt_for_da.argtypes = [C.POINTER(Params), d, d, d]
     L.nyxpm_dt_for_da.restype = d
+    L.nyxpm_default_dt_params.argtypes = [C.POINTER(DtParams)]
+    L.nyxpm_default_dt_params.restype = None
+    L.nyxpm_est_time_step.argtypes = [vp, vp, d, d, C.POINTER(d)]
+    L.nyxpm_comoving_est_dt.argtypes = [C.POINTER(Params), d, d, C.POINTER(DtParams), C.POINTER(d)]
+    L.nyxpm_compute_new_dt.argtypes = [vp, vp, C.POINTER(DtParams), d, d, d, C.POINTER(d),
+                                       C.POINTER(d)]
     L.nyxpm_set_profiling.argtypes = [vp, C.c_int]
     L.nyxpm_get_profile.argtypes = [vp, C.POINTER(Profile), C.c_int]
     L.nyxpm_launch_count.argtypes = [vp]

@@ -254,11 +254,11 @@ size_t nyxpm_box_bytes(int n, int64_t np, nyxpm_precision prec)
     double per_particle, per_cell;
     if (prec == NYXPM_MIXED) {
         // cell + 3 offsets + 3 vel + mass + id, double-buffered; key, perm; staging
-        per_particle = 2.0 * (4 + 12 + 12 + 4 + 4) + 8 + 56;
-        per_cell = 4 + 4 + 4 + 8 + 24 + 8 + 12 + 16.0 * 8 / 7 + 8.0 * 8 / 7;
+        per_particle = 2.0 * (4 + 12 + 12 + 4 + 4) + 8 + 56 + 2;
+        per_cell = 4 + 4 + 4 + 4 + 8 + 24 + 8 + 12 + 16.0 * 8 / 7 + 8.0 * 8 / 7;
     } else {
-        per_particle = 2.0 * (7 * 8 + 4) + 8 + 56;
-        per_cell = 4 + 4 + 8 + 24 + 8 + 16.0 * 8 / 7;
+        per_particle = 2.0 * (7 * 8 + 4) + 8 + 56 + 2;
+        per_cell = 4 + 4 + 4 + 8 + 24 + 8 + 64 + 16.0 * 8 / 7;
     }
     return (size_t)(per_particle * (double)np + per_cell * nc + 8.0 * n * n + (1 << 20));
 }
@@ -301,6 +301,7 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
         ALLOC(b->vx, np); ALLOC(b->vy, np); ALLOC(b->vz, np); ALLOC(b->m, np); ALLOC(b->id, np);
         ALLOC(b->x2, np); ALLOC(b->y2, np); ALLOC(b->z2, np);
         ALLOC(b->vx2, np); ALLOC(b->vy2, np); ALLOC(b->vz2, np); ALLOC(b->m2, np); ALLOC(b->id2, np);
+        ALLOC(b->key_part, 8 * nc);
     } else {
         ALLOC(b->cell, np); ALLOC(b->ox, np); ALLOC(b->oy, np); ALLOC(b->oz, np);
         ALLOC(b->fvx, np); ALLOC(b->fvy, np); ALLOC(b->fvz, np); ALLOC(b->fm, np); ALLOC(b->id, np);
@@ -317,6 +318,8 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
     ALLOC(b->tile_sums, b->ntiles);
     ALLOC(b->long_list, nc);
     ALLOC(b->long_count, 1);
+    ALLOC(b->heavy_part, 8 * (size_t)(np / (kDepositLanes + 1) + 1));
+    ALLOC(b->key_slot, nc);
     ALLOC(b->rho, nc);
     ALLOC(b->g, 3 * nc);
     ALLOC(b->nat, nc);
@@ -638,6 +641,157 @@ double nyxpm_dt_for_da(const nyxpm_params* p, double a_old, double a_value, doub
                    (end_a - start_a) * Dt;
     }
     return dt;
+}
+
+// ---------------------------------------------------------------------------
+// time-step control
+// ---------------------------------------------------------------------------
+void nyxpm_default_dt_params(nyxpm_dt_params* dp)
+{
+    if (!dp) return;
+    dp->cfl = 0.5;
+    dp->change_max = 1.1;
+    dp->relative_max_change_a = 0.01;
+    dp->absolute_max_change_a = -1.0;
+    dp->final_a = -1.0;
+    dp->stop_time = -1.0;
+    dp->dt_binpow = -1.0;
+}
+
+nyxpm_status nyxpm_est_time_step(nyxpm_ctx* c, nyxpm_box* b, double cfl, double a, double* dt)
+{
+    CHECK_BOX(c, b);
+    if (!dt) return fail(c, NYXPM_INVALID_ARG, "null dt");
+    if (!(cfl > 0) || !(a > 0)) return fail(c, NYXPM_INVALID_ARG, "cfl and a must be positive");
+    if (!b->uploaded || b->np == 0) {
+        *dt = -1.0e50;  // no particles at this level (NyxParticleContainer.H:455)
+        return NYXPM_OK;
+    }
+    if (!b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field: solve, step or set phi first");
+    TRY(b->prec == NYXPM_MIXED ? mixed_est_dt(*c, *b, cfl, a) : launch_est_dt(*c, *b, cfl, a));
+    cudaMemcpyAsync(b->h_norms + 3, b->norms + 3, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                    c->stream);
+    TRY(check_launch(*c, "time-step readback"));
+    TRY(nyxpm_synchronize(c));
+    const unsigned long long bits = ~b->h_norms[3];
+    std::memcpy(dt, &bits, sizeof(double));
+    return NYXPM_OK;
+}
+
+namespace {
+
+// est_maxdt_comoving_a (comoving.cpp:191-215): at most a 5% change of a per
+// forward-Euler step
+double cap_dt_by_hubble(const nyxpm_params* p, double a, double dt)
+{
+    const double H0 = p->comoving_h * 100.0;
+    if (H0 == 0.0) return dt;
+    const double OmL = 1.0 - p->comoving_OmM - p->comoving_OmR;
+    const double a3 = a * a * a;
+    const double lim = 0.05 / H0 / std::sqrt(p->comoving_OmM / a3 + p->comoving_OmR / (a3 * a) + OmL);
+    return std::min(dt, lim);
+}
+
+// est_lindt_comoving_a (comoving.cpp:217-237)
+double linear_dt_guess(const nyxpm_params* p, double a_from, double a_to, double dt)
+{
+    const double H0 = p->comoving_h * 100.0;
+    if (H0 == 0.0) return dt;
+    const double s = std::pow(0.75, 2.0 / 3.0);
+    return (std::pow(a_to / s, 0.75) - std::pow(a_from / s, 0.75)) / H0;
+}
+
+}  // namespace
+
+nyxpm_status nyxpm_comoving_est_dt(const nyxpm_params* p, double a, double estdt,
+                                   const nyxpm_dt_params* dp, double* out)
+{
+    if (!p || !dp || !out) return NYXPM_INVALID_ARG;
+    if (p->comoving_h == 0.0) {
+        *out = estdt;
+        return NYXPM_OK;
+    }
+    // estdt_comoving_a (comoving.cpp:239-280)
+    double dt = estdt, a_next;
+    if (dp->absolute_max_change_a <= 0.0) {
+        dt = cap_dt_by_hubble(p, a, dt);
+        a_next = nyxpm_integrate_a(p, a, dt);
+        // enforce_percent_change (comoving.cpp:282-317)
+        if (((a_next - a) / a) / dp->relative_max_change_a > 1.0) {
+            for (int it = 1; it <= 100; ++it) {
+                const double factor = ((a_next - a) / a) / dp->relative_max_change_a;
+                if (factor > 1.0) {
+                    dt = (1.0 / factor) * dt * 0.99;
+                    a_next = nyxpm_integrate_a(p, a, dt);
+                } else if (it < 100) {
+                    a_next = nyxpm_integrate_a(p, a, dt);
+                    break;
+                } else {
+                    return NYXPM_INVALID_ARG;  // the reference aborts here
+                }
+            }
+        }
+    } else {
+        a_next = a + dp->absolute_max_change_a;
+        dt = linear_dt_guess(p, a, a_next, dt);
+        dt = cap_dt_by_hubble(p, a, dt);
+        dt = nyxpm_dt_for_da(p, a, a_next, dt);
+    }
+    // enforce_final_a (comoving.cpp:319-350)
+    if (dp->final_a > 0.0) {
+        if (a > dp->final_a) return NYXPM_INVALID_ARG;
+        if (a_next > dp->final_a) {
+            for (int it = 1; it <= 100; ++it) {
+                if (a_next > dp->final_a + 1.0e-10 || a_next < dp->final_a) {
+                    dt = dt * ((dp->final_a - a) / (a_next - a));
+                    a_next = nyxpm_integrate_a(p, a, dt);
+                } else if (it < 100) {
+                    break;
+                } else {
+                    return NYXPM_INVALID_ARG;  // the reference aborts here
+                }
+            }
+        }
+    }
+    // comoving_est_time_step (comoving.cpp:353-483): power-of-two binning or min
+    if (dp->dt_binpow >= 0) {
+        if (estdt >= dt) {
+            estdt = dt;
+        } else {
+            double frac = 0.5;
+            for (; frac >= 0.0625; frac *= 0.5)
+                if (estdt > frac * dt) break;
+            estdt = frac >= 0.0625 ? frac * dt : dt * std::pow(2.0, -std::ceil(std::log2(dt / estdt)));
+        }
+    } else {
+        estdt = std::min(estdt, dt);
+    }
+    *out = estdt;
+    return NYXPM_OK;
+}
+
+nyxpm_status nyxpm_compute_new_dt(nyxpm_ctx* c, nyxpm_box* b, const nyxpm_dt_params* dp,
+                                  double time, double a, double dt_old, double* dt_new,
+                                  double* a_new)
+{
+    CHECK_BOX(c, b);
+    if (!dp || !dt_new) return fail(c, NYXPM_INVALID_ARG, "null argument");
+    // Nyx::est_time_step (Nyx.cpp:912-1020): particles, then the a-change limit
+    double est = 1.0e200;
+    double part = 0;
+    TRY(nyxpm_est_time_step(c, b, dp->cfl, a, &part));
+    if (part > 0) est = std::min(est, part);
+    if (nyxpm_comoving_est_dt(&c->p, a, est, dp, &est) != NYXPM_OK)
+        return fail(c, NYXPM_INVALID_ARG, "comoving time-step limit did not converge or a > final_a");
+    // computeNewDt (Nyx.cpp:1023-1208), one level, no subcycling
+    if (dt_old > 0) est = std::min(est, dp->change_max * dt_old);
+    if (dp->stop_time >= 0.0) {
+        const double eps = 0.001 * est;
+        if (time + est > dp->stop_time - eps) est = dp->stop_time - time;
+    }
+    *dt_new = est;
+    if (a_new) *a_new = nyxpm_integrate_a(&c->p, a, est);
+    return NYXPM_OK;
 }
 
 nyxpm_status nyxpm_set_profiling(nyxpm_ctx* c, int on)

@@ -23,6 +23,11 @@
 namespace nyxpm {
 
 constexpr int kMaxBottom = 8;          // largest coarsest-grid edge (solved exactly)
+// A deposit key with more particles than this is summed by a whole warp in
+// lane-strided partials (lane l: particles l, l+32, ...) and an xor butterfly;
+// shorter keys are summed in order by one thread.  The sort queues exactly
+// these keys (segments longer than a warp) in long_list.
+constexpr int kDepositLanes = 32;
 constexpr int kCoarsenAbove = 4;       // levels halve while the edge is even and above this
 
 // |v| as ordered bits: for non-negative doubles the bit patterns order like the
@@ -205,6 +210,11 @@ struct Box {
     int ntiles = 0;
     int* long_list = nullptr;          // keys of segments longer than a warp
     int* long_count = nullptr;
+    // deposit partials of the keys in long_list (8 corners each), and the slot
+    // of each such key (read only for keys longer than kDepositLanes)
+    double* heavy_part = nullptr;
+    int* key_slot = nullptr;
+    double* key_part = nullptr;        // FP64: 8 n^3 per-key corner sums (two-pass deposit)
 
     // fields
     double* rho = nullptr;             // n^3
@@ -261,6 +271,9 @@ nyxpm_status launch_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur,
                          int do_wrap);
 
 nyxpm_status launch_make_rhs(Ctx& c, Box& b, double a);
+// particle time-step limit into norms[3] (as ~bits of the minimum dt)
+nyxpm_status launch_est_dt(Ctx& c, Box& b, double cfl, double a);
+nyxpm_status mixed_est_dt(Ctx& c, Box& b, double cfl, double a);
 double beta_scale(const Box& b);  // (h*h)/6 of level 0: rhs -> smoother units
 nyxpm_status launch_zero_phi(Ctx& c, Box& b);
 nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info);

@@ -171,12 +171,76 @@ constexpr int kTx = 8, kTy = 8, kTz = 8;
 constexpr int kKx = kTx + 1, kKy = kTy + 1, kKz = kTz + 1;
 constexpr int kNKeys = kKx * kKy * kKz;
 
+// adds particle q's eight CIC weights (times its mass, if m) to s
+__device__ __forceinline__ void mx_add_weights(int q, int n, const int* __restrict__ cell,
+                                               const float* __restrict__ ox,
+                                               const float* __restrict__ oy,
+                                               const float* __restrict__ oz,
+                                               const float* __restrict__ m, float s[8])
+{
+    const int c = cell[q];
+    float fx, fy, fz;
+    key_frac(cell_i(c), ox[q], n, &fx);
+    key_frac(cell_j(c), oy[q], n, &fy);
+    key_frac(cell_k(c), oz[q], n, &fz);
+    const float sx[2] = {1.f - fx, fx};
+    const float sy[2] = {1.f - fy, fy};
+    const float sz[2] = {1.f - fz, fz};
+    const float mq = m ? m[q] : 1.f;
+#pragma unroll
+    for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+        for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+            for (int cx = 0; cx < 2; ++cx)
+                s[cx + 2 * cy + 4 * cz] += (sx[cx] * sy[cy]) * sz[cz] * mq;
+}
+
+// keys longer than a warp (the sort's long_list), one warp each: lane-strided
+// partials and an xor butterfly, as the FP64 deposit sums them
+__global__ void __launch_bounds__(256) k_mx_deposit_heavy(int n, const int* __restrict__ cell,
+                                                          const float* __restrict__ ox,
+                                                          const float* __restrict__ oy,
+                                                          const float* __restrict__ oz,
+                                                          const float* __restrict__ m,
+                                                          const int* __restrict__ start,
+                                                          const int* __restrict__ long_list,
+                                                          const int* __restrict__ long_count,
+                                                          int* key_slot, float* heavy_part)
+{
+    const int lane = threadIdx.x & 31;
+    const int total = *long_count;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < total; li += nwarps) {
+        const int K = long_list[li];
+        const int e = start[K + 1];
+        float s[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s[c] = 0.f;
+        for (int q = start[K] + lane; q < e; q += 32) mx_add_weights(q, n, cell, ox, oy, oz, m, s);
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) s[c] += __shfl_xor_sync(0xffffffffu, s[c], off);
+        if (lane < 8) {
+            float v = s[0];
+#pragma unroll
+            for (int c = 1; c < 8; ++c)
+                if (lane == c) v = s[c];
+            heavy_part[8LL * li + lane] = v;
+        }
+        if (lane == 0) key_slot[K] = li;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_mx_deposit(int n, float scale, const int* __restrict__ cell,
                                                     const float* __restrict__ ox,
                                                     const float* __restrict__ oy,
                                                     const float* __restrict__ oz,
                                                     const float* __restrict__ m,
-                                                    const int* __restrict__ start, float* rho)
+                                                    const int* __restrict__ start,
+                                                    const int* __restrict__ key_slot,
+                                                    const float* __restrict__ heavy_part, float* rho)
 {
     __shared__ float part[kNKeys * 8];
     const int i0 = blockIdx.x * kTx, j0 = blockIdx.y * kTy, k0 = blockIdx.z * kTz;
@@ -184,26 +248,15 @@ __global__ void __launch_bounds__(256) k_mx_deposit(int n, float scale, const in
         const int ki = kl % kKx, kj = (kl / kKx) % kKy, kk = kl / (kKx * kKy);
         const long long K = cidx(wrapi(i0 + ki, n), wrapi(j0 + kj, n), wrapi(k0 + kk, n), n);
         float s[8];
+        const int b0 = start[K], e = start[K + 1];
+        if (e - b0 > kDepositLanes) {
+            const float* hp = heavy_part + 8LL * key_slot[K];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) s[c] = 0.f;
-        const int e = start[K + 1];
-        for (int q = start[K]; q < e; ++q) {
-            const int c = cell[q];
-            float fx, fy, fz;
-            key_frac(cell_i(c), ox[q], n, &fx);
-            key_frac(cell_j(c), oy[q], n, &fy);
-            key_frac(cell_k(c), oz[q], n, &fz);
-            const float sx[2] = {1.f - fx, fx};
-            const float sy[2] = {1.f - fy, fy};
-            const float sz[2] = {1.f - fz, fz};
-            const float mq = m ? m[q] : 1.f;
+            for (int c = 0; c < 8; ++c) s[c] = hp[c];
+        } else {
 #pragma unroll
-            for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-                for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-                    for (int cx = 0; cx < 2; ++cx)
-                        s[cx + 2 * cy + 4 * cz] += (sx[cx] * sy[cy]) * sz[cz] * mq;
+            for (int c = 0; c < 8; ++c) s[c] = 0.f;
+            for (int q = b0; q < e; ++q) mx_add_weights(q, n, cell, ox, oy, oz, m, s);
         }
 #pragma unroll
         for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
@@ -403,6 +456,65 @@ __global__ void __launch_bounds__(256) k_gsrb_f(int n, int color, float* __restr
     const long long t = ((long long)j + (long long)n * k) * half + ih;
     const float s = nbr_sum_split<float>(other, n, half, ih, j, k, q);
     mine[t] = fmaf(s, kSixthF, -beta[t]);
+}
+
+// The same half sweep, four cells of a row per thread (one 16-byte load per
+// neighbour row) marching over kMarchZ consecutive planes: the row of the plane
+// above becomes the row of this plane and the one below it, so each plane
+// loads three neighbour rows (y-1, y+1, z+1), the right-hand side and one edge
+// value for the x neighbours.  The sums are the scalar kernel's, term for term.
+// Needs half % 4 == 0 (rows start on 16 bytes).
+constexpr int kMarchZ = 4;
+
+__global__ void __launch_bounds__(256) k_gsrb_f4(int n, int color, float* __restrict__ mine,
+                                                 const float* __restrict__ other,
+                                                 const float* __restrict__ beta)
+{
+    const int half = n >> 1, h4 = half >> 2;
+    const int t4 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k0 = blockIdx.z * kMarchZ;
+    if (t4 >= h4 || j >= n) return;
+    const int ih = 4 * t4;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const long long plane = (long long)n * half;
+    const float4* o4 = reinterpret_cast<const float4*>(other);
+    auto row4 = [&](int jj, int kk) -> long long {  // float4 index of (ih, jj, kk)
+        return (((long long)jj + (long long)n * kk) * half + ih) >> 2;
+    };
+    const int kfirst = k0 == 0 ? n - 1 : k0 - 1;
+    float4 zm = __ldg(o4 + row4(j, kfirst));
+    float4 c = __ldg(o4 + row4(j, k0));
+    const int kend = min(k0 + kMarchZ, n);
+    for (int k = k0; k < kend; ++k) {
+        const int kp = k == n - 1 ? 0 : k + 1;
+        const float4 zp = __ldg(o4 + row4(j, kp));
+        const float4 ym = __ldg(o4 + row4(jm, k));
+        const float4 yp = __ldg(o4 + row4(jp, k));
+        const long long t = ((long long)j + (long long)n * k) * half + ih;
+        const float4 b = __ldg(reinterpret_cast<const float4*>(beta) + (t >> 2));
+        const int q = (j + k + color) & 1;
+        // x neighbours: q = 1 -> (ih, ih+1), q = 0 -> (ih-1, ih) of the other colour
+        const long long rowbase = t - ih;
+        float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
+        if (q) {
+            const float edge = __ldg(other + rowbase + (ih + 4 == half ? 0 : ih + 4));
+            xm0 = c.x; xm1 = c.y; xm2 = c.z; xm3 = c.w;
+            xp0 = c.y; xp1 = c.z; xp2 = c.w; xp3 = edge;
+        } else {
+            const float edge = __ldg(other + rowbase + (ih == 0 ? half - 1 : ih - 1));
+            xm0 = edge; xm1 = c.x; xm2 = c.y; xm3 = c.z;
+            xp0 = c.x; xp1 = c.y; xp2 = c.z; xp3 = c.w;
+        }
+        float4 r;
+        r.x = fmaf(((((xm0 + xp0) + ym.x) + yp.x) + zm.x) + zp.x, kSixthF, -b.x);
+        r.y = fmaf(((((xm1 + xp1) + ym.y) + yp.y) + zm.y) + zp.y, kSixthF, -b.y);
+        r.z = fmaf(((((xm2 + xp2) + ym.z) + yp.z) + zm.z) + zp.z, kSixthF, -b.z);
+        r.w = fmaf(((((xm3 + xp3) + ym.w) + yp.w) + zm.w) + zp.w, kSixthF, -b.w);
+        reinterpret_cast<float4*>(mine)[t >> 2] = r;
+        zm = c;
+        c = zp;
+    }
 }
 
 __device__ __forceinline__ float resid_f(const LevelViewF& L, int i, int j, int k)
@@ -607,12 +719,24 @@ double read_norm(Box& b, int slot)
 nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine)
 {
     const long long half_cells = (long long)l.n * l.n * l.n / 2;
-    const Geo g = geo3(l.n / 2, l.n, l.n);
+    const int half = l.n / 2;
+    const bool vec = half % 4 == 0;
+    Geo g;
+    if (vec) {
+        g = geo3(half / 4, l.n, 1);
+        g.grid.z = (l.n + kMarchZ - 1) / kMarchZ;
+    } else {
+        g = geo3(half, l.n, l.n);
+    }
     for (int color = 0; color < 2; ++color) {
+        float* mine = color ? l.fphi_b : l.fphi_r;
+        const float* other = color ? l.fphi_r : l.fphi_b;
+        const float* beta = color ? l.fbeta_b : l.fbeta_r;
         prof_begin(c);
-        k_gsrb_f<<<g.grid, g.block, 0, c.stream>>>(l.n, color, color ? l.fphi_b : l.fphi_r,
-                                                  color ? l.fphi_r : l.fphi_b,
-                                                  color ? l.fbeta_b : l.fbeta_r);
+        if (vec)
+            k_gsrb_f4<<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
+        else
+            k_gsrb_f<<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
         prof_end(c, NYXPM_ST_SMOOTH, 12.0 * half_cells, fine);
     }
     return check_launch(c, "gsrb f32");
@@ -689,6 +813,36 @@ nyxpm_status launch_mx_update(Ctx& c, Box& b)
     return check_launch(c, "mixed update");
 }
 
+// particle time-step limit of the mixed form: the same formula as the FP64
+// form (NyxParticleContainer.H:329-465), from the FP32 velocities and the FP32
+// gravity vector the kicks use, evaluated in FP64; the cell is the particle's
+// stored cell (floor(x*dxi)).  out must start at 0 (complemented-bits max).
+__global__ void __launch_bounds__(256) k_mx_est_dt(long long np, int n, double dxi, double adxi,
+                                                   double cfl, const int* __restrict__ cell,
+                                                   const float* __restrict__ vx,
+                                                   const float* __restrict__ vy,
+                                                   const float* __restrict__ vz,
+                                                   const float* __restrict__ g,
+                                                   unsigned long long* out)
+{
+    const long long nc = (long long)n * n * n;
+    double best = 1.0e50;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < np;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int cq = cell[q];
+        const double ux = fabs((double)vx[q]) * adxi, uy = fabs((double)vy[q]) * adxi,
+                     uz = fabs((double)vz[q]) * adxi;
+        const double um = fmax(fmax(ux, uy), uz);
+        double dtp = um > 0 ? cfl / um : 1.0e50;
+        const long long c = cidx(cell_i(cq), cell_j(cq), cell_k(cq), n);
+        const double gx = __ldg(g + c), gy = __ldg(g + nc + c), gz = __ldg(g + 2 * nc + c);
+        const double ga = sqrt((gx * gx + gy * gy) + gz * gz);
+        if (ga > 0) dtp = fmin(dtp, 1.0 / sqrt(ga * dxi));
+        best = fmin(best, dtp);
+    }
+    block_umax_store(~(unsigned long long)__double_as_longlong(best), out);
+}
+
 }  // namespace
 
 nyxpm_status mixed_unpack(Ctx& c, Box& b, const double* d_pos, const double* d_vel,
@@ -749,9 +903,17 @@ nyxpm_status mixed_deposit(Ctx& c, Box& b)
     const double inv_vol = 1.0 / (dx * dx * dx);
     const float scale = (float)(b.uniform_mass ? b.mscalar * inv_vol : inv_vol);
     const double nc = (double)n * n * n;
+    const float* mq = b.uniform_mass ? nullptr : b.fm;
+    // the FP32 partials of long keys live in the box's heavy-key array (8 floats
+    // in the room of 8 doubles per slot)
+    float* heavy = reinterpret_cast<float*>(b.heavy_part);
     prof_begin(c);
-    k_mx_deposit<<<grid, 256, 0, c.stream>>>(n, scale, b.cell, b.ox, b.oy, b.oz,
-                                             b.uniform_mass ? nullptr : b.fm, b.cell_start, b.frho);
+    k_mx_deposit_heavy<<<c.sm_count * 4, 256, 0, c.stream>>>(n, b.cell, b.ox, b.oy, b.oz, mq,
+                                                             b.cell_start, b.long_list, b.long_count,
+                                                             b.key_slot, heavy);
+    k_mx_deposit<<<grid, 256, 0, c.stream>>>(n, scale, b.cell, b.ox, b.oy, b.oz, mq, b.cell_start,
+                                             b.key_slot, heavy, b.frho);
+    c.launches += 1;
     prof_end(c, NYXPM_ST_DEPOSIT, (b.uniform_mass ? 16.0 : 20.0) * b.np + 8.0 * nc);
     return check_launch(c, "mixed deposit");
 }
@@ -879,6 +1041,16 @@ nyxpm_status mixed_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, 
     prof_end(c, NYXPM_ST_KICK, (do_move ? 56.0 : 40.0) * b.np + 12.0 * nc);
     if (do_move) b.sorted = 0;
     return check_launch(c, "mixed kick");
+}
+
+nyxpm_status mixed_est_dt(Ctx& c, Box& b, double cfl, double a)
+{
+    cudaMemsetAsync(b.norms + 3, 0, sizeof(unsigned long long), c.stream);
+    const unsigned blocks = std::min(blocks_for(b.np), (unsigned)(c.sm_count * 8));
+    k_mx_est_dt<<<blocks, kThreads, 0, c.stream>>>(b.np, b.n, b.dxi, b.dxi / a, cfl, b.cell, b.fvx,
+                                                    b.fvy, b.fvz, b.g32, b.norms + 3);
+    c.launches += 1;
+    return check_launch(c, "mixed time-step estimate");
 }
 
 }  // namespace nyxpm

@@ -260,6 +260,51 @@ constexpr int kTx = 8, kTy = 8, kTz = 8;
 constexpr int kKx = kTx + 1, kKy = kTy + 1, kKz = kTz + 1;
 constexpr int kNKeys = kKx * kKy * kKz;
 
+__device__ __forceinline__ void na_add_weights(int q, int n, double dxi,
+                                               const double* __restrict__ x,
+                                               const double* __restrict__ y,
+                                               const double* __restrict__ z, double s[8])
+{
+    double fx, fy, fz;
+    na_key1(x[q], dxi, n, &fx);
+    na_key1(y[q], dxi, n, &fy);
+    na_key1(z[q], dxi, n, &fz);
+    const double sx[2] = {1.0 - fx, fx};
+    const double sy[2] = {1.0 - fy, fy};
+    const double sz[2] = {1.0 - fz, fz};
+#pragma unroll
+    for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+        for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+            for (int cx = 0; cx < 2; ++cx)
+                s[cx + 2 * cy + 4 * cz] = s[cx + 2 * cy + 4 * cz] + (sx[cx] * sy[cy]) * sz[cz];
+}
+
+// A key longer than a warp, summed in the order the allocating deposit sums it
+// with a whole warp: 32 lane partials (lane l: particles l, l+32, ... in order)
+// combined by the xor butterfly 16, 8, 4, 2, 1.  Here one thread does it: the
+// butterfly's result is the pairwise tree over the lanes taken in bit-reversed
+// order, built with a stack of finished subtrees (a binary counter).
+__device__ void na_long_key(int b0, int e, int n, double dxi, const double* __restrict__ x,
+                            const double* __restrict__ y, const double* __restrict__ z,
+                            double out[8])
+{
+    double stack[6][8];
+    int depth = 0;
+    for (int t = 0; t < 32; ++t) {
+        const int lane = (int)(__brev((unsigned)t) >> 27);
+        double* p = stack[depth++];
+        for (int c = 0; c < 8; ++c) p[c] = 0.0;
+        for (int q = b0 + lane; q < e; q += 32) na_add_weights(q, n, dxi, x, y, z, p);
+        for (int v = t + 1; (v & 1) == 0; v >>= 1) {
+            for (int c = 0; c < 8; ++c) stack[depth - 2][c] = stack[depth - 2][c] + stack[depth - 1][c];
+            --depth;
+        }
+    }
+    for (int c = 0; c < 8; ++c) out[c] = stack[0][c];
+}
+
 // per-key partial sums of the 8 corner weights, then cell sums in a fixed order
 __global__ void __launch_bounds__(256) na_deposit(int n, double dxi, double scale,
                                                   const double* __restrict__ x,
@@ -273,24 +318,13 @@ __global__ void __launch_bounds__(256) na_deposit(int n, double dxi, double scal
         const int ki = kl % kKx, kj = (kl / kKx) % kKy, kk = kl / (kKx * kKy);
         const long long K = cidx(wrapi(i0 + ki, n), wrapi(j0 + kj, n), wrapi(k0 + kk, n), n);
         double s[8];
+        const int b0 = start[K], e = start[K + 1];
+        if (e - b0 > 32) {
+            na_long_key(b0, e, n, dxi, x, y, z, s);
+        } else {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) s[c] = 0.0;
-        const int e = start[K + 1];
-        for (int q = start[K]; q < e; ++q) {
-            double fx, fy, fz;
-            na_key1(x[q], dxi, n, &fx);
-            na_key1(y[q], dxi, n, &fy);
-            na_key1(z[q], dxi, n, &fz);
-            const double sx[2] = {1.0 - fx, fx};
-            const double sy[2] = {1.0 - fy, fy};
-            const double sz[2] = {1.0 - fz, fz};
-#pragma unroll
-            for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-                for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-                    for (int cx = 0; cx < 2; ++cx)
-                        s[cx + 2 * cy + 4 * cz] = s[cx + 2 * cy + 4 * cz] + (sx[cx] * sy[cy]) * sz[cz];
+            for (int c = 0; c < 8; ++c) s[c] = 0.0;
+            for (int q = b0; q < e; ++q) na_add_weights(q, n, dxi, x, y, z, s);
         }
 #pragma unroll
         for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];

@@ -10,6 +10,7 @@
 // small fraction of its FP32 rate, so every FP64 instruction saved counts.
 #include "pm_common.cuh"
 
+#include <algorithm>
 #include <cstdio>
 
 namespace nyxpm {
@@ -298,13 +299,150 @@ __global__ void k_scan_down(const int* __restrict__ in, int n, const int* __rest
 constexpr int kTx = 8, kTy = 8, kTz = 8;
 constexpr int kKx = kTx + 1, kKy = kTy + 1, kKz = kTz + 1;
 constexpr int kNKeys = kKx * kKy * kKz;
+static_assert(kDepositLanes == 32, "long keys are summed by one warp; the sort queues keys > 32");
 
+// adds particle q's eight CIC weights (times its mass, fused, if m) to s
+__device__ __forceinline__ void add_weights(int q, int n, double dxi, const double* __restrict__ x,
+                                            const double* __restrict__ y,
+                                            const double* __restrict__ z,
+                                            const double* __restrict__ m, double s[8])
+{
+    double fx, fy, fz;
+    key1(x[q], dxi, n, &fx);
+    key1(y[q], dxi, n, &fy);
+    key1(z[q], dxi, n, &fz);
+    const double sx[2] = {1.0 - fx, fx};
+    const double sy[2] = {1.0 - fy, fy};
+    const double sz[2] = {1.0 - fz, fz};
+    if (m) {
+        const double mq = m[q];
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+            for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                for (int cx = 0; cx < 2; ++cx)
+                    s[cx + 2 * cy + 4 * cz] = fma((sx[cx] * sy[cy]) * sz[cz], mq, s[cx + 2 * cy + 4 * cz]);
+    } else {
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+            for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                for (int cx = 0; cx < 2; ++cx)
+                    s[cx + 2 * cy + 4 * cz] = s[cx + 2 * cy + 4 * cz] + (sx[cx] * sy[cy]) * sz[cz];
+    }
+}
+
+// Keys longer than a warp (the sort's long_list), one warp each: lane l sums
+// particles l, l+32, l+64, ... of the key in order, then the xor butterfly
+// (offsets 16, 8, 4, 2, 1) combines the lanes.  The eight corner sums go to
+// heavy_part[slot], and key_slot[K] = slot tells the tile kernel where.
+__global__ void __launch_bounds__(256) k_deposit_heavy(int n, double dxi,
+                                                       const double* __restrict__ x,
+                                                       const double* __restrict__ y,
+                                                       const double* __restrict__ z,
+                                                       const double* __restrict__ m,
+                                                       const int* __restrict__ start,
+                                                       const int* __restrict__ long_list,
+                                                       const int* __restrict__ long_count,
+                                                       int* key_slot, double* heavy_part)
+{
+    const int lane = threadIdx.x & 31;
+    const int total = *long_count;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < total; li += nwarps) {
+        const int K = long_list[li];
+        const int e = start[K + 1];
+        double s[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s[c] = 0.0;
+        for (int q = start[K] + lane; q < e; q += 32) add_weights(q, n, dxi, x, y, z, m, s);
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) s[c] = s[c] + __shfl_xor_sync(0xffffffffu, s[c], off);
+        if (lane < 8) {
+            double v = s[0];
+#pragma unroll
+            for (int c = 1; c < 8; ++c)
+                if (lane == c) v = s[c];
+            heavy_part[8LL * li + lane] = v;
+        }
+        if (lane == 0) key_slot[K] = li;
+    }
+}
+
+// Pass 1 of the FP64 deposit, one thread per key: the key's eight corner sums
+// (a short key in sorted order; a long key's from k_deposit_heavy) into
+// part[corner * nc + K].  Every key is summed exactly once, with the whole SM
+// free for latency hiding (no shared memory).
+__global__ void __launch_bounds__(256) k_deposit_keys(long long nc, int n, double dxi,
+                                                      const double* __restrict__ x,
+                                                      const double* __restrict__ y,
+                                                      const double* __restrict__ z,
+                                                      const double* __restrict__ m,
+                                                      const int* __restrict__ start,
+                                                      const int* __restrict__ key_slot,
+                                                      const double* __restrict__ heavy_part,
+                                                      double* __restrict__ part)
+{
+    const long long K = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (K >= nc) return;
+    const int b0 = start[K], e = start[K + 1];
+    double s[8];
+    if (e - b0 > kDepositLanes) {
+        const double* hp = heavy_part + 8LL * key_slot[K];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s[c] = hp[c];
+    } else {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s[c] = 0.0;
+        for (int q = b0; q < e; ++q) add_weights(q, n, dxi, x, y, z, m, s);
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) part[c * nc + K] = s[c];
+}
+
+// Pass 2, one thread per cell: the eight keys' corners in the fixed (dk, dj, di)
+// order, times the scale -- the same sums as the tile kernel's, term for term.
+__global__ void __launch_bounds__(256) k_deposit_cells(int n, double scale,
+                                                       const double* __restrict__ part,
+                                                       double* __restrict__ rho)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n || j >= n) return;
+    const long long nc = (long long)n * n * n;
+    const int ip = i == n - 1 ? 0 : i + 1, jp = j == n - 1 ? 0 : j + 1, kp = k == n - 1 ? 0 : k + 1;
+    const int is[2] = {i, ip}, js[2] = {j, jp}, ks[2] = {k, kp};
+    double acc = 0.0;
+#pragma unroll
+    for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+            for (int di = 0; di < 2; ++di) {
+                const int corner = (1 - di) + 2 * (1 - dj) + 4 * (1 - dk);
+                acc = acc + __ldg(part + corner * nc + cidx(is[di], js[dj], ks[dk], n));
+            }
+    rho[cidx(i, j, k, n)] = acc * scale;
+}
+
+// One CTA per 8x8x8 tile of cells: the 9x9x9 keys whose particles touch the
+// tile are summed into eight corner partials each (a short key by one thread
+// in sorted order; a long key's partials come from k_deposit_heavy), then each
+// cell adds its eight keys' corners in the fixed (dk, dj, di) order.  No
+// atomics: the result does not depend on scheduling.
 __global__ void __launch_bounds__(256) k_deposit(int n, double dxi, double scale,
                                                  const double* __restrict__ x,
                                                  const double* __restrict__ y,
                                                  const double* __restrict__ z,
                                                  const double* __restrict__ m,
-                                                 const int* __restrict__ start, double* rho)
+                                                 const int* __restrict__ start,
+                                                 const int* __restrict__ key_slot,
+                                                 const double* __restrict__ heavy_part, double* rho)
 {
     __shared__ double part[kNKeys * 8];
     const int i0 = blockIdx.x * kTx, j0 = blockIdx.y * kTy, k0 = blockIdx.z * kTz;
@@ -312,35 +450,15 @@ __global__ void __launch_bounds__(256) k_deposit(int n, double dxi, double scale
         const int ki = kl % kKx, kj = (kl / kKx) % kKy, kk = kl / (kKx * kKy);
         const long long K = cidx(wrapi(i0 + ki, n), wrapi(j0 + kj, n), wrapi(k0 + kk, n), n);
         double s[8];
+        const int b0 = start[K], e = start[K + 1];
+        if (e - b0 > kDepositLanes) {
+            const double* hp = heavy_part + 8LL * key_slot[K];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) s[c] = 0.0;
-        const int e = start[K + 1];
-        for (int q = start[K]; q < e; ++q) {
-            double fx, fy, fz;
-            key1(x[q], dxi, n, &fx);
-            key1(y[q], dxi, n, &fy);
-            key1(z[q], dxi, n, &fz);
-            const double sx[2] = {1.0 - fx, fx};
-            const double sy[2] = {1.0 - fy, fy};
-            const double sz[2] = {1.0 - fz, fz};
-            if (m) {
-                const double mq = m[q];
+            for (int c = 0; c < 8; ++c) s[c] = hp[c];
+        } else {
 #pragma unroll
-                for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-                    for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-                        for (int cx = 0; cx < 2; ++cx)
-                            s[cx + 2 * cy + 4 * cz] = fma((sx[cx] * sy[cy]) * sz[cz], mq, s[cx + 2 * cy + 4 * cz]);
-            } else {
-#pragma unroll
-                for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-                    for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-                        for (int cx = 0; cx < 2; ++cx)
-                            s[cx + 2 * cy + 4 * cz] = s[cx + 2 * cy + 4 * cz] + (sx[cx] * sy[cy]) * sz[cz];
-            }
+            for (int c = 0; c < 8; ++c) s[c] = 0.0;
+            for (int q = b0; q < e; ++q) add_weights(q, n, dxi, x, y, z, m, s);
         }
 #pragma unroll
         for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
@@ -436,6 +554,45 @@ __global__ void __launch_bounds__(256) k_kick(long long np, KickArgs A, double* 
         y[q] = wrap_pos(y[q], A.L);
         z[q] = wrap_pos(z[q], A.L);
     }
+}
+
+// ---------------------------------------------------------------------------
+// particle time-step limit (NyxParticleContainer::estTimestep,
+// NyxParticleContainer.H:329-465): per particle
+//   dt_p = cfl / max_d(|v_d| * adxi)   (adxi = dxi / a; 1e50 when v = 0),
+//   dt_p = min(dt_p, 1 / sqrt(|g| * dxi)) when |g| > 0,
+// |g| = sqrt((gx*gx + gy*gy) + gz*gz) at the cell floor(x*dxi) (wrapped), and
+// the minimum over particles.  A positive double orders like its bit pattern,
+// so the minimum is an integer max of the complemented bits: the result does
+// not depend on the order the blocks finish in.  out must start at 0.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_est_dt(long long np, int n, double dxi, double adxi,
+                                                double cfl, const double* __restrict__ x,
+                                                const double* __restrict__ y,
+                                                const double* __restrict__ z,
+                                                const double* __restrict__ vx,
+                                                const double* __restrict__ vy,
+                                                const double* __restrict__ vz,
+                                                const double* __restrict__ g,
+                                                unsigned long long* out)
+{
+    const long long nc = (long long)n * n * n;
+    double best = 1.0e50;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < np;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int i = wrapi((int)floor(x[q] * dxi), n);
+        const int j = wrapi((int)floor(y[q] * dxi), n);
+        const int k = wrapi((int)floor(z[q] * dxi), n);
+        const double ux = fabs(vx[q]) * adxi, uy = fabs(vy[q]) * adxi, uz = fabs(vz[q]) * adxi;
+        const double um = fmax(fmax(ux, uy), uz);
+        double dtp = um > 0 ? cfl / um : 1.0e50;
+        const long long c = cidx(i, j, k, n);
+        const double gx = __ldg(g + c), gy = __ldg(g + nc + c), gz = __ldg(g + 2 * nc + c);
+        const double ga = sqrt((gx * gx + gy * gy) + gz * gz);
+        if (ga > 0) dtp = fmin(dtp, 1.0 / sqrt(ga * dxi));
+        best = fmin(best, dtp);
+    }
+    block_umax_store(~(unsigned long long)__double_as_longlong(best), out);
 }
 
 }  // namespace
@@ -549,9 +706,24 @@ nyxpm_status launch_deposit(Ctx& c, Box& b)
     // per-particle masses: keys sum w*m, cells scale by 1/dx^3; uniform: keys sum w, cells by m/dx^3
     const double scale = b.uniform_mass ? b.mscalar * inv_vol : inv_vol;
     const double nc = (double)n * n * n;
+    const double* mq = b.uniform_mass ? nullptr : b.m;
     prof_begin(c);
-    k_deposit<<<grid, 256, 0, c.stream>>>(n, b.dxi, scale, b.x, b.y, b.z,
-                                          b.uniform_mass ? nullptr : b.m, b.cell_start, b.rho);
+    k_deposit_heavy<<<c.sm_count * 4, 256, 0, c.stream>>>(n, b.dxi, b.x, b.y, b.z, mq, b.cell_start,
+                                                          b.long_list, b.long_count, b.key_slot,
+                                                          b.heavy_part);
+    if (b.key_part) {
+        const long long ncl = (long long)n * n * n;
+        k_deposit_keys<<<blocks_for(ncl), kThreads, 0, c.stream>>>(ncl, n, b.dxi, b.x, b.y, b.z, mq,
+                                                                    b.cell_start, b.key_slot,
+                                                                    b.heavy_part, b.key_part);
+        const Geo g = geo3(n, n, n);
+        k_deposit_cells<<<g.grid, g.block, 0, c.stream>>>(n, scale, b.key_part, b.rho);
+        c.launches += 2;
+    } else {
+        k_deposit<<<grid, 256, 0, c.stream>>>(n, b.dxi, scale, b.x, b.y, b.z, mq, b.cell_start,
+                                              b.key_slot, b.heavy_part, b.rho);
+        c.launches += 1;
+    }
     prof_end(c, NYXPM_ST_DEPOSIT, (b.uniform_mass ? 24.0 : 32.0) * b.np + 12.0 * nc);
     return check_launch(c, "deposit");
 }
@@ -576,6 +748,16 @@ nyxpm_status launch_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur,
     prof_end(c, NYXPM_ST_KICK, (do_move ? 96.0 : 72.0) * b.np + 24.0 * nc);
     b.sorted = b.sorted && !do_move && !do_wrap;
     return check_launch(c, "kick");
+}
+
+nyxpm_status launch_est_dt(Ctx& c, Box& b, double cfl, double a)
+{
+    cudaMemsetAsync(b.norms + 3, 0, sizeof(unsigned long long), c.stream);
+    const unsigned blocks = std::min(blocks_for(b.np), (unsigned)(c.sm_count * 8));
+    k_est_dt<<<blocks, kThreads, 0, c.stream>>>(b.np, b.n, b.dxi, b.dxi / a, cfl, b.x, b.y, b.z,
+                                                 b.vx, b.vy, b.vz, b.g, b.norms + 3);
+    c.launches += 1;
+    return check_launch(c, "time-step estimate");
 }
 
 }  // namespace nyxpm

@@ -102,6 +102,24 @@ class Context:
     def integrate_comoving_a_to_a(self, a_old: float, a_value: float, dt_window: float) -> float:
         return self.lib.nyxpm_dt_for_da(C.byref(self.params), a_old, a_value, dt_window)
 
+    def dt_params(self, **overrides) -> "_L.DtParams":
+        """nyxpm_dt_params with the reference defaults, then the given fields."""
+        dp = _L.DtParams()
+        self.lib.nyxpm_default_dt_params(C.byref(dp))
+        for k, v in overrides.items():
+            setattr(dp, k, float(v))
+        return dp
+
+    def comoving_est_dt(self, a: float, estdt: float, **dt_params) -> float:
+        """Nyx::comoving_est_time_step (comoving.cpp:353-483): estdt limited by how fast a
+        may change."""
+        out = C.c_double(0)
+        st = self.lib.nyxpm_comoving_est_dt(C.byref(self.params), float(a), float(estdt),
+                                            C.byref(self.dt_params(**dt_params)), C.byref(out))
+        if st != _L.NYXPM_OK:
+            raise NyxPMError(st, "comoving_est_dt: a past final_a or no convergence")
+        return out.value
+
     def hubble(self, a: float) -> float:
         p = self.params
         OmL = 1.0 - p.comoving_OmM - p.comoving_OmR
@@ -223,6 +241,22 @@ class Box:
         self._c(self.ctx.lib.nyxpm_init_field, float(a), C.byref(info), what="init_field")
         return info.as_dict()
 
+    def est_time_step(self, cfl: float, a: float) -> float:
+        """Particle time-step limit (NyxParticleContainer::estTimestep) with the box's field."""
+        out = C.c_double(0)
+        self._c(self.ctx.lib.nyxpm_est_time_step, float(cfl), float(a), C.byref(out),
+                what="est_time_step")
+        return out.value
+
+    def compute_new_dt(self, time: float, a: float, dt_old: float, **dt_params):
+        """Nyx::computeNewDt at level 0 (particles, a-change limit, change_max, stop_time);
+        returns (dt, a_new)."""
+        dt, a_new = C.c_double(0), C.c_double(0)
+        self._c(self.ctx.lib.nyxpm_compute_new_dt, C.byref(self.ctx.dt_params(**dt_params)),
+                float(time), float(a), float(dt_old), C.byref(dt), C.byref(a_new),
+                what="compute_new_dt")
+        return dt.value, a_new.value
+
     def step(self, a_old, a_new, dt, reuse_field: bool = False) -> dict:
         info = _L.StepInfo()
         flags = _L.NYXPM_STEP_REUSE_FIELD if reuse_field else 0
@@ -297,6 +331,15 @@ class DarkMatterParticleContainer:
     def RedistributeLocal(self, lev_min: int = 0, lev_max: int = -1, nGrow: int = 0):
         self.box.redistribute()
 
+    def estTimestep(self, acceleration=None, a: float = 1.0, lev: int = 0, cfl: float = 0.5) -> float:
+        """NyxParticleContainer::estTimestep (NyxParticleContainer.H:329-465) with the box's
+        own gravity vector."""
+        if acceleration is not None:
+            raise NyxPMError(1, "estTimestep uses the box's own field; pass acceleration=None")
+        if lev != 0:
+            raise NyxPMError(1, "single level only")
+        return self.box.est_time_step(cfl, a)
+
     def sumParticleMass(self, lev: int = 0) -> float:
         return self.box.mass_offset() * self.box.L ** 3
 
@@ -359,3 +402,8 @@ class Nyx:
     def advance_particles_only(self, a_old: float, a_new: float, dt: float,
                                reuse_field: bool = False) -> dict:
         return self.box.step(a_old, a_new, dt, reuse_field=reuse_field)
+
+    def computeNewDt(self, time: float, a: float, dt_old: float, **dt_params):
+        """Nyx::computeNewDt at level 0 without subcycling (Nyx.cpp:1023-1208);
+        returns (dt, a_new)."""
+        return self.box.compute_new_dt(time, a, dt_old, **dt_params)

@@ -76,6 +76,11 @@ def lib():
         L.orc_integrate_a.argtypes = [C.c_double] * 5
         L.orc_dt_for_da.restype = C.c_double
         L.orc_dt_for_da.argtypes = [C.c_double] * 6
+        L.orc_est_time_step.restype = C.c_double
+        L.orc_est_time_step.argtypes = [C.c_int, C.c_double, C.c_long, _dp, _dp, _dp, _dp, _dp, _dp,
+                                        _dp, C.c_double, C.c_double]
+        L.orc_comoving_est_dt.restype = C.c_double
+        L.orc_comoving_est_dt.argtypes = [C.c_double] * 9 + [C.POINTER(C.c_int)]
         L.orc_step.restype = C.c_int
         L.orc_step.argtypes = [C.POINTER(_Cfg), C.c_long, _dp, _dp, _dp, _dp, _dp, _dp, C.c_void_p,
                                C.c_double, C.c_void_p, C.c_double, C.c_double, C.c_double, _dp, _dp,
@@ -216,6 +221,22 @@ def integrate_a(OmM, OmR, h, a_old, dt) -> float:
 def dt_for_da(OmM, OmR, h, a_old, a_value, dt_window) -> float:
     """integrate_comoving_a_to_a (comoving.cpp:74-130)."""
     return lib().orc_dt_for_da(OmM, OmR, h, a_old, a_value, dt_window)
+
+
+def est_time_step(n, L, p: Particles, g, cfl, a) -> float:
+    """Particle time-step limit (NyxParticleContainer::estTimestep,
+    NyxParticleContainer.H:329-465) with the cell-centred gravity g."""
+    return lib().orc_est_time_step(n, L, p.np, p.x, p.y, p.z, p.vx, p.vy, p.vz,
+                                   np.ascontiguousarray(g, dtype=np.float64), cfl, a)
+
+
+def comoving_est_dt(OmM, OmR, h, a, estdt, relative_max_change_a=0.01,
+                    absolute_max_change_a=-1.0, final_a=-1.0, dt_binpow=-1.0):
+    """Nyx::comoving_est_time_step (comoving.cpp:353-483); returns (dt, status)."""
+    st = C.c_int(0)
+    dt = lib().orc_comoving_est_dt(OmM, OmR, h, a, estdt, relative_max_change_a,
+                                   absolute_max_change_a, final_a, dt_binpow, C.byref(st))
+    return dt, st.value
 
 
 class PMOracle:

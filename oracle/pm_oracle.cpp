@@ -27,8 +27,10 @@
 // in the reference tree.  The oracle fixes them to one deterministic definition
 // that the GPU library implements as well:
 //   * deposit: rho(c) = inv_vol * sum over the 8 deposit keys K of c, in the
-//     order (dk,dj,di) = (0,0,0),(0,0,1),...,(1,1,1), of the sequential sum over
-//     the particles of K (sorted order) of ((sx*sy)*sz)*m;
+//     order (dk,dj,di) = (0,0,0),(0,0,1),...,(1,1,1), of the sum over the
+//     particles of K of ((sx*sy)*sz)*m -- sequential in sorted order for up to
+//     32 particles, else 32 lane-strided sequential partials combined by an
+//     xor butterfly (the order one warp sums a long key in);
 //   * mean: row sums by 32 strided lane partials and a halving tree, then a
 //     sequential sum over rows of a plane, then over planes;
 //   * MG: V(nu1,nu2) cycles, red then black, full-weighting (8-cell average)
@@ -90,6 +92,9 @@ namespace {
 inline int wrapi(int i, int n) { i %= n; return i < 0 ? i + n : i; }
 
 inline long cidx(int i, int j, int k, int n) { return (long)i + (long)n * ((long)j + (long)n * k); }
+
+// keys with more particles than this sum them in lane-strided partials
+constexpr int kDepositLanes = 32;
 
 // deposit key of one coordinate: floor((x - plo) * dxi + 0.5), plo = 0
 // (NeutrinoParticles_K.H:15-21, DarkMatterParticleContainer.cpp:263-269),
@@ -186,26 +191,45 @@ void orc_deposit(int n, double L, long np, const double* x, const double* y, con
     const double inv_vol = 1.0 / (dx * dx * dx);
     const double scale = m ? inv_vol : mscalar * inv_vol;
     // per-key partial sums: part[K*8 + corner], corner = cx + 2*cy + 4*cz where
-    // cx = 0 is the cell i-1 (weight 1-f) and cx = 1 the cell i (weight f)
+    // cx = 0 is the cell i-1 (weight 1-f) and cx = 1 the cell i (weight f).
+    // A key of at most kDepositLanes particles sums them in sorted order.  A
+    // longer key sums in kDepositLanes lane partials -- lane l takes particles
+    // l, l + 32, l + 64, ... in order -- combined by the xor butterfly: for
+    // off = 16, 8, 4, 2, 1 every lane adds the partial of lane l ^ off.
     std::vector<double> part(nc * 8);
+    auto accumulate = [&](int q, double* s) {
+        double fx, fy, fz;
+        key1(x[q], dxi, n, &fx);
+        key1(y[q], dxi, n, &fy);
+        key1(z[q], dxi, n, &fz);
+        const double sx[2] = {1.0 - fx, fx};
+        const double sy[2] = {1.0 - fy, fy};
+        const double sz[2] = {1.0 - fz, fz};
+        for (int cz = 0; cz < 2; ++cz)
+            for (int cy = 0; cy < 2; ++cy)
+                for (int cx = 0; cx < 2; ++cx) {
+                    const double w = (sx[cx] * sy[cy]) * sz[cz];
+                    double& a = s[cx + 2 * cy + 4 * cz];
+                    a = m ? std::fma(w, m[q], a) : a + w;
+                }
+    };
 #pragma omp parallel for schedule(dynamic, 64)
     for (long K = 0; K < nc; ++K) {
+        const int s0 = cell_start[K], e = cell_start[K + 1];
         double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int q = cell_start[K]; q < cell_start[K + 1]; ++q) {
-            double fx, fy, fz;
-            key1(x[q], dxi, n, &fx);
-            key1(y[q], dxi, n, &fy);
-            key1(z[q], dxi, n, &fz);
-            const double sx[2] = {1.0 - fx, fx};
-            const double sy[2] = {1.0 - fy, fy};
-            const double sz[2] = {1.0 - fz, fz};
-            for (int cz = 0; cz < 2; ++cz)
-                for (int cy = 0; cy < 2; ++cy)
-                    for (int cx = 0; cx < 2; ++cx) {
-                        const double w = (sx[cx] * sy[cy]) * sz[cz];
-                        double& a = s[cx + 2 * cy + 4 * cz];
-                        a = m ? std::fma(w, m[q], a) : a + w;
-                    }
+        if (e - s0 <= kDepositLanes) {
+            for (int q = s0; q < e; ++q) accumulate(q, s);
+        } else {
+            double lane[kDepositLanes][8] = {};
+            for (int l = 0; l < kDepositLanes; ++l)
+                for (int q = s0 + l; q < e; q += kDepositLanes) accumulate(q, lane[l]);
+            for (int off = kDepositLanes / 2; off >= 1; off >>= 1) {
+                double nxt[kDepositLanes][8];
+                for (int l = 0; l < kDepositLanes; ++l)
+                    for (int c = 0; c < 8; ++c) nxt[l][c] = lane[l][c] + lane[l ^ off][c];
+                std::memcpy(lane, nxt, sizeof(lane));
+            }
+            for (int c = 0; c < 8; ++c) s[c] = lane[0][c];
         }
         for (int c = 0; c < 8; ++c) part[K * 8 + c] = s[c];
     }
@@ -686,6 +710,153 @@ double orc_dt_for_da(double OmM, double OmR, double h, double a_old, double a_va
         }
     }
     return dt;
+}
+
+// ----------------------------------------------------------------------------
+// time-step control
+// ----------------------------------------------------------------------------
+
+// Particle time-step limit, NyxParticleContainer::estTimestep
+// (NyxParticleContainer.H:329-465): per particle
+//   dt_p = cfl / max_d(|v_d| * (dxi / a))     (1e50 when all components are 0),
+//   dt_p = min(dt_p, 1 / sqrt(|g| * dxi))    when |g| > 0,
+// with |g| = sqrt((gx*gx + gy*gy) + gz*gz) taken at the cell floor(x * dxi)
+// (no interpolation; the index wraps periodically, as the ghost cells of the
+// reference's field do).  Returns the minimum over particles, 1e50 when no
+// particle limits it and -1e50 when there are no particles.
+double orc_est_time_step(int n, double L, long np, const double* x, const double* y,
+                         const double* z, const double* vx, const double* vy, const double* vz,
+                         const double* g, double cfl, double a)
+{
+    if (np <= 0) return -1.0e50;
+    const long nc = (long)n * n * n;
+    const double dxi = (double)n / L;
+    const double adxi = dxi / a;
+    double dt = 1.0e50;
+#pragma omp parallel for schedule(static) reduction(min : dt)
+    for (long q = 0; q < np; ++q) {
+        const int i = wrapi((int)std::floor(x[q] * dxi), n);
+        const int j = wrapi((int)std::floor(y[q] * dxi), n);
+        const int k = wrapi((int)std::floor(z[q] * dxi), n);
+        const double ux = std::fabs(vx[q]) * adxi;
+        const double uy = std::fabs(vy[q]) * adxi;
+        const double uz = std::fabs(vz[q]) * adxi;
+        const double um = std::max(std::max(ux, uy), uz);
+        double dtp = (um > 0) ? (cfl / um) : 1.0e50;
+        const long c = cidx(i, j, k, n);
+        const double gx = g[c], gy = g[nc + c], gz = g[2 * nc + c];
+        const double ga = std::sqrt((gx * gx + gy * gy) + gz * gz);
+        if (ga > 0) dtp = std::min(dtp, 1.0 / std::sqrt(ga * dxi));
+        dt = std::min(dt, dtp);
+    }
+    return dt;
+}
+
+// est_maxdt_comoving_a (comoving.cpp:191-215): a must not change by more than
+// 5% in one forward-Euler step.
+static double est_maxdt_a(double OmM, double OmR, double h, double a, double dt)
+{
+    const double H0 = h * 100.0;
+    const double OmL = 1.0 - OmM - OmR;
+    if (H0 != 0.0) {
+        const double max_dt = 0.05 / H0 / std::sqrt(OmM / (a * a * a) + OmR / (a * a * a * a) + OmL);
+        dt = std::min(dt, max_dt);
+    }
+    return dt;
+}
+
+// est_lindt_comoving_a (comoving.cpp:217-237): the EdS-like first guess of the
+// dt that takes a_old to a_new.
+static double est_lindt_a(double h, double a_old, double a_new, double dt)
+{
+    const double H0 = h * 100.0;
+    if (H0 != 0.0) {
+        const double s = std::pow(0.75, 2.0 / 3.0);
+        dt = (std::pow(a_new / s, 0.75) - std::pow(a_old / s, 0.75)) / H0;
+    }
+    return dt;
+}
+
+// Nyx::comoving_est_time_step (comoving.cpp:353-483) from the current a (its
+// new-a and old-a branches differ only in which a they pass), through
+// estdt_comoving_a (:239-280), enforce_percent_change (:282-317) and
+// enforce_final_a (:319-350).  estdt is
+// the estimate so far (particles); relative_max_change_a bounds da/a when
+// absolute_max_change_a <= 0, otherwise a steps by absolute_max_change_a;
+// final_a > 0 stops a there; dt_binpow >= 0 snaps the estimate to the a-limited
+// dt divided by a power of two.  Returns the new estimate; *status = 1 where
+// the reference aborts (a past final_a, no convergence in 100 iterations).
+double orc_comoving_est_dt(double OmM, double OmR, double h, double a, double estdt,
+                           double relative_max_change_a, double absolute_max_change_a,
+                           double final_a, double dt_binpow, int* status)
+{
+    *status = 0;
+    if (h == 0.0) return estdt;
+    double dt = estdt;
+    double new_a;
+    if (absolute_max_change_a <= 0.0) {
+        dt = est_maxdt_a(OmM, OmR, h, a, dt);
+        new_a = orc_integrate_a(OmM, OmR, h, a, dt);
+        double factor = ((new_a - a) / a) / relative_max_change_a;
+        if (factor > 1.0) {
+            for (int i = 1; i <= 100; ++i) {
+                factor = ((new_a - a) / a) / relative_max_change_a;
+                if (factor > 1.0) {
+                    dt = (1.0 / factor) * dt * 0.99;
+                    new_a = orc_integrate_a(OmM, OmR, h, a, dt);
+                } else if (i < 100) {
+                    new_a = orc_integrate_a(OmM, OmR, h, a, dt);
+                    break;
+                } else {
+                    *status = 1;
+                    return dt;
+                }
+            }
+        }
+    } else {
+        new_a = a + absolute_max_change_a;
+        dt = est_lindt_a(h, a, new_a, dt);
+        dt = est_maxdt_a(OmM, OmR, h, a, dt);
+        dt = orc_dt_for_da(OmM, OmR, h, a, new_a, dt);
+    }
+    if (final_a > 0.0) {
+        const double eps = 1.0e-10;
+        if (a > final_a) {
+            *status = 1;
+            return dt;
+        }
+        if (new_a > final_a) {
+            for (int i = 1; i <= 100; ++i) {
+                if (new_a > final_a + eps || new_a < final_a) {
+                    const double factor = (final_a - a) / (new_a - a);
+                    dt = dt * factor;
+                    new_a = orc_integrate_a(OmM, OmR, h, a, dt);
+                } else if (i < 100) {
+                    break;
+                } else {
+                    *status = 1;
+                    return dt;
+                }
+            }
+        }
+    }
+    if (dt_binpow >= 0) {
+        if (estdt >= dt)
+            estdt = dt;
+        else if (estdt > 0.5 * dt)
+            estdt = 0.5 * dt;
+        else if (estdt > 0.25 * dt)
+            estdt = 0.25 * dt;
+        else if (estdt > 0.125 * dt)
+            estdt = 0.125 * dt;
+        else if (estdt > 0.0625 * dt)
+            estdt = 0.0625 * dt;
+        else
+            estdt = dt * std::pow(2.0, -std::ceil(std::log2(dt / estdt)));
+    } else {
+        estdt = std::min(estdt, dt);
+    }
+    return estdt;
 }
 
 // ----------------------------------------------------------------------------

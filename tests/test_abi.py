@@ -75,3 +75,40 @@ def test_null_handles_are_rejected():
     assert lib.nyxpm_synchronize(None) == 1
     assert lib.nyxpm_deposit(None, None, None) == 1
     assert lib.nyxpm_step(None, None, 0.1, 0.2, 1e-3, 0, None) == 1
+
+
+def test_dt_params_defaults_are_the_references():
+    lib = L.load()
+    dp = L.DtParams()
+    lib.nyxpm_default_dt_params(C.byref(dp))
+    assert (dp.cfl, dp.change_max, dp.relative_max_change_a) == (0.5, 1.1, 0.01)
+    assert dp.absolute_max_change_a < 0 and dp.final_a < 0 and dp.stop_time < 0 and dp.dt_binpow < 0
+
+
+@pytest.mark.parametrize("OmM,OmR,h", [(1.0, 0.0, 0.675), (0.3, 1e-4, 0.7)])
+def test_comoving_time_step_limit_equals_oracle_exactly(OmM, OmR, h):
+    """Nyx::comoving_est_time_step on the host: the relative and absolute a-change
+    limits, final_a and the power-of-two binning, bit for bit against the oracle."""
+    lib = L.load()
+    p = L.Params()
+    lib.nyxpm_default_params(C.byref(p))
+    p.comoving_OmM, p.comoving_OmR, p.comoving_h = OmM, OmR, h
+    cases = 0
+    for a in (0.01, 0.02, 0.1, 0.45, 0.9):
+        for estdt in (1e200, 1e-7, 2e-6, 3e-4):
+            for rel, absc in ((0.01, -1.0), (0.05, -1.0), (0.01, 0.0096), (0.01, 0.001)):
+                for final_a in (-1.0, 0.5):
+                    for binpow in (-1.0, 0.0):
+                        dp = L.DtParams()
+                        lib.nyxpm_default_dt_params(C.byref(dp))
+                        dp.relative_max_change_a, dp.absolute_max_change_a = rel, absc
+                        dp.final_a, dp.dt_binpow = final_a, binpow
+                        out = C.c_double(0)
+                        st = lib.nyxpm_comoving_est_dt(C.byref(p), a, estdt, C.byref(dp), C.byref(out))
+                        want, ost = O.comoving_est_dt(OmM, OmR, h, a, estdt, rel, absc, final_a, binpow)
+                        assert (st != 0) == (ost != 0), (a, estdt, rel, absc, final_a, binpow)
+                        if st == 0:
+                            assert out.value == want, (a, estdt, rel, absc, final_a, binpow)
+                            assert 0 < out.value <= estdt
+                            cases += 1
+    assert cases > 200

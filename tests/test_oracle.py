@@ -183,3 +183,23 @@ def test_zeldovich_pancake_known_answer():
         assert ex < 0.03, ex
         assert ev < 0.05, ev
         assert np.abs(ps[:, 1] - pos[:, 1]).max() < 1e-12
+
+
+def test_particle_time_step_limit():
+    """estTimestep (NyxParticleContainer.H:329-465): velocity CFL, the acceleration
+    limit and the no-particle / no-limit sentinels."""
+    n, L, a, cfl = 16, 1.0, 0.1, 0.5
+    dx = L / n
+    g = np.zeros(3 * n ** 3)
+    pos = np.array([[0.30, 0.41, 0.77], [0.9, 0.1, 0.5]])
+    vel = np.array([[2.0, -3.0, 1.0], [0.0, 0.0, 0.0]])
+    p = O.Particles(pos, vel, 1.0)
+    assert O.est_time_step(n, L, p, g, cfl, a) == cfl / (3.0 * (n / L / a))
+    p0 = O.Particles(pos, np.zeros_like(vel), 1.0)
+    assert O.est_time_step(n, L, p0, g, cfl, a) == 1e50
+    # acceleration at the particle's cell floor(x / dx) limits dt to 1/sqrt(|g|/dx)
+    c = 4 + n * (6 + n * 12)      # cell of particle 0: (0.30, 0.41, 0.77) * 16
+    g[c], g[n ** 3 + c], g[2 * n ** 3 + c] = 3.0, 4.0, 0.0
+    assert O.est_time_step(n, L, p0, g, cfl, a) == 1.0 / math.sqrt(5.0 / dx)
+    empty = O.Particles(np.zeros((0, 3)), np.zeros((0, 3)), 1.0)
+    assert O.est_time_step(n, L, empty, g, cfl, a) == -1e50

@@ -4,8 +4,9 @@ one (nyxpm_deposit), through the C ABI.
 nyxpm_deposit_noalloc serves callers that cannot allocate device memory (a host
 code whose arena owns the GPU's memory): the caller passes device input and
 output buffers, and the sort scratch is a static device array.  Its density must
-equal the allocating deposit's bit for bit (tolerance: exact), on two calls in a
-row -- the second call reuses the scratch the first one left behind.
+equal the allocating deposit's bit for bit (tolerance: exact), on calls in a row
+-- each call reuses the scratch the one before left behind -- including keys
+with far more particles than a warp (summed in lane-strided order).
 
 This file is collected last so that a failure here comes after every other test.
 """
@@ -41,15 +42,21 @@ def test_noalloc_deposit_equals_allocating_deposit_twice():
     ctx = Context(device=0)
     err = C.create_string_buffer(256)
     stream = torch.cuda.current_stream(0).cuda_stream
-    for call, (n, seed, slope) in enumerate([(64, 3, -2.0), (48, 4, -2.5)]):
-        ic = zeldovich_ics(n, 1.0, slope, seed, 0.05, rms_disp_cells=0.4)
-        box = Box(ctx, n, 1.0, len(ic.pos))
-        box.upload(ic.pos, ic.vel, ic.mass)
+    # two Zel'dovich particle sets, then one with keys far longer than a warp
+    rng = np.random.default_rng(11)
+    crowd = np.concatenate([0.40 + 0.02 * rng.random((3000, 3)), 0.7 + 0.01 * rng.random((700, 3)),
+                            rng.random((20000, 3))])
+    cases = [(64, zeldovich_ics(64, 1.0, -2.0, 3, 0.05, rms_disp_cells=0.4).pos, 2e9),
+             (48, zeldovich_ics(48, 1.0, -2.5, 4, 0.05, rms_disp_cells=0.4).pos, 3e9),
+             (32, crowd, 5e8)]
+    for call, (n, pos, mass) in enumerate(cases):
+        box = Box(ctx, n, 1.0, len(pos))
+        box.upload(pos, np.zeros_like(pos), mass)
         expect = box.deposit()
         box.close()
-        x, y, z, rho = _device_arrays(torch, ic.pos, n)
+        x, y, z, rho = _device_arrays(torch, pos, n)
         st = lib.nyxpm_deposit_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
-                                       C.c_void_p(z.data_ptr()), len(ic.pos), ic.mass, n, 1.0,
+                                       C.c_void_p(z.data_ptr()), len(pos), mass, n, 1.0,
                                        C.c_void_p(rho.data_ptr()), C.c_void_p(stream), err, len(err))
         assert st == 0, err.value.decode()
         torch.cuda.synchronize()
@@ -57,7 +64,7 @@ def test_noalloc_deposit_equals_allocating_deposit_twice():
         assert np.array_equal(got, expect), (call, float(np.nanmax(np.abs(got - expect))))
     # sizes beyond the static scratch are refused with a message, nothing launched
     st = lib.nyxpm_deposit_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
-                                   C.c_void_p(z.data_ptr()), len(ic.pos), ic.mass, 128, 1.0,
+                                   C.c_void_p(z.data_ptr()), len(pos), mass, 128, 1.0,
                                    C.c_void_p(rho.data_ptr()), C.c_void_p(stream), err, len(err))
     assert st == 1 and b"64" in err.value
     ctx.close()

@@ -750,6 +750,71 @@ __global__ void __launch_bounds__(256) e_gsrb(const Item* __restrict__ items, in
     }
 }
 
+// The same half sweep for levels whose compact rows hold a multiple of four
+// cells: four cells per thread, one 16-byte load per neighbour row.  The
+// item's rows are sized so that (rows x half/4) fills the block; the sums are
+// e_gsrb's, term for term, so the results are bitwise the same.
+__host__ __device__ inline int vec_rows(int n, int nthreads)
+{
+    const int h4 = (n >> 1) >> 2;
+    const int r = nthreads / h4;
+    return r < 1 ? 1 : (r > n ? n : r);
+}
+
+__global__ void __launch_bounds__(256) e_gsrb4(const Item* __restrict__ items, int nitems,
+                                               const EDesc* __restrict__ D,
+                                               const EState* __restrict__ S, int color)
+{
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        const ELevel& L = d.lv[it.a];
+        const int n = L.n, half = n >> 1, h4 = half >> 2, k = it.b;
+        const int rows = vec_rows(n, nthreads);
+        float* mine = color ? L.phi_b : L.phi_r;
+        const float* other = color ? L.phi_r : L.phi_b;
+        const float4* o4 = reinterpret_cast<const float4*>(other);
+        const float4* b4 = reinterpret_cast<const float4*>(color ? L.beta_b : L.beta_r);
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        for (int task = tid; task < rows * h4; task += nthreads) {
+            const int r = task / h4, t4 = task - r * h4;
+            const int j = it.c + r;
+            if (j >= n) continue;
+            const int ih = 4 * t4;
+            const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+            const long long rowbase = ((long long)j + (long long)n * k) * half;
+            const long long t = rowbase + ih;
+            const float4 c = __ldg(o4 + (t >> 2));
+            const float4 ym = __ldg(o4 + ((((long long)jm + (long long)n * k) * half + ih) >> 2));
+            const float4 yp = __ldg(o4 + ((((long long)jp + (long long)n * k) * half + ih) >> 2));
+            const float4 zm = __ldg(o4 + ((((long long)j + (long long)n * km) * half + ih) >> 2));
+            const float4 zp = __ldg(o4 + ((((long long)j + (long long)n * kp) * half + ih) >> 2));
+            const float4 b = __ldg(b4 + (t >> 2));
+            const int q = (j + k + color) & 1;
+            float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
+            if (q) {
+                const float edge = __ldg(other + rowbase + (ih + 4 == half ? 0 : ih + 4));
+                xm0 = c.x; xm1 = c.y; xm2 = c.z; xm3 = c.w;
+                xp0 = c.y; xp1 = c.z; xp2 = c.w; xp3 = edge;
+            } else {
+                const float edge = __ldg(other + rowbase + (ih == 0 ? half - 1 : ih - 1));
+                xm0 = edge; xm1 = c.x; xm2 = c.y; xm3 = c.z;
+                xp0 = c.x; xp1 = c.y; xp2 = c.z; xp3 = c.w;
+            }
+            float4 o;
+            o.x = fmaf(((((xm0 + xp0) + ym.x) + yp.x) + zm.x) + zp.x, kSixthF, -b.x);
+            o.y = fmaf(((((xm1 + xp1) + ym.y) + yp.y) + zm.y) + zp.y, kSixthF, -b.y);
+            o.z = fmaf(((((xm2 + xp2) + ym.z) + yp.z) + zm.z) + zp.z, kSixthF, -b.z);
+            o.w = fmaf(((((xm3 + xp3) + ym.w) + yp.w) + zm.w) + zp.w, kSixthF, -b.w);
+            reinterpret_cast<float4*>(mine)[t >> 2] = o;
+        }
+    }
+}
+
 __device__ __forceinline__ float resid_f(const ELevel& L, int i, int j, int k)
 {
     const int n = L.n;
@@ -1023,6 +1088,11 @@ struct nyxpm_ensemble {
     Range r_part, r_scan, r_keys, r_tile, r_rows_rho;
     Range r_rows_split[nyxpm::kMaxLev];   // rows of split levels (compact extent)
     Range r_rows_nat[nyxpm::kMaxLev];     // rows of levels >= 1 (natural coordinates)
+    // the smoother's items: levels whose compact rows hold a multiple of four
+    // cells take the vectorised kernel (row groups sized to fill a block), the
+    // others the row items above
+    Range r_smooth_vec[nyxpm::kMaxLev];
+    Range r_smooth_row[nyxpm::kMaxLev];
     nyxpm::EDesc* d_desc = nullptr;
     nyxpm::EState* d_state = nullptr;
     nyxpm::EStep* d_step = nullptr;
@@ -1148,6 +1218,27 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
                 for (int j0 = 0; j0 < nl; j0 += R) items.push_back(Item{b, l, k, j0});
         }
         end(E->r_rows_split[l]);
+        begin(E->r_smooth_vec[l]);
+        for (int b = 0; b < nbox; ++b) {
+            const EnsSlot& s = E->slots[b];
+            if (!s.used || l >= s.desc.nlev - 1) continue;
+            const int nl = s.desc.lv[l].n;
+            if ((nl / 2) % 4 != 0) continue;
+            const int rv = vec_rows(nl, 32 * R);
+            for (int k = 0; k < nl; ++k)
+                for (int j0 = 0; j0 < nl; j0 += rv) items.push_back(Item{b, l, k, j0});
+        }
+        end(E->r_smooth_vec[l]);
+        begin(E->r_smooth_row[l]);
+        for (int b = 0; b < nbox; ++b) {
+            const EnsSlot& s = E->slots[b];
+            if (!s.used || l >= s.desc.nlev - 1) continue;
+            const int nl = s.desc.lv[l].n;
+            if ((nl / 2) % 4 == 0) continue;
+            for (int k = 0; k < nl; ++k)
+                for (int j0 = 0; j0 < nl; j0 += R) items.push_back(Item{b, l, k, j0});
+        }
+        end(E->r_smooth_row[l]);
         begin(E->r_rows_nat[l]);
         for (int b = 0; b < nbox; ++b) {
             const EnsSlot& s = E->slots[b];
@@ -1279,17 +1370,30 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer)
     EState* S = E->d_state;
     const unsigned bb = (unsigned)((nbox + 127) / 128);
     const dim3 rb(32, E->tune.smooth_rows);
+    // one red or black half sweep of level l over every box: the vectorised
+    // kernel for the boxes whose level-l rows allow it, the row kernel for the rest
+    auto smooth = [&](int l, int color) {
+        const auto& rv = E->r_smooth_vec[l];
+        const auto& rr = E->r_smooth_row[l];
+        if (rv.cnt) {
+            e_gsrb4<<<pgrid(E, rv.cnt), rb, 0, s>>>(it + rv.off, rv.cnt, D, S, color);
+            c->launches += 1;
+        }
+        if (rr.cnt) {
+            e_gsrb<<<pgrid(E, rr.cnt), rb, 0, s>>>(it + rr.off, rr.cnt, D, S, color);
+            c->launches += 1;
+        }
+    };
     for (int o = 0; o < outer; ++o) {
         for (int v = 0; v < E->tune.inner_vcycles; ++v) {
             for (int l = 0; l < E->max_lev - 1; ++l) {
                 const auto& rs = E->r_rows_split[l];
                 if (rs.cnt == 0) continue;
                 for (int sw = 0; sw < c->p.nu1; ++sw)
-                    for (int color = 0; color < 2; ++color)
-                        e_gsrb<<<pgrid(E, rs.cnt), rb, 0, s>>>(it + rs.off, rs.cnt, D, S, color);
+                    for (int color = 0; color < 2; ++color) smooth(l, color);
                 const auto& rn = E->r_rows_nat[l + 1];
                 e_restrict<<<pgrid(E, rn.cnt), rb, 0, s>>>(it + rn.off, rn.cnt, D, S);
-                c->launches += 2 * c->p.nu1 + 1;
+                c->launches += 1;
             }
             e_bottom<<<nbox, 128, 0, s>>>(nbox, D, S);
             c->launches += 1;
@@ -1298,9 +1402,8 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer)
                 if (rs.cnt == 0) continue;
                 e_prolong<<<pgrid(E, rs.cnt), rb, 0, s>>>(it + rs.off, rs.cnt, D, S);
                 for (int sw = 0; sw < c->p.nu2; ++sw)
-                    for (int color = 0; color < 2; ++color)
-                        e_gsrb<<<pgrid(E, rs.cnt), rb, 0, s>>>(it + rs.off, rs.cnt, D, S, color);
-                c->launches += 2 * c->p.nu2 + 1;
+                    for (int color = 0; color < 2; ++color) smooth(l, color);
+                c->launches += 1;
             }
         }
         const auto& r0 = E->r_rows_split[0];

@@ -224,6 +224,40 @@ nyxpm_status nyxpm_compute_new_dt(nyxpm_ctx* ctx, nyxpm_box* box, const nyxpm_dt
                                   double time, double a, double dt_old, double* dt_new,
                                   double* a_new);
 
+/* ---- particle files and the comoving_a file (host I/O) ---------------------------- */
+
+/* Nyx's particle initial-condition files (nyx.particle_init_type, read by
+ * Nyx::init_particles, Source/Particle/NyxParticles.cpp:506-560; formats of
+ * Docs/sphinx_documentation/source/ICs.rst:13-78):
+ *   ASCII        first line the particle count, then "x y z mass vx vy vz" per line;
+ *   BINARY       int64 NP, int32 DM = 3, int32 NX >= 4, then NP records of DM + NX
+ *                float32 "x y z mass vx vy vz [extras]";
+ *   BINARY_META  a text file listing BINARY files, one per line, read in order. */
+typedef enum {
+    NYXPM_FILE_ASCII = 0,
+    NYXPM_FILE_BINARY = 1,
+    NYXPM_FILE_BINARY_META = 2
+} nyxpm_file_format;
+
+/* Number of particles the file holds (reads only the headers). */
+nyxpm_status nyxpm_particle_file_count(const char* path, nyxpm_file_format fmt, int64_t* np,
+                                       char* errbuf, size_t errlen);
+/* Reads the particles into host arrays laid out as nyxpm_box_upload takes them:
+ * pos[3 np], vel[3 np], mass[np].  capacity = the arrays' particle count. */
+nyxpm_status nyxpm_particle_file_read(const char* path, nyxpm_file_format fmt, int64_t capacity,
+                                      double* pos, double* vel, double* mass, int64_t* np_read,
+                                      char* errbuf, size_t errlen);
+/* Writes an ASCII (17 significant digits) or BINARY (float32) particle file;
+ * mass NULL writes mass_scalar for every particle. */
+nyxpm_status nyxpm_particle_file_write(const char* path, nyxpm_file_format fmt, int64_t np,
+                                       const double* pos, const double* vel, const double* mass,
+                                       double mass_scalar, char* errbuf, size_t errlen);
+/* The comoving_a file of a checkpoint or plotfile directory: written as
+ * Nyx::checkPointPost does (Source/IO/Nyx_output.cpp:994-1010, 15 significant
+ * digits), read as Nyx::comoving_a_post_restart does (comoving.cpp:690-705). */
+nyxpm_status nyxpm_write_comoving_a(const char* dir, double a, char* errbuf, size_t errlen);
+nyxpm_status nyxpm_read_comoving_a(const char* dir, double* a, char* errbuf, size_t errlen);
+
 /* ---- ensembles and serving ------------------------------------------------------ */
 
 /* An ensemble holds many independent periodic boxes of uneven sizes in the

@@ -36,8 +36,10 @@ EXPORTS = [
     "nyxpm_ensemble_grav_vector", "nyxpm_ensemble_set_tuning", "nyxpm_ensemble_get_tuning",
     "nyxpm_ensemble_step", "nyxpm_deposit_noalloc",
     "nyxpm_default_dt_params", "nyxpm_est_time_step", "nyxpm_comoving_est_dt",
-    "nyxpm_compute_new_dt",
+    "nyxpm_compute_new_dt", "nyxpm_particle_file_count", "nyxpm_particle_file_read",
+    "nyxpm_particle_file_write", "nyxpm_write_comoving_a", "nyxpm_read_comoving_a",
 ]
+NYXPM_FILE_ASCII, NYXPM_FILE_BINARY, NYXPM_FILE_BINARY_META = 0, 1, 2
 
 
 class Params(C.Structure):
@@ -169,6 +171,12 @@ def load(path: str | None = None):
     L.nyxpm_comoving_est_dt.argtypes = [C.POINTER(Params), d, d, C.POINTER(DtParams), C.POINTER(d)]
     L.nyxpm_compute_new_dt.argtypes = [vp, vp, C.POINTER(DtParams), d, d, d, C.POINTER(d),
                                        C.POINTER(d)]
+    cp, sz = C.c_char_p, C.c_size_t
+    L.nyxpm_particle_file_count.argtypes = [cp, C.c_int, C.POINTER(i64), cp, sz]
+    L.nyxpm_particle_file_read.argtypes = [cp, C.c_int, i64, vp, vp, vp, C.POINTER(i64), cp, sz]
+    L.nyxpm_particle_file_write.argtypes = [cp, C.c_int, i64, vp, vp, vp, d, cp, sz]
+    L.nyxpm_write_comoving_a.argtypes = [cp, d, cp, sz]
+    L.nyxpm_read_comoving_a.argtypes = [cp, C.POINTER(d), cp, sz]
     L.nyxpm_set_profiling.argtypes = [vp, C.c_int]
     L.nyxpm_get_profile.argtypes = [vp, C.POINTER(Profile), C.c_int]
     L.nyxpm_launch_count.argtypes = [vp]

@@ -30,6 +30,7 @@ UNITS = {
     "pm_mixed.cu": [],
     "pm_ensemble.cu": [],
     "pm_noalloc.cu": ["--fmad=false"],
+    "pm_io.cpp": [],
 }
 
 

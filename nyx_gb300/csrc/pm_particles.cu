@@ -373,35 +373,114 @@ __global__ void __launch_bounds__(256) k_deposit_heavy(int n, double dxi,
     }
 }
 
-// Pass 1 of the FP64 deposit, one thread per key: the key's eight corner sums
-// (a short key in sorted order; a long key's from k_deposit_heavy) into
-// part[corner * nc + K].  Every key is summed exactly once, with the whole SM
-// free for latency hiding (no shared memory).
-__global__ void __launch_bounds__(256) k_deposit_keys(long long nc, int n, double dxi,
-                                                      const double* __restrict__ x,
-                                                      const double* __restrict__ y,
-                                                      const double* __restrict__ z,
-                                                      const double* __restrict__ m,
-                                                      const int* __restrict__ start,
-                                                      const int* __restrict__ key_slot,
-                                                      const double* __restrict__ heavy_part,
-                                                      double* __restrict__ part)
+// Pass 1 of the FP64 deposit: the eight corner sums of every key into
+// part[corner * nc + K].  One warp takes 32 consecutive keys.  Their particles
+// (sorted, so contiguous) are numbered densely across the warp and each lane
+// computes the CIC weights of one particle per batch of 32, into shared
+// memory; then the adds run with eight lanes per key, one per corner, each
+// adding its key's particles of the batch in sorted order.  So every key is
+// summed in order, exactly as one thread would, while the expensive part (the
+// weights) is spread evenly over the lanes whatever the keys' occupancy.
+// Keys longer than a warp take their sums from k_deposit_heavy.
+constexpr int kKeyWarps = 8;
+
+__global__ void __launch_bounds__(32 * kKeyWarps) k_deposit_keys(long long nc, int n, double dxi,
+                                                                 const double* __restrict__ x,
+                                                                 const double* __restrict__ y,
+                                                                 const double* __restrict__ z,
+                                                                 const double* __restrict__ m,
+                                                                 const int* __restrict__ start,
+                                                                 const int* __restrict__ key_slot,
+                                                                 const double* __restrict__ heavy_part,
+                                                                 double* __restrict__ part)
 {
-    const long long K = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (K >= nc) return;
-    const int b0 = start[K], e = start[K + 1];
-    double s[8];
-    if (e - b0 > kDepositLanes) {
+    __shared__ double wbuf[kKeyWarps][32][9];   // a batch's weights (and masses)
+    __shared__ double acc[kKeyWarps][32][8];    // the warp's 32 keys' corner sums
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long K0 = ((long long)blockIdx.x * kKeyWarps + wid) * 32;
+    if (K0 >= nc) return;                        // the whole warp leaves together
+    const long long K = K0 + lane;
+    const bool valid = K < nc;
+    int b0 = 0, cnt = 0;
+    if (valid) {
+        b0 = start[K];
+        cnt = start[K + 1] - b0;
+    }
+    const bool heavy = cnt > kDepositLanes;
+    const int ml = heavy ? 0 : cnt;
+    int incl = ml;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int v = __shfl_up_sync(full, incl, off);
+        if (lane >= off) incl += v;
+    }
+    const int excl = incl - ml;
+    const int total = __shfl_sync(full, incl, 31);
+    double* mine = acc[wid][lane];
+    if (heavy) {
         const double* hp = heavy_part + 8LL * key_slot[K];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) s[c] = hp[c];
+        for (int c = 0; c < 8; ++c) mine[c] = hp[c];
     } else {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) s[c] = 0.0;
-        for (int q = b0; q < e; ++q) add_weights(q, n, dxi, x, y, z, m, s);
+        for (int c = 0; c < 8; ++c) mine[c] = 0.0;
     }
+    __syncwarp();
+    const int corner = lane & 7;
+    for (int base = 0; base < total; base += 32) {
+        // the lane owning particle number q: the first lane whose inclusive count exceeds q
+        const int q = base + lane;
+        int o = 0;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) part[c * nc + K] = s[c];
+        for (int bit = 16; bit >= 1; bit >>= 1) {
+            const int v = __shfl_sync(full, incl, o + bit - 1);
+            if (v <= q) o += bit;
+        }
+        const int ob0 = __shfl_sync(full, b0, o & 31);
+        const int oex = __shfl_sync(full, excl, o & 31);
+        if (q < total) {
+            const int p = ob0 + (q - oex);
+            double fx, fy, fz;
+            key1(x[p], dxi, n, &fx);
+            key1(y[p], dxi, n, &fy);
+            key1(z[p], dxi, n, &fz);
+            const double sx[2] = {1.0 - fx, fx};
+            const double sy[2] = {1.0 - fy, fy};
+            const double sz[2] = {1.0 - fz, fz};
+            double* w = wbuf[wid][lane];
+#pragma unroll
+            for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+                for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                    for (int cx = 0; cx < 2; ++cx) w[cx + 2 * cy + 4 * cz] = (sx[cx] * sy[cy]) * sz[cz];
+            if (m) w[8] = m[p];
+        }
+        __syncwarp();
+        // eight rounds of four keys x eight corners
+#pragma unroll 1
+        for (int r = 0; r < 8; ++r) {
+            const int ow = 4 * r + (lane >> 3);
+            const int oi = __shfl_sync(full, incl, ow);
+            const int oe = __shfl_sync(full, excl, ow);
+            const int lo = max(oe, base) - base, hi = min(oi, base + 32) - base;
+            if (lo < hi) {
+                double a = acc[wid][ow][corner];
+                if (m) {
+                    for (int t = lo; t < hi; ++t) a = fma(wbuf[wid][t][corner], wbuf[wid][t][8], a);
+                } else {
+                    for (int t = lo; t < hi; ++t) a = a + wbuf[wid][t][corner];
+                }
+                acc[wid][ow][corner] = a;
+            }
+        }
+        __syncwarp();
+    }
+    if (valid) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) part[c * nc + K] = mine[c];
+    }
 }
 
 // Pass 2, one thread per cell: the eight keys' corners in the fixed (dk, dj, di)
@@ -713,9 +792,10 @@ nyxpm_status launch_deposit(Ctx& c, Box& b)
                                                           b.heavy_part);
     if (b.key_part) {
         const long long ncl = (long long)n * n * n;
-        k_deposit_keys<<<blocks_for(ncl), kThreads, 0, c.stream>>>(ncl, n, b.dxi, b.x, b.y, b.z, mq,
-                                                                    b.cell_start, b.key_slot,
-                                                                    b.heavy_part, b.key_part);
+        const unsigned kb = (unsigned)((ncl + 32LL * kKeyWarps - 1) / (32LL * kKeyWarps));
+        k_deposit_keys<<<kb, 32 * kKeyWarps, 0, c.stream>>>(ncl, n, b.dxi, b.x, b.y, b.z, mq,
+                                                             b.cell_start, b.key_slot, b.heavy_part,
+                                                             b.key_part);
         const Geo g = geo3(n, n, n);
         k_deposit_cells<<<g.grid, g.block, 0, c.stream>>>(n, scale, b.key_part, b.rho);
         c.launches += 2;

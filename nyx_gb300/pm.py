@@ -178,9 +178,11 @@ class Box:
         vel = _f64(vel, (self.np, 3))
         if np.ndim(mass) == 0:
             self._c(self.ctx.lib.nyxpm_box_upload, _ptr(pos), _ptr(vel), None, float(mass), what="upload")
+            self.mass = float(mass)
         else:
             m = _f64(mass, (self.np,))
             self._c(self.ctx.lib.nyxpm_box_upload, _ptr(pos), _ptr(vel), _ptr(m), 0.0, what="upload")
+            self.mass = m.copy()
 
     def upload_ptr(self, pos_ptr: int, vel_ptr: int, mass: float):
         """Upload from raw host pointers (pinned buffers), uniform mass."""
@@ -277,6 +279,61 @@ class Box:
 
 
 # ---------------------------------------------------------------------------
+# particle files and the comoving_a file (host I/O in the library)
+# ---------------------------------------------------------------------------
+FILE_FORMATS = {"ascii": _L.NYXPM_FILE_ASCII, "binary": _L.NYXPM_FILE_BINARY,
+                "binary_meta": _L.NYXPM_FILE_BINARY_META}
+
+
+def _io_call(fn, *args):
+    err = C.create_string_buffer(512)
+    st = fn(*args, err, len(err))
+    if st != _L.NYXPM_OK:
+        raise NyxPMError(st, err.value.decode(errors="replace"))
+
+
+def read_particle_file(path: str, fmt: str = "ascii"):
+    """Nyx's AsciiFile / BinaryFile / BinaryMetaFile particle ICs -> (pos, vel, mass),
+    pos and vel (np, 3) float64, mass (np,) float64."""
+    lib = _L.load()
+    f = FILE_FORMATS[fmt]
+    np_ = C.c_int64(0)
+    _io_call(lib.nyxpm_particle_file_count, str(path).encode(), f, C.byref(np_))
+    n = np_.value
+    pos, vel, mass = np.empty((n, 3)), np.empty((n, 3)), np.empty(n)
+    got = C.c_int64(0)
+    _io_call(lib.nyxpm_particle_file_read, str(path).encode(), f, n, _ptr(pos), _ptr(vel),
+             _ptr(mass), C.byref(got))
+    return pos[:got.value], vel[:got.value], mass[:got.value]
+
+
+def write_particle_file(path: str, pos, vel, mass, fmt: str = "ascii"):
+    """Write particles as an AsciiFile or BinaryFile; mass is an array or a scalar."""
+    lib = _L.load()
+    pos = _f64(pos)
+    vel = _f64(vel)
+    marr = None if np.ndim(mass) == 0 else _f64(mass)
+    _io_call(lib.nyxpm_particle_file_write, str(path).encode(), FILE_FORMATS[fmt], len(pos),
+             _ptr(pos), _ptr(vel), _ptr(marr), float(mass) if marr is None else 0.0)
+
+
+def uniform_mass(mass):
+    """The scalar mass if every particle has the same one, else the array."""
+    mass = np.asarray(mass, dtype=np.float64)
+    return float(mass[0]) if mass.size and np.all(mass == mass[0]) else mass
+
+
+def write_comoving_a(directory: str, a: float):
+    _io_call(_L.load().nyxpm_write_comoving_a, str(directory).encode(), float(a))
+
+
+def read_comoving_a(directory: str) -> float:
+    a = C.c_double(0)
+    _io_call(_L.load().nyxpm_read_comoving_a, str(directory).encode(), C.byref(a))
+    return a.value
+
+
+# ---------------------------------------------------------------------------
 # the reference-named facade
 # ---------------------------------------------------------------------------
 class DarkMatterParticleContainer:
@@ -288,6 +345,29 @@ class DarkMatterParticleContainer:
     def InitFromArrays(self, pos, vel, mass):
         """Particle fill (init_particles AsciiFile/BinaryFile/Cosmological, NyxParticles.cpp:378-591)."""
         self.box.upload(pos, vel, mass)
+
+    def _init_from_file(self, path, fmt):
+        pos, vel, mass = read_particle_file(path, fmt)
+        if len(pos) != self.box.np:
+            raise NyxPMError(1, f"{path} holds {len(pos)} particles, the box {self.box.np}")
+        self.box.upload(pos, vel, uniform_mass(mass))
+
+    def InitFromAsciiFile(self, path, nextra: int = 4):
+        """nyx.particle_init_type = AsciiFile (NyxParticles.cpp:506-523)."""
+        self._init_from_file(path, "ascii")
+
+    def InitFromBinaryFile(self, path, nextra: int = 4):
+        """nyx.particle_init_type = BinaryFile (NyxParticles.cpp:525-543)."""
+        self._init_from_file(path, "binary")
+
+    def InitFromBinaryMetaFile(self, path, nextra: int = 4):
+        """nyx.particle_init_type = BinaryMetaFile (NyxParticles.cpp:545-560)."""
+        self._init_from_file(path, "binary_meta")
+
+    def WriteAsciiFile(self, path):
+        """The particles in AsciiFile layout (count line, then x y z mass vx vy vz)."""
+        pos, vel = self.box.download()
+        write_particle_file(path, pos, vel, self.box.mass)
 
     def moveKickDrift(self, acceleration=None, lev: int = 0, dt: float = 0.0, a_old: float = 1.0,
                       a_half: float = 1.0, where_width: int = 0):
@@ -394,6 +474,14 @@ class Nyx:
         self.particles.InitFromArrays(pos, vel, mass)
         self.gravity = Gravity(self.box)
         self.gravity.set_mass_offset()
+
+    def comoving_a_post_restart(self, restart_dir: str) -> float:
+        """Nyx::comoving_a_post_restart (comoving.cpp:690-705): a from <dir>/comoving_a."""
+        return read_comoving_a(restart_dir)
+
+    def write_comoving_a(self, directory: str, a: float):
+        """The comoving_a file of Nyx::checkPointPost (Nyx_output.cpp:994-1010)."""
+        write_comoving_a(directory, a)
 
     def post_init(self, a: float):
         """Nyx::post_init (Nyx.cpp:1957-2005): solve for phi at the initial a."""

@@ -258,6 +258,31 @@ nyxpm_status nyxpm_particle_file_write(const char* path, nyxpm_file_format fmt, 
 nyxpm_status nyxpm_write_comoving_a(const char* dir, double a, char* errbuf, size_t errlen);
 nyxpm_status nyxpm_read_comoving_a(const char* dir, double* a, char* errbuf, size_t errlen);
 
+/* Nyx's one-particle-per-cell cosmological ICs on a single level
+ * (DarkMatterParticleContainer::InitCosmo1ppcMultiLevel,
+ * Source/Particle/DarkMatterParticleContainer.cpp:309-450, called by Nyx::initcosmo,
+ * Source/Initialization/Nyx_initcosmo.cpp:100-427).  The particle of cell (i, j, k)
+ * sits at ((i + 1/2) dx + disp_x(i,j,k) * disp_fac[0], ...), shifted periodically
+ * into [0, L), with velocity vel_d(i,j,k) * vel_fac[d].  disp and vel hold 3 n^3
+ * values each, one component after another, x fastest: the displacement and
+ * velocity components of the IC MultiFab.  pos_out / vel_out: n^3 x 3.  Host only. */
+nyxpm_status nyxpm_cosmo_1ppc_particles(int n, double L, const double* disp, const double* vel,
+                                        const double* disp_fac, const double* vel_fac,
+                                        double* pos_out, double* vel_out);
+/* The factors and the particle mass Nyx::initcosmo takes for an IC source
+ * (Nyx_initcosmo.cpp:185-294), dark matter only: source 0 = MUSIC (disp_fac = L,
+ * vel_fac = L h, mass = rho_m dx^3), 1 = nyx (disp_fac = L,
+ * vel_fac = L a sqrt(OmM / a^3 + 1 - OmM) 100 h with a = 1 / (1 + redshift),
+ * mass = rho_m L^3 / n^3); rho_m = 3 (100 h)^2 OmM / (8 pi G). */
+nyxpm_status nyxpm_cosmo_ic_factors(const nyxpm_params* p, int source, int n, double L,
+                                    double redshift, double* disp_fac, double* vel_fac,
+                                    double* particle_mass);
+/* nyxpm_cosmo_1ppc_particles into the box (np must be n^3) with the uniform
+ * particle mass, as nyxpm_box_upload. */
+nyxpm_status nyxpm_box_init_cosmo_1ppc(nyxpm_ctx* ctx, nyxpm_box* box, const double* disp,
+                                       const double* vel, const double* disp_fac,
+                                       const double* vel_fac, double particle_mass);
+
 /* ---- ensembles and serving ------------------------------------------------------ */
 
 /* An ensemble holds many independent periodic boxes of uneven sizes in the

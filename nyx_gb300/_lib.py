@@ -38,6 +38,7 @@ EXPORTS = [
     "nyxpm_default_dt_params", "nyxpm_est_time_step", "nyxpm_comoving_est_dt",
     "nyxpm_compute_new_dt", "nyxpm_particle_file_count", "nyxpm_particle_file_read",
     "nyxpm_particle_file_write", "nyxpm_write_comoving_a", "nyxpm_read_comoving_a",
+    "nyxpm_cosmo_1ppc_particles", "nyxpm_cosmo_ic_factors", "nyxpm_box_init_cosmo_1ppc",
 ]
 NYXPM_FILE_ASCII, NYXPM_FILE_BINARY, NYXPM_FILE_BINARY_META = 0, 1, 2
 
@@ -177,6 +178,10 @@ def load(path: str | None = None):
     L.nyxpm_particle_file_write.argtypes = [cp, C.c_int, i64, vp, vp, vp, d, cp, sz]
     L.nyxpm_write_comoving_a.argtypes = [cp, d, cp, sz]
     L.nyxpm_read_comoving_a.argtypes = [cp, C.POINTER(d), cp, sz]
+    L.nyxpm_cosmo_1ppc_particles.argtypes = [C.c_int, d, vp, vp, vp, vp, vp, vp]
+    L.nyxpm_cosmo_ic_factors.argtypes = [C.POINTER(Params), C.c_int, C.c_int, d, d, vp, vp,
+                                         C.POINTER(d)]
+    L.nyxpm_box_init_cosmo_1ppc.argtypes = [vp, vp, vp, vp, vp, vp, d]
     L.nyxpm_set_profiling.argtypes = [vp, C.c_int]
     L.nyxpm_get_profile.argtypes = [vp, C.POINTER(Profile), C.c_int]
     L.nyxpm_launch_count.argtypes = [vp]

@@ -444,6 +444,20 @@ nyxpm_status nyxpm_box_upload(nyxpm_ctx* c, nyxpm_box* b, const double* pos, con
     return NYXPM_OK;
 }
 
+nyxpm_status nyxpm_box_init_cosmo_1ppc(nyxpm_ctx* c, nyxpm_box* b, const double* disp,
+                                       const double* vel, const double* disp_fac,
+                                       const double* vel_fac, double particle_mass)
+{
+    CHECK_BOX(c, b);
+    const int64_t nc = (int64_t)b->n * b->n * b->n;
+    if (b->np != nc) return fail(c, NYXPM_INVALID_ARG, "one particle per cell needs np = n^3");
+    std::vector<double> pos(3 * (size_t)nc), v(3 * (size_t)nc);
+    if (nyxpm_cosmo_1ppc_particles(b->n, b->L, disp, vel, disp_fac, vel_fac, pos.data(), v.data()) !=
+        NYXPM_OK)
+        return fail(c, NYXPM_INVALID_ARG, "null displacement/velocity field or factors");
+    return nyxpm_box_upload(c, b, pos.data(), v.data(), nullptr, particle_mass);
+}
+
 nyxpm_status nyxpm_box_download(nyxpm_ctx* c, nyxpm_box* b, double* pos, double* vel)
 {
     CHECK_BOX(c, b);

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cerrno>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -259,6 +260,68 @@ nyxpm_status nyxpm_particle_file_write(const char* path, nyxpm_file_format fmt, 
     }
     ok = (std::fclose(f) == 0) && ok;
     return ok ? NYXPM_OK : io_fail(errbuf, errlen, std::string("write failed: ") + path);
+}
+
+// ---------------------------------------------------------------------------
+// one-particle-per-cell cosmological ICs
+// ---------------------------------------------------------------------------
+nyxpm_status nyxpm_cosmo_1ppc_particles(int n, double L, const double* disp, const double* vel,
+                                        const double* disp_fac, const double* vel_fac, double* pos_out,
+                                        double* vel_out)
+{
+    if (n < 1 || !(L > 0) || !disp || !vel || !disp_fac || !vel_fac || !pos_out || !vel_out)
+        return NYXPM_INVALID_ARG;
+    const int64_t nc = (int64_t)n * n * n;
+    const double dx = L / n;
+    for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) {
+                const int64_t c = i + (int64_t)n * (j + (int64_t)n * k);
+                const int idx[3] = {i, j, k};
+                for (int d = 0; d < 3; ++d) {
+                    // cell centre, then the displacement (DarkMatterParticleContainer.cpp:376-386)
+                    double x = (idx[d] + 0.5) * dx;
+                    x = x + disp[d * nc + c] * disp_fac[d];
+                    // periodic shift into [0, L)
+                    if (x >= L) x = x - L;
+                    else if (x < 0.0) x = x + L;
+                    if (x >= L || x < 0.0) x = x - L * std::floor(x / L);
+                    if (x >= L) x = 0.0;
+                    pos_out[3 * c + d] = x;
+                    vel_out[3 * c + d] = vel[d * nc + c] * vel_fac[d];
+                }
+            }
+    return NYXPM_OK;
+}
+
+nyxpm_status nyxpm_cosmo_ic_factors(const nyxpm_params* p, int source, int n, double L,
+                                    double redshift, double* disp_fac, double* vel_fac,
+                                    double* particle_mass)
+{
+    if (!p || n < 1 || !(L > 0) || !disp_fac || !vel_fac || !particle_mass) return NYXPM_INVALID_ARG;
+    const double h = p->comoving_h, OmM = p->comoving_OmM;
+    // dark matter carries all the matter when there is no hydro (Nyx_initcosmo.cpp:185-208)
+    const double rho_m = 3.0 * h * 100.0 * h * 100.0 * OmM / (8.0 * M_PI * p->gconst);
+    const double dx = L / n;
+    if (source == 0) {              // MUSIC (Nyx_initcosmo.cpp:259-266)
+        for (int d = 0; d < 3; ++d) {
+            vel_fac[d] = L * h;
+            disp_fac[d] = L;
+        }
+        *particle_mass = rho_m * dx * dx * dx;
+    } else if (source == 1) {       // nyx (Nyx_initcosmo.cpp:281-294)
+        if (!(redshift > -1.0)) return NYXPM_INVALID_ARG;
+        const double a = 1.0 / (1.0 + redshift);
+        const double OmL = 1.0 - OmM;
+        for (int d = 0; d < 3; ++d) {
+            vel_fac[d] = L * a * std::sqrt(OmM / std::pow(a, 3) + OmL) * h * 100.0;
+            disp_fac[d] = L;
+        }
+        *particle_mass = rho_m * (L * L * L) / ((double)n * n * n);
+    } else {
+        return NYXPM_INVALID_ARG;
+    }
+    return NYXPM_OK;
 }
 
 nyxpm_status nyxpm_write_comoving_a(const char* dir, double a, char* errbuf, size_t errlen)

@@ -120,6 +120,16 @@ class Context:
             raise NyxPMError(st, "comoving_est_dt: a past final_a or no convergence")
         return out.value
 
+    def cosmo_ic_factors(self, source: str, n: int, L: float, redshift: float = -1.0):
+        """Nyx::initcosmo's (disp_fac, vel_fac, particle_mass) for ic-source "MUSIC" or "nyx"."""
+        df, vf, m = (C.c_double * 3)(), (C.c_double * 3)(), C.c_double(0)
+        src = {"MUSIC": 0, "nyx": 1}[source]
+        st = self.lib.nyxpm_cosmo_ic_factors(C.byref(self.params), src, int(n), float(L),
+                                             float(redshift), df, vf, C.byref(m))
+        if st != _L.NYXPM_OK:
+            raise NyxPMError(st, "cosmo_ic_factors: bad arguments")
+        return list(df), list(vf), m.value
+
     def hubble(self, a: float) -> float:
         p = self.params
         OmL = 1.0 - p.comoving_OmM - p.comoving_OmR
@@ -183,6 +193,16 @@ class Box:
             m = _f64(mass, (self.np,))
             self._c(self.ctx.lib.nyxpm_box_upload, _ptr(pos), _ptr(vel), _ptr(m), 0.0, what="upload")
             self.mass = m.copy()
+
+    def init_cosmo_1ppc(self, disp, vel, disp_fac, vel_fac, particle_mass: float):
+        """InitCosmo1ppcMultiLevel on this level: one particle per cell from the IC fields."""
+        disp = _f64(np.asarray(disp).reshape(3, -1))
+        vel = _f64(np.asarray(vel).reshape(3, -1))
+        df = _f64(np.asarray(disp_fac, dtype=np.float64))
+        vf = _f64(np.asarray(vel_fac, dtype=np.float64))
+        self._c(self.ctx.lib.nyxpm_box_init_cosmo_1ppc, _ptr(disp), _ptr(vel), _ptr(df), _ptr(vf),
+                float(particle_mass), what="init_cosmo_1ppc")
+        self.mass = float(particle_mass)
 
     def upload_ptr(self, pos_ptr: int, vel_ptr: int, mass: float):
         """Upload from raw host pointers (pinned buffers), uniform mass."""
@@ -321,6 +341,21 @@ def uniform_mass(mass):
     """The scalar mass if every particle has the same one, else the array."""
     mass = np.asarray(mass, dtype=np.float64)
     return float(mass[0]) if mass.size and np.all(mass == mass[0]) else mass
+
+
+def cosmo_1ppc_particles(n: int, L: float, disp, vel, disp_fac, vel_fac):
+    """One particle per cell from displacement and velocity fields (3, n^3) or
+    (3, n, n, n) in Nyx's component order (InitCosmo1ppcMultiLevel) -> (pos, vel)."""
+    lib = _L.load()
+    disp = _f64(np.asarray(disp).reshape(3, -1))
+    vel = _f64(np.asarray(vel).reshape(3, -1))
+    df, vf = _f64(np.asarray(disp_fac, dtype=np.float64)), _f64(np.asarray(vel_fac, dtype=np.float64))
+    pos, v = np.empty((n ** 3, 3)), np.empty((n ** 3, 3))
+    st = lib.nyxpm_cosmo_1ppc_particles(n, float(L), _ptr(disp), _ptr(vel), _ptr(df), _ptr(vf),
+                                        _ptr(pos), _ptr(v))
+    if st != _L.NYXPM_OK:
+        raise NyxPMError(st, "cosmo_1ppc_particles: bad arguments")
+    return pos, v
 
 
 def write_comoving_a(directory: str, a: float):

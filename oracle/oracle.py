@@ -79,6 +79,7 @@ def lib():
         L.orc_est_time_step.restype = C.c_double
         L.orc_est_time_step.argtypes = [C.c_int, C.c_double, C.c_long, _dp, _dp, _dp, _dp, _dp, _dp,
                                         _dp, C.c_double, C.c_double]
+        L.orc_cosmo_1ppc.argtypes = [C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_comoving_est_dt.restype = C.c_double
         L.orc_comoving_est_dt.argtypes = [C.c_double] * 9 + [C.POINTER(C.c_int)]
         L.orc_step.restype = C.c_int
@@ -228,6 +229,18 @@ def est_time_step(n, L, p: Particles, g, cfl, a) -> float:
     NyxParticleContainer.H:329-465) with the cell-centred gravity g."""
     return lib().orc_est_time_step(n, L, p.np, p.x, p.y, p.z, p.vx, p.vy, p.vz,
                                    np.ascontiguousarray(g, dtype=np.float64), cfl, a)
+
+
+def cosmo_1ppc(n, L, disp, vel, disp_fac, vel_fac):
+    """InitCosmo1ppcMultiLevel on one level (DarkMatterParticleContainer.cpp:309-450);
+    disp, vel (3, n^3) component-major -> (pos, vel) (n^3, 3)."""
+    pos = np.zeros((n ** 3, 3))
+    velo = np.zeros((n ** 3, 3))
+    lib().orc_cosmo_1ppc(n, L, np.ascontiguousarray(disp, dtype=np.float64).ravel(),
+                         np.ascontiguousarray(vel, dtype=np.float64).ravel(),
+                         np.ascontiguousarray(disp_fac, dtype=np.float64),
+                         np.ascontiguousarray(vel_fac, dtype=np.float64), pos, velo)
+    return pos, velo
 
 
 def comoving_est_dt(OmM, OmR, h, a, estdt, relative_max_change_a=0.01,

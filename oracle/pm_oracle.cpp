@@ -713,6 +713,35 @@ double orc_dt_for_da(double OmM, double OmR, double h, double a_old, double a_va
 }
 
 // ----------------------------------------------------------------------------
+// one-particle-per-cell cosmological ICs, InitCosmo1ppcMultiLevel on one level
+// (DarkMatterParticleContainer.cpp:309-450): the particle of cell (i,j,k) at
+// the cell centre plus disp * disp_fac (positions :376-386), shifted
+// periodically into [0, L); velocity vel * vel_fac.  disp, vel: 3 n^3,
+// component-major, x fastest.  pos/vel out: n^3 x 3.
+// ----------------------------------------------------------------------------
+void orc_cosmo_1ppc(int n, double L, const double* disp, const double* vel, const double* disp_fac,
+                    const double* vel_fac, double* pos, double* velo)
+{
+    const long nc = (long)n * n * n;
+    const double dx = L / n;
+    for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) {
+                const long c = cidx(i, j, k, n);
+                const int ijk[3] = {i, j, k};
+                for (int d = 0; d < 3; ++d) {
+                    double x = (ijk[d] + 0.5) * dx;
+                    x = x + disp[d * nc + c] * disp_fac[d];
+                    if (x >= L) x = x - L; else if (x < 0.0) x = x + L;
+                    if (x >= L || x < 0.0) x = x - L * std::floor(x / L);
+                    if (x >= L) x = 0.0;
+                    pos[3 * c + d] = x;
+                    velo[3 * c + d] = vel[d * nc + c] * vel_fac[d];
+                }
+            }
+}
+
+// ----------------------------------------------------------------------------
 // time-step control
 // ----------------------------------------------------------------------------
 

@@ -102,3 +102,44 @@ def test_comoving_a_file(tmp_path):
     text = (tmp_path / "comoving_a").read_text()
     assert text == f"{a:.15g}\n"                  # File.precision(15) << a
     assert read_comoving_a(tmp_path) == float(f"{a:.15g}")
+
+
+def test_cosmo_1ppc_particles_equal_oracle():
+    """InitCosmo1ppcMultiLevel: cell centres plus scaled displacements, periodic
+    shift (also of displacements beyond a box length), scaled velocities."""
+    from nyx_gb300.pm import cosmo_1ppc_particles
+    from oracle import oracle as O
+    n, L = 16, 7.5
+    rng = np.random.default_rng(9)
+    disp = rng.standard_normal((3, n ** 3)) * 0.05
+    disp[0, :10] = 1.7            # more than one box length (in units of L)
+    disp[1, 10:20] = -0.999
+    vel = rng.standard_normal((3, n ** 3))
+    df, vf = [L, L, L], [3.1, 3.1, 3.1]
+    pos, v = cosmo_1ppc_particles(n, L, disp, vel, df, vf)
+    opos, ov = O.cosmo_1ppc(n, L, disp, vel, df, vf)
+    assert np.array_equal(pos, opos) and np.array_equal(v, ov)
+    assert pos.min() >= 0.0 and pos.max() < L
+
+
+def test_cosmo_ic_factors_match_initcosmo():
+    """Nyx_initcosmo.cpp:185-294 for ic-source MUSIC and nyx, dark matter only."""
+    import math
+    from nyx_gb300.pm import Context
+    from oracle import oracle as O
+    ctx = Context.__new__(Context)          # host-only: no device context needed
+    import ctypes as C
+    from nyx_gb300 import _lib as L
+    ctx.lib = L.load()
+    ctx.params = L.Params()
+    ctx.lib.nyxpm_default_params(C.byref(ctx.params))
+    ctx.params.comoving_OmM, ctx.params.comoving_h = 0.3, 0.7
+    G = O.gconst()
+    rho = 3 * 0.7 * 100 * 0.7 * 100 * 0.3 / (8 * math.pi * G)
+    df, vf, m = ctx.cosmo_ic_factors("MUSIC", 64, 100.0)
+    assert df == [100.0] * 3 and vf == [100.0 * 0.7] * 3
+    assert m == rho * (100.0 / 64) ** 3
+    df, vf, m = ctx.cosmo_ic_factors("nyx", 64, 100.0, redshift=99.0)
+    a = 1 / (1 + 99.0)
+    assert vf[0] == 100.0 * a * math.sqrt(0.3 / math.pow(a, 3) + (1 - 0.3)) * 0.7 * 100
+    assert m == rho * (100.0 * 100.0 * 100.0) / (64.0 * 64 * 64)

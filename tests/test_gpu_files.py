@@ -37,3 +37,29 @@ def test_run_from_particle_file(ctx, tmp_path, fmt):
     rp, rv, rm = read_particle_file(out, "ascii")
     assert np.array_equal(rp, gpos) and np.array_equal(rv, gvel)
     box.close()
+
+
+def test_run_from_cosmological_fields(ctx):
+    """Nyx::initcosmo on one level: IC displacement and velocity fields (here the
+    Zel'dovich fields of the ICs generator, in box-length units) -> one particle
+    per cell on the GPU, then steps equal to the oracle's from the same particles."""
+    from nyx_gb300.pm import cosmo_1ppc_particles
+    n, L = 32, 1.0
+    ic = config1_ics(n, seed=6)
+    disp = (ic.pos - ic.lattice + 0.5 * L) % L - 0.5 * L       # displacement of each cell's particle
+    vel = ic.vel
+    df, vf = [L] * 3, [1.0] * 3
+    box = Box(ctx, n, L, n ** 3)
+    box.init_cosmo_1ppc(disp.T / L, vel.T, df, vf, ic.mass)
+    pos, v = cosmo_1ppc_particles(n, L, disp.T / L, vel.T, df, vf)
+    assert np.abs(min_image(pos - ic.pos, L)).max() < 1e-12
+    p = O.Particles(pos, v, ic.mass)
+    pm = O.PMOracle(n, L, p)
+    for a0, a1, dt in equal_da_schedule(0.02, 0.03, 2):
+        box.step(a0, a1, dt)
+        pm.step(a0, a1, dt)
+    gpos, gvel = box.download()
+    opos, ovel = p.by_id()
+    assert np.linalg.norm(min_image(gpos - opos, L)) / np.linalg.norm(opos) <= 1e-12
+    assert rel_l2(gvel, ovel) <= 1e-12
+    box.close()

@@ -859,6 +859,100 @@ __global__ void __launch_bounds__(256) e_restrict(const Item* __restrict__ items
     }
 }
 
+// The residual of four fine cells of one fine row (i = 4t .. 4t+3) of a split
+// level with half % 4 == 0, as resid_f computes each of them: in a row of parity
+// p the cells are colour p at compact 2t, colour 1-p at 2t, colour p at 2t+1 and
+// colour 1-p at 2t+1, so each colour array gives an 8-byte pair per row.
+__device__ __forceinline__ void fine_row_resid(const ELevel& F, int j, int k, unsigned t, float r[4])
+{
+    const int n = F.n;
+    const unsigned half = (unsigned)n >> 1;
+    const int p = (j + k) & 1;
+    const float* Pp = p ? F.phi_b : F.phi_r;
+    const float* Pq = p ? F.phi_r : F.phi_b;
+    const float* Bp = p ? F.beta_b : F.beta_r;
+    const float* Bq = p ? F.beta_r : F.beta_b;
+    const unsigned c2 = 2 * t;
+    auto row = [&](int jj, int kk) -> unsigned { return ((unsigned)jj + (unsigned)n * (unsigned)kk) * half; };
+    const unsigned r0 = row(j, k);
+    const float2 ep = __ldg(reinterpret_cast<const float2*>(Pp + r0 + c2));
+    const float2 eq = __ldg(reinterpret_cast<const float2*>(Pq + r0 + c2));
+    const float left = __ldg(Pq + r0 + (c2 == 0 ? half - 1 : c2 - 1));
+    const float right = __ldg(Pp + r0 + (c2 + 2 == half ? 0u : c2 + 2));
+    const float2 bp = __ldg(reinterpret_cast<const float2*>(Bp + r0 + c2));
+    const float2 bq = __ldg(reinterpret_cast<const float2*>(Bq + r0 + c2));
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    const unsigned nr[4] = {row(jm, k), row(jp, k), row(j, km), row(j, kp)};
+    float2 ne[4], no[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        ne[a] = __ldg(reinterpret_cast<const float2*>(Pq + nr[a] + c2));
+        no[a] = __ldg(reinterpret_cast<const float2*>(Pp + nr[a] + c2));
+    }
+    const float self[4] = {ep.x, eq.x, ep.y, eq.y};
+    const float xm[4] = {left, ep.x, eq.x, ep.y};
+    const float xp[4] = {eq.x, ep.y, eq.y, right};
+    const float beta[4] = {bp.x, bq.x, bp.y, bq.y};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const bool even = (c & 1) == 0;
+        const int h = c >> 1;
+        float s = xm[c] + xp[c];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const float2 v = even ? ne[a] : no[a];
+            s += h ? v.y : v.x;
+        }
+        r[c] = beta[c] - fmaf(s, kSixthF, -self[c]);
+    }
+}
+
+// e_restrict for boxes whose fine level allows the paired loads (fine
+// half % 4 == 0): two coarse cells per task, on e_restrict's row items.  The
+// coarse sums add the fine residuals in e_restrict's order.
+__global__ void __launch_bounds__(256) e_restrict4(const Item* __restrict__ items, int nitems,
+                                                   const EDesc* __restrict__ D,
+                                                   const EState* __restrict__ S)
+{
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int R = blockDim.y;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        const ELevel& F = d.lv[it.a - 1];
+        const ELevel& C = d.lv[it.a];
+        const int nc = C.n, K = it.b;
+        const int npair = nc >> 1;
+        for (int task = tid; task < R * npair; task += nthreads) {
+            const int rr = task / npair, t = task - rr * npair;
+            const int J = it.c + rr;
+            if (J >= nc) continue;
+            float r[2][2][4];
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+                for (int dj = 0; dj < 2; ++dj) fine_row_resid(F, 2 * J + dj, 2 * K + dk, (unsigned)t, r[dk][dj]);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                float s = 0.f;
+#pragma unroll
+                for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+                    for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+                        for (int di = 0; di < 2; ++di) s += r[dk][dj][2 * u + di];
+                const int I = 2 * t + u;
+                *lv_ptr<float>(C.beta_r, C.beta_b, nc, C.split, I, J, K) = s * 0.5f;
+                *lv_ptr<float>(C.phi_r, C.phi_b, nc, C.split, I, J, K) = 0.f;
+            }
+        }
+    }
+}
+
 // item level = the fine level (split); rows of the fine level
 __global__ void __launch_bounds__(256) e_prolong(const Item* __restrict__ items, int nitems,
                                                  const EDesc* __restrict__ D, const EState* __restrict__ S)
@@ -894,6 +988,113 @@ __global__ void __launch_bounds__(256) e_prolong(const Item* __restrict__ items,
                 float* p = (((i + j + k) & 1) ? F.phi_b : F.phi_r) + t;
                 *p += s;
             }
+        }
+    }
+}
+
+// The prolongation on the smoother's vectorised items: four compact columns
+// (eight fine cells) per task where the coarse level is split too (the six
+// coarse x-neighbours of each (J', K') row are a pair plus one in each colour
+// array), otherwise one column per task as e_prolong.  Same sums, same order.
+__global__ void __launch_bounds__(256) e_prolong4(const Item* __restrict__ items, int nitems,
+                                                  const EDesc* __restrict__ D,
+                                                  const EState* __restrict__ S)
+{
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        const ELevel& F = d.lv[it.a];
+        const ELevel& C = d.lv[it.a + 1];
+        const int n = F.n, nc = C.n, half = n >> 1, h4 = half >> 2, k = it.b;
+        const int rows = vec_rows(n, nthreads);
+        const int K = k >> 1;
+        const int Ks[2] = {K, wrap1((k & 1) ? K + 1 : K - 1, nc)};
+        if (!C.split) {
+            for (int task = tid; task < rows * half; task += nthreads) {
+                const int r = task / half, ih = task - r * half;
+                const int j = it.c + r;
+                if (j >= n) continue;
+                const int J = j >> 1;
+                const int Js[2] = {J, wrap1((j & 1) ? J + 1 : J - 1, nc)};
+                const long long t = ((long long)j + (long long)n * k) * half + ih;
+#pragma unroll
+                for (int odd = 0; odd < 2; ++odd) {
+                    const int i = 2 * ih + odd;
+                    const int Is[2] = {ih, wrap1(odd ? ih + 1 : ih - 1, nc)};
+                    float s = 0.f;
+#pragma unroll
+                    for (int b = 0; b < 2; ++b)
+#pragma unroll
+                        for (int a = 0; a < 2; ++a)
+#pragma unroll
+                            for (int tt = 0; tt < 2; ++tt)
+                                s = fmaf(kProlongWE[tt + 2 * a + 4 * b],
+                                         *lv_ptr<const float>(C.phi_r, C.phi_b, nc, C.split, Is[tt], Js[a],
+                                                              Ks[b]),
+                                         s);
+                    float* p = (((i + j + k) & 1) ? F.phi_b : F.phi_r) + t;
+                    *p += s;
+                }
+            }
+            continue;
+        }
+        const unsigned chalf = (unsigned)nc >> 1;
+        for (int task = tid; task < rows * h4; task += nthreads) {
+            const int r = task / h4, t4 = task - r * h4;
+            const int j = it.c + r;
+            if (j >= n) continue;
+            const int J = j >> 1;
+            const int Js[2] = {J, wrap1((j & 1) ? J + 1 : J - 1, nc)};
+            const unsigned c2 = 2 * (unsigned)t4;
+            float v[2][2][6];
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    const unsigned row = ((unsigned)Js[a] + (unsigned)nc * (unsigned)Ks[b]) * chalf;
+                    const bool even_red = ((Js[a] + Ks[b]) & 1) == 0;
+                    const float* ev = even_red ? C.phi_r : C.phi_b;
+                    const float* od = even_red ? C.phi_b : C.phi_r;
+                    const float2 e01 = __ldg(reinterpret_cast<const float2*>(ev + row + c2));
+                    const float e2 = __ldg(ev + row + (c2 + 2 == chalf ? 0u : c2 + 2));
+                    const float2 o01 = __ldg(reinterpret_cast<const float2*>(od + row + c2));
+                    const float om = __ldg(od + row + (c2 == 0 ? chalf - 1 : c2 - 1));
+                    v[b][a][0] = om;
+                    v[b][a][1] = e01.x;
+                    v[b][a][2] = o01.x;
+                    v[b][a][3] = e01.y;
+                    v[b][a][4] = o01.y;
+                    v[b][a][5] = e2;
+                }
+            float s0[4], s1[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float se = 0.f, so = 0.f;
+#pragma unroll
+                for (int b = 0; b < 2; ++b)
+#pragma unroll
+                    for (int a = 0; a < 2; ++a) {
+                        se = fmaf(kProlongWE[0 + 2 * a + 4 * b], v[b][a][q + 1], se);
+                        se = fmaf(kProlongWE[1 + 2 * a + 4 * b], v[b][a][q], se);
+                        so = fmaf(kProlongWE[0 + 2 * a + 4 * b], v[b][a][q + 1], so);
+                        so = fmaf(kProlongWE[1 + 2 * a + 4 * b], v[b][a][q + 2], so);
+                    }
+                s0[q] = se;
+                s1[q] = so;
+            }
+            const unsigned t = ((unsigned)j + (unsigned)n * (unsigned)k) * (unsigned)half + 4 * (unsigned)t4;
+            const bool even_fine_red = ((j + k) & 1) == 0;
+            float4* fe = reinterpret_cast<float4*>(even_fine_red ? F.phi_r : F.phi_b) + (t >> 2);
+            float4* fo = reinterpret_cast<float4*>(even_fine_red ? F.phi_b : F.phi_r) + (t >> 2);
+            float4 pe = *fe, po = *fo;
+            pe.x += s0[0]; pe.y += s0[1]; pe.z += s0[2]; pe.w += s0[3];
+            po.x += s1[0]; po.y += s1[1]; po.z += s1[2]; po.w += s1[3];
+            *fe = pe;
+            *fo = po;
         }
     }
 }
@@ -1093,6 +1294,9 @@ struct nyxpm_ensemble {
     // others the row items above
     Range r_smooth_vec[nyxpm::kMaxLev];
     Range r_smooth_row[nyxpm::kMaxLev];
+    // the restriction's coarse-row items, split the same way by the fine level
+    Range r_restrict_vec[nyxpm::kMaxLev];
+    Range r_restrict_row[nyxpm::kMaxLev];
     nyxpm::EDesc* d_desc = nullptr;
     nyxpm::EState* d_state = nullptr;
     nyxpm::EStep* d_step = nullptr;
@@ -1239,6 +1443,19 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
                 for (int j0 = 0; j0 < nl; j0 += R) items.push_back(Item{b, l, k, j0});
         }
         end(E->r_smooth_row[l]);
+        for (int vec = 1; vec >= 0; --vec) {
+            auto& rg = vec ? E->r_restrict_vec[l] : E->r_restrict_row[l];
+            begin(rg);
+            for (int b = 0; b < nbox; ++b) {
+                const EnsSlot& s = E->slots[b];
+                if (!s.used || l == 0 || l >= s.desc.nlev) continue;
+                if ((((s.desc.lv[l - 1].n / 2) % 4) == 0) != (vec == 1)) continue;
+                const int nl = s.desc.lv[l].n;
+                for (int k = 0; k < nl; ++k)
+                    for (int j0 = 0; j0 < nl; j0 += R) items.push_back(Item{b, l, k, j0});
+            }
+            end(rg);
+        }
         begin(E->r_rows_nat[l]);
         for (int b = 0; b < nbox; ++b) {
             const EnsSlot& s = E->slots[b];
@@ -1323,6 +1540,23 @@ nyxpm_status pull_state(nyxpm_ctx* c, nyxpm_ensemble* E)
     return NYXPM_OK;
 }
 
+// Stage timing of the eager profiling step (nyxpm_set_profiling on): CUDA
+// events around each group of launches.  Never active while a graph is being
+// captured (the profiled step runs without graphs), and the launch counts are
+// kept by the enqueue functions themselves.
+inline void ep_begin(nyxpm_ctx* c)
+{
+    if (!c->prof_on) return;
+    const int64_t l = c->launches;
+    prof_begin(*c);
+    c->launches = l;
+}
+
+inline void ep_end(nyxpm_ctx* c, int stage)
+{
+    if (c->prof_on) prof_end(*c, stage, 0.0);
+}
+
 // sort + deposit + RHS + first residual + targets of the active boxes
 void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
 {
@@ -1332,16 +1566,25 @@ void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
     const EDesc* D = E->d_desc;
     EState* S = E->d_state;
     const unsigned bb = (unsigned)((nbox + 127) / 128);
+    ep_begin(c);
     e_sort_reset<<<bb, 128, 0, s>>>(nbox, D, S);
     e_keys<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S);
+    ep_end(c, NYXPM_ST_KEYS);
+    ep_begin(c);
     e_scan_reduce<<<pgrid(E, E->r_scan.cnt), kScanT, 0, s>>>(it + E->r_scan.off, E->r_scan.cnt, D, S);
     e_scan_top<<<nbox, 1024, 0, s>>>(nbox, D, S);
     e_scan_down<<<pgrid(E, E->r_scan.cnt), kScanT, 0, s>>>(it + E->r_scan.off, E->r_scan.cnt, D, S);
+    ep_end(c, NYXPM_ST_SCAN);
+    ep_begin(c);
     e_scatter<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S);
     e_fix_short<<<pgrid(E, E->r_keys.cnt), 256, 0, s>>>(it + E->r_keys.off, E->r_keys.cnt, D, S);
     e_fix_long<<<E->sm * 2, 512, 0, s>>>(nbox, D, S);
+    ep_end(c, NYXPM_ST_SCATTER);
+    ep_begin(c);
     e_gather<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S);
     e_flip<<<bb, 128, 0, s>>>(nbox, S);
+    ep_end(c, NYXPM_ST_GATHER);
+    ep_begin(c);
     const unsigned gt = pgrid(E, E->r_tile.cnt, 4);
     if (E->tune.deposit_tile == 1)
         e_deposit<8, 8, 4><<<gt, 256, 0, s>>>(it + E->r_tile.off, E->r_tile.cnt, D, S);
@@ -1349,6 +1592,8 @@ void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
         e_deposit<16, 8, 4><<<gt, 256, 0, s>>>(it + E->r_tile.off, E->r_tile.cnt, D, S);
     else
         e_deposit<8, 8, 8><<<gt, 256, 0, s>>>(it + E->r_tile.off, E->r_tile.cnt, D, S);
+    ep_end(c, NYXPM_ST_DEPOSIT);
+    ep_begin(c);
     e_rowsum<<<pgrid(E, E->r_rows_rho.cnt), 256, 0, s>>>(it + E->r_rows_rho.off, E->r_rows_rho.cnt, D, S);
     e_mean<<<nbox, 512, 0, s>>>(nbox, D, S);
     const dim3 rb(32, E->tune.smooth_rows);
@@ -1357,6 +1602,7 @@ void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
     e_make_beta<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, ggrav);
     e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
     e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 1);
+    ep_end(c, NYXPM_ST_RHS);
     c->launches += 16;
 }
 
@@ -1375,6 +1621,7 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer)
     auto smooth = [&](int l, int color) {
         const auto& rv = E->r_smooth_vec[l];
         const auto& rr = E->r_smooth_row[l];
+        ep_begin(c);
         if (rv.cnt) {
             e_gsrb4<<<pgrid(E, rv.cnt), rb, 0, s>>>(it + rv.off, rv.cnt, D, S, color);
             c->launches += 1;
@@ -1383,6 +1630,7 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer)
             e_gsrb<<<pgrid(E, rr.cnt), rb, 0, s>>>(it + rr.off, rr.cnt, D, S, color);
             c->launches += 1;
         }
+        ep_end(c, NYXPM_ST_SMOOTH);
     };
     for (int o = 0; o < outer; ++o) {
         for (int v = 0; v < E->tune.inner_vcycles; ++v) {
@@ -1391,26 +1639,41 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer)
                 if (rs.cnt == 0) continue;
                 for (int sw = 0; sw < c->p.nu1; ++sw)
                     for (int color = 0; color < 2; ++color) smooth(l, color);
-                const auto& rn = E->r_rows_nat[l + 1];
-                e_restrict<<<pgrid(E, rn.cnt), rb, 0, s>>>(it + rn.off, rn.cnt, D, S);
+                const auto& qv = E->r_restrict_vec[l + 1];
+                const auto& qr = E->r_restrict_row[l + 1];
+                ep_begin(c);
+                if (qv.cnt) e_restrict4<<<pgrid(E, qv.cnt), rb, 0, s>>>(it + qv.off, qv.cnt, D, S);
+                if (qr.cnt) e_restrict<<<pgrid(E, qr.cnt), rb, 0, s>>>(it + qr.off, qr.cnt, D, S);
+                ep_end(c, NYXPM_ST_RESTRICT);
+                c->launches += (qv.cnt ? 1 : 0) + (qr.cnt ? 1 : 0) - 1;
                 c->launches += 1;
             }
+            ep_begin(c);
             e_bottom<<<nbox, 128, 0, s>>>(nbox, D, S);
+            ep_end(c, NYXPM_ST_BOTTOM);
             c->launches += 1;
             for (int l = E->max_lev - 2; l >= 0; --l) {
                 const auto& rs = E->r_rows_split[l];
                 if (rs.cnt == 0) continue;
-                e_prolong<<<pgrid(E, rs.cnt), rb, 0, s>>>(it + rs.off, rs.cnt, D, S);
+                const auto& pv = E->r_smooth_vec[l];
+                const auto& pr = E->r_smooth_row[l];
+                ep_begin(c);
+                if (pv.cnt) e_prolong4<<<pgrid(E, pv.cnt), rb, 0, s>>>(it + pv.off, pv.cnt, D, S);
+                if (pr.cnt) e_prolong<<<pgrid(E, pr.cnt), rb, 0, s>>>(it + pr.off, pr.cnt, D, S);
+                ep_end(c, NYXPM_ST_PROLONG);
+                c->launches += (pv.cnt ? 1 : 0) + (pr.cnt ? 1 : 0) - 1;
                 for (int sw = 0; sw < c->p.nu2; ++sw)
                     for (int color = 0; color < 2; ++color) smooth(l, color);
                 c->launches += 1;
             }
         }
         const auto& r0 = E->r_rows_split[0];
+        ep_begin(c);
         e_count_inner<<<bb, 128, 0, s>>>(nbox, S, E->tune.inner_vcycles);
         e_update<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
         e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
         e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 0);
+        ep_end(c, NYXPM_ST_NORM);
         c->launches += 4;
     }
 }
@@ -1419,14 +1682,18 @@ void enqueue_grav(nyxpm_ctx* c, nyxpm_ensemble* E)
 {
     const dim3 rb(32, E->tune.smooth_rows);
     const auto& r0 = E->r_rows_split[0];
+    ep_begin(c);
     e_grav<<<pgrid(E, r0.cnt), rb, 0, c->stream>>>(E->d_items + r0.off, r0.cnt, E->d_desc, E->d_state);
+    ep_end(c, NYXPM_ST_KICK);
     c->launches += 1;
 }
 
 void enqueue_kick(nyxpm_ctx* c, nyxpm_ensemble* E, int phase)
 {
+    ep_begin(c);
     e_kick<<<pgrid(E, E->r_part.cnt), kPT, 0, c->stream>>>(E->d_items + E->r_part.off, E->r_part.cnt,
                                                             E->d_desc, E->d_state, phase);
+    ep_end(c, NYXPM_ST_KICK);
     c->launches += 1;
 }
 
@@ -1461,6 +1728,7 @@ nyxpm_status capture(nyxpm_ctx* c, nyxpm_ensemble* E, cudaGraphExec_t* exec, int
 {
     cudaGraph_t g = nullptr;
     const int64_t l0 = c->launches;
+    if (c->prof_on) return efail(c, NYXPM_INVALID_ARG, "ensemble graphs are not captured while profiling");
     if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return echeck(c, "ensemble capture begin");
     if (which == 0) {
@@ -1854,15 +2122,29 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* c, nyxpm_ensemble* E, const double* 
         E->h_step[b].a_new = a_new[b];
         E->h_step[b].dt = dt[b];
     }
-    if (!E->exec_solve) ETRY(capture(c, E, &E->exec_solve, 0));
-    if (!E->exec_finish) ETRY(capture(c, E, &E->exec_finish, 1));
-    if (cudaGraphLaunch(E->exec_solve, c->stream) != cudaSuccess) return echeck(c, "ensemble solve graph");
-    c->launches += E->graph_launches_solve;
-    int more = 0;
-    ETRY(finish_unconverged(c, E, &more));
-    extra += more;
-    if (cudaGraphLaunch(E->exec_finish, c->stream) != cudaSuccess) return echeck(c, "ensemble finish graph");
-    c->launches += E->graph_launches_finish;
+    if (c->prof_on) {
+        // profiling: the same launches eagerly, with stage events (no graphs)
+        enqueue_load(c, E, E->h_step);
+        enqueue_kick(c, E, 0);
+        enqueue_solve_head(c, E);
+        enqueue_iterations(c, E, E->tune.max_outer);
+        ETRY(echeck(c, "ensemble profiled step"));
+        int more = 0;
+        ETRY(finish_unconverged(c, E, &more));
+        extra += more;
+        enqueue_grav(c, E);
+        enqueue_kick(c, E, 1);
+    } else {
+        if (!E->exec_solve) ETRY(capture(c, E, &E->exec_solve, 0));
+        if (!E->exec_finish) ETRY(capture(c, E, &E->exec_finish, 1));
+        if (cudaGraphLaunch(E->exec_solve, c->stream) != cudaSuccess) return echeck(c, "ensemble solve graph");
+        c->launches += E->graph_launches_solve;
+        int more = 0;
+        ETRY(finish_unconverged(c, E, &more));
+        extra += more;
+        if (cudaGraphLaunch(E->exec_finish, c->stream) != cudaSuccess) return echeck(c, "ensemble finish graph");
+        c->launches += E->graph_launches_finish;
+    }
     cudaEventRecord(ev1, c->stream);
     if (cudaEventSynchronize(ev1) != cudaSuccess) return echeck(c, "ensemble step");
     float ms = 0.f;

@@ -409,6 +409,67 @@ __global__ void k_mx_resid(int n, const double* __restrict__ phi_r, const double
     block_umax_store(v, norm);
 }
 
+// The same residual, two compact cells of each colour per thread (16-byte
+// loads of FP64 pairs) for rows of an even number of compact cells.  Every
+// residual is k_mx_resid's, term for term.
+__global__ void k_mx_resid2(int n, const double* __restrict__ phi_r, const double* __restrict__ phi_b,
+                            const double* __restrict__ beta_r, const double* __restrict__ beta_b,
+                            float* r_r, float* r_b, unsigned long long* norm)
+{
+    const unsigned half = (unsigned)n >> 1;
+    const unsigned t2 = blockIdx.x * blockDim.x + threadIdx.x;   // compact cells 2 t2, 2 t2 + 1
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    unsigned long long v = 0;
+    if (t2 < half / 2 && j < n) {
+        const unsigned ih = 2 * t2;
+        const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        auto row = [&](int jj, int kk) -> unsigned { return ((unsigned)jj + (unsigned)n * (unsigned)kk) * half; };
+        const unsigned r0 = row(j, k);
+        const unsigned t = r0 + ih;
+#pragma unroll
+        for (int color = 0; color < 2; ++color) {
+            const int q = (j + k + color) & 1;
+            const double* other = color ? phi_r : phi_b;
+            const double* mine = color ? phi_b : phi_r;
+            const double* beta = color ? beta_b : beta_r;
+            const double2 c = __ldg(reinterpret_cast<const double2*>(other + t));
+            double xm0, xm1, xp0, xp1;
+            if (q) {   // neighbours ih, ih + 1
+                const double e = __ldg(other + r0 + (ih + 2 == half ? 0u : ih + 2));
+                xm0 = c.x; xp0 = c.y; xm1 = c.y; xp1 = e;
+            } else {   // neighbours ih - 1, ih
+                const double e = __ldg(other + r0 + (ih == 0 ? half - 1 : ih - 1));
+                xm0 = e; xp0 = c.x; xm1 = c.x; xp1 = c.y;
+            }
+            const double2 ym = __ldg(reinterpret_cast<const double2*>(other + row(jm, k) + ih));
+            const double2 yp = __ldg(reinterpret_cast<const double2*>(other + row(jp, k) + ih));
+            const double2 zm = __ldg(reinterpret_cast<const double2*>(other + row(j, km) + ih));
+            const double2 zp = __ldg(reinterpret_cast<const double2*>(other + row(j, kp) + ih));
+            const double2 b = __ldg(reinterpret_cast<const double2*>(beta + t));
+            const double2 m = __ldg(reinterpret_cast<const double2*>(mine + t));
+            double s0 = xm0 + xp0;
+            s0 = s0 + ym.x;
+            s0 = s0 + yp.x;
+            s0 = s0 + zm.x;
+            s0 = s0 + zp.x;
+            double s1 = xm1 + xp1;
+            s1 = s1 + ym.y;
+            s1 = s1 + yp.y;
+            s1 = s1 + zm.y;
+            s1 = s1 + zp.y;
+            const double r0v = b.x - fma(s0, kSixth, -m.x);
+            const double r1v = b.y - fma(s1, kSixth, -m.y);
+            reinterpret_cast<float2*>(color ? r_b : r_r)[t >> 1] = make_float2((float)r0v, (float)r1v);
+            const unsigned long long u0 = absbits(r0v), u1 = absbits(r1v);
+            v = u0 > v ? u0 : v;
+            v = u1 > v ? u1 : v;
+        }
+    }
+    block_umax_store(v, norm);
+}
+
 // the same for a natural-layout level 0 (n <= 8)
 __global__ void k_mx_resid_nat(int n, const double* __restrict__ phi, const double* __restrict__ beta,
                                float* r, unsigned long long* norm)
@@ -470,35 +531,40 @@ __global__ void __launch_bounds__(256) k_gsrb_f4(int n, int color, float* __rest
                                                  const float* __restrict__ other,
                                                  const float* __restrict__ beta)
 {
-    const int half = n >> 1, h4 = half >> 2;
-    const int t4 = blockIdx.x * blockDim.x + threadIdx.x;
+    // 32-bit offsets: a level holds at most 1024^3 / 2 cells of a colour
+    const unsigned half = (unsigned)n >> 1, h4 = half >> 2;
+    const unsigned t4 = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k0 = blockIdx.z * kMarchZ;
     if (t4 >= h4 || j >= n) return;
-    const int ih = 4 * t4;
+    const unsigned ih = 4 * t4;
+    const unsigned plane = (unsigned)n * half;
     const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
-    const long long plane = (long long)n * half;
+    const unsigned rj = (unsigned)j * half + ih, rjm = (unsigned)jm * half + ih,
+                   rjp = (unsigned)jp * half + ih;
     const float4* o4 = reinterpret_cast<const float4*>(other);
-    auto row4 = [&](int jj, int kk) -> long long {  // float4 index of (ih, jj, kk)
-        return (((long long)jj + (long long)n * kk) * half + ih) >> 2;
-    };
+    const float4* b4 = reinterpret_cast<const float4*>(beta);
+    float4* m4 = reinterpret_cast<float4*>(mine);
     const int kfirst = k0 == 0 ? n - 1 : k0 - 1;
-    float4 zm = __ldg(o4 + row4(j, kfirst));
-    float4 c = __ldg(o4 + row4(j, k0));
-    const int kend = min(k0 + kMarchZ, n);
-    for (int k = k0; k < kend; ++k) {
+    float4 zm = __ldg(o4 + (((unsigned)kfirst * plane + rj) >> 2));
+    float4 c = __ldg(o4 + (((unsigned)k0 * plane + rj) >> 2));
+    // the levels this kernel runs on have n % 8 == 0: every block marches kMarchZ planes
+#pragma unroll
+    for (int kk = 0; kk < kMarchZ; ++kk) {
+        const int k = k0 + kk;
         const int kp = k == n - 1 ? 0 : k + 1;
-        const float4 zp = __ldg(o4 + row4(j, kp));
-        const float4 ym = __ldg(o4 + row4(jm, k));
-        const float4 yp = __ldg(o4 + row4(jp, k));
-        const long long t = ((long long)j + (long long)n * k) * half + ih;
-        const float4 b = __ldg(reinterpret_cast<const float4*>(beta) + (t >> 2));
+        const unsigned pk = (unsigned)k * plane;
+        const float4 zp = __ldg(o4 + (((unsigned)kp * plane + rj) >> 2));
+        const float4 ym = __ldg(o4 + ((pk + rjm) >> 2));
+        const float4 yp = __ldg(o4 + ((pk + rjp) >> 2));
+        const unsigned t = pk + rj;
+        const float4 b = __ldg(b4 + (t >> 2));
         const int q = (j + k + color) & 1;
         // x neighbours: q = 1 -> (ih, ih+1), q = 0 -> (ih-1, ih) of the other colour
-        const long long rowbase = t - ih;
+        const unsigned rowbase = t - ih;
         float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
         if (q) {
-            const float edge = __ldg(other + rowbase + (ih + 4 == half ? 0 : ih + 4));
+            const float edge = __ldg(other + rowbase + (ih + 4 == half ? 0u : ih + 4));
             xm0 = c.x; xm1 = c.y; xm2 = c.z; xm3 = c.w;
             xp0 = c.y; xp1 = c.z; xp2 = c.w; xp3 = edge;
         } else {
@@ -511,7 +577,7 @@ __global__ void __launch_bounds__(256) k_gsrb_f4(int n, int color, float* __rest
         r.y = fmaf(((((xm1 + xp1) + ym.y) + yp.y) + zm.y) + zp.y, kSixthF, -b.y);
         r.z = fmaf(((((xm2 + xp2) + ym.z) + yp.z) + zm.z) + zp.z, kSixthF, -b.z);
         r.w = fmaf(((((xm3 + xp3) + ym.w) + yp.w) + zm.w) + zp.w, kSixthF, -b.w);
-        reinterpret_cast<float4*>(mine)[t >> 2] = r;
+        m4[t >> 2] = r;
         zm = c;
         c = zp;
     }
@@ -551,6 +617,87 @@ __global__ void k_restrict_f(LevelViewF F, LevelViewF Cv)
     *lv_ptr<float>(Cv.phi_r, Cv.phi_b, nc, Cv.split, I, J, K) = 0.f;
 }
 
+// The residual + restriction for a split fine level with half % 4 == 0: two
+// coarse cells (four fine cells of each of their four fine rows) per thread.
+// In a fine row of parity p = (j + k) & 1 the cells i = 4t .. 4t+3 are, in
+// order, colour p at compact 2t, colour 1-p at 2t, colour p at 2t+1, colour
+// 1-p at 2t+1: one 8-byte pair per colour array and row.  Every fine residual
+// is resid_f's, term for term, and the coarse sums add them in the same
+// (dk, dj, di) order.
+__device__ __forceinline__ void fine_row_resid(const LevelViewF& F, int j, int k, unsigned t,
+                                               float r[4])
+{
+    const int n = F.n;
+    const unsigned half = (unsigned)n >> 1;
+    const int p = (j + k) & 1;
+    const float* Pp = p ? F.phi_b : F.phi_r;      // colour of even i in this row
+    const float* Pq = p ? F.phi_r : F.phi_b;
+    const float* Bp = p ? F.beta_b : F.beta_r;
+    const float* Bq = p ? F.beta_r : F.beta_b;
+    const unsigned c2 = 2 * t;
+    auto row = [&](int jj, int kk) -> unsigned { return ((unsigned)jj + (unsigned)n * (unsigned)kk) * half; };
+    const unsigned r0 = row(j, k);
+    const float2 ep = __ldg(reinterpret_cast<const float2*>(Pp + r0 + c2));   // phi(4t), phi(4t+2)
+    const float2 eq = __ldg(reinterpret_cast<const float2*>(Pq + r0 + c2));   // phi(4t+1), phi(4t+3)
+    const float left = __ldg(Pq + r0 + (c2 == 0 ? half - 1 : c2 - 1));        // phi(4t-1)
+    const float right = __ldg(Pp + r0 + (c2 + 2 == half ? 0u : c2 + 2));      // phi(4t+4)
+    const float2 bp = __ldg(reinterpret_cast<const float2*>(Bp + r0 + c2));
+    const float2 bq = __ldg(reinterpret_cast<const float2*>(Bq + r0 + c2));
+    // neighbour rows have the other parity: even i there is colour 1-p
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    const unsigned nr[4] = {row(jm, k), row(jp, k), row(j, km), row(j, kp)};
+    float2 ne[4], no[4];   // neighbour rows: values at even i (colour 1-p), odd i (colour p)
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        ne[a] = __ldg(reinterpret_cast<const float2*>(Pq + nr[a] + c2));
+        no[a] = __ldg(reinterpret_cast<const float2*>(Pp + nr[a] + c2));
+    }
+    const float self[4] = {ep.x, eq.x, ep.y, eq.y};
+    const float xm[4] = {left, ep.x, eq.x, ep.y};
+    const float xp[4] = {eq.x, ep.y, eq.y, right};
+    const float beta[4] = {bp.x, bq.x, bp.y, bq.y};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const bool even = (c & 1) == 0;
+        const int h = c >> 1;
+        float s = xm[c] + xp[c];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const float2 v = even ? ne[a] : no[a];
+            s += h ? v.y : v.x;
+        }
+        r[c] = beta[c] - fmaf(s, kSixthF, -self[c]);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_restrict_f4(LevelViewF F, LevelViewF Cv)
+{
+    const int nc = Cv.n;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // coarse cells 2t, 2t+1
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z;
+    if (t >= (unsigned)nc / 2 || J >= nc) return;
+    float r[2][2][4];
+#pragma unroll
+    for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj) fine_row_resid(F, 2 * J + dj, 2 * K + dk, t, r[dk][dj]);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        float s = 0.f;
+#pragma unroll
+        for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+            for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+                for (int di = 0; di < 2; ++di) s += r[dk][dj][2 * u + di];
+        const int I = 2 * (int)t + u;
+        *lv_ptr<float>(Cv.beta_r, Cv.beta_b, nc, Cv.split, I, J, K) = s * 0.5f;
+        *lv_ptr<float>(Cv.phi_r, Cv.phi_b, nc, Cv.split, I, J, K) = 0.f;
+    }
+}
+
 __global__ void k_prolong_f(LevelViewF Cv, LevelViewF F)
 {
     const int n = F.n, nc = Cv.n, half = n >> 1;
@@ -578,6 +725,74 @@ __global__ void k_prolong_f(LevelViewF Cv, LevelViewF F)
         float* p = (((i + j + k) & 1) ? F.phi_b : F.phi_r) + t;
         *p += s;
     }
+}
+
+// The same prolongation for a split fine level over a split coarse level with
+// half % 4 == 0: four compact columns (eight fine cells of a row) per thread.
+// The coarse neighbours of those cells along x are the six coarse cells
+// ih0-1 .. ih0+4 of each of the four (J', K') rows; in the split layout the
+// even ones are three consecutive values of one colour array and the odd ones
+// three of the other, loaded as a pair plus one.  Each fine cell sums its
+// eight weighted coarse values in e_prolong's order, so the results are the
+// scalar kernel's; the corrections go to two float4 of the fine arrays.
+__global__ void __launch_bounds__(256) k_prolong_f4(LevelViewF Cv, LevelViewF F)
+{
+    const int n = F.n, nc = Cv.n;
+    const unsigned half = (unsigned)n >> 1, chalf = (unsigned)nc >> 1, h4 = half >> 2;
+    const unsigned t4 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (t4 >= h4 || j >= n) return;
+    const int J = j >> 1, K = k >> 1;
+    const int Js[2] = {J, wrap1((j & 1) ? J + 1 : J - 1, nc)};
+    const int Ks[2] = {K, wrap1((k & 1) ? K + 1 : K - 1, nc)};
+    const unsigned c2 = 2 * t4;                       // compact index of coarse I = ih0 (even)
+    // v[b][a][0..5] = coarse values at I = ih0-1 .. ih0+4 of row (Js[a], Ks[b])
+    float v[2][2][6];
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+            const unsigned row = ((unsigned)Js[a] + (unsigned)nc * (unsigned)Ks[b]) * chalf;
+            const bool even_red = ((Js[a] + Ks[b]) & 1) == 0;   // colour of an even I
+            const float* ev = even_red ? Cv.phi_r : Cv.phi_b;
+            const float* od = even_red ? Cv.phi_b : Cv.phi_r;
+            const float2 e01 = __ldg(reinterpret_cast<const float2*>(ev + row + c2));
+            const float e2 = __ldg(ev + row + (c2 + 2 == chalf ? 0u : c2 + 2));
+            const float2 o01 = __ldg(reinterpret_cast<const float2*>(od + row + c2));
+            const float om = __ldg(od + row + (c2 == 0 ? chalf - 1 : c2 - 1));
+            v[b][a][0] = om;       // I = ih0 - 1
+            v[b][a][1] = e01.x;    // ih0
+            v[b][a][2] = o01.x;    // ih0 + 1
+            v[b][a][3] = e01.y;    // ih0 + 2
+            v[b][a][4] = o01.y;    // ih0 + 3
+            v[b][a][5] = e2;       // ih0 + 4
+        }
+    float s0[4], s1[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        float se = 0.f, so = 0.f;   // fine i = 2 ih (tt1: I - 1) and 2 ih + 1 (tt1: I + 1)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                se = fmaf(kProlongWF[0 + 2 * a + 4 * b], v[b][a][r + 1], se);
+                se = fmaf(kProlongWF[1 + 2 * a + 4 * b], v[b][a][r], se);
+                so = fmaf(kProlongWF[0 + 2 * a + 4 * b], v[b][a][r + 1], so);
+                so = fmaf(kProlongWF[1 + 2 * a + 4 * b], v[b][a][r + 2], so);
+            }
+        s0[r] = se;
+        s1[r] = so;
+    }
+    const unsigned t = ((unsigned)j + (unsigned)n * (unsigned)k) * half + 4 * t4;
+    const bool even_fine_red = ((j + k) & 1) == 0;   // colour of fine i = 2 ih
+    float4* fe = reinterpret_cast<float4*>(even_fine_red ? F.phi_r : F.phi_b) + (t >> 2);
+    float4* fo = reinterpret_cast<float4*>(even_fine_red ? F.phi_b : F.phi_r) + (t >> 2);
+    float4 pe = *fe, po = *fo;
+    pe.x += s0[0]; pe.y += s0[1]; pe.z += s0[2]; pe.w += s0[3];
+    po.x += s1[0]; po.y += s1[1]; po.z += s1[2]; po.w += s1[3];
+    *fe = pe;
+    *fo = po;
 }
 
 __global__ void k_bottom_f(int nb, const float* __restrict__ G, const float* __restrict__ beta, float* phi)
@@ -720,7 +935,7 @@ nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine)
 {
     const long long half_cells = (long long)l.n * l.n * l.n / 2;
     const int half = l.n / 2;
-    const bool vec = half % 4 == 0;
+    const bool vec = half % 4 == 0;   // then n % 8 == 0, a whole number of kMarchZ planes
     Geo g;
     if (vec) {
         g = geo3(half / 4, l.n, 1);
@@ -758,17 +973,27 @@ nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li)
     const long long ncc = (long long)cl.n * cl.n * cl.n;
     const long long ncf = (long long)f.n * f.n * f.n;
     {
-        const Geo g = geo3(cl.n, cl.n, cl.n);
         prof_begin(c);
-        k_restrict_f<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+        if ((f.n / 2) % 4 == 0) {
+            const Geo g = geo3(cl.n / 2, cl.n, cl.n);
+            k_restrict_f4<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+        } else {
+            const Geo g = geo3(cl.n, cl.n, cl.n);
+            k_restrict_f<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+        }
         prof_end(c, NYXPM_ST_RESTRICT, 8.0 * ncf + 8.0 * ncc);
     }
     if ((st = check_launch(c, "restrict f32")) != NYXPM_OK) return st;
     if ((st = vcycle_f(c, b, li + 1)) != NYXPM_OK) return st;
     {
-        const Geo g = geo3(f.n / 2, f.n, f.n);
         prof_begin(c);
-        k_prolong_f<<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+        if (cl.split && (f.n / 2) % 4 == 0) {
+            const Geo g = geo3(f.n / 8, f.n, f.n);
+            k_prolong_f4<<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+        } else {
+            const Geo g = geo3(f.n / 2, f.n, f.n);
+            k_prolong_f<<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+        }
         prof_end(c, NYXPM_ST_PROLONG, 8.0 * ncf + 4.0 * ncc);
     }
     if ((st = check_launch(c, "prolong f32")) != NYXPM_OK) return st;
@@ -786,8 +1011,15 @@ nyxpm_status launch_mx_resid(Ctx& c, Box& b)
     cudaMemsetAsync(b.norms + 1, 0, sizeof(unsigned long long), c.stream);
     if (l.split) {
         const Geo g = geo3(l.n / 2, l.n, l.n);
-        k_mx_resid<<<g.grid, g.block, 0, c.stream>>>(l.n, l.phi_r, l.phi_b, l.beta_r, l.beta_b,
-                                                     l.fbeta_r, l.fbeta_b, b.norms + 1);
+        if ((l.n / 2) % 2 == 0) {
+            const Geo g2 = geo3(l.n / 4, l.n, l.n);
+            k_mx_resid2<<<g2.grid, g2.block, 0, c.stream>>>(l.n, l.phi_r, l.phi_b, l.beta_r,
+                                                            l.beta_b, l.fbeta_r, l.fbeta_b,
+                                                            b.norms + 1);
+        } else {
+            k_mx_resid<<<g.grid, g.block, 0, c.stream>>>(l.n, l.phi_r, l.phi_b, l.beta_r, l.beta_b,
+                                                         l.fbeta_r, l.fbeta_b, b.norms + 1);
+        }
     } else {
         const Geo g = geo3(l.n, l.n, l.n);
         k_mx_resid_nat<<<g.grid, g.block, 0, c.stream>>>(l.n, l.phi_r, l.beta_r, l.fbeta_r,

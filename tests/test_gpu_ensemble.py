@@ -94,3 +94,21 @@ def test_budget_and_reuse(ctx):
     with pytest.raises(Exception):
         ens.add(18, 1.0, 100)                          # 18 = 9 * 2 is not supported
     ens.close()
+
+
+def test_profiled_eager_step_equals_graph_step(ctx):
+    """With profiling on, the ensemble step runs its launches eagerly with stage
+    events instead of replaying the captured graphs; the results are the same."""
+    ics = [box_ics(s, 0.05) for s in SPECS[:3]]
+    sched = equal_da_schedule(0.05, 0.07, 3)
+    graphs, g0, _ = run_ensemble(ctx, SPECS[:3], ics, sched)
+    ctx.set_profiling(True)
+    ctx.profile(reset=True)
+    try:
+        eager, g1, _ = run_ensemble(ctx, SPECS[:3], ics, sched)
+        prof = ctx.profile(reset=True)
+    finally:
+        ctx.set_profiling(False)
+    for (p0, v0), (p1, v1), a, b in zip(graphs, eager, g0, g1):
+        assert np.array_equal(p0, p1) and np.array_equal(v0, v1) and np.array_equal(a, b)
+    assert prof["stages"]["smooth"]["launches"] > 0 and prof["stages"]["deposit"]["ms"] > 0

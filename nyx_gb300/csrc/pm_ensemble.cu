@@ -54,6 +54,8 @@ struct EDesc {
     int n, nlev, nb, used;
     long long np;
     double L, dx, dxi, mass_offset, mscalar, beta_scale;
+    float dep_scale;                  // (float)(mscalar / dx^3), the FP32 deposit's cell scale
+    int pad_scale;
     // particle arrays: buffer 0 and buffer 1 (the sort gathers from one into the other)
     int *cell0, *id0, *cell1, *id1;
     float *ox0, *oy0, *oz0, *vx0, *vy0, *vz0;
@@ -76,6 +78,9 @@ struct EState {
     int pad;
     double target;                    // convergence target of the current solve (smoother units)
     double a_old, a_new, dt;
+    // the kicks' FP32 scalars per phase (0: kick-drift to a_half, 1: kick to a_new):
+    // a_prev, 1 / a_cur, dt / 2, drift in cells; formed once per box in FP64
+    float kick[2][4];
 };
 
 // step scalars written by the host each step (pinned) and copied in by the graph
@@ -121,14 +126,24 @@ __device__ __forceinline__ int key_frac(int ci, float o, int n, float* f)
 // ---------------------------------------------------------------------------
 // step scalars
 // ---------------------------------------------------------------------------
-__global__ void e_load_step(int nbox, const EStep* __restrict__ st, EState* S)
+__global__ void e_load_step(int nbox, const EStep* __restrict__ st, const EDesc* __restrict__ D,
+                            EState* S)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbox) return;
-    S[b].a_old = st[b].a_old;
-    S[b].a_new = st[b].a_new;
-    S[b].dt = st[b].dt;
+    const double a_old = st[b].a_old, a_new = st[b].a_new, dt = st[b].dt;
+    S[b].a_old = a_old;
+    S[b].a_new = a_new;
+    S[b].dt = dt;
     S[b].active = st[b].active;
+    const double a_half = 0.5 * (a_old + a_new);
+    for (int phase = 0; phase < 2; ++phase) {
+        const double a_cur = phase == 0 ? a_half : a_new;
+        S[b].kick[phase][0] = (float)(phase == 0 ? a_old : a_half);
+        S[b].kick[phase][1] = (float)(1.0 / a_cur);
+        S[b].kick[phase][2] = (float)(0.5 * dt);
+        S[b].kick[phase][3] = (float)(dt / a_cur * D[b].dxi);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -149,12 +164,10 @@ __global__ void __launch_bounds__(kPT) e_kick(const Item* __restrict__ items, in
         const PArr P = parr(d, st.parity);
         const int n = d.n;
         const long long nc = (long long)n * n * n;
-        const double a_half = 0.5 * (st.a_old + st.a_new);
-        const float a_prev = (float)(phase == 0 ? st.a_old : a_half);
-        const double a_cur = phase == 0 ? a_half : st.a_new;
-        const float a_cur_inv = (float)(1.0 / a_cur);
-        const float half_dt = (float)(0.5 * st.dt);
-        const float drift = (float)(st.dt / a_cur * d.dxi);
+        const float a_prev = st.kick[phase][0];
+        const float a_cur_inv = st.kick[phase][1];
+        const float half_dt = st.kick[phase][2];
+        const float drift = st.kick[phase][3];
         const int c = P.cell[q];
         const int ci = cell_i(c), cj = cell_j(c), ck = cell_k(c);
         float o[3] = {P.ox[q], P.oy[q], P.oz[q]};
@@ -501,7 +514,7 @@ __global__ void __launch_bounds__(256) e_deposit(const Item* __restrict__ items,
             for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
         }
         __syncthreads();
-        const float scale = (float)(d.mscalar / (d.dx * d.dx * d.dx));
+        const float scale = d.dep_scale;
         for (int cl = threadIdx.x; cl < TX * TY * TZ; cl += blockDim.x) {
             const int ci = cl % TX, cj = (cl / TX) % TY, ck = cl / (TX * TY);
             const int i = i0 + ci, j = j0 + cj, k = k0 + ck;
@@ -1701,7 +1714,7 @@ void enqueue_load(nyxpm_ctx* c, nyxpm_ensemble* E, const EStep* host_src)
 {
     const int nbox = (int)E->slots.size();
     cudaMemcpyAsync(E->d_step, host_src, nbox * sizeof(EStep), cudaMemcpyHostToDevice, c->stream);
-    e_load_step<<<(nbox + 127) / 128, 128, 0, c->stream>>>(nbox, E->d_step, E->d_state);
+    e_load_step<<<(nbox + 127) / 128, 128, 0, c->stream>>>(nbox, E->d_step, E->d_desc, E->d_state);
     c->launches += 1;
 }
 
@@ -1990,6 +2003,7 @@ nyxpm_status nyxpm_ensemble_upload(nyxpm_ctx* c, nyxpm_ensemble* E, int slot, co
     cudaMemsetAsync(&E->d_state[slot].parity, 0, sizeof(int), c->stream);
     d.mscalar = mass;
     d.mass_offset = mass * (double)np / (d.L * d.L * d.L);
+    d.dep_scale = (float)(d.mscalar / (d.dx * d.dx * d.dx));
     // the descriptor changed (mass): push it
     cudaMemcpyAsync(E->d_desc + slot, &d, sizeof(EDesc), cudaMemcpyHostToDevice, c->stream);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return echeck(c, "ensemble upload");

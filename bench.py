@@ -545,6 +545,10 @@ def run_ours(args):
                 "frac": round(achieved / peak, 4),
                 "traffic": (tr * (n / traffic.get("n", n)) ** 3 if tr else None),
                 "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms,
+                "fp64_pipe_active_ncu": (traffic.get("k_gsrb_fine_fp64_pipe_active")
+                                         if args.precision == "fp64" else None),
+                "note": ("the FP64 smoother is bound by GB300's FP64 pipe (the ncu fraction "
+                         "above), not by HBM" if args.precision == "fp64" else None),
                 "dominant_stage_share": round(stages[dom]["ms"] / sum(v["ms"] for v in stages.values()), 3)}
 
     line = {

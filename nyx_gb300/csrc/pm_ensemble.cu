@@ -774,6 +774,14 @@ __host__ __device__ inline int vec_rows(int n, int nthreads)
     return r < 1 ? 1 : (r > n ? n : r);
 }
 
+// Items of this kernel cover kMarchE consecutive planes (k0 = it.b): each task
+// marches over them, so the row of the plane above becomes this plane's row and
+// then the one below, and each plane loads three neighbour rows, the right-hand
+// side and one edge value.  32-bit offsets (a level has at most 1024^3 / 2
+// cells of a colour).  Levels with half % 4 == 0 have n % 8 == 0, so every item
+// holds exactly kMarchE planes.
+constexpr int kMarchE = 4;
+
 __global__ void __launch_bounds__(256) e_gsrb4(const Item* __restrict__ items, int nitems,
                                                const EDesc* __restrict__ D,
                                                const EState* __restrict__ S, int color)
@@ -786,44 +794,56 @@ __global__ void __launch_bounds__(256) e_gsrb4(const Item* __restrict__ items, i
         if (!(st.active && st.solve_active)) continue;
         const EDesc& d = D[it.box];
         const ELevel& L = d.lv[it.a];
-        const int n = L.n, half = n >> 1, h4 = half >> 2, k = it.b;
+        const int n = L.n;
+        const unsigned half = (unsigned)n >> 1, h4 = half >> 2, plane = (unsigned)n * half;
+        const int k0 = it.b;
         const int rows = vec_rows(n, nthreads);
-        float* mine = color ? L.phi_b : L.phi_r;
+        float4* m4 = reinterpret_cast<float4*>(color ? L.phi_b : L.phi_r);
         const float* other = color ? L.phi_r : L.phi_b;
         const float4* o4 = reinterpret_cast<const float4*>(other);
         const float4* b4 = reinterpret_cast<const float4*>(color ? L.beta_b : L.beta_r);
-        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
-        for (int task = tid; task < rows * h4; task += nthreads) {
-            const int r = task / h4, t4 = task - r * h4;
+        for (int task = tid; task < rows * (int)h4; task += nthreads) {
+            const int r = task / (int)h4, t4 = task - r * (int)h4;
             const int j = it.c + r;
             if (j >= n) continue;
-            const int ih = 4 * t4;
+            const unsigned ih = 4 * (unsigned)t4;
             const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
-            const long long rowbase = ((long long)j + (long long)n * k) * half;
-            const long long t = rowbase + ih;
-            const float4 c = __ldg(o4 + (t >> 2));
-            const float4 ym = __ldg(o4 + ((((long long)jm + (long long)n * k) * half + ih) >> 2));
-            const float4 yp = __ldg(o4 + ((((long long)jp + (long long)n * k) * half + ih) >> 2));
-            const float4 zm = __ldg(o4 + ((((long long)j + (long long)n * km) * half + ih) >> 2));
-            const float4 zp = __ldg(o4 + ((((long long)j + (long long)n * kp) * half + ih) >> 2));
-            const float4 b = __ldg(b4 + (t >> 2));
-            const int q = (j + k + color) & 1;
-            float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
-            if (q) {
-                const float edge = __ldg(other + rowbase + (ih + 4 == half ? 0 : ih + 4));
-                xm0 = c.x; xm1 = c.y; xm2 = c.z; xm3 = c.w;
-                xp0 = c.y; xp1 = c.z; xp2 = c.w; xp3 = edge;
-            } else {
-                const float edge = __ldg(other + rowbase + (ih == 0 ? half - 1 : ih - 1));
-                xm0 = edge; xm1 = c.x; xm2 = c.y; xm3 = c.z;
-                xp0 = c.x; xp1 = c.y; xp2 = c.z; xp3 = c.w;
+            const unsigned rj = (unsigned)j * half + ih, rjm = (unsigned)jm * half + ih,
+                           rjp = (unsigned)jp * half + ih;
+            const int kfirst = k0 == 0 ? n - 1 : k0 - 1;
+            float4 zm = __ldg(o4 + (((unsigned)kfirst * plane + rj) >> 2));
+            float4 c = __ldg(o4 + (((unsigned)k0 * plane + rj) >> 2));
+#pragma unroll
+            for (int kk = 0; kk < kMarchE; ++kk) {
+                const int k = k0 + kk;
+                const int kp = k == n - 1 ? 0 : k + 1;
+                const unsigned pk = (unsigned)k * plane;
+                const float4 zp = __ldg(o4 + (((unsigned)kp * plane + rj) >> 2));
+                const float4 ym = __ldg(o4 + ((pk + rjm) >> 2));
+                const float4 yp = __ldg(o4 + ((pk + rjp) >> 2));
+                const unsigned t = pk + rj;
+                const float4 b = __ldg(b4 + (t >> 2));
+                const int q = (j + k + color) & 1;
+                const unsigned rowbase = t - ih;
+                float xm0, xm1, xm2, xm3, xp0, xp1, xp2, xp3;
+                if (q) {
+                    const float edge = __ldg(other + rowbase + (ih + 4 == half ? 0u : ih + 4));
+                    xm0 = c.x; xm1 = c.y; xm2 = c.z; xm3 = c.w;
+                    xp0 = c.y; xp1 = c.z; xp2 = c.w; xp3 = edge;
+                } else {
+                    const float edge = __ldg(other + rowbase + (ih == 0 ? half - 1 : ih - 1));
+                    xm0 = edge; xm1 = c.x; xm2 = c.y; xm3 = c.z;
+                    xp0 = c.x; xp1 = c.y; xp2 = c.z; xp3 = c.w;
+                }
+                float4 o;
+                o.x = fmaf(((((xm0 + xp0) + ym.x) + yp.x) + zm.x) + zp.x, kSixthF, -b.x);
+                o.y = fmaf(((((xm1 + xp1) + ym.y) + yp.y) + zm.y) + zp.y, kSixthF, -b.y);
+                o.z = fmaf(((((xm2 + xp2) + ym.z) + yp.z) + zm.z) + zp.z, kSixthF, -b.z);
+                o.w = fmaf(((((xm3 + xp3) + ym.w) + yp.w) + zm.w) + zp.w, kSixthF, -b.w);
+                m4[t >> 2] = o;
+                zm = c;
+                c = zp;
             }
-            float4 o;
-            o.x = fmaf(((((xm0 + xp0) + ym.x) + yp.x) + zm.x) + zp.x, kSixthF, -b.x);
-            o.y = fmaf(((((xm1 + xp1) + ym.y) + yp.y) + zm.y) + zp.y, kSixthF, -b.y);
-            o.z = fmaf(((((xm2 + xp2) + ym.z) + yp.z) + zm.z) + zp.z, kSixthF, -b.z);
-            o.w = fmaf(((((xm3 + xp3) + ym.w) + yp.w) + zm.w) + zp.w, kSixthF, -b.w);
-            reinterpret_cast<float4*>(mine)[t >> 2] = o;
         }
     }
 }
@@ -1307,6 +1327,8 @@ struct nyxpm_ensemble {
     // others the row items above
     Range r_smooth_vec[nyxpm::kMaxLev];
     Range r_smooth_row[nyxpm::kMaxLev];
+    // the vectorised smoother's items: the same row groups, kMarchE planes each
+    Range r_smooth_march[nyxpm::kMaxLev];
     // the restriction's coarse-row items, split the same way by the fine level
     Range r_restrict_vec[nyxpm::kMaxLev];
     Range r_restrict_row[nyxpm::kMaxLev];
@@ -1446,6 +1468,17 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
                 for (int j0 = 0; j0 < nl; j0 += rv) items.push_back(Item{b, l, k, j0});
         }
         end(E->r_smooth_vec[l]);
+        begin(E->r_smooth_march[l]);
+        for (int b = 0; b < nbox; ++b) {
+            const EnsSlot& s = E->slots[b];
+            if (!s.used || l >= s.desc.nlev - 1) continue;
+            const int nl = s.desc.lv[l].n;
+            if ((nl / 2) % 4 != 0) continue;
+            const int rv = vec_rows(nl, 32 * R);
+            for (int k = 0; k < nl; k += kMarchE)
+                for (int j0 = 0; j0 < nl; j0 += rv) items.push_back(Item{b, l, k, j0});
+        }
+        end(E->r_smooth_march[l]);
         begin(E->r_smooth_row[l]);
         for (int b = 0; b < nbox; ++b) {
             const EnsSlot& s = E->slots[b];
@@ -1632,7 +1665,7 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer)
     // one red or black half sweep of level l over every box: the vectorised
     // kernel for the boxes whose level-l rows allow it, the row kernel for the rest
     auto smooth = [&](int l, int color) {
-        const auto& rv = E->r_smooth_vec[l];
+        const auto& rv = E->r_smooth_march[l];
         const auto& rr = E->r_smooth_row[l];
         ep_begin(c);
         if (rv.cnt) {

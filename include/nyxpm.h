@@ -157,8 +157,9 @@ nyxpm_status nyxpm_set_phi(nyxpm_ctx* ctx, nyxpm_box* box, const double* phi);
 nyxpm_status nyxpm_grav_vector(nyxpm_ctx* ctx, nyxpm_box* box, double* g_out);
 
 /* DarkMatterParticleContainer::moveKickDrift (Source/Particle/DarkMatterParticleContainer.cpp:76-181):
- * CIC-interpolated g from the current phi (gradient fused), v = (a_old v + dt/2 g)/a_half,
- * x += dt/a_half v (update_dm_particle_single, :250-306, do_move = 1). */
+ * the box's cell-centred gravity vector (kept in step with phi) interpolated to the
+ * particle by CIC, v = (a_old v + dt/2 g)/a_half, x += dt/a_half v
+ * (update_dm_particle_single, :250-306, do_move = 1). */
 nyxpm_status nyxpm_kick_drift(nyxpm_ctx* ctx, nyxpm_box* box, double dt, double a_old,
                               double a_half);
 

@@ -296,9 +296,6 @@ __global__ void k_scan_down(const int* __restrict__ in, int n, const int* __rest
 // the 8 corner partials of its keys in a fixed order.  No atomics; the order is
 // fixed, so the density is bitwise reproducible.
 // ---------------------------------------------------------------------------
-constexpr int kTx = 8, kTy = 8, kTz = 8;
-constexpr int kKx = kTx + 1, kKy = kTy + 1, kKz = kTz + 1;
-constexpr int kNKeys = kKx * kKy * kKz;
 static_assert(kDepositLanes == 32, "long keys are summed by one warp; the sort queues keys > 32");
 
 // adds particle q's eight CIC weights (times its mass, fused, if m) to s
@@ -507,59 +504,6 @@ __global__ void __launch_bounds__(256) k_deposit_cells(int n, double scale,
                 acc = acc + __ldg(part + corner * nc + cidx(is[di], js[dj], ks[dk], n));
             }
     rho[cidx(i, j, k, n)] = acc * scale;
-}
-
-// One CTA per 8x8x8 tile of cells: the 9x9x9 keys whose particles touch the
-// tile are summed into eight corner partials each (a short key by one thread
-// in sorted order; a long key's partials come from k_deposit_heavy), then each
-// cell adds its eight keys' corners in the fixed (dk, dj, di) order.  No
-// atomics: the result does not depend on scheduling.
-__global__ void __launch_bounds__(256) k_deposit(int n, double dxi, double scale,
-                                                 const double* __restrict__ x,
-                                                 const double* __restrict__ y,
-                                                 const double* __restrict__ z,
-                                                 const double* __restrict__ m,
-                                                 const int* __restrict__ start,
-                                                 const int* __restrict__ key_slot,
-                                                 const double* __restrict__ heavy_part, double* rho)
-{
-    __shared__ double part[kNKeys * 8];
-    const int i0 = blockIdx.x * kTx, j0 = blockIdx.y * kTy, k0 = blockIdx.z * kTz;
-    for (int kl = threadIdx.x; kl < kNKeys; kl += blockDim.x) {
-        const int ki = kl % kKx, kj = (kl / kKx) % kKy, kk = kl / (kKx * kKy);
-        const long long K = cidx(wrapi(i0 + ki, n), wrapi(j0 + kj, n), wrapi(k0 + kk, n), n);
-        double s[8];
-        const int b0 = start[K], e = start[K + 1];
-        if (e - b0 > kDepositLanes) {
-            const double* hp = heavy_part + 8LL * key_slot[K];
-#pragma unroll
-            for (int c = 0; c < 8; ++c) s[c] = hp[c];
-        } else {
-#pragma unroll
-            for (int c = 0; c < 8; ++c) s[c] = 0.0;
-            for (int q = b0; q < e; ++q) add_weights(q, n, dxi, x, y, z, m, s);
-        }
-#pragma unroll
-        for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
-    }
-    __syncthreads();
-    for (int cl = threadIdx.x; cl < kTx * kTy * kTz; cl += blockDim.x) {
-        const int ci = cl % kTx, cj = (cl / kTx) % kTy, ck = cl / (kTx * kTy);
-        const int i = i0 + ci, j = j0 + cj, k = k0 + ck;
-        if (i >= n || j >= n || k >= n) continue;
-        double acc = 0.0;
-#pragma unroll
-        for (int dk = 0; dk < 2; ++dk)
-#pragma unroll
-            for (int dj = 0; dj < 2; ++dj)
-#pragma unroll
-                for (int di = 0; di < 2; ++di) {
-                    const int kl = (ci + di) + kKx * ((cj + dj) + kKy * (ck + dk));
-                    const int corner = (1 - di) + 2 * (1 - dj) + 4 * (1 - dk);
-                    acc = acc + part[kl * 8 + corner];
-                }
-        rho[cidx(i, j, k, n)] = acc * scale;
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -779,7 +723,6 @@ nyxpm_status launch_sort(Ctx& c, Box& b)
 nyxpm_status launch_deposit(Ctx& c, Box& b)
 {
     const int n = b.n;
-    dim3 grid((n + kTx - 1) / kTx, (n + kTy - 1) / kTy, (n + kTz - 1) / kTz);
     const double dx = b.L / n;
     const double inv_vol = 1.0 / (dx * dx * dx);
     // per-particle masses: keys sum w*m, cells scale by 1/dx^3; uniform: keys sum w, cells by m/dx^3
@@ -790,20 +733,14 @@ nyxpm_status launch_deposit(Ctx& c, Box& b)
     k_deposit_heavy<<<c.sm_count * 4, 256, 0, c.stream>>>(n, b.dxi, b.x, b.y, b.z, mq, b.cell_start,
                                                           b.long_list, b.long_count, b.key_slot,
                                                           b.heavy_part);
-    if (b.key_part) {
-        const long long ncl = (long long)n * n * n;
-        const unsigned kb = (unsigned)((ncl + 32LL * kKeyWarps - 1) / (32LL * kKeyWarps));
-        k_deposit_keys<<<kb, 32 * kKeyWarps, 0, c.stream>>>(ncl, n, b.dxi, b.x, b.y, b.z, mq,
-                                                             b.cell_start, b.key_slot, b.heavy_part,
-                                                             b.key_part);
-        const Geo g = geo3(n, n, n);
-        k_deposit_cells<<<g.grid, g.block, 0, c.stream>>>(n, scale, b.key_part, b.rho);
-        c.launches += 2;
-    } else {
-        k_deposit<<<grid, 256, 0, c.stream>>>(n, b.dxi, scale, b.x, b.y, b.z, mq, b.cell_start,
-                                              b.key_slot, b.heavy_part, b.rho);
-        c.launches += 1;
-    }
+    const long long ncl = (long long)n * n * n;
+    const unsigned kb = (unsigned)((ncl + 32LL * kKeyWarps - 1) / (32LL * kKeyWarps));
+    k_deposit_keys<<<kb, 32 * kKeyWarps, 0, c.stream>>>(ncl, n, b.dxi, b.x, b.y, b.z, mq,
+                                                         b.cell_start, b.key_slot, b.heavy_part,
+                                                         b.key_part);
+    const Geo g = geo3(n, n, n);
+    k_deposit_cells<<<g.grid, g.block, 0, c.stream>>>(n, scale, b.key_part, b.rho);
+    c.launches += 2;
     prof_end(c, NYXPM_ST_DEPOSIT, (b.uniform_mass ? 24.0 : 32.0) * b.np + 12.0 * nc);
     return check_launch(c, "deposit");
 }

@@ -232,7 +232,8 @@ nyxpm_status nyxpm_compute_new_dt(nyxpm_ctx* ctx, nyxpm_box* box, const nyxpm_dt
  * Docs/sphinx_documentation/source/ICs.rst:13-78):
  *   ASCII        first line the particle count, then "x y z mass vx vy vz" per line;
  *   BINARY       int64 NP, int32 DM = 3, int32 NX >= 4, then NP records of DM + NX
- *                float32 "x y z mass vx vy vz [extras]";
+ *                float32 or float64 values "x y z mass vx vy vz [extras]" (the
+ *                precision follows from the file size);
  *   BINARY_META  a text file listing BINARY files, one per line, read in order. */
 typedef enum {
     NYXPM_FILE_ASCII = 0,

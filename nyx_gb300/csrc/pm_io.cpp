@@ -6,8 +6,9 @@
 //   AsciiFile       first line: the particle count; then one line per particle
 //                   "x y z mass vx vy vz".
 //   BinaryFile      header: int64 NP, int32 DM (= 3), int32 NX (extra fields,
-//                   at least 4); then NP records of DM + NX float32 values
-//                   "x y z mass vx vy vz [more extras, skipped]"; native byte order.
+//                   at least 4); then NP records of DM + NX values
+//                   "x y z mass vx vy vz [more extras, skipped]", float32 or
+//                   float64 (told apart by the file size); native byte order.
 //   BinaryMetaFile  a text file listing binary particle files, one path per
 //                   line, read in the order listed.
 // comoving_a: one number written with 15 significant digits
@@ -204,15 +205,37 @@ nyxpm_status nyxpm_particle_file_read(const char* path, nyxpm_file_format fmt, i
             return io_fail(errbuf, errlen, "bad header in " + fn);
         }
         const int rec = h.dm + h.nx;
-        std::vector<float> buf((size_t)rec * 65536);
+        // the record precision follows from the file size: DM + NX float32 or float64
+        // values per particle (the ICs doc writes floats; Exec/LyA/32.nyx holds doubles)
+        long long data_bytes = -1;
+        if (std::fseek(f, 0, SEEK_END) == 0) data_bytes = (long long)std::ftell(f) - 16;
+        std::fseek(f, 16, SEEK_SET);
+        int width = 0;
+        if (data_bytes == h.np * rec * 4LL) width = 4;
+        else if (data_bytes == h.np * rec * 8LL) width = 8;
+        if (width == 0 && h.np > 0) {
+            std::fclose(f);
+            return io_fail(errbuf, errlen, "size of " + fn + " fits neither float32 nor float64 records");
+        }
+        std::vector<unsigned char> buf((size_t)rec * width * 65536);
         for (int64_t done = 0; done < h.np;) {
             const int64_t chunk = std::min<int64_t>(65536, h.np - done);
-            if (std::fread(buf.data(), sizeof(float) * rec, (size_t)chunk, f) != (size_t)chunk) {
+            if (std::fread(buf.data(), (size_t)width * rec, (size_t)chunk, f) != (size_t)chunk) {
                 std::fclose(f);
                 return io_fail(errbuf, errlen, "short record data in " + fn);
             }
             for (int64_t r = 0; r < chunk; ++r, ++q) {
-                const float* v = buf.data() + (size_t)rec * r;
+                double v[7];
+                const unsigned char* src = buf.data() + (size_t)width * rec * r;
+                for (int c = 0; c < 7; ++c) {
+                    if (width == 4) {
+                        float x;
+                        std::memcpy(&x, src + 4 * c, 4);
+                        v[c] = x;
+                    } else {
+                        std::memcpy(&v[c], src + 8 * c, 8);
+                    }
+                }
                 pos[3 * q] = v[0];
                 pos[3 * q + 1] = v[1];
                 pos[3 * q + 2] = v[2];

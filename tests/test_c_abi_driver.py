@@ -1,0 +1,68 @@
+"""The C ABI used from C++ the way a Nyx-side shim would use it.
+
+tests/c_abi/pm_driver.cpp includes include/nyxpm.h and links
+nyx_gb300/libnyxpm.so with nothing else.  It reads an AsciiFile and takes PM
+steps with dt from nyxpm_compute_new_dt, then writes the particles back.  On CPU
+the program must compile and link.  On the GPU its result must equal the Python
+(ctypes) path's, which the parity tests tie to the oracle, bit for bit.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from nyx_gb300 import _lib
+from nyx_gb300.pm import Box, read_particle_file, write_particle_file
+from tests.conftest import gpu_available
+from tests.pm_cases import config1_ics
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def build_driver(out_dir):
+    _lib.load()   # builds the library if needed
+    exe = os.path.join(out_dir, "pm_driver")
+    libdir = os.path.join(REPO, "nyx_gb300")
+    cmd = ["g++", "-O2", "-std=c++17", os.path.join(REPO, "tests", "c_abi", "pm_driver.cpp"),
+           "-I", os.path.join(REPO, "include"), "-L", libdir, "-lnyxpm", f"-Wl,-rpath,{libdir}",
+           "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
+def test_driver_compiles_and_links_against_the_header_alone(tmp_path):
+    exe = build_driver(str(tmp_path))
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no GPU")
+def test_driver_result_equals_python_path(ctx, tmp_path):
+    exe = build_driver(str(tmp_path))
+    n = 32
+    ic = config1_ics(n, seed=8)
+    inp, out = str(tmp_path / "in.ascii"), str(tmp_path / "out.ascii")
+    write_particle_file(inp, ic.pos, ic.vel, ic.mass)
+    r = subprocess.run([exe, inp, str(n), "1.0", "0.02", "4", out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    cpos, cvel, _ = read_particle_file(out)
+    pos, vel, _ = read_particle_file(inp)
+    box = Box(ctx, n, 1.0, len(pos))
+    box.upload(pos, vel, ic.mass)
+    box.init_field(0.02)
+    t, a, dt_old = 0.0, 0.02, -1.0
+    for line in r.stdout.strip().splitlines():
+        dt, a_new = box.compute_new_dt(t, a, dt_old)
+        assert f"a {a_new:.17g} dt {dt:.17g}" in line
+        box.step(a, a_new, dt)
+        t, a, dt_old = t + dt, a_new, dt
+    ppos, pvel = box.download()
+    assert np.array_equal(cpos, ppos) and np.array_equal(cvel, pvel)
+    box.close()

@@ -255,3 +255,31 @@ def test_config2_full_size_properties(ctx):
         b2.step(a0, a1, dt)
     pos2, vel2 = b2.download()
     assert np.array_equal(pos, pos2) and np.array_equal(vel, vel2)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_vcycle_cap_reports_not_converged(precision):
+    """A solve that reaches max_vcycles above the tolerance returns
+    NYXPM_NOT_CONVERGED (where MLMG aborts) and leaves a usable field; the FP64
+    form stops at the same V-cycle as the oracle with the same cap."""
+    from nyx_gb300.pm import Context
+    n = 32
+    ic = config1_ics(n, seed=2)
+    c2 = Context(device=0, max_vcycles=2)
+    b = Box(c2, n, 1.0, len(ic.pos), precision=precision)
+    b.upload(ic.pos, ic.vel, ic.mass)
+    b.deposit(read_back=False)
+    with pytest.raises(NyxPMError) as e:
+        b.solve_phi(0.02, zero_guess=True)
+    assert e.value.status == 4 and "max_vcycles" in str(e.value)
+    g = b.grav_vector()
+    assert np.all(np.isfinite(g)) and np.abs(g).max() > 0
+    if precision == "fp64":
+        p = O.Particles(ic.pos, ic.vel, ic.mass)
+        rho = O.deposit(n, 1.0, p, O.sort(n, 1.0, p))
+        rhs, _ = O.make_rhs(n, 1.0, rho, p.total_mass(), ggrav(), 0.02)
+        phi_o, st, cyc, r0, r = O.mg_solve(n, 1.0, rhs, None, max_cycles=2)
+        assert st != 0 and cyc == 2
+        assert rel_l2(mean_removed(b.get_phi()), mean_removed(phi_o)) <= TOL
+    b.close()
+    c2.close()

@@ -238,7 +238,8 @@ nyxpm_status nyxpm_compute_new_dt(nyxpm_ctx* ctx, nyxpm_box* box, const nyxpm_dt
 typedef enum {
     NYXPM_FILE_ASCII = 0,
     NYXPM_FILE_BINARY = 1,
-    NYXPM_FILE_BINARY_META = 2
+    NYXPM_FILE_BINARY_META = 2,
+    NYXPM_FILE_BINARY_F64 = 3     /* BINARY written with float64 records (read as BINARY) */
 } nyxpm_file_format;
 
 /* Number of particles the file holds (reads only the headers). */
@@ -249,8 +250,8 @@ nyxpm_status nyxpm_particle_file_count(const char* path, nyxpm_file_format fmt, 
 nyxpm_status nyxpm_particle_file_read(const char* path, nyxpm_file_format fmt, int64_t capacity,
                                       double* pos, double* vel, double* mass, int64_t* np_read,
                                       char* errbuf, size_t errlen);
-/* Writes an ASCII (17 significant digits) or BINARY (float32) particle file;
- * mass NULL writes mass_scalar for every particle. */
+/* Writes an ASCII (17 significant digits), BINARY (float32) or BINARY_F64
+ * (float64, exact) particle file; mass NULL writes mass_scalar for every particle. */
 nyxpm_status nyxpm_particle_file_write(const char* path, nyxpm_file_format fmt, int64_t np,
                                        const double* pos, const double* vel, const double* mass,
                                        double mass_scalar, char* errbuf, size_t errlen);

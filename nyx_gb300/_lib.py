@@ -40,7 +40,7 @@ EXPORTS = [
     "nyxpm_particle_file_write", "nyxpm_write_comoving_a", "nyxpm_read_comoving_a",
     "nyxpm_cosmo_1ppc_particles", "nyxpm_cosmo_ic_factors", "nyxpm_box_init_cosmo_1ppc",
 ]
-NYXPM_FILE_ASCII, NYXPM_FILE_BINARY, NYXPM_FILE_BINARY_META = 0, 1, 2
+NYXPM_FILE_ASCII, NYXPM_FILE_BINARY, NYXPM_FILE_BINARY_META, NYXPM_FILE_BINARY_F64 = 0, 1, 2, 3
 
 
 class Params(C.Structure):

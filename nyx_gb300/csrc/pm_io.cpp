@@ -130,7 +130,7 @@ nyxpm_status nyxpm_particle_file_count(const char* path, nyxpm_file_format fmt, 
         *np = v;
         return NYXPM_OK;
     }
-    if (fmt == NYXPM_FILE_BINARY) {
+    if (fmt == NYXPM_FILE_BINARY || fmt == NYXPM_FILE_BINARY_F64) {
         BinHeader h;
         const nyxpm_status st = bin_header(path, &h, errbuf, errlen);
         if (st == NYXPM_OK) *np = h.np;
@@ -190,7 +190,7 @@ nyxpm_status nyxpm_particle_file_read(const char* path, nyxpm_file_format fmt, i
         return NYXPM_OK;
     }
     std::vector<std::string> files;
-    if (fmt == NYXPM_FILE_BINARY) {
+    if (fmt == NYXPM_FILE_BINARY || fmt == NYXPM_FILE_BINARY_F64) {
         files.push_back(path);
     } else if ((st = meta_list(path, &files, errbuf, errlen)) != NYXPM_OK) {
         return st;
@@ -258,7 +258,7 @@ nyxpm_status nyxpm_particle_file_write(const char* path, nyxpm_file_format fmt, 
 {
     if (errbuf && errlen) errbuf[0] = '\0';
     if (!path || np < 0 || (np > 0 && (!pos || !vel))) return io_fail(errbuf, errlen, "null argument");
-    if (fmt != NYXPM_FILE_ASCII && fmt != NYXPM_FILE_BINARY)
+    if (fmt != NYXPM_FILE_ASCII && fmt != NYXPM_FILE_BINARY && fmt != NYXPM_FILE_BINARY_F64)
         return io_fail(errbuf, errlen, "writes AsciiFile or BinaryFile only");
     FILE* f = std::fopen(path, fmt == NYXPM_FILE_ASCII ? "w" : "wb");
     if (!f) return io_fail(errbuf, errlen, std::string("cannot create ") + path);
@@ -275,10 +275,15 @@ nyxpm_status nyxpm_particle_file_write(const char* path, nyxpm_file_format fmt, 
         ok = std::fwrite(&n64, sizeof(n64), 1, f) == 1 && std::fwrite(&dm, sizeof(dm), 1, f) == 1 &&
              std::fwrite(&nx, sizeof(nx), 1, f) == 1;
         for (int64_t q = 0; ok && q < np; ++q) {
-            const float v[7] = {(float)pos[3 * q], (float)pos[3 * q + 1], (float)pos[3 * q + 2],
-                                (float)(mass ? mass[q] : mass_scalar), (float)vel[3 * q],
-                                (float)vel[3 * q + 1], (float)vel[3 * q + 2]};
-            ok = std::fwrite(v, sizeof(float), 7, f) == 7;
+            const double d[7] = {pos[3 * q], pos[3 * q + 1], pos[3 * q + 2], mass ? mass[q] : mass_scalar,
+                                 vel[3 * q], vel[3 * q + 1], vel[3 * q + 2]};
+            if (fmt == NYXPM_FILE_BINARY_F64) {
+                ok = std::fwrite(d, sizeof(double), 7, f) == 7;
+            } else {
+                float v[7];
+                for (int c = 0; c < 7; ++c) v[c] = (float)d[c];
+                ok = std::fwrite(v, sizeof(float), 7, f) == 7;
+            }
         }
     }
     ok = (std::fclose(f) == 0) && ok;

@@ -302,7 +302,7 @@ class Box:
 # particle files and the comoving_a file (host I/O in the library)
 # ---------------------------------------------------------------------------
 FILE_FORMATS = {"ascii": _L.NYXPM_FILE_ASCII, "binary": _L.NYXPM_FILE_BINARY,
-                "binary_meta": _L.NYXPM_FILE_BINARY_META}
+                "binary_meta": _L.NYXPM_FILE_BINARY_META, "binary64": _L.NYXPM_FILE_BINARY_F64}
 
 
 def _io_call(fn, *args):

@@ -143,3 +143,12 @@ def test_cosmo_ic_factors_match_initcosmo():
     a = 1 / (1 + 99.0)
     assert vf[0] == 100.0 * a * math.sqrt(0.3 / math.pow(a, 3) + (1 - 0.3)) * 0.7 * 100
     assert m == rho * (100.0 * 100.0 * 100.0) / (64.0 * 64 * 64)
+
+
+def test_float64_binary_round_trip_is_exact(tmp_path):
+    pos, vel, mass = particles(333, seed=5)
+    p = tmp_path / "exact.bin"
+    write_particle_file(p, pos, vel, mass, "binary64")
+    assert p.stat().st_size == 16 + 333 * 7 * 8
+    rp, rv, rm = read_particle_file(p, "binary")
+    assert np.array_equal(rp, pos) and np.array_equal(rv, vel) and np.array_equal(rm, mass)

@@ -40,6 +40,44 @@ nyxpm_status check_launch(Ctx& c, const char* what)
     return e == cudaErrorMemoryAllocation ? NYXPM_OOM : NYXPM_CUDA_ERROR;
 }
 
+nyxpm_status run_iteration(Ctx& c, IterGraph& g, const std::function<nyxpm_status()>& body)
+{
+    if (c.prof_on || g.failed) return body();
+    if (!g.exec) {
+        const int64_t l0 = c.launches;
+        if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            g.failed = 1;
+            return body();
+        }
+        const nyxpm_status st = body();
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(c.stream, &graph);
+        const int64_t n = c.launches - l0;
+        c.launches = l0;
+        if (st != NYXPM_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return st;
+        }
+        cudaError_t ei = e;
+        if (ei == cudaSuccess && graph) ei = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ei != cudaSuccess || !graph) {
+            // the stream would not capture (e.g. a caller's stream in another
+            // capture): the same launches, eagerly, from now on
+            cudaGetLastError();
+            g.exec = nullptr;
+            g.failed = 1;
+            return body();
+        }
+        g.launches = n;
+    }
+    c.launches += g.launches;
+    if (cudaGraphLaunch(g.exec, c.stream) != cudaSuccess) return check_launch(c, "solver iteration graph");
+    return NYXPM_OK;
+}
+
 }  // namespace nyxpm
 
 namespace {
@@ -255,7 +293,7 @@ size_t nyxpm_box_bytes(int n, int64_t np, nyxpm_precision prec)
     if (prec == NYXPM_MIXED) {
         // cell + 3 offsets + 3 vel + mass + id, double-buffered; key, perm; staging
         per_particle = 2.0 * (4 + 12 + 12 + 4 + 4) + 8 + 56 + 2;
-        per_cell = 4 + 4 + 4 + 4 + 8 + 24 + 8 + 12 + 16.0 * 8 / 7 + 8.0 * 8 / 7;
+        per_cell = 4 + 4 + 4 + 4 + 8 + 24 + 8 + 12 + 4 + 16.0 * 8 / 7 + 8.0 * 8 / 7;
     } else {
         per_particle = 2.0 * (7 * 8 + 4) + 8 + 56 + 2;
         per_cell = 4 + 4 + 4 + 8 + 24 + 8 + 64 + 16.0 * 8 / 7;
@@ -309,6 +347,7 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
         ALLOC(b->fvx2, np); ALLOC(b->fvy2, np); ALLOC(b->fvz2, np); ALLOC(b->fm2, np); ALLOC(b->id2, np);
         ALLOC(b->frho, nc);
         ALLOC(b->g32, 3 * nc);
+        ALLOC(b->r_lo, nc);
     }
     ALLOC(b->key, np);
     ALLOC(b->perm, np);
@@ -392,6 +431,8 @@ nyxpm_status nyxpm_box_destroy(nyxpm_ctx* c, nyxpm_box* b)
     CHECK_BOX(c, b);
     cudaSetDevice(c->p.device);
     cudaStreamSynchronize(c->stream);
+    for (IterGraph& g : b->iter_graph)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     for (void* q : b->allocs) cudaFree(q);
     if (b->h_norms) cudaFreeHost(b->h_norms);
     delete b;

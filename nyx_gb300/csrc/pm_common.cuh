@@ -15,6 +15,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -151,6 +152,48 @@ __host__ __device__ inline long long cidx(int i, int j, int k, int n)
     return (long long)i + (long long)n * ((long long)j + (long long)n * k);
 }
 
+// ---------------------------------------------------------------------------
+// double-float (a pair hi + lo of FP32 numbers, |lo| <= ulp(hi)/2) arithmetic on
+// the FP32 pipe, after Dekker (1971) and Knuth's TwoSum: the sum and product
+// errors of FP32 operations are recovered exactly and carried in lo.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& err)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void df_fast_two_sum(float a, float b, float& s, float& err)
+{
+    // |a| >= |b| or a = 0
+    s = __fadd_rn(a, b);
+    err = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// r -= L e at one cell, in double-float: L e = s/6 - e_m (smoother units), s the
+// sum of the six neighbours v of the FP32 correction e, (c_hi, c_lo) = 1/6
+__device__ __forceinline__ void df_residual_update(const float (&v)[6], float em, float c_hi,
+                                                   float c_lo, float& rh, float& rl)
+{
+    float sh = v[0], sl = 0.f, err;
+#pragma unroll
+    for (int w = 1; w < 6; ++w) {
+        df_two_sum(sh, v[w], sh, err);
+        sl = __fadd_rn(sl, err);
+    }
+    const float ph = __fmul_rn(sh, c_hi);
+    float pl = __fmaf_rn(sh, c_hi, -ph);
+    pl = __fadd_rn(pl, __fadd_rn(__fmul_rn(sh, c_lo), __fmul_rn(sl, c_hi)));
+    float dh;
+    df_two_sum(ph, -em, dh, err);
+    const float dl = __fadd_rn(pl, err);
+    float uh;
+    df_two_sum(rh, -dh, uh, err);
+    const float ul = __fadd_rn(err, __fsub_rn(rl, dl));
+    df_fast_two_sum(uh, ul, rh, rl);
+}
+
 // pointer to phi (or rhs) at cell (i,j,k) of a level in either layout
 template <typename T>
 __device__ inline T* lv_ptr(T* r, T* b, int n, int split, int i, int j, int k)
@@ -171,6 +214,15 @@ struct ProfRec {
 };
 
 struct Ctx;
+
+// One solver iteration (V-cycle or defect-correction step, its residual norm and
+// the norm's copy to the host) captured once per box and replayed: the launches
+// of a box never change between solves, only the host reads the norm.
+struct IterGraph {
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;              // kernel launches one replay stands for
+    int failed = 0;                    // capture refused: enqueue eagerly from then on
+};
 
 struct Box {
     int n = 0;
@@ -229,9 +281,11 @@ struct Box {
     double* G = nullptr;               // bottom Green's function (smoother units)
     float* Gf = nullptr;               // the same in FP32 (mixed inner V-cycles)
     float* g32 = nullptr;              // mixed: 3 n^3 FP32 gravity vector for the kicks
+    float* r_lo = nullptr;             // mixed: low words of the level-0 residual (red, black)
     double mscalar32_scale = 0;        // mixed: m / dx^3 applied to the FP32 deposit
     int nb = 0;
     std::vector<Level> levels;
+    IterGraph iter_graph[2];           // [0] a solve's first iteration, [1] the later ones
 
     // host<->device staging: AoS pos (3 np), vel (3 np), mass (np) doubles
     double* staging = nullptr;
@@ -257,6 +311,9 @@ struct Ctx {
 void prof_begin(Ctx& c);
 void prof_end(Ctx& c, int stage, double bytes, int fine = 0);
 nyxpm_status check_launch(Ctx& c, const char* what);
+// Enqueue one solver iteration: eagerly while profiling (per-launch events), else
+// by replaying the box's captured graph (captured on first use).
+nyxpm_status run_iteration(Ctx& c, IterGraph& g, const std::function<nyxpm_status()>& body);
 
 // ---------------------------------------------------------------------------
 // launchers (defined in pm_particles.cu / pm_multigrid.cu / pm_mixed.cu)

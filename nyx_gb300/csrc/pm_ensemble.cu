@@ -64,6 +64,7 @@ struct EDesc {
     float *frho, *g32;
     double *rows, *scal;              // scal[0] mean
     double *phi_r, *phi_b, *beta_r, *beta_b;   // level-0 FP64, split layout
+    float* r_lo;                      // low words of the level-0 residual (red n^3/2, black n^3/2)
     float* Gf;
     unsigned long long* norms;        // [0] ||beta||, [1] ||r||, [2] bad uploads
     ELevel lv[kMaxLev];
@@ -644,9 +645,11 @@ __device__ __forceinline__ T nbr_sum_split(const T* other, int n, int half, int 
 }
 
 // FP64 residual of level 0 -> FP32 inner rhs (level-0 FP32 beta) with e = 0;
-// max |r| into norms[1]; boxes still iterating
+// max |r| into norms[1]; boxes still iterating.  low_words: also the residual's
+// low words (r - (float)r) for the double-float updates of e_correct
 __global__ void __launch_bounds__(256) e_resid(const Item* __restrict__ items, int nitems,
-                                               const EDesc* __restrict__ D, const EState* __restrict__ S)
+                                               const EDesc* __restrict__ D, const EState* __restrict__ S,
+                                               int low_words)
 {
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
@@ -667,7 +670,9 @@ __global__ void __launch_bounds__(256) e_resid(const Item* __restrict__ items, i
                     const double* beta = color ? d.beta_b : d.beta_r;
                     const double s = nbr_sum_split<double>(other, n, half, ih, j, k, q);
                     const double r = beta[t] - fma(s, kSixth, -mine[t]);
-                    (color ? d.lv[0].beta_b : d.lv[0].beta_r)[t] = (float)r;
+                    const float h = (float)r;
+                    (color ? d.lv[0].beta_b : d.lv[0].beta_r)[t] = h;
+                    if (low_words) d.r_lo[(color ? (long long)n * n * half : 0LL) + t] = (float)(r - (double)h);
                     (color ? d.lv[0].phi_b : d.lv[0].phi_r)[t] = 0.f;
                     const unsigned long long u = absbits(r);
                     vmax = u > vmax ? u : vmax;
@@ -713,6 +718,78 @@ __global__ void e_count_inner(int nbox, EState* S, int cycles)
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbox) return;
     if (S[b].active && S[b].solve_active) S[b].inner += cycles;
+}
+
+// phi += e and r -= L e in double-float on level 0 (the single-box k_mx_correct
+// over item rows): the defect-correction steps after a solve's first, which
+// refreshes r with the FP64 stencil (e_resid with low words); max |r| into
+// norms[1]; boxes still iterating
+__global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items, int nitems,
+                                                 const EDesc* __restrict__ D,
+                                                 const EState* __restrict__ S, float c_hi, float c_lo)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;  // uniform across the block
+        const EDesc& d = D[it.box];
+        float vmax = 0.f;
+        const int n = d.n, half = n >> 1, k = it.b;
+        const int j = it.c + threadIdx.y;
+        if (j < n) {
+            const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+            const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+            const long long row = (long long)j + (long long)n * k;
+            const long long nh = (long long)n * n * half;
+            for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
+                const long long t = row * half + ih;
+#pragma unroll
+                for (int color = 0; color < 2; ++color) {
+                    const int q = (j + k + color) & 1;
+                    const float* other = color ? d.lv[0].phi_r : d.lv[0].phi_b;
+                    const float em = (color ? d.lv[0].phi_b : d.lv[0].phi_r)[t];
+                    const int ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
+                    const int ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
+                    const float v[6] = {other[row * half + ihm], other[row * half + ihp],
+                                        other[((long long)jm + (long long)n * k) * half + ih],
+                                        other[((long long)jp + (long long)n * k) * half + ih],
+                                        other[((long long)j + (long long)n * km) * half + ih],
+                                        other[((long long)j + (long long)n * kp) * half + ih]};
+                    float* rh_p = color ? d.lv[0].beta_b : d.lv[0].beta_r;
+                    float* rl_p = d.r_lo + (color ? nh : 0LL);
+                    float rh = rh_p[t], rl = rl_p[t];
+                    df_residual_update(v, em, c_hi, c_lo, rh, rl);
+                    rh_p[t] = rh;
+                    rl_p[t] = rl;
+                    double* pp = color ? d.phi_b : d.phi_r;
+                    pp[t] = pp[t] + (double)em;
+                    vmax = fmaxf(vmax, fabsf(rh));
+                }
+            }
+        }
+        block_umax_store(absbits((double)vmax), d.norms + 1);
+    }
+}
+
+// e = 0 on level 0 for the next inner solve (after e_correct), boxes still iterating
+__global__ void __launch_bounds__(256) e_zero_inner(const Item* __restrict__ items, int nitems,
+                                                    const EDesc* __restrict__ D,
+                                                    const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        const int n = d.n, half = n >> 1, k = it.b;
+        const int j = it.c + threadIdx.y;
+        if (j >= n) continue;
+        for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
+            const long long t = ((long long)j + (long long)n * k) * half + ih;
+            d.lv[0].phi_r[t] = 0.f;
+            d.lv[0].phi_b[t] = 0.f;
+        }
+    }
 }
 
 // phi += e on level 0 (split), boxes still iterating
@@ -1646,14 +1723,16 @@ void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
     const double ggrav = -4.0 * M_PI * c->p.gconst;
     const auto& r0 = E->r_rows_split[0];
     e_make_beta<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, ggrav);
-    e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+    e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, 0);
     e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 1);
     ep_end(c, NYXPM_ST_RHS);
     c->launches += 16;
 }
 
-// `outer` defect-correction iterations (boxes that converged skip them)
-void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer)
+// `outer` defect-correction iterations (boxes that converged skip them).  The
+// first iteration of a solve (first = 1) refreshes the residual with the FP64
+// stencil; the others update it in double-float from the correction.
+void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
 {
     cudaStream_t s = c->stream;
     const int nbox = (int)E->slots.size();
@@ -1716,8 +1795,15 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer)
         const auto& r0 = E->r_rows_split[0];
         ep_begin(c);
         e_count_inner<<<bb, 128, 0, s>>>(nbox, S, E->tune.inner_vcycles);
-        e_update<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
-        e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+        if (first && o == 0) {
+            e_update<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+            e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, 1);
+        } else {
+            const float c_hi = (float)(1.0 / 6.0);
+            const float c_lo = (float)(1.0 / 6.0 - (double)c_hi);
+            e_correct<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, c_hi, c_lo);
+            e_zero_inner<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+        }
         e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 0);
         ep_end(c, NYXPM_ST_NORM);
         c->launches += 4;
@@ -1763,7 +1849,7 @@ nyxpm_status finish_unconverged(nyxpm_ctx* c, nyxpm_ensemble* E, int* extra)
             if (E->slots[b].used && E->h_state[b].active && E->h_state[b].solve_active) any = true;
         if (!any) return NYXPM_OK;
         if (guard == c->p.max_vcycles) break;
-        enqueue_iterations(c, E, 1);
+        enqueue_iterations(c, E, 1, 0);
         ETRY(echeck(c, "ensemble iterations"));
         *extra += 1;
     }
@@ -1781,7 +1867,7 @@ nyxpm_status capture(nyxpm_ctx* c, nyxpm_ensemble* E, cudaGraphExec_t* exec, int
         enqueue_load(c, E, E->h_step);
         enqueue_kick(c, E, 0);
         enqueue_solve_head(c, E);
-        enqueue_iterations(c, E, E->tune.max_outer);
+        enqueue_iterations(c, E, E->tune.max_outer, 1);
     } else {
         enqueue_grav(c, E);
         enqueue_kick(c, E, 1);
@@ -1808,8 +1894,9 @@ size_t nyxpm_ensemble_box_bytes(int n, int64_t np)
 {
     const double nc = (double)n * n * n;
     // particles: 2 x (cell, id, 3 offsets, 3 velocities) + key + perm + staging for upload
-    // cells: count, start, FP32 rho, FP32 g (3), FP64 phi + beta, FP32 levels (phi + beta, 8/7)
-    return (size_t)(np * (2.0 * 32 + 8) + nc * (4 + 4 + 4 + 12 + 16 + 16 + 8.0 * 8 / 7) + 8.0 * n * n +
+    // cells: count, start, FP32 rho, FP32 g (3), FP64 phi + beta, residual low words,
+    // FP32 levels (phi + beta, 8/7)
+    return (size_t)(np * (2.0 * 32 + 8) + nc * (4 + 4 + 4 + 12 + 16 + 4 + 16 + 8.0 * 8 / 7) + 8.0 * n * n +
                     4.0 * (np / 32 + 2) + 256.0 * 64 + 4.0 * nc / 4096);
 }
 
@@ -1915,6 +2002,7 @@ nyxpm_status nyxpm_ensemble_add(nyxpm_ctx* c, nyxpm_ensemble* E, int n, double L
     d.norms = (unsigned long long*)A(256);
     d.phi_r = (double*)A(8 * nc / 2); d.phi_b = (double*)A(8 * nc / 2);
     d.beta_r = (double*)A(8 * nc / 2); d.beta_b = (double*)A(8 * nc / 2);
+    d.r_lo = (float*)A(4 * nc);
     for (int l = 0, nl = n; l < d.nlev; ++l, nl /= 2) {
         ELevel& lv = d.lv[l];
         lv.n = nl;
@@ -2152,7 +2240,7 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* c, nyxpm_ensemble* E, const double* 
     if (any_init) {
         enqueue_load(c, E, E->h_init);
         enqueue_solve_head(c, E);
-        enqueue_iterations(c, E, E->tune.max_outer);
+        enqueue_iterations(c, E, E->tune.max_outer, 1);
         ETRY(echeck(c, "ensemble init"));
         int more = 0;
         ETRY(finish_unconverged(c, E, &more));
@@ -2174,7 +2262,7 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* c, nyxpm_ensemble* E, const double* 
         enqueue_load(c, E, E->h_step);
         enqueue_kick(c, E, 0);
         enqueue_solve_head(c, E);
-        enqueue_iterations(c, E, E->tune.max_outer);
+        enqueue_iterations(c, E, E->tune.max_outer, 1);
         ETRY(echeck(c, "ensemble profiled step"));
         int more = 0;
         ETRY(finish_unconverged(c, E, &more));

@@ -242,7 +242,8 @@ __global__ void __launch_bounds__(256) k_mx_deposit(int n, float scale, const in
                                                     const int* __restrict__ key_slot,
                                                     const float* __restrict__ heavy_part, float* rho)
 {
-    __shared__ float part[kNKeys * 8];
+    // corner-major: a warp's 32 consecutive keys (or cells) touch 32 banks
+    __shared__ float part[8 * kNKeys];
     const int i0 = blockIdx.x * kTx, j0 = blockIdx.y * kTy, k0 = blockIdx.z * kTz;
     for (int kl = threadIdx.x; kl < kNKeys; kl += blockDim.x) {
         const int ki = kl % kKx, kj = (kl / kKx) % kKy, kk = kl / (kKx * kKy);
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(256) k_mx_deposit(int n, float scale, const in
             for (int q = b0; q < e; ++q) mx_add_weights(q, n, cell, ox, oy, oz, m, s);
         }
 #pragma unroll
-        for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
+        for (int c = 0; c < 8; ++c) part[c * kNKeys + kl] = s[c];
     }
     __syncthreads();
     for (int cl = threadIdx.x; cl < kTx * kTy * kTz; cl += blockDim.x) {
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(256) k_mx_deposit(int n, float scale, const in
 #pragma unroll
                 for (int di = 0; di < 2; ++di) {
                     const int kl = (ci + di) + kKx * ((cj + dj) + kKy * (ck + dk));
-                    acc += part[kl * 8 + (1 - di) + 2 * (1 - dj) + 4 * (1 - dk)];
+                    acc += part[((1 - di) + 2 * (1 - dj) + 4 * (1 - dk)) * kNKeys + kl];
                 }
         rho[cidx(i, j, k, n)] = acc * scale;
     }
@@ -384,7 +385,8 @@ __device__ __forceinline__ T nbr_sum_split(const T* other, int n, int half, int 
 // residual of both colours of a split level 0: r = beta - (s/6 - phi), one thread per (ih, j, k)
 __global__ void k_mx_resid(int n, const double* __restrict__ phi_r, const double* __restrict__ phi_b,
                            const double* __restrict__ beta_r, const double* __restrict__ beta_b,
-                           float* r_r, float* r_b, unsigned long long* norm)
+                           float* r_r, float* r_b, float* rl_r, float* rl_b,
+                           unsigned long long* norm)
 {
     const int half = n >> 1;
     const int ih = blockIdx.x * blockDim.x + threadIdx.x;
@@ -401,7 +403,9 @@ __global__ void k_mx_resid(int n, const double* __restrict__ phi_r, const double
             const double* beta = color ? beta_b : beta_r;
             const double s = nbr_sum_split<double>(other, n, half, ih, j, k, q);
             const double r = beta[t] - fma(s, kSixth, -mine[t]);
-            (color ? r_b : r_r)[t] = (float)r;
+            const float h = (float)r;
+            (color ? r_b : r_r)[t] = h;
+            if (rl_r) (color ? rl_b : rl_r)[t] = (float)(r - (double)h);
             const unsigned long long u = absbits(r);
             v = u > v ? u : v;
         }
@@ -414,7 +418,8 @@ __global__ void k_mx_resid(int n, const double* __restrict__ phi_r, const double
 // residual is k_mx_resid's, term for term.
 __global__ void k_mx_resid2(int n, const double* __restrict__ phi_r, const double* __restrict__ phi_b,
                             const double* __restrict__ beta_r, const double* __restrict__ beta_b,
-                            float* r_r, float* r_b, unsigned long long* norm)
+                            float* r_r, float* r_b, float* rl_r, float* rl_b,
+                            unsigned long long* norm)
 {
     const unsigned half = (unsigned)n >> 1;
     const unsigned t2 = blockIdx.x * blockDim.x + threadIdx.x;   // compact cells 2 t2, 2 t2 + 1
@@ -461,7 +466,11 @@ __global__ void k_mx_resid2(int n, const double* __restrict__ phi_r, const doubl
             s1 = s1 + zp.y;
             const double r0v = b.x - fma(s0, kSixth, -m.x);
             const double r1v = b.y - fma(s1, kSixth, -m.y);
-            reinterpret_cast<float2*>(color ? r_b : r_r)[t >> 1] = make_float2((float)r0v, (float)r1v);
+            const float h0 = (float)r0v, h1 = (float)r1v;
+            reinterpret_cast<float2*>(color ? r_b : r_r)[t >> 1] = make_float2(h0, h1);
+            if (rl_r)
+                reinterpret_cast<float2*>(color ? rl_b : rl_r)[t >> 1] =
+                    make_float2((float)(r0v - (double)h0), (float)(r1v - (double)h1));
             const unsigned long long u0 = absbits(r0v), u1 = absbits(r1v);
             v = u0 > v ? u0 : v;
             v = u1 > v ? u1 : v;
@@ -499,6 +508,113 @@ __global__ void k_mx_update(long long cnt, double* phi, const float* __restrict_
 {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < cnt) phi[t] = phi[t] + (double)e[t];
+}
+
+// Defect-correction step without an FP64 stencil: phi += e (FP64) and the
+// residual r = beta - L phi, kept as a double-float (r_hi = the FP32 inner
+// right-hand side, r_lo), is updated by r -= L e with L e = s(e)/6 - e formed in
+// double-float from the FP32 correction e.  The error this adds is of order
+// 2^-48 |e| per step; the first step of a solve (|e| ~ |phi|) refreshes r with
+// the FP64 stencil instead, so the later steps, whose e are small against phi,
+// keep the residual within the FP64 residual's own rounding.  One thread per
+// compact cell of each colour of a split level 0.
+__global__ void k_mx_correct(int n, float c_hi, float c_lo, const float* __restrict__ e_r,
+                             const float* __restrict__ e_b, double* phi_r, double* phi_b,
+                             float* r_r, float* r_b, float* rl_r, float* rl_b,
+                             unsigned long long* norm)
+{
+    const int half = n >> 1;
+    const int ih = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    float vmax = 0.f;
+    if (ih < half && j < n) {
+        const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        const long long row = (long long)j + (long long)n * k;
+        const long long t = row * half + ih;
+#pragma unroll
+        for (int color = 0; color < 2; ++color) {
+            const int q = (j + k + color) & 1;
+            const float* other = color ? e_r : e_b;
+            const float em = (color ? e_b : e_r)[t];
+            const int ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
+            const int ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
+            const float v[6] = {other[row * half + ihm], other[row * half + ihp],
+                                other[((long long)jm + (long long)n * k) * half + ih],
+                                other[((long long)jp + (long long)n * k) * half + ih],
+                                other[((long long)j + (long long)n * km) * half + ih],
+                                other[((long long)j + (long long)n * kp) * half + ih]};
+            float* rh_p = color ? r_b : r_r;
+            float* rl_p = color ? rl_b : rl_r;
+            float rh = rh_p[t], rl = rl_p[t];
+            df_residual_update(v, em, c_hi, c_lo, rh, rl);
+            rh_p[t] = rh;
+            rl_p[t] = rl;
+            double* pp = color ? phi_b : phi_r;
+            pp[t] = pp[t] + (double)em;
+            vmax = fmaxf(vmax, fabsf(rh));
+        }
+    }
+    block_umax_store(absbits((double)vmax), norm);
+}
+
+// k_mx_correct with two compact cells of each colour per thread (8- and 16-byte
+// accesses) for rows of an even number of compact cells; every cell's update is
+// k_mx_correct's, term for term.
+__global__ void k_mx_correct2(int n, float c_hi, float c_lo, const float* __restrict__ e_r,
+                              const float* __restrict__ e_b, double* phi_r, double* phi_b,
+                              float* r_r, float* r_b, float* rl_r, float* rl_b,
+                              unsigned long long* norm)
+{
+    const unsigned half = (unsigned)n >> 1;
+    const unsigned t2 = blockIdx.x * blockDim.x + threadIdx.x;   // compact cells 2 t2, 2 t2 + 1
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    float vmax = 0.f;
+    if (t2 < half / 2 && j < n) {
+        const unsigned ih = 2 * t2;
+        const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        auto row = [&](int jj, int kk) -> unsigned { return ((unsigned)jj + (unsigned)n * (unsigned)kk) * half; };
+        const unsigned r0 = row(j, k);
+        const unsigned t = r0 + ih;
+#pragma unroll
+        for (int color = 0; color < 2; ++color) {
+            const int q = (j + k + color) & 1;
+            const float* other = color ? e_r : e_b;
+            const float2 em = __ldg(reinterpret_cast<const float2*>((color ? e_b : e_r) + t));
+            const float2 c = __ldg(reinterpret_cast<const float2*>(other + t));
+            float xm0, xm1, xp0, xp1;
+            if (q) {   // neighbours ih, ih + 1
+                const float e = __ldg(other + r0 + (ih + 2 == half ? 0u : ih + 2));
+                xm0 = c.x; xp0 = c.y; xm1 = c.y; xp1 = e;
+            } else {   // neighbours ih - 1, ih
+                const float e = __ldg(other + r0 + (ih == 0 ? half - 1 : ih - 1));
+                xm0 = e; xp0 = c.x; xm1 = c.x; xp1 = c.y;
+            }
+            const float2 ym = __ldg(reinterpret_cast<const float2*>(other + row(jm, k) + ih));
+            const float2 yp = __ldg(reinterpret_cast<const float2*>(other + row(jp, k) + ih));
+            const float2 zm = __ldg(reinterpret_cast<const float2*>(other + row(j, km) + ih));
+            const float2 zp = __ldg(reinterpret_cast<const float2*>(other + row(j, kp) + ih));
+            float2* rh_p = reinterpret_cast<float2*>((color ? r_b : r_r) + t);
+            float2* rl_p = reinterpret_cast<float2*>((color ? rl_b : rl_r) + t);
+            float2 rh = *rh_p, rl = *rl_p;
+            const float v0[6] = {xm0, xp0, ym.x, yp.x, zm.x, zp.x};
+            const float v1[6] = {xm1, xp1, ym.y, yp.y, zm.y, zp.y};
+            df_residual_update(v0, em.x, c_hi, c_lo, rh.x, rl.x);
+            df_residual_update(v1, em.y, c_hi, c_lo, rh.y, rl.y);
+            *rh_p = rh;
+            *rl_p = rl;
+            double2* pp = reinterpret_cast<double2*>((color ? phi_b : phi_r) + t);
+            double2 ph = *pp;
+            ph.x = ph.x + (double)em.x;
+            ph.y = ph.y + (double)em.y;
+            *pp = ph;
+            vmax = fmaxf(vmax, fmaxf(fabsf(rh.x), fabsf(rh.y)));
+        }
+    }
+    block_umax_store(absbits((double)vmax), norm);
 }
 
 // ---------------------------------------------------------------------------
@@ -1003,10 +1119,12 @@ nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li)
 }
 
 // FP64 residual of level 0 into the FP32 inner right-hand side, its norm into norms[1]
-nyxpm_status launch_mx_resid(Ctx& c, Box& b)
+nyxpm_status launch_mx_resid(Ctx& c, Box& b, bool low_words)
 {
     const Level& l = b.levels[0];
     const long long nc = (long long)l.n * l.n * l.n;
+    float* rl_r = (low_words && l.split) ? b.r_lo : nullptr;
+    float* rl_b = rl_r ? b.r_lo + nc / 2 : nullptr;
     prof_begin(c);
     cudaMemsetAsync(b.norms + 1, 0, sizeof(unsigned long long), c.stream);
     if (l.split) {
@@ -1014,11 +1132,12 @@ nyxpm_status launch_mx_resid(Ctx& c, Box& b)
         if ((l.n / 2) % 2 == 0) {
             const Geo g2 = geo3(l.n / 4, l.n, l.n);
             k_mx_resid2<<<g2.grid, g2.block, 0, c.stream>>>(l.n, l.phi_r, l.phi_b, l.beta_r,
-                                                            l.beta_b, l.fbeta_r, l.fbeta_b,
-                                                            b.norms + 1);
+                                                            l.beta_b, l.fbeta_r, l.fbeta_b, rl_r,
+                                                            rl_b, b.norms + 1);
         } else {
             k_mx_resid<<<g.grid, g.block, 0, c.stream>>>(l.n, l.phi_r, l.phi_b, l.beta_r, l.beta_b,
-                                                         l.fbeta_r, l.fbeta_b, b.norms + 1);
+                                                         l.fbeta_r, l.fbeta_b, rl_r, rl_b,
+                                                         b.norms + 1);
         }
     } else {
         const Geo g = geo3(l.n, l.n, l.n);
@@ -1027,6 +1146,30 @@ nyxpm_status launch_mx_resid(Ctx& c, Box& b)
     }
     prof_end(c, NYXPM_ST_NORM, 20.0 * nc);
     return check_launch(c, "mixed residual");
+}
+
+// phi += e and the double-float residual update of a split level 0 (k_mx_correct)
+nyxpm_status launch_mx_correct(Ctx& c, Box& b)
+{
+    const Level& l = b.levels[0];
+    const long long nc = (long long)l.n * l.n * l.n;
+    const float c_hi = (float)(1.0 / 6.0);
+    const float c_lo = (float)(1.0 / 6.0 - (double)c_hi);
+    prof_begin(c);
+    cudaMemsetAsync(b.norms + 1, 0, sizeof(unsigned long long), c.stream);
+    if ((l.n / 2) % 2 == 0) {
+        const Geo g = geo3(l.n / 4, l.n, l.n);
+        k_mx_correct2<<<g.grid, g.block, 0, c.stream>>>(l.n, c_hi, c_lo, l.fphi_r, l.fphi_b,
+                                                        l.phi_r, l.phi_b, l.fbeta_r, l.fbeta_b,
+                                                        b.r_lo, b.r_lo + nc / 2, b.norms + 1);
+    } else {
+        const Geo g = geo3(l.n / 2, l.n, l.n);
+        k_mx_correct<<<g.grid, g.block, 0, c.stream>>>(l.n, c_hi, c_lo, l.fphi_r, l.fphi_b,
+                                                       l.phi_r, l.phi_b, l.fbeta_r, l.fbeta_b,
+                                                       b.r_lo, b.r_lo + nc / 2, b.norms + 1);
+    }
+    prof_end(c, NYXPM_ST_NORM, 36.0 * nc);
+    return check_launch(c, "mixed correction");
 }
 
 nyxpm_status launch_mx_update(Ctx& c, Box& b)
@@ -1203,7 +1346,7 @@ nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
     }
     prof_end(c, NYXPM_ST_NORM, 8.0 * nc);
     if ((st = check_launch(c, "mixed rhs norm")) != NYXPM_OK) return st;
-    if ((st = launch_mx_resid(c, b)) != NYXPM_OK) return st;
+    if ((st = launch_mx_resid(c, b, false)) != NYXPM_OK) return st;
     cudaMemcpyAsync(b.h_norms, b.norms, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                     c.stream);
     if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "mixed sync");
@@ -1215,20 +1358,37 @@ nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
     nyxpm_status result = NYXPM_OK;
     const size_t half_bytes = (size_t)nc / 2 * sizeof(float);
     if (!(r0 <= target)) {
-        for (it = 1; it <= c.p.max_vcycles; ++it) {
-            // inner FP32 solve of L e = r from e = 0
+        // A split level 0 keeps its residual as a double-float between steps: the
+        // first step of a solve recomputes it with the FP64 stencil, the later
+        // ones update it from the correction alone (k_mx_correct).
+        const bool incremental = l0.split != 0;
+        auto iteration = [&](bool first) -> nyxpm_status {
+            // inner FP32 solve of L e = r from e = 0, phi += e, the new residual
+            nyxpm_status s;
             if (l0.split) {
                 cudaMemsetAsync(l0.fphi_r, 0, half_bytes, c.stream);
                 cudaMemsetAsync(l0.fphi_b, 0, half_bytes, c.stream);
             } else {
                 cudaMemsetAsync(l0.fphi_r, 0, (size_t)nc * sizeof(float), c.stream);
             }
-            for (int v = 0; v < c.p.mixed_inner_vcycles; ++v, ++inner)
-                if ((st = vcycle_f(c, b, 0)) != NYXPM_OK) return st;
-            if ((st = launch_mx_update(c, b)) != NYXPM_OK) return st;
-            if ((st = launch_mx_resid(c, b)) != NYXPM_OK) return st;
+            for (int v = 0; v < c.p.mixed_inner_vcycles; ++v)
+                if ((s = vcycle_f(c, b, 0)) != NYXPM_OK) return s;
+            if (incremental && !first) {
+                if ((s = launch_mx_correct(c, b)) != NYXPM_OK) return s;
+            } else {
+                if ((s = launch_mx_update(c, b)) != NYXPM_OK) return s;
+                if ((s = launch_mx_resid(c, b, incremental)) != NYXPM_OK) return s;
+            }
             cudaMemcpyAsync(b.h_norms + 1, b.norms + 1, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, c.stream);
+            return check_launch(c, "norm copy");
+        };
+        for (it = 1; it <= c.p.max_vcycles; ++it) {
+            const bool first = it == 1;
+            if ((st = run_iteration(c, b.iter_graph[first ? 0 : 1],
+                                    [&]() { return iteration(first); })) != NYXPM_OK)
+                return st;
+            inner += c.p.mixed_inner_vcycles;
             if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "mixed sync");
             r = read_norm(b, 1);
             if (r != r) {

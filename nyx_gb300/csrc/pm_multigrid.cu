@@ -548,11 +548,16 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
     nyxpm_status result = NYXPM_OK;
     const int red_only = (c.p.nu2 > 0 && b.levels.size() > 1) ? 1 : 0;
     if (!(r0 <= target)) {
-        for (it = 1; it <= c.p.max_vcycles; ++it) {
-            if ((st = vcycle(c, b, 0)) != NYXPM_OK) return st;
-            if ((st = launch_resnorm(c, b, 1, red_only)) != NYXPM_OK) return st;
+        auto iteration = [&]() -> nyxpm_status {
+            nyxpm_status s;
+            if ((s = vcycle(c, b, 0)) != NYXPM_OK) return s;
+            if ((s = launch_resnorm(c, b, 1, red_only)) != NYXPM_OK) return s;
             cudaMemcpyAsync(b.h_norms + 1, b.norms + 1, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, c.stream);
+            return check_launch(c, "norm copy");
+        };
+        for (it = 1; it <= c.p.max_vcycles; ++it) {
+            if ((st = run_iteration(c, b.iter_graph[0], iteration)) != NYXPM_OK) return st;
             if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "solve sync");
             r = read_norm(b, 1);
             if (r != r) {

@@ -31,6 +31,17 @@ def min_image(d, L):
     return (d + 0.5 * L) % L - 0.5 * L
 
 
+def true_resnorm(box, n, L, a):
+    """||rhs - L phi||_inf of the box's phi under the oracle's FP64 operator, with
+    the rhs built by the oracle from the box's own density and mass offset (the
+    check of a solve's residual independent of the norm the solver tracked);
+    returns (resnorm, ||rhs||_inf)."""
+    from oracle import oracle as O
+    rhs, _ = O.make_rhs(n, L, box.deposit(), box.mass_offset(), -4.0 * math.pi * O.gconst(), a)
+    _, _, _, r0, _ = O.mg_solve(n, L, rhs, box.get_phi(), max_cycles=0)
+    return r0, float(np.abs(rhs).max())
+
+
 def config1_ics(n=64, seed=1, slope=-2.0, a_init=0.02, fraction=1.0):
     """Plain PM, CPU-runnable config: unit box, EdS, rms displacement 0.2 cell at a=0.02."""
     return zeldovich_ics(n, 1.0, slope, seed, a_init, rms_disp_cells=0.2, fraction=fraction)

@@ -13,7 +13,8 @@ import pytest
 
 from nyx_gb300.pm import Box
 from oracle import oracle as O
-from tests.pm_cases import config1_ics, equal_da_schedule, mean_removed, min_image, rel_l2
+from tests.pm_cases import (config1_ics, equal_da_schedule, mean_removed, min_image, rel_l2,
+                            true_resnorm)
 
 pytestmark = pytest.mark.gpu
 
@@ -26,9 +27,10 @@ def displacement_err(gpos, opos, lattice, L):
     return float(np.linalg.norm(d) / np.linalg.norm(disp))
 
 
-@pytest.mark.parametrize("reuse", [False, True])
-def test_mixed_step_by_step_vs_oracle(ctx, reuse):
-    n, L = 64, 1.0
+@pytest.mark.parametrize("reuse,n", [(False, 64), (True, 64), (False, 10)])
+def test_mixed_step_by_step_vs_oracle(ctx, reuse, n):
+    """n = 10 has rows of 5 compact cells: the one-cell-per-thread residual kernels."""
+    L = 1.0
     ic = config1_ics(n, seed=1)
     p = O.Particles(ic.pos, ic.vel, ic.mass)
     pm = O.PMOracle(n, L, p, reuse_field=reuse)
@@ -45,6 +47,9 @@ def test_mixed_step_by_step_vs_oracle(ctx, reuse):
         new = info["new_solve"]
         assert new["resnorm"] <= 1e-10 * max(new["bnorm"], new["resnorm0"]) * (1 + 1e-9)
         assert new["inner_vcycles"] >= new["vcycles"]
+        # the residual of the returned phi, recomputed in FP64 by the oracle
+        r_true, bnorm = true_resnorm(b, n, L, a1)
+        assert r_true <= 1.05e-10 * max(bnorm, new["resnorm0"]), (r_true, bnorm)
         e_rho = rel_l2(b.deposit(), pm.rho)
         e_phi = rel_l2(mean_removed(b.get_phi()), mean_removed(pm.phi))
         e_g = rel_l2(b.grav_vector(), pm.g)

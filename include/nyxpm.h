@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define NYXPM_ABI_VERSION 1
+#define NYXPM_ABI_VERSION 2
 
 typedef enum nyxpm_status {
     NYXPM_OK = 0,
@@ -61,6 +61,9 @@ typedef struct nyxpm_params {
     int nu1, nu2;           /* red-black Gauss-Seidel sweeps before / after the coarse correction */
     int verbose;
     int mixed_inner_vcycles;/* NYXPM_MIXED: FP32 V-cycles per FP64 defect-correction iteration */
+    int mg_fused_edge;      /* NYXPM_MIXED: the FP32 V-cycle levels of at most this many cells
+                               per edge run as one launch (one CTA per box) per V-cycle, same
+                               results; 0: one launch per pass on every level (default 16) */
 } nyxpm_params;
 
 typedef struct nyxpm_ctx nyxpm_ctx;

@@ -57,6 +57,7 @@ class Params(C.Structure):
         ("nu2", C.c_int),
         ("verbose", C.c_int),
         ("mixed_inner_vcycles", C.c_int),
+        ("mg_fused_edge", C.c_int),
     ]
 
 

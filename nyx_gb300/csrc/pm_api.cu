@@ -228,6 +228,7 @@ void nyxpm_default_params(nyxpm_params* p)
     p->nu2 = 2;
     p->verbose = 0;
     p->mixed_inner_vcycles = 2;
+    p->mg_fused_edge = 16;
 }
 
 nyxpm_status nyxpm_create(const nyxpm_params* p, nyxpm_ctx** out)
@@ -235,7 +236,7 @@ nyxpm_status nyxpm_create(const nyxpm_params* p, nyxpm_ctx** out)
     if (!p || !out) return NYXPM_INVALID_ARG;
     *out = nullptr;
     if (p->nu1 < 0 || p->nu2 < 0 || p->max_vcycles < 1 || !(p->rel_tol > 0) ||
-        p->mixed_inner_vcycles < 1)
+        p->mixed_inner_vcycles < 1 || p->mg_fused_edge < 0)
         return NYXPM_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {

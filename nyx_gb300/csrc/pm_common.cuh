@@ -71,6 +71,18 @@ __device__ inline void block_umax_store(unsigned long long v, unsigned long long
     __syncthreads();  // sm may be reused by the caller's next loop iteration
 }
 
+// warp max of bits into *out; the whole warp calls it (blocks of 32-wide rows)
+__device__ inline void warp_umax_atomic(unsigned long long v, unsigned long long* out)
+{
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, off);
+        v = o > v ? o : v;
+    }
+    const int lane = (threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z)) & 31;
+    if (lane == 0 && v != 0ULL) atomicMax(out, v);
+}
+
 // One multigrid level.  The right-hand side is stored in smoother units,
 // beta = h^2 rhs / 6, so a Gauss-Seidel update is phi = s/6 - beta (s = sum of
 // the 6 neighbours) and the h factors of coarser levels are exact powers of 2.

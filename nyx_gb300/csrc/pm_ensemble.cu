@@ -20,6 +20,7 @@
 // and boxes still above tolerance get further iterations before the gravity +
 // kick graph runs.
 #include "pm_common.cuh"
+#include "pm_tail.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -65,6 +66,8 @@ struct EDesc {
     double *rows, *scal;              // scal[0] mean
     double *phi_r, *phi_b, *beta_r, *beta_b;   // level-0 FP64, split layout
     float* r_lo;                      // low words of the level-0 residual (red n^3/2, black n^3/2)
+    int tail_l;                       // first level of the fused coarse V-cycle (e_tail)
+    int pad_tail;
     float* Gf;
     unsigned long long* norms;        // [0] ||beta||, [1] ||r||, [2] bad uploads
     ELevel lv[kMaxLev];
@@ -624,7 +627,7 @@ __global__ void __launch_bounds__(256) e_make_beta(const Item* __restrict__ item
                 }
             }
         }
-        block_umax_store(vmax, d.norms + 0);
+        warp_umax_atomic(vmax, d.norms + 0);
     }
 }
 
@@ -679,7 +682,7 @@ __global__ void __launch_bounds__(256) e_resid(const Item* __restrict__ items, i
                 }
             }
         }
-        block_umax_store(vmax, d.norms + 1);
+        warp_umax_atomic(vmax, d.norms + 1);
     }
 }
 
@@ -733,41 +736,88 @@ __global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items,
         const EState st = S[it.box];
         if (!(st.active && st.solve_active)) continue;  // uniform across the block
         const EDesc& d = D[it.box];
-        float vmax = 0.f;
-        const int n = d.n, half = n >> 1, k = it.b;
+        const int n = d.n, k = it.b;
         const int j = it.c + threadIdx.y;
-        if (j < n) {
-            const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
-            const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
-            const long long row = (long long)j + (long long)n * k;
-            const long long nh = (long long)n * n * half;
-            for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
-                const long long t = row * half + ih;
+        if (j >= n) continue;                           // uniform across the warp
+        const unsigned half = (unsigned)n >> 1;
+        const unsigned nh = (unsigned)n * (unsigned)n * half;
+        const float* e_r = d.lv[0].phi_r;
+        const float* e_b = d.lv[0].phi_b;
+        float* rh_r = d.lv[0].beta_r;
+        float* rh_b = d.lv[0].beta_b;
+        float* rl = d.r_lo;
+        double* p_r = d.phi_r;
+        double* p_b = d.phi_b;
+        const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        auto row = [&](int jj, int kk) -> unsigned { return ((unsigned)jj + (unsigned)n * (unsigned)kk) * half; };
+        const unsigned r0 = row(j, k), rym = row(jm, k), ryp = row(jp, k), rzm = row(j, km),
+                       rzp = row(j, kp);
+        float vmax = 0.f;
+        if ((half & 1u) == 0) {
+            // two compact cells per thread: the k_mx_correct2 pattern
+            for (unsigned ih = 2 * threadIdx.x; ih < half; ih += 2 * blockDim.x) {
+                const unsigned t = r0 + ih;
 #pragma unroll
                 for (int color = 0; color < 2; ++color) {
                     const int q = (j + k + color) & 1;
-                    const float* other = color ? d.lv[0].phi_r : d.lv[0].phi_b;
-                    const float em = (color ? d.lv[0].phi_b : d.lv[0].phi_r)[t];
-                    const int ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
-                    const int ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
-                    const float v[6] = {other[row * half + ihm], other[row * half + ihp],
-                                        other[((long long)jm + (long long)n * k) * half + ih],
-                                        other[((long long)jp + (long long)n * k) * half + ih],
-                                        other[((long long)j + (long long)n * km) * half + ih],
-                                        other[((long long)j + (long long)n * kp) * half + ih]};
-                    float* rh_p = color ? d.lv[0].beta_b : d.lv[0].beta_r;
-                    float* rl_p = d.r_lo + (color ? nh : 0LL);
-                    float rh = rh_p[t], rl = rl_p[t];
-                    df_residual_update(v, em, c_hi, c_lo, rh, rl);
-                    rh_p[t] = rh;
-                    rl_p[t] = rl;
-                    double* pp = color ? d.phi_b : d.phi_r;
-                    pp[t] = pp[t] + (double)em;
+                    const float* other = color ? e_r : e_b;
+                    const float2 em = *reinterpret_cast<const float2*>((color ? e_b : e_r) + t);
+                    const float2 cc = *reinterpret_cast<const float2*>(other + t);
+                    float xm0, xm1, xp0, xp1;
+                    if (q) {
+                        const float e = other[r0 + (ih + 2 == half ? 0u : ih + 2)];
+                        xm0 = cc.x; xp0 = cc.y; xm1 = cc.y; xp1 = e;
+                    } else {
+                        const float e = other[r0 + (ih == 0 ? half - 1 : ih - 1)];
+                        xm0 = e; xp0 = cc.x; xm1 = cc.x; xp1 = cc.y;
+                    }
+                    const float2 ym = *reinterpret_cast<const float2*>(other + rym + ih);
+                    const float2 yp = *reinterpret_cast<const float2*>(other + ryp + ih);
+                    const float2 zm = *reinterpret_cast<const float2*>(other + rzm + ih);
+                    const float2 zp = *reinterpret_cast<const float2*>(other + rzp + ih);
+                    float2* rh_p = reinterpret_cast<float2*>((color ? rh_b : rh_r) + t);
+                    float2* rl_p = reinterpret_cast<float2*>(rl + (color ? nh : 0u) + t);
+                    float2 rh = *rh_p, rlo = *rl_p;
+                    const float v0[6] = {xm0, xp0, ym.x, yp.x, zm.x, zp.x};
+                    const float v1[6] = {xm1, xp1, ym.y, yp.y, zm.y, zp.y};
+                    df_residual_update(v0, em.x, c_hi, c_lo, rh.x, rlo.x);
+                    df_residual_update(v1, em.y, c_hi, c_lo, rh.y, rlo.y);
+                    *rh_p = rh;
+                    *rl_p = rlo;
+                    double2* pp = reinterpret_cast<double2*>((color ? p_b : p_r) + t);
+                    double2 ph = *pp;
+                    ph.x = ph.x + (double)em.x;
+                    ph.y = ph.y + (double)em.y;
+                    *pp = ph;
+                    vmax = fmaxf(vmax, fmaxf(fabsf(rh.x), fabsf(rh.y)));
+                }
+            }
+        } else {
+            for (unsigned ih = threadIdx.x; ih < half; ih += blockDim.x) {
+                const unsigned t = r0 + ih;
+#pragma unroll
+                for (int color = 0; color < 2; ++color) {
+                    const int q = (j + k + color) & 1;
+                    const float* other = color ? e_r : e_b;
+                    const float em = (color ? e_b : e_r)[t];
+                    const unsigned ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
+                    const unsigned ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
+                    const float v[6] = {other[r0 + ihm], other[r0 + ihp], other[rym + ih],
+                                        other[ryp + ih], other[rzm + ih], other[rzp + ih]};
+                    float* rh_p = (color ? rh_b : rh_r) + t;
+                    float* rl_p = rl + (color ? nh : 0u) + t;
+                    float rh = *rh_p, rlo = *rl_p;
+                    df_residual_update(v, em, c_hi, c_lo, rh, rlo);
+                    *rh_p = rh;
+                    *rl_p = rlo;
+                    double* pp = (color ? p_b : p_r) + t;
+                    *pp = *pp + (double)em;
                     vmax = fmaxf(vmax, fabsf(rh));
                 }
             }
         }
-        block_umax_store(absbits((double)vmax), d.norms + 1);
+        warp_umax_atomic(absbits((double)vmax), d.norms + 1);
     }
 }
 
@@ -1209,8 +1259,10 @@ __global__ void __launch_bounds__(256) e_prolong4(const Item* __restrict__ items
     }
 }
 
-// exact coarsest solve of every iterating box: one block per box
-__global__ void e_bottom(int nbox, const EDesc* __restrict__ D, const EState* __restrict__ S)
+// the coarse end of every box's V-cycle (levels tail_l .. bottom), one CTA per
+// box: the per-pass kernels' arithmetic (pm_tail.cuh), so the same bits
+__global__ void __launch_bounds__(kTailThreads) e_tail(int nbox, const EDesc* __restrict__ D,
+                                                       const EState* __restrict__ S, int nu1, int nu2)
 {
     __shared__ float r[kMaxBottom * kMaxBottom * kMaxBottom];
     __shared__ float g[kMaxBottom * kMaxBottom * kMaxBottom];
@@ -1218,26 +1270,13 @@ __global__ void e_bottom(int nbox, const EDesc* __restrict__ D, const EState* __
     if (b >= nbox) return;
     if (!(S[b].active && S[b].solve_active)) return;
     const EDesc& d = D[b];
-    const ELevel& L = d.lv[d.nlev - 1];
-    const int nb = L.n, nc = nb * nb * nb;
-    for (int t = threadIdx.x; t < nc; t += blockDim.x) {
-        r[t] = L.beta_r[t];
-        g[t] = d.Gf[t];
+    LevelViewF lv[kMaxTail];
+    const int nl = d.nlev - d.tail_l;
+    for (int l = 0; l < nl; ++l) {
+        const ELevel& e = d.lv[d.tail_l + l];
+        lv[l] = LevelViewF{e.n, e.split, e.phi_r, e.phi_b, e.beta_r, e.beta_b};
     }
-    __syncthreads();
-    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-        const int i = c % nb, j = (c / nb) % nb, k = c / (nb * nb);
-        float s = 0.f;
-        int y = 0;
-        for (int yk = 0; yk < nb; ++yk) {
-            const int dk = wrap1(k - yk, nb) * nb * nb;
-            for (int yj = 0; yj < nb; ++yj) {
-                const int djk = dk + wrap1(j - yj, nb) * nb;
-                for (int yi = 0; yi < nb; ++yi, ++y) s = fmaf(g[djk + wrap1(i - yi, nb)], r[y], s);
-            }
-        }
-        L.phi_r[c] = s;
-    }
+    vcycle_tail(lv, nl, nu1, nu2, d.Gf, d.nb, r, g);
 }
 
 // FP32 gravity vector from the FP64 phi (level-0 rows, natural coordinates)
@@ -1475,6 +1514,19 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
     E->max_lev = 0;
     for (auto& s : E->slots)
         if (s.used) E->max_lev = std::max(E->max_lev, s.desc.nlev);
+    // first level of each box's fused coarse V-cycle: the first of at most
+    // mg_fused_edge cells per edge (at most kMaxTail levels), else the bottom
+    for (auto& s : E->slots) {
+        if (!s.used) continue;
+        EDesc& d = s.desc;
+        d.tail_l = d.nlev - 1;
+        if (c->p.mg_fused_edge > 0)
+            for (int l = std::max(0, d.nlev - kMaxTail); l < d.nlev; ++l)
+                if (d.lv[l].n <= c->p.mg_fused_edge) {
+                    d.tail_l = l;
+                    break;
+                }
+    }
     auto begin = [&](nyxpm_ensemble::Range& r) { r.off = (int)items.size(); };
     auto end = [&](nyxpm_ensemble::Range& r) { r.cnt = (int)items.size() - r.off; };
     begin(E->r_part);
@@ -1537,7 +1589,7 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
         begin(E->r_smooth_vec[l]);
         for (int b = 0; b < nbox; ++b) {
             const EnsSlot& s = E->slots[b];
-            if (!s.used || l >= s.desc.nlev - 1) continue;
+            if (!s.used || l >= s.desc.tail_l) continue;
             const int nl = s.desc.lv[l].n;
             if ((nl / 2) % 4 != 0) continue;
             const int rv = vec_rows(nl, 32 * R);
@@ -1548,7 +1600,7 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
         begin(E->r_smooth_march[l]);
         for (int b = 0; b < nbox; ++b) {
             const EnsSlot& s = E->slots[b];
-            if (!s.used || l >= s.desc.nlev - 1) continue;
+            if (!s.used || l >= s.desc.tail_l) continue;
             const int nl = s.desc.lv[l].n;
             if ((nl / 2) % 4 != 0) continue;
             const int rv = vec_rows(nl, 32 * R);
@@ -1559,7 +1611,7 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
         begin(E->r_smooth_row[l]);
         for (int b = 0; b < nbox; ++b) {
             const EnsSlot& s = E->slots[b];
-            if (!s.used || l >= s.desc.nlev - 1) continue;
+            if (!s.used || l >= s.desc.tail_l) continue;
             const int nl = s.desc.lv[l].n;
             if ((nl / 2) % 4 == 0) continue;
             for (int k = 0; k < nl; ++k)
@@ -1571,7 +1623,7 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
             begin(rg);
             for (int b = 0; b < nbox; ++b) {
                 const EnsSlot& s = E->slots[b];
-                if (!s.used || l == 0 || l >= s.desc.nlev) continue;
+                if (!s.used || l == 0 || l > s.desc.tail_l) continue;
                 if ((((s.desc.lv[l - 1].n / 2) % 4) == 0) != (vec == 1)) continue;
                 const int nl = s.desc.lv[l].n;
                 for (int k = 0; k < nl; ++k)
@@ -1774,7 +1826,7 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
                 c->launches += 1;
             }
             ep_begin(c);
-            e_bottom<<<nbox, 128, 0, s>>>(nbox, D, S);
+            e_tail<<<nbox, kTailThreads, 0, s>>>(nbox, D, S, c->p.nu1, c->p.nu2);
             ep_end(c, NYXPM_ST_BOTTOM);
             c->launches += 1;
             for (int l = E->max_lev - 2; l >= 0; --l) {

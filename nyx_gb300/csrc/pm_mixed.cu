@@ -13,6 +13,7 @@
 // FP32 arithmetic is compiled with multiply-add contraction (the default): this
 // form is checked against the FP64 oracle by a stated tolerance, not bitwise.
 #include "pm_common.cuh"
+#include "pm_tail.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -642,7 +643,9 @@ __global__ void __launch_bounds__(256) k_gsrb_f(int n, int color, float* __restr
 // value for the x neighbours.  The sums are the scalar kernel's, term for term.
 // Needs half % 4 == 0 (rows start on 16 bytes).
 constexpr int kMarchZ = 4;
+constexpr int kMarchMinEdge = 256;
 
+template <int MZ>
 __global__ void __launch_bounds__(256) k_gsrb_f4(int n, int color, float* __restrict__ mine,
                                                  const float* __restrict__ other,
                                                  const float* __restrict__ beta)
@@ -651,7 +654,7 @@ __global__ void __launch_bounds__(256) k_gsrb_f4(int n, int color, float* __rest
     const unsigned half = (unsigned)n >> 1, h4 = half >> 2;
     const unsigned t4 = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k0 = blockIdx.z * kMarchZ;
+    const int k0 = blockIdx.z * MZ;
     if (t4 >= h4 || j >= n) return;
     const unsigned ih = 4 * t4;
     const unsigned plane = (unsigned)n * half;
@@ -664,9 +667,9 @@ __global__ void __launch_bounds__(256) k_gsrb_f4(int n, int color, float* __rest
     const int kfirst = k0 == 0 ? n - 1 : k0 - 1;
     float4 zm = __ldg(o4 + (((unsigned)kfirst * plane + rj) >> 2));
     float4 c = __ldg(o4 + (((unsigned)k0 * plane + rj) >> 2));
-    // the levels this kernel runs on have n % 8 == 0: every block marches kMarchZ planes
+    // the levels this kernel runs on have n % 8 == 0: every block marches MZ planes
 #pragma unroll
-    for (int kk = 0; kk < kMarchZ; ++kk) {
+    for (int kk = 0; kk < MZ; ++kk) {
         const int k = k0 + kk;
         const int kp = k == n - 1 ? 0 : k + 1;
         const unsigned pk = (unsigned)k * plane;
@@ -936,6 +939,22 @@ __global__ void k_bottom_f(int nb, const float* __restrict__ G, const float* __r
     }
 }
 
+// the coarse end of a V-cycle (levels of at most mg_fused_edge cells per edge
+// down to the bottom) by one CTA; the arithmetic of the per-pass kernels
+struct TailF {
+    int nl;                  // levels in the tail; the last is the bottom (natural layout)
+    int nu1, nu2, nb;
+    const float* Gf;
+    LevelViewF lv[kMaxTail];
+};
+
+__global__ void __launch_bounds__(kTailThreads) k_vcycle_tail_f(TailF A)
+{
+    __shared__ float r[kMaxBottom * kMaxBottom * kMaxBottom];
+    __shared__ float g[kMaxBottom * kMaxBottom * kMaxBottom];
+    vcycle_tail(A.lv, A.nl, A.nu1, A.nu2, A.Gf, A.nb, r, g);
+}
+
 // FP32 gravity vector from the FP64 phi: the difference in FP64, the scaling in FP32
 // (component-major, 3 n^3)
 __global__ void k_mx_grav(LevelView L, float half_dxi, float* g)
@@ -1052,10 +1071,12 @@ nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine)
     const long long half_cells = (long long)l.n * l.n * l.n / 2;
     const int half = l.n / 2;
     const bool vec = half % 4 == 0;   // then n % 8 == 0, a whole number of kMarchZ planes
+    // marching pays on the large levels; below, more threads hide more latency
+    const bool march = vec && l.n >= kMarchMinEdge;
     Geo g;
     if (vec) {
         g = geo3(half / 4, l.n, 1);
-        g.grid.z = (l.n + kMarchZ - 1) / kMarchZ;
+        g.grid.z = march ? (l.n + kMarchZ - 1) / kMarchZ : l.n;
     } else {
         g = geo3(half, l.n, l.n);
     }
@@ -1064,8 +1085,10 @@ nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine)
         const float* other = color ? l.fphi_r : l.fphi_b;
         const float* beta = color ? l.fbeta_b : l.fbeta_r;
         prof_begin(c);
-        if (vec)
-            k_gsrb_f4<<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
+        if (march)
+            k_gsrb_f4<kMarchZ><<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
+        else if (vec)
+            k_gsrb_f4<1><<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
         else
             k_gsrb_f<<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
         prof_end(c, NYXPM_ST_SMOOTH, 12.0 * half_cells, fine);
@@ -1073,9 +1096,38 @@ nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine)
     return check_launch(c, "gsrb f32");
 }
 
+// levels li .. last in one k_vcycle_tail_f launch
+nyxpm_status vcycle_tail_f(Ctx& c, Box& b, size_t li)
+{
+    TailF A;
+    A.nl = (int)(b.levels.size() - li);
+    A.nu1 = c.p.nu1;
+    A.nu2 = c.p.nu2;
+    A.nb = b.nb;
+    A.Gf = b.Gf;
+    double bytes = 0;
+    for (int l = 0; l < A.nl; ++l) {
+        const Level& lv = b.levels[li + l];
+        A.lv[l] = viewf(lv);
+        const double cells = (double)lv.n * lv.n * lv.n;
+        bytes += (l + 1 < A.nl) ? 6.0 * cells * 2 * (c.p.nu1 + c.p.nu2) + 16.0 * cells : 8.0 * cells;
+    }
+    prof_begin(c);
+    k_vcycle_tail_f<<<1, kTailThreads, 0, c.stream>>>(A);
+    prof_end(c, NYXPM_ST_SMOOTH, bytes);
+    return check_launch(c, "fused coarse V-cycle f32");
+}
+
+bool tail_fits(const Ctx& c, const Box& b, size_t li)
+{
+    return c.p.mg_fused_edge > 0 && b.levels[li].n <= c.p.mg_fused_edge &&
+           b.levels.size() - li <= (size_t)kMaxTail;
+}
+
 nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li)
 {
     nyxpm_status st;
+    if (tail_fits(c, b, li)) return vcycle_tail_f(c, b, li);
     const Level& f = b.levels[li];
     if (li + 1 == b.levels.size()) {
         prof_begin(c);

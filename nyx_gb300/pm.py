@@ -51,7 +51,8 @@ class Context:
 
     def __init__(self, device: int = 0, stream: int | None = None, OmM: float = 1.0,
                  OmR: float = 0.0, h: float = 0.675, rel_tol: float = 1e-10,
-                 max_vcycles: int = 100, nu1: int = 2, nu2: int = 2, gconst: float | None = None):
+                 max_vcycles: int = 100, nu1: int = 2, nu2: int = 2, gconst: float | None = None,
+                 mg_fused_edge: int | None = None):
         self.lib = _L.load()
         p = _L.Params()
         self.lib.nyxpm_default_params(C.byref(p))
@@ -61,6 +62,8 @@ class Context:
         if gconst is not None:
             p.gconst = gconst
         p.rel_tol, p.max_vcycles, p.nu1, p.nu2 = rel_tol, max_vcycles, nu1, nu2
+        if mg_fused_edge is not None:
+            p.mg_fused_edge = mg_fused_edge
         self.params = p
         h_ = C.c_void_p()
         st = self.lib.nyxpm_create(C.byref(p), C.byref(h_))

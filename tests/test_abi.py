@@ -31,7 +31,7 @@ def test_library_loads_and_exports_every_symbol():
     lib = L.load()
     for name in header_functions():
         assert hasattr(lib, name), name
-    assert lib.nyxpm_abi_version() == 1
+    assert lib.nyxpm_abi_version() == 2
 
 
 def test_default_params_match_reference_constants():

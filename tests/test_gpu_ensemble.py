@@ -112,3 +112,19 @@ def test_profiled_eager_step_equals_graph_step(ctx):
     for (p0, v0), (p1, v1), a, b in zip(graphs, eager, g0, g1):
         assert np.array_equal(p0, p1) and np.array_equal(v0, v1) and np.array_equal(a, b)
     assert prof["stages"]["smooth"]["launches"] > 0 and prof["stages"]["deposit"]["ms"] > 0
+
+
+def test_fused_coarse_vcycle_gives_the_same_bits(ctx):
+    """The coarse levels (<= 16 cells per edge) of every box cycled by one CTA per
+    box (e_tail) against one launch per pass over all boxes: the same bits."""
+    from nyx_gb300.pm import Context
+    ics = [box_ics(s, 0.05) for s in SPECS]
+    sched = equal_da_schedule(0.05, 0.07, 2)
+    plain = Context(mg_fused_edge=0)
+    try:
+        out_p, g_p, _ = run_ensemble(plain, SPECS, ics, sched)
+    finally:
+        plain.close()
+    out_f, g_f, _ = run_ensemble(ctx, SPECS, ics, sched)
+    for (p0, v0), (p1, v1), a, b in zip(out_p, out_f, g_p, g_f):
+        assert np.array_equal(p0, p1) and np.array_equal(v0, v1) and np.array_equal(a, b)

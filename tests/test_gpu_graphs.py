@@ -42,3 +42,24 @@ def test_graph_replay_equals_eager_launches(ctx, precision):
     assert ie == ig                      # the same iteration counts and norms
     assert le == lg
     assert all(i["new_solve"]["vcycles"] >= 1 for i in ig)
+
+
+@pytest.mark.parametrize("n,edge", [(16, 16), (48, 16), (64, 16), (32, 32)])
+def test_fused_coarse_vcycle_equals_one_launch_per_pass(ctx, n, edge):
+    """mg_fused_edge = e cycles the levels of <= e cells per edge in one launch;
+    0 launches every pass.  The mixed results are the same bits (n = 16: the
+    whole V-cycle is fused; 48: levels 12, 6 and the 3^3 bottom, rows of odd
+    length and non-power-of-two edges)."""
+    from nyx_gb300.pm import Context
+    assert ctx.params.mg_fused_edge == 16
+    fused = Context(mg_fused_edge=edge)
+    plain = Context(mg_fused_edge=0)
+    try:
+        a = run(fused, "mixed", profiling=False, n=n, steps=2)
+        b = run(plain, "mixed", profiling=False, n=n, steps=2)
+    finally:
+        fused.close()
+        plain.close()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    assert a[3] == b[3]
+    assert a[4] < b[4]                   # fewer launches

@@ -169,7 +169,7 @@ nyxpm_status do_solve(Ctx& c, Box& b, double a, int zero_guess, nyxpm_solve_info
     const bool mixed = b.prec == NYXPM_MIXED;
     if ((st = mixed ? mixed_make_rhs(c, b, a) : launch_make_rhs(c, b, a)) != NYXPM_OK) return st;
     if (zero_guess && (st = launch_zero_phi(c, b)) != NYXPM_OK) return st;
-    nyxpm_status solved = mixed ? mixed_solve(c, b, info) : mg_solve(c, b, info);
+    nyxpm_status solved = mixed ? mixed_solve(c, b, zero_guess, info) : mg_solve(c, b, info);
     if (solved != NYXPM_OK && solved != NYXPM_NOT_CONVERGED) return solved;
     // the mixed solve leaves its FP32 gravity vector in g32 itself
     if (!mixed && (st = launch_grav_vector(c, b)) != NYXPM_OK) return st;
@@ -366,9 +366,9 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
     ALLOC(b->rows, (size_t)n * n);
     ALLOC(b->planes, n);
     ALLOC(b->scal, 4);
-    ALLOC(b->norms, 4);
+    ALLOC(b->norms, 8);
     ALLOC(b->staging, 7 * (size_t)np + 1);
-    if (cudaMallocHost(&b->h_norms, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+    if (cudaMallocHost(&b->h_norms, 8 * sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();
         b->h_norms = nullptr;
         return cleanup(fail(c, NYXPM_OOM, "cudaMallocHost"));
@@ -432,8 +432,7 @@ nyxpm_status nyxpm_box_destroy(nyxpm_ctx* c, nyxpm_box* b)
     CHECK_BOX(c, b);
     cudaSetDevice(c->p.device);
     cudaStreamSynchronize(c->stream);
-    for (IterGraph& g : b->iter_graph)
-        if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (b->iter_graph.exec) cudaGraphExecDestroy(b->iter_graph.exec);
     for (void* q : b->allocs) cudaFree(q);
     if (b->h_norms) cudaFreeHost(b->h_norms);
     delete b;

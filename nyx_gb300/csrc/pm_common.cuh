@@ -183,6 +183,12 @@ __device__ __forceinline__ void df_fast_two_sum(float a, float b, float& s, floa
     err = __fsub_rn(b, __fsub_rn(s, a));
 }
 
+// A bound on the error df_residual_update adds to a tracked residual, per unit
+// of max|e| over the cells it reads: the rounding of the six neighbour errors
+// summed in FP32 (at most 150 * 2^-48), of the product by the two-word 1/6, of
+// the subtraction of e and of the update of r (a few 2^-48 each).
+constexpr double kDfUpdateErr = 160.0 / 281474976710656.0;   // 160 * 2^-48
+
 // r -= L e at one cell, in double-float: L e = s/6 - e_m (smoother units), s the
 // sum of the six neighbours v of the FP32 correction e, (c_hi, c_lo) = 1/6
 __device__ __forceinline__ void df_residual_update(const float (&v)[6], float em, float c_hi,
@@ -288,7 +294,8 @@ struct Box {
     double* rows = nullptr;            // n^2 row sums
     double* planes = nullptr;          // n plane sums
     double* scal = nullptr;            // [0] mean
-    unsigned long long* norms = nullptr;   // [0] ||rhs||inf, [1] ||r||inf, [2] bad uploads
+    unsigned long long* norms = nullptr;   // [0] ||rhs||inf, [1] ||r||inf, [2] bad uploads,
+                                           // [3] time-step limit, [4] mixed: max |e|
     unsigned long long* h_norms = nullptr; // pinned host mirror
     double* G = nullptr;               // bottom Green's function (smoother units)
     float* Gf = nullptr;               // the same in FP32 (mixed inner V-cycles)
@@ -297,7 +304,7 @@ struct Box {
     double mscalar32_scale = 0;        // mixed: m / dx^3 applied to the FP32 deposit
     int nb = 0;
     std::vector<Level> levels;
-    IterGraph iter_graph[2];           // [0] a solve's first iteration, [1] the later ones
+    IterGraph iter_graph;              // one solver iteration (V-cycle or defect correction)
 
     // host<->device staging: AoS pos (3 np), vel (3 np), mass (np) doubles
     double* staging = nullptr;
@@ -357,7 +364,7 @@ nyxpm_status mixed_pack(Ctx& c, Box& b, double* d_pos, double* d_vel);
 nyxpm_status mixed_sort(Ctx& c, Box& b);
 nyxpm_status mixed_deposit(Ctx& c, Box& b);
 nyxpm_status mixed_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move);
-nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info);
+nyxpm_status mixed_solve(Ctx& c, Box& b, int zero_guess, nyxpm_solve_info* info);
 
 nyxpm_status mixed_make_rhs(Ctx& c, Box& b, double a);
 nyxpm_status mixed_grav32(Ctx& c, Box& b);  // FP32 gravity vector of the FP64 phi

@@ -81,6 +81,7 @@ struct EState {
     int outer, inner;                 // defect-correction / FP32 V-cycle counts of the last solve
     int pad;
     double target;                    // convergence target of the current solve (smoother units)
+    double err;                       // bound on |tracked residual - residual of phi| (e_correct)
     double a_old, a_new, dt;
     // the kicks' FP32 scalars per phase (0: kick-drift to a_half, 1: kick to a_new):
     // a_prev, 1 / a_cur, dt / 2, drift in cells; formed once per box in FP64
@@ -686,34 +687,40 @@ __global__ void __launch_bounds__(256) e_resid(const Item* __restrict__ items, i
     }
 }
 
-// per-box convergence after a residual pass.  first = 1: set the target from
-// ||beta|| and ||r0|| and start iterating if above it
-__global__ void e_flags(int nbox, const EDesc* __restrict__ D, EState* S, double rel_tol, int first)
+// per-box convergence after a residual pass.  mode 1: after the solve's first
+// residual -- set the target from ||beta|| and ||r0|| and start iterating if
+// above it; 2: after a defect-correction step that recomputed r with the FP64
+// stencil; 0: after a step that updated r in double-float (e_correct) -- the
+// error bound grows by kDfUpdateErr * max|e| and the box stops when the tracked
+// residual plus the bound meets the target
+__global__ void e_flags(int nbox, const EDesc* __restrict__ D, EState* S, double rel_tol, int mode)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbox) return;
     EState& st = S[b];
     if (!st.active) return;
     const EDesc& d = D[b];
-    if (!first && !st.solve_active) return;
-    double r;
-    {
-        const unsigned long long u = d.norms[1];
-        memcpy(&r, &u, sizeof(r));
-    }
-    if (first) {
-        double bn;
-        const unsigned long long u = d.norms[0];
-        memcpy(&bn, &u, sizeof(bn));
+    if (mode != 1 && !st.solve_active) return;
+    auto bits = [](unsigned long long u) {
+        double v;
+        memcpy(&v, &u, sizeof(v));
+        return v;
+    };
+    const double r = bits(d.norms[1]);
+    if (mode == 1) {
+        const double bn = bits(d.norms[0]);
         st.target = rel_tol * (bn > r ? bn : r);
+        st.err = 0.0;
         st.outer = 0;
         st.inner = 0;
         st.solve_active = (r <= st.target) ? 0 : 1;
     } else {
         st.outer += 1;
-        if (r <= st.target) st.solve_active = 0;
+        st.err = mode == 2 ? 0.0 : st.err + kDfUpdateErr * bits(d.norms[3]);
+        if (r + st.err <= st.target) st.solve_active = 0;
     }
     d.norms[1] = 0ULL;
+    d.norms[3] = 0ULL;
 }
 
 __global__ void e_count_inner(int nbox, EState* S, int cycles)
@@ -753,7 +760,7 @@ __global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items,
         auto row = [&](int jj, int kk) -> unsigned { return ((unsigned)jj + (unsigned)n * (unsigned)kk) * half; };
         const unsigned r0 = row(j, k), rym = row(jm, k), ryp = row(jp, k), rzm = row(j, km),
                        rzp = row(j, kp);
-        float vmax = 0.f;
+        float vmax = 0.f, emax = 0.f;
         if ((half & 1u) == 0) {
             // two compact cells per thread: the k_mx_correct2 pattern
             for (unsigned ih = 2 * threadIdx.x; ih < half; ih += 2 * blockDim.x) {
@@ -791,6 +798,7 @@ __global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items,
                     ph.y = ph.y + (double)em.y;
                     *pp = ph;
                     vmax = fmaxf(vmax, fmaxf(fabsf(rh.x), fabsf(rh.y)));
+                    emax = fmaxf(emax, fmaxf(fabsf(em.x), fabsf(em.y)));
                 }
             }
         } else {
@@ -814,10 +822,12 @@ __global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items,
                     double* pp = (color ? p_b : p_r) + t;
                     *pp = *pp + (double)em;
                     vmax = fmaxf(vmax, fabsf(rh));
+                    emax = fmaxf(emax, fabsf(em));
                 }
             }
         }
         warp_umax_atomic(absbits((double)vmax), d.norms + 1);
+        warp_umax_atomic(absbits((double)emax), d.norms + 3);
     }
 }
 
@@ -1775,15 +1785,17 @@ void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
     const double ggrav = -4.0 * M_PI * c->p.gconst;
     const auto& r0 = E->r_rows_split[0];
     e_make_beta<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, ggrav);
-    e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, 0);
+    e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, 1);
     e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 1);
     ep_end(c, NYXPM_ST_RHS);
     c->launches += 16;
 }
 
-// `outer` defect-correction iterations (boxes that converged skip them).  The
-// first iteration of a solve (first = 1) refreshes the residual with the FP64
-// stencil; the others update it in double-float from the correction.
+// `outer` defect-correction iterations (boxes that converged skip them).  With
+// first = 1 the first of them recomputes the residual with the FP64 stencil (a
+// zero-guess solve, whose first correction is as large as phi, or a retry of
+// boxes whose error bound kept them from converging); the others update it in
+// double-float from the correction.
 void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
 {
     cudaStream_t s = c->stream;
@@ -1856,7 +1868,7 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
             e_correct<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, c_hi, c_lo);
             e_zero_inner<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
         }
-        e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 0);
+        e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, (first && o == 0) ? 2 : 0);
         ep_end(c, NYXPM_ST_NORM);
         c->launches += 4;
     }
@@ -1901,7 +1913,7 @@ nyxpm_status finish_unconverged(nyxpm_ctx* c, nyxpm_ensemble* E, int* extra)
             if (E->slots[b].used && E->h_state[b].active && E->h_state[b].solve_active) any = true;
         if (!any) return NYXPM_OK;
         if (guard == c->p.max_vcycles) break;
-        enqueue_iterations(c, E, 1, 0);
+        enqueue_iterations(c, E, 1, guard == 0 ? 1 : 0);
         ETRY(echeck(c, "ensemble iterations"));
         *extra += 1;
     }
@@ -1919,7 +1931,7 @@ nyxpm_status capture(nyxpm_ctx* c, nyxpm_ensemble* E, cudaGraphExec_t* exec, int
         enqueue_load(c, E, E->h_step);
         enqueue_kick(c, E, 0);
         enqueue_solve_head(c, E);
-        enqueue_iterations(c, E, E->tune.max_outer, 1);
+        enqueue_iterations(c, E, E->tune.max_outer, 0);
     } else {
         enqueue_grav(c, E);
         enqueue_kick(c, E, 1);
@@ -2314,7 +2326,7 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* c, nyxpm_ensemble* E, const double* 
         enqueue_load(c, E, E->h_step);
         enqueue_kick(c, E, 0);
         enqueue_solve_head(c, E);
-        enqueue_iterations(c, E, E->tune.max_outer, 1);
+        enqueue_iterations(c, E, E->tune.max_outer, 0);
         ETRY(echeck(c, "ensemble profiled step"));
         int more = 0;
         ETRY(finish_unconverged(c, E, &more));

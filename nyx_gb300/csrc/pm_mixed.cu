@@ -514,21 +514,21 @@ __global__ void k_mx_update(long long cnt, double* phi, const float* __restrict_
 // Defect-correction step without an FP64 stencil: phi += e (FP64) and the
 // residual r = beta - L phi, kept as a double-float (r_hi = the FP32 inner
 // right-hand side, r_lo), is updated by r -= L e with L e = s(e)/6 - e formed in
-// double-float from the FP32 correction e.  The error this adds is of order
-// 2^-48 |e| per step; the first step of a solve (|e| ~ |phi|) refreshes r with
-// the FP64 stencil instead, so the later steps, whose e are small against phi,
-// keep the residual within the FP64 residual's own rounding.  One thread per
-// compact cell of each colour of a split level 0.
+// double-float from the FP32 correction e.  The error this adds is at most
+// kDfUpdateErr * max|e|; the kernel reports max|e| (enorm) so that the solve can
+// bound the difference between the tracked residual and the residual of phi,
+// and recompute r with the FP64 stencil when the bound could matter.  One
+// thread per compact cell of each colour of a split level 0.
 __global__ void k_mx_correct(int n, float c_hi, float c_lo, const float* __restrict__ e_r,
                              const float* __restrict__ e_b, double* phi_r, double* phi_b,
                              float* r_r, float* r_b, float* rl_r, float* rl_b,
-                             unsigned long long* norm)
+                             unsigned long long* norm, unsigned long long* enorm)
 {
     const int half = n >> 1;
     const int ih = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
-    float vmax = 0.f;
+    float vmax = 0.f, emax = 0.f;
     if (ih < half && j < n) {
         const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
         const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
@@ -555,9 +555,11 @@ __global__ void k_mx_correct(int n, float c_hi, float c_lo, const float* __restr
             double* pp = color ? phi_b : phi_r;
             pp[t] = pp[t] + (double)em;
             vmax = fmaxf(vmax, fabsf(rh));
+            emax = fmaxf(emax, fabsf(em));
         }
     }
     block_umax_store(absbits((double)vmax), norm);
+    block_umax_store(absbits((double)emax), enorm);
 }
 
 // k_mx_correct with two compact cells of each colour per thread (8- and 16-byte
@@ -566,13 +568,13 @@ __global__ void k_mx_correct(int n, float c_hi, float c_lo, const float* __restr
 __global__ void k_mx_correct2(int n, float c_hi, float c_lo, const float* __restrict__ e_r,
                               const float* __restrict__ e_b, double* phi_r, double* phi_b,
                               float* r_r, float* r_b, float* rl_r, float* rl_b,
-                              unsigned long long* norm)
+                              unsigned long long* norm, unsigned long long* enorm)
 {
     const unsigned half = (unsigned)n >> 1;
     const unsigned t2 = blockIdx.x * blockDim.x + threadIdx.x;   // compact cells 2 t2, 2 t2 + 1
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
-    float vmax = 0.f;
+    float vmax = 0.f, emax = 0.f;
     if (t2 < half / 2 && j < n) {
         const unsigned ih = 2 * t2;
         const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
@@ -613,9 +615,26 @@ __global__ void k_mx_correct2(int n, float c_hi, float c_lo, const float* __rest
             ph.y = ph.y + (double)em.y;
             *pp = ph;
             vmax = fmaxf(vmax, fmaxf(fabsf(rh.x), fabsf(rh.y)));
+            emax = fmaxf(emax, fmaxf(fabsf(em.x), fabsf(em.y)));
         }
     }
     block_umax_store(absbits((double)vmax), norm);
+    block_umax_store(absbits((double)emax), enorm);
+}
+
+// r0 = beta of a split level 0 as its two words (the residual of phi = 0)
+__global__ void k_mx_split_beta(long long cnt, const double* __restrict__ beta_r,
+                                const double* __restrict__ beta_b, float* r_r, float* r_b,
+                                float* rl_r, float* rl_b)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    const double br = beta_r[t], bb = beta_b[t];
+    const float hr = (float)br, hb = (float)bb;
+    r_r[t] = hr;
+    r_b[t] = hb;
+    rl_r[t] = (float)(br - (double)hr);
+    rl_b[t] = (float)(bb - (double)hb);
 }
 
 // ---------------------------------------------------------------------------
@@ -1209,19 +1228,33 @@ nyxpm_status launch_mx_correct(Ctx& c, Box& b)
     const float c_lo = (float)(1.0 / 6.0 - (double)c_hi);
     prof_begin(c);
     cudaMemsetAsync(b.norms + 1, 0, sizeof(unsigned long long), c.stream);
+    cudaMemsetAsync(b.norms + 4, 0, sizeof(unsigned long long), c.stream);
     if ((l.n / 2) % 2 == 0) {
         const Geo g = geo3(l.n / 4, l.n, l.n);
         k_mx_correct2<<<g.grid, g.block, 0, c.stream>>>(l.n, c_hi, c_lo, l.fphi_r, l.fphi_b,
                                                         l.phi_r, l.phi_b, l.fbeta_r, l.fbeta_b,
-                                                        b.r_lo, b.r_lo + nc / 2, b.norms + 1);
+                                                        b.r_lo, b.r_lo + nc / 2, b.norms + 1,
+                                                        b.norms + 4);
     } else {
         const Geo g = geo3(l.n / 2, l.n, l.n);
         k_mx_correct<<<g.grid, g.block, 0, c.stream>>>(l.n, c_hi, c_lo, l.fphi_r, l.fphi_b,
                                                        l.phi_r, l.phi_b, l.fbeta_r, l.fbeta_b,
-                                                       b.r_lo, b.r_lo + nc / 2, b.norms + 1);
+                                                       b.r_lo, b.r_lo + nc / 2, b.norms + 1,
+                                                       b.norms + 4);
     }
     prof_end(c, NYXPM_ST_NORM, 36.0 * nc);
     return check_launch(c, "mixed correction");
+}
+
+nyxpm_status launch_mx_split_beta(Ctx& c, Box& b)
+{
+    const Level& l = b.levels[0];
+    const long long half_cells = (long long)l.n * l.n * l.n / 2;
+    prof_begin(c);
+    k_mx_split_beta<<<blocks_for(half_cells), kThreads, 0, c.stream>>>(
+        half_cells, l.beta_r, l.beta_b, l.fbeta_r, l.fbeta_b, b.r_lo, b.r_lo + half_cells);
+    prof_end(c, NYXPM_ST_NORM, 32.0 * half_cells);
+    return check_launch(c, "mixed split beta");
 }
 
 nyxpm_status launch_mx_update(Ctx& c, Box& b)
@@ -1382,11 +1415,15 @@ nyxpm_status mixed_grav32(Ctx& c, Box& b)
     return check_launch(c, "mixed grav");
 }
 
-nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
+nyxpm_status mixed_solve(Ctx& c, Box& b, int zero_guess, nyxpm_solve_info* info)
 {
     nyxpm_status st;
     const Level& l0 = b.levels[0];
     const long long nc = (long long)l0.n * l0.n * l0.n;
+    // A split level 0 keeps its residual as a double-float pair (r_hi, the FP32
+    // inner right-hand side, and r_lo) and updates it from each correction
+    // (k_mx_correct) instead of applying the FP64 stencil to phi.
+    const bool incremental = l0.split != 0;
     prof_begin(c);
     cudaMemsetAsync(b.norms, 0, sizeof(unsigned long long), c.stream);
     if (l0.split) {
@@ -1398,23 +1435,27 @@ nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
     }
     prof_end(c, NYXPM_ST_NORM, 8.0 * nc);
     if ((st = check_launch(c, "mixed rhs norm")) != NYXPM_OK) return st;
-    if ((st = launch_mx_resid(c, b, false)) != NYXPM_OK) return st;
-    cudaMemcpyAsync(b.h_norms, b.norms, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                    c.stream);
+    if (zero_guess && incremental) {
+        // r0 = beta exactly: its two words, no stencil
+        if ((st = launch_mx_split_beta(c, b)) != NYXPM_OK) return st;
+        cudaMemcpyAsync(b.h_norms, b.norms, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                        c.stream);
+    } else {
+        if ((st = launch_mx_resid(c, b, incremental)) != NYXPM_OK) return st;
+        cudaMemcpyAsync(b.h_norms, b.norms, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                        c.stream);
+    }
     if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "mixed sync");
     const double bnorm = read_norm(b, 0);
-    const double r0 = read_norm(b, 1);
+    const double r0 = (zero_guess && incremental) ? bnorm : read_norm(b, 1);
     const double target = c.p.rel_tol * std::max(bnorm, r0);
     double r = r0;
+    double err = 0.0;   // bound on |tracked residual - residual of phi|
     int it = 0, inner = 0;
     nyxpm_status result = NYXPM_OK;
     const size_t half_bytes = (size_t)nc / 2 * sizeof(float);
     if (!(r0 <= target)) {
-        // A split level 0 keeps its residual as a double-float between steps: the
-        // first step of a solve recomputes it with the FP64 stencil, the later
-        // ones update it from the correction alone (k_mx_correct).
-        const bool incremental = l0.split != 0;
-        auto iteration = [&](bool first) -> nyxpm_status {
+        auto iteration = [&]() -> nyxpm_status {
             // inner FP32 solve of L e = r from e = 0, phi += e, the new residual
             nyxpm_status s;
             if (l0.split) {
@@ -1425,29 +1466,43 @@ nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
             }
             for (int v = 0; v < c.p.mixed_inner_vcycles; ++v)
                 if ((s = vcycle_f(c, b, 0)) != NYXPM_OK) return s;
-            if (incremental && !first) {
+            if (incremental) {
                 if ((s = launch_mx_correct(c, b)) != NYXPM_OK) return s;
+                cudaMemcpyAsync(b.h_norms + 4, b.norms + 4, sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, c.stream);
             } else {
                 if ((s = launch_mx_update(c, b)) != NYXPM_OK) return s;
-                if ((s = launch_mx_resid(c, b, incremental)) != NYXPM_OK) return s;
+                if ((s = launch_mx_resid(c, b, false)) != NYXPM_OK) return s;
             }
             cudaMemcpyAsync(b.h_norms + 1, b.norms + 1, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, c.stream);
             return check_launch(c, "norm copy");
         };
         for (it = 1; it <= c.p.max_vcycles; ++it) {
-            const bool first = it == 1;
-            if ((st = run_iteration(c, b.iter_graph[first ? 0 : 1],
-                                    [&]() { return iteration(first); })) != NYXPM_OK)
-                return st;
+            if ((st = run_iteration(c, b.iter_graph, iteration)) != NYXPM_OK) return st;
             inner += c.p.mixed_inner_vcycles;
             if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "mixed sync");
             r = read_norm(b, 1);
+            if (incremental) {
+                err += kDfUpdateErr * read_norm(b, 4);
+                if (err > 0.5 * target && r == r) {
+                    // the bound could hide the tolerance: recompute r from phi with
+                    // the FP64 stencil (a zero-guess solve's first correction is as
+                    // large as phi, so it always lands here once)
+                    if ((st = launch_mx_resid(c, b, true)) != NYXPM_OK) return st;
+                    cudaMemcpyAsync(b.h_norms + 1, b.norms + 1, sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, c.stream);
+                    if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+                        return check_launch(c, "mixed sync");
+                    r = read_norm(b, 1);
+                    err = 0.0;
+                }
+            }
             if (r != r) {
                 c.err = "mixed defect correction residual is NaN";
                 return NYXPM_NOT_CONVERGED;
             }
-            if (r <= target) break;
+            if (r + err <= target) break;
         }
         if (it > c.p.max_vcycles) {
             it = c.p.max_vcycles;
@@ -1462,7 +1517,7 @@ nyxpm_status mixed_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
         info->vcycles = it;
         info->inner_vcycles = inner;
         info->resnorm0 = r0 * inv_k0;
-        info->resnorm = r * inv_k0;
+        info->resnorm = (r + err) * inv_k0;   // a bound on the residual of phi
         info->bnorm = bnorm * inv_k0;
     }
     return result;

@@ -557,7 +557,7 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
             return check_launch(c, "norm copy");
         };
         for (it = 1; it <= c.p.max_vcycles; ++it) {
-            if ((st = run_iteration(c, b.iter_graph[0], iteration)) != NYXPM_OK) return st;
+            if ((st = run_iteration(c, b.iter_graph, iteration)) != NYXPM_OK) return st;
             if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "solve sync");
             r = read_norm(b, 1);
             if (r != r) {

@@ -294,7 +294,7 @@ size_t nyxpm_box_bytes(int n, int64_t np, nyxpm_precision prec)
     if (prec == NYXPM_MIXED) {
         // cell + 3 offsets + 3 vel + mass + id, double-buffered; key, perm; staging
         per_particle = 2.0 * (4 + 12 + 12 + 4 + 4) + 8 + 56 + 2;
-        per_cell = 4 + 4 + 4 + 4 + 8 + 24 + 8 + 12 + 4 + 16.0 * 8 / 7 + 8.0 * 8 / 7;
+        per_cell = 4 + 4 + 4 + 4 + 8 + 24 + 8 + 16 + 4 + 16.0 * 8 / 7 + 8.0 * 8 / 7;
     } else {
         per_particle = 2.0 * (7 * 8 + 4) + 8 + 56 + 2;
         per_cell = 4 + 4 + 4 + 8 + 24 + 8 + 64 + 16.0 * 8 / 7;
@@ -347,7 +347,7 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
         ALLOC(b->cell2, np); ALLOC(b->ox2, np); ALLOC(b->oy2, np); ALLOC(b->oz2, np);
         ALLOC(b->fvx2, np); ALLOC(b->fvy2, np); ALLOC(b->fvz2, np); ALLOC(b->fm2, np); ALLOC(b->id2, np);
         ALLOC(b->frho, nc);
-        ALLOC(b->g32, 3 * nc);
+        ALLOC(b->g32, 4 * nc);
         ALLOC(b->r_lo, nc);
     }
     ALLOC(b->key, np);

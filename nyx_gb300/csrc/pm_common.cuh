@@ -299,7 +299,7 @@ struct Box {
     unsigned long long* h_norms = nullptr; // pinned host mirror
     double* G = nullptr;               // bottom Green's function (smoother units)
     float* Gf = nullptr;               // the same in FP32 (mixed inner V-cycles)
-    float* g32 = nullptr;              // mixed: 3 n^3 FP32 gravity vector for the kicks
+    float* g32 = nullptr;              // mixed: FP32 gravity vector for the kicks, float4 per cell
     float* r_lo = nullptr;             // mixed: low words of the level-0 residual (red, black)
     double mscalar32_scale = 0;        // mixed: m / dx^3 applied to the FP32 deposit
     int nb = 0;

@@ -168,7 +168,6 @@ __global__ void __launch_bounds__(kPT) e_kick(const Item* __restrict__ items, in
         if (q >= d.np) continue;
         const PArr P = parr(d, st.parity);
         const int n = d.n;
-        const long long nc = (long long)n * n * n;
         const float a_prev = st.kick[phase][0];
         const float a_cur_inv = st.kick[phase][1];
         const float half_dt = st.kick[phase][2];
@@ -196,14 +195,17 @@ __global__ void __launch_bounds__(kPT) e_kick(const Item* __restrict__ items, in
                     cc[t] = cidx(wrap1(i - ii, n), wrap1(j - jj, n), wrap1(k - kk, n), n);
                 }
         float v[3] = {P.vx[q], P.vy[q], P.vz[q]};
+        float val[3] = {0.f, 0.f, 0.f};
+        const float4* g4 = reinterpret_cast<const float4*>(d.g32);
 #pragma unroll
-        for (int dd = 0; dd < 3; ++dd) {
-            const float* gd = d.g32 + dd * nc;
-            float val = 0.f;
-#pragma unroll
-            for (int t = 0; t < 8; ++t) val = fmaf(wgt[t], __ldg(gd + cc[t]), val);
-            v[dd] = fmaf(a_prev, v[dd], half_dt * val) * a_cur_inv;
+        for (int t = 0; t < 8; ++t) {
+            const float4 gc = __ldg(g4 + cc[t]);
+            val[0] = fmaf(wgt[t], gc.x, val[0]);
+            val[1] = fmaf(wgt[t], gc.y, val[1]);
+            val[2] = fmaf(wgt[t], gc.z, val[2]);
         }
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd) v[dd] = fmaf(a_prev, v[dd], half_dt * val[dd]) * a_cur_inv;
         P.vx[q] = v[0];
         P.vy[q] = v[1];
         P.vz[q] = v[2];
@@ -561,18 +563,23 @@ __global__ void __launch_bounds__(256) e_rowsum(const Item* __restrict__ items, 
         const int n = d.n;
         const long long row = (long long)it.a * 8 + wr;
         if (row >= (long long)n * n) continue;
+        // double-float lane sums of the FP32 densities (k_mx_rowsum's scheme)
         const float* r = d.frho + row * n;
-        double s = 0.0, c = 0.0;
-        for (int i = lane; i < n; i += 32) kahan_add(s, c, (double)r[i] - d.mass_offset);
-        s -= c;
+        float sh = 0.f, sl = 0.f;
+        for (int i = lane; i < n; i += 32) {
+            float err;
+            df_two_sum(sh, r[i], sh, err);
+            sl = __fadd_rn(sl, err);
+        }
+        double s = (double)sh + (double)sl;
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-        if (lane == 0) d.rows[row] = s;
+        if (lane == 0) d.rows[row] = s - (double)n * d.mass_offset;
     }
 }
 
 // per-box mean (one block per box); also opens the solve of every active box
-__global__ void e_mean(int nbox, const EDesc* __restrict__ D, EState* S)
+__global__ void e_mean(int nbox, const EDesc* __restrict__ D, EState* S, double ggrav)
 {
     __shared__ double ss[32];
     const int b = blockIdx.x;
@@ -592,6 +599,9 @@ __global__ void e_mean(int nbox, const EDesc* __restrict__ D, EState* S)
         for (int q = 0; q < (int)(blockDim.x >> 5); ++q) kahan_add(t, tc, ss[q]);
         t -= tc;
         d.scal[0] = (t * (d.dx * d.dx * d.dx)) / (d.L * d.L * d.L);
+        // e_make_beta's folded offset and scale for this solve
+        d.scal[1] = d.mass_offset + d.scal[0];
+        d.scal[2] = (ggrav * (1.0 / S[b].a_new)) * d.beta_scale;
         d.norms[0] = 0ULL;
         d.norms[1] = 0ULL;
         S[b].solve_active = 1;
@@ -602,7 +612,7 @@ __global__ void e_mean(int nbox, const EDesc* __restrict__ D, EState* S)
 // item = (box, level 0, plane k, first row j0), block (32, R)
 __global__ void __launch_bounds__(256) e_make_beta(const Item* __restrict__ items, int nitems,
                                                    const EDesc* __restrict__ D,
-                                                   const EState* __restrict__ S, double ggrav)
+                                                   const EState* __restrict__ S)
 {
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
@@ -613,15 +623,14 @@ __global__ void __launch_bounds__(256) e_make_beta(const Item* __restrict__ item
         const int n = d.n, half = n >> 1, k = it.b;
         const int j = it.c + threadIdx.y;
         if (j < n) {
-            const double mean = d.scal[0];
-            const double ainv = 1.0 / st.a_new;
+            const double off = d.scal[1], scale = d.scal[2];
             for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
                 const long long t = ((long long)j + (long long)n * k) * half + ih;
 #pragma unroll
                 for (int odd = 0; odd < 2; ++odd) {
                     const int i = 2 * ih + odd;
                     const double v = (double)d.frho[cidx(i, j, k, n)];
-                    const double bt = ((((v - d.mass_offset) - mean) * ggrav) * ainv) * d.beta_scale;
+                    const double bt = (v - off) * scale;
                     (((i + j + k) & 1) ? d.beta_b : d.beta_r)[t] = bt;
                     const unsigned long long u = absbits(bt);
                     vmax = u > vmax ? u : vmax;
@@ -1310,9 +1319,10 @@ __global__ void __launch_bounds__(256) e_grav(const Item* __restrict__ items, in
                 return *lv_ptr<const double>(d.phi_r, d.phi_b, n, 1, a, b2, c2);
             };
             const long long c = cidx(i, j, k, n);
-            d.g32[c] = (float)(P(ip, j, k) - P(im, j, k)) * hdxi;
-            d.g32[nc + c] = (float)(P(i, jp, k) - P(i, jm, k)) * hdxi;
-            d.g32[2 * nc + c] = (float)(P(i, j, kp) - P(i, j, km)) * hdxi;
+            reinterpret_cast<float4*>(d.g32)[c] =
+                make_float4((float)(P(ip, j, k) - P(im, j, k)) * hdxi,
+                            (float)(P(i, jp, k) - P(i, jm, k)) * hdxi,
+                            (float)(P(i, j, kp) - P(i, j, km)) * hdxi, 0.f);
         }
     }
 }
@@ -1327,10 +1337,15 @@ __global__ void e_phi_to_natural(int n, const double* __restrict__ pr, const dou
     out[cidx(i, j, k, n)] = *lv_ptr<const double>(pr, pb, n, 1, i, j, k);
 }
 
-__global__ void e_g32_to_double(long long cnt, const float* __restrict__ a, double* b)
+// the float4-per-cell FP32 gravity vector as 3 component-major FP64 arrays
+__global__ void e_g32_to_double(long long nc, const float* __restrict__ a, double* b)
 {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < cnt) b[t] = a[t];
+    if (t >= nc) return;
+    const float4 g = reinterpret_cast<const float4*>(a)[t];
+    b[t] = g.x;
+    b[nc + t] = g.y;
+    b[2 * nc + t] = g.z;
 }
 
 // ---------------------------------------------------------------------------
@@ -1780,11 +1795,11 @@ void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
     ep_end(c, NYXPM_ST_DEPOSIT);
     ep_begin(c);
     e_rowsum<<<pgrid(E, E->r_rows_rho.cnt), 256, 0, s>>>(it + E->r_rows_rho.off, E->r_rows_rho.cnt, D, S);
-    e_mean<<<nbox, 512, 0, s>>>(nbox, D, S);
-    const dim3 rb(32, E->tune.smooth_rows);
     const double ggrav = -4.0 * M_PI * c->p.gconst;
+    e_mean<<<nbox, 512, 0, s>>>(nbox, D, S, ggrav);
+    const dim3 rb(32, E->tune.smooth_rows);
     const auto& r0 = E->r_rows_split[0];
-    e_make_beta<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, ggrav);
+    e_make_beta<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
     e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, 1);
     e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 1);
     ep_end(c, NYXPM_ST_RHS);
@@ -1958,9 +1973,9 @@ size_t nyxpm_ensemble_box_bytes(int n, int64_t np)
 {
     const double nc = (double)n * n * n;
     // particles: 2 x (cell, id, 3 offsets, 3 velocities) + key + perm + staging for upload
-    // cells: count, start, FP32 rho, FP32 g (3), FP64 phi + beta, residual low words,
-    // FP32 levels (phi + beta, 8/7)
-    return (size_t)(np * (2.0 * 32 + 8) + nc * (4 + 4 + 4 + 12 + 16 + 4 + 16 + 8.0 * 8 / 7) + 8.0 * n * n +
+    // cells: count, start, FP32 rho, FP32 g (float4), FP64 phi + beta, residual low
+    // words, FP32 levels (phi + beta, 8/7)
+    return (size_t)(np * (2.0 * 32 + 8) + nc * (4 + 4 + 4 + 16 + 16 + 4 + 16 + 8.0 * 8 / 7) + 8.0 * n * n +
                     4.0 * (np / 32 + 2) + 256.0 * 64 + 4.0 * nc / 4096);
 }
 
@@ -2060,7 +2075,7 @@ nyxpm_status nyxpm_ensemble_add(nyxpm_ctx* c, nyxpm_ensemble* E, int n, double L
     d.long_list = (int*)A(4 * (np / 32 + 2));
     d.long_count = (int*)A(256);
     d.frho = (float*)A(4 * nc);
-    d.g32 = (float*)A(12 * nc);
+    d.g32 = (float*)A(16 * nc);
     d.rows = (double*)A(8 * (size_t)n * n);
     d.scal = (double*)A(256);
     d.norms = (unsigned long long*)A(256);
@@ -2249,7 +2264,8 @@ nyxpm_status nyxpm_ensemble_grav_vector(nyxpm_ctx* c, nyxpm_ensemble* E, int slo
     const long long cnt = 3LL * d.n * d.n * d.n;
     void* tmp = E->arena.alloc(8 * cnt);
     if (!tmp) return efail(c, NYXPM_OOM, "ensemble g staging");
-    e_g32_to_double<<<(unsigned)((cnt + 255) / 256), 256, 0, c->stream>>>(cnt, d.g32, (double*)tmp);
+    const long long ncell = cnt / 3;
+    e_g32_to_double<<<(unsigned)((ncell + 255) / 256), 256, 0, c->stream>>>(ncell, d.g32, (double*)tmp);
     cudaMemcpyAsync(g_out, tmp, 8 * cnt, cudaMemcpyDeviceToHost, c->stream);
     const cudaError_t e = cudaStreamSynchronize(c->stream);
     E->arena.release(tmp);

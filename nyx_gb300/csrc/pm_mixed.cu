@@ -299,22 +299,28 @@ __device__ __forceinline__ void kahan_add(double& s, double& c, double v)
     s = t;
 }
 
-// one warp per plane row: compensated lane sums, then the compensated totals of the lanes
+// one warp per plane row: each lane sums its FP32 densities as a double-float
+// pair (TwoSum on the FP32 pipe, exact to ~2^-48), the lanes' pairs are added in
+// FP64 and n * mass_offset is taken off once per row
 __global__ void k_mx_rowsum(int n, const float* __restrict__ rho, double mo, double* rows)
 {
     const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (row >= (long long)n * n) return;
     const float* r = rho + row * n;
-    double s = 0.0, c = 0.0;
-    for (int i = lane; i < n; i += 32) kahan_add(s, c, (double)r[i] - mo);
-    s -= c;
+    float sh = 0.f, sl = 0.f;
+    for (int i = lane; i < n; i += 32) {
+        float err;
+        df_two_sum(sh, r[i], sh, err);
+        sl = __fadd_rn(sl, err);
+    }
+    double s = (double)sh + (double)sl;
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
         const double t = __shfl_down_sync(0xffffffffu, s, off);
         if (lane < off) s = s + t;
     }
-    if (lane == 0) rows[row] = s;
+    if (lane == 0) rows[row] = s - (double)n * mo;
 }
 
 __global__ void k_mx_mean(int n, double dx, double L, const double* __restrict__ rows, double* scal)
@@ -337,16 +343,19 @@ __global__ void k_mx_mean(int n, double dx, double L, const double* __restrict__
     }
 }
 
+// beta = (rho - mass_offset - mean) * (-4 pi G / a) * h^2/6: one FP64 subtraction
+// and one product per cell (offset and scale folded once)
 __global__ void k_mx_make_beta(int n, int split, const float* __restrict__ rho, double mo,
-                               const double* __restrict__ scal, double ggrav, double ainv, double k0,
-                               double* beta_r, double* beta_b)
+                               const double* __restrict__ scal, double scale, double* beta_r,
+                               double* beta_b)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= n || j >= n) return;
+    const double off = mo + scal[0];
     const double v = (double)rho[cidx(i, j, k, n)];
-    *lv_ptr<double>(beta_r, beta_b, n, split, i, j, k) = ((((v - mo) - scal[0]) * ggrav) * ainv) * k0;
+    *lv_ptr<double>(beta_r, beta_b, n, split, i, j, k) = (v - off) * scale;
 }
 
 // ---------------------------------------------------------------------------
@@ -975,7 +984,7 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail_f(TailF A)
 }
 
 // FP32 gravity vector from the FP64 phi: the difference in FP64, the scaling in FP32
-// (component-major, 3 n^3)
+// (one float4 {gx, gy, gz, 0} per cell: a CIC corner is one 16-byte load)
 __global__ void k_mx_grav(LevelView L, float half_dxi, float* g)
 {
     const int n = L.n;
@@ -983,7 +992,6 @@ __global__ void k_mx_grav(LevelView L, float half_dxi, float* g)
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= n || j >= n) return;
-    const long long nc = (long long)n * n * n;
     const long long c = cidx(i, j, k, n);
     auto P = [&](int a, int b, int d) {
         return *lv_ptr<const double>(L.phi_r, L.phi_b, n, L.split, a, b, d);
@@ -991,9 +999,9 @@ __global__ void k_mx_grav(LevelView L, float half_dxi, float* g)
     const int im = i == 0 ? n - 1 : i - 1, ip = i == n - 1 ? 0 : i + 1;
     const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
     const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
-    g[c] = (float)(P(ip, j, k) - P(im, j, k)) * half_dxi;
-    g[nc + c] = (float)(P(i, jp, k) - P(i, jm, k)) * half_dxi;
-    g[2 * nc + c] = (float)(P(i, j, kp) - P(i, j, km)) * half_dxi;
+    reinterpret_cast<float4*>(g)[c] = make_float4((float)(P(ip, j, k) - P(im, j, k)) * half_dxi,
+                                                  (float)(P(i, jp, k) - P(i, jm, k)) * half_dxi,
+                                                  (float)(P(i, j, kp) - P(i, j, km)) * half_dxi, 0.f);
 }
 
 // ---------------------------------------------------------------------------
@@ -1012,7 +1020,6 @@ __global__ void __launch_bounds__(256) k_mx_kick(long long np, MxKickArgs A, int
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
     const int n = A.n;
-    const long long nc = (long long)n * n * n;
     const int c = cell[q];
     int ci = cell_i(c), cj = cell_j(c), ck = cell_k(c);
     float o[3] = {ox[q], oy[q], oz[q]};
@@ -1036,14 +1043,17 @@ __global__ void __launch_bounds__(256) k_mx_kick(long long np, MxKickArgs A, int
                 cc[t] = cidx(wrap1(i - ii, n), wrap1(j - jj, n), wrap1(k - kk, n), n);
             }
     float v[3] = {vx[q], vy[q], vz[q]};
+    float val[3] = {0.f, 0.f, 0.f};
+    const float4* g4 = reinterpret_cast<const float4*>(A.g);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const float* gd = A.g + d * nc;
-        float val = 0.f;
-#pragma unroll
-        for (int t = 0; t < 8; ++t) val = fmaf(w[t], __ldg(gd + cc[t]), val);
-        v[d] = fmaf(A.a_prev, v[d], A.half_dt * val) * A.a_cur_inv;
+    for (int t = 0; t < 8; ++t) {
+        const float4 gc = __ldg(g4 + cc[t]);
+        val[0] = fmaf(w[t], gc.x, val[0]);
+        val[1] = fmaf(w[t], gc.y, val[1]);
+        val[2] = fmaf(w[t], gc.z, val[2]);
     }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d] = fmaf(A.a_prev, v[d], A.half_dt * val[d]) * A.a_cur_inv;
     vx[q] = v[0];
     vy[q] = v[1];
     vz[q] = v[2];
@@ -1285,7 +1295,6 @@ __global__ void __launch_bounds__(256) k_mx_est_dt(long long np, int n, double d
                                                    const float* __restrict__ g,
                                                    unsigned long long* out)
 {
-    const long long nc = (long long)n * n * n;
     double best = 1.0e50;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < np;
          q += (long long)gridDim.x * blockDim.x) {
@@ -1295,7 +1304,8 @@ __global__ void __launch_bounds__(256) k_mx_est_dt(long long np, int n, double d
         const double um = fmax(fmax(ux, uy), uz);
         double dtp = um > 0 ? cfl / um : 1.0e50;
         const long long c = cidx(cell_i(cq), cell_j(cq), cell_k(cq), n);
-        const double gx = __ldg(g + c), gy = __ldg(g + nc + c), gz = __ldg(g + 2 * nc + c);
+        const float4 gc = __ldg(reinterpret_cast<const float4*>(g) + c);
+        const double gx = gc.x, gy = gc.y, gz = gc.z;
         const double ga = sqrt((gx * gx + gy * gy) + gz * gz);
         if (ga > 0) dtp = fmin(dtp, 1.0 / sqrt(ga * dxi));
         best = fmin(best, dtp);
@@ -1397,9 +1407,9 @@ nyxpm_status mixed_make_rhs(Ctx& c, Box& b, double a)
     k_mx_rowsum<<<blocks_for((long long)n * n * 32), kThreads, 0, c.stream>>>(n, b.frho,
                                                                              b.mass_offset, b.rows);
     k_mx_mean<<<1, 1024, 0, c.stream>>>(n, dx, b.L, b.rows, b.scal);
+    const double scale = ((-4.0 * M_PI * c.p.gconst) * (1.0 / a)) * beta_scale(b);
     k_mx_make_beta<<<g.grid, g.block, 0, c.stream>>>(n, l0.split, b.frho, b.mass_offset, b.scal,
-                                                     -4.0 * M_PI * c.p.gconst, 1.0 / a,
-                                                     beta_scale(b), l0.beta_r, l0.beta_b);
+                                                     scale, l0.beta_r, l0.beta_b);
     prof_end(c, NYXPM_ST_RHS, 20.0 * nc);
     c.launches += 2;
     return check_launch(c, "mixed rhs");

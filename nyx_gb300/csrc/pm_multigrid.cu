@@ -208,6 +208,11 @@ __global__ void __launch_bounds__(256) k_gsrb(int n, int color, double* __restri
 }
 
 // coarse beta = 1/2 of the 8 fine residuals (summed dk, dj, di); coarse phi = 0
+// RED = 1 after pre-smoothing (the last half sweep was black): the black
+// children's residuals are round-off by construction and count as 0, so the 4 red
+// children (di + dj + dk even) are summed in the same (dk, dj, di) order -- half
+// the FP64 residual work
+template <int RED>
 __global__ void k_restrict(LevelView F, LevelView Cv)
 {
     const int nc = Cv.n;
@@ -221,7 +226,9 @@ __global__ void k_restrict(LevelView F, LevelView Cv)
 #pragma unroll
         for (int dj = 0; dj < 2; ++dj)
 #pragma unroll
-            for (int di = 0; di < 2; ++di) s = s + resid_at(F, 2 * I + di, 2 * J + dj, 2 * K + dk);
+            for (int di = 0; di < 2; ++di)
+                if (!RED || ((di + dj + dk) & 1) == 0)
+                    s = s + resid_at(F, 2 * I + di, 2 * J + dj, 2 * K + dk);
     *lv_ptr<double>(Cv.beta_r, Cv.beta_b, nc, Cv.split, I, J, K) = s * 0.5;
     *lv_ptr<double>(Cv.phi_r, Cv.phi_b, nc, Cv.split, I, J, K) = 0.0;
 }
@@ -427,7 +434,10 @@ nyxpm_status vcycle(Ctx& c, Box& b, size_t li)
     {
         const Geo g = geo3(cl.n, cl.n, cl.n);
         prof_begin(c);
-        k_restrict<<<g.grid, g.block, 0, c.stream>>>(view(f), view(cl));
+        if (c.p.nu1 > 0)
+            k_restrict<1><<<g.grid, g.block, 0, c.stream>>>(view(f), view(cl));
+        else
+            k_restrict<0><<<g.grid, g.block, 0, c.stream>>>(view(f), view(cl));
         prof_end(c, NYXPM_ST_RESTRICT, 16.0 * ncf + 16.0 * ncc);
     }
     if ((st = check_launch(c, "restrict")) != NYXPM_OK) return st;

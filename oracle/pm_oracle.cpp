@@ -384,8 +384,12 @@ double inf_norm(const double* f, long nc)
 }
 
 // coarse beta = 1/2 of the sum of the 8 fine residuals (summed dk, dj, di):
-// the 8-cell average of rhs - lap phi, rescaled by h_c^2/6 = 4 h_f^2/6
-void restrict_resid(const Level& f, Level& c)
+// the 8-cell average of rhs - lap phi, rescaled by h_c^2/6 = 4 h_f^2/6.
+// red_only = 1 (the level was just pre-smoothed, ending with a black half
+// sweep): the black children's residuals are round-off by construction and are
+// taken as 0, so only the 4 red children (di + dj + dk even) are summed, in the
+// same (dk, dj, di) order.
+void restrict_resid(const Level& f, Level& c, int red_only)
 {
     const int nc = c.n;
 #pragma omp parallel for schedule(static)
@@ -396,7 +400,8 @@ void restrict_resid(const Level& f, Level& c)
                 for (int dk = 0; dk < 2; ++dk)
                     for (int dj = 0; dj < 2; ++dj)
                         for (int di = 0; di < 2; ++di)
-                            s = s + resid_at(f, 2 * I + di, 2 * J + dj, 2 * K + dk);
+                            if (!red_only || ((di + dj + dk) & 1) == 0)
+                                s = s + resid_at(f, 2 * I + di, 2 * J + dj, 2 * K + dk);
                 c.beta[cidx(I, J, K, nc)] = s * 0.5;
             }
 }
@@ -516,7 +521,7 @@ void vcycle(Hierarchy& H, size_t l, int nu1, int nu2)
     if (l + 1 == H.lv.size()) { bottom_solve(f, H.G); return; }
     for (int s = 0; s < nu1; ++s) gsrb(f);
     Level& c = H.lv[l + 1];
-    restrict_resid(f, c);
+    restrict_resid(f, c, nu1 > 0 ? 1 : 0);
     std::fill(c.phi.begin(), c.phi.end(), 0.0);
     vcycle(H, l + 1, nu1, nu2);
     prolong_add(c, f);

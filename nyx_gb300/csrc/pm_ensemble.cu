@@ -1133,8 +1133,11 @@ __global__ void __launch_bounds__(256) e_restrict4(const Item* __restrict__ item
 }
 
 // item level = the fine level (split); rows of the fine level
+// black: only the black fine cells take the correction (post-smoothing follows
+// and overwrites the red ones unread; the same bits)
 __global__ void __launch_bounds__(256) e_prolong(const Item* __restrict__ items, int nitems,
-                                                 const EDesc* __restrict__ D, const EState* __restrict__ S)
+                                                 const EDesc* __restrict__ D, const EState* __restrict__ S,
+                                                 int black)
 {
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
@@ -1154,6 +1157,7 @@ __global__ void __launch_bounds__(256) e_prolong(const Item* __restrict__ items,
 #pragma unroll
             for (int odd = 0; odd < 2; ++odd) {
                 const int i = 2 * ih + odd;
+                if (black && ((i + j + k) & 1) == 0) continue;
                 const int Is[2] = {ih, wrap1(odd ? ih + 1 : ih - 1, nc)};
                 float s = 0.f;
 #pragma unroll
@@ -1177,7 +1181,7 @@ __global__ void __launch_bounds__(256) e_prolong(const Item* __restrict__ items,
 // array), otherwise one column per task as e_prolong.  Same sums, same order.
 __global__ void __launch_bounds__(256) e_prolong4(const Item* __restrict__ items, int nitems,
                                                   const EDesc* __restrict__ D,
-                                                  const EState* __restrict__ S)
+                                                  const EState* __restrict__ S, int black)
 {
     const int nthreads = blockDim.x * blockDim.y;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
@@ -1203,6 +1207,7 @@ __global__ void __launch_bounds__(256) e_prolong4(const Item* __restrict__ items
 #pragma unroll
                 for (int odd = 0; odd < 2; ++odd) {
                     const int i = 2 * ih + odd;
+                    if (black && ((i + j + k) & 1) == 0) continue;
                     const int Is[2] = {ih, wrap1(odd ? ih + 1 : ih - 1, nc)};
                     float s = 0.f;
 #pragma unroll
@@ -1269,11 +1274,16 @@ __global__ void __launch_bounds__(256) e_prolong4(const Item* __restrict__ items
             const bool even_fine_red = ((j + k) & 1) == 0;
             float4* fe = reinterpret_cast<float4*>(even_fine_red ? F.phi_r : F.phi_b) + (t >> 2);
             float4* fo = reinterpret_cast<float4*>(even_fine_red ? F.phi_b : F.phi_r) + (t >> 2);
-            float4 pe = *fe, po = *fo;
-            pe.x += s0[0]; pe.y += s0[1]; pe.z += s0[2]; pe.w += s0[3];
-            po.x += s1[0]; po.y += s1[1]; po.z += s1[2]; po.w += s1[3];
-            *fe = pe;
-            *fo = po;
+            if (!black || !even_fine_red) {
+                float4 pe = *fe;
+                pe.x += s0[0]; pe.y += s0[1]; pe.z += s0[2]; pe.w += s0[3];
+                *fe = pe;
+            }
+            if (!black || even_fine_red) {
+                float4 po = *fo;
+                po.x += s1[0]; po.y += s1[1]; po.z += s1[2]; po.w += s1[3];
+                *fo = po;
+            }
         }
     }
 }
@@ -1862,8 +1872,9 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
                 const auto& pv = E->r_smooth_vec[l];
                 const auto& pr = E->r_smooth_row[l];
                 ep_begin(c);
-                if (pv.cnt) e_prolong4<<<pgrid(E, pv.cnt), rb, 0, s>>>(it + pv.off, pv.cnt, D, S);
-                if (pr.cnt) e_prolong<<<pgrid(E, pr.cnt), rb, 0, s>>>(it + pr.off, pr.cnt, D, S);
+                const int black = c->p.nu2 > 0 ? 1 : 0;
+                if (pv.cnt) e_prolong4<<<pgrid(E, pv.cnt), rb, 0, s>>>(it + pv.off, pv.cnt, D, S, black);
+                if (pr.cnt) e_prolong<<<pgrid(E, pr.cnt), rb, 0, s>>>(it + pr.off, pr.cnt, D, S, black);
                 ep_end(c, NYXPM_ST_PROLONG);
                 c->launches += (pv.cnt ? 1 : 0) + (pr.cnt ? 1 : 0) - 1;
                 for (int sw = 0; sw < c->p.nu2; ++sw)

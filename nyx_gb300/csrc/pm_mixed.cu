@@ -845,6 +845,9 @@ __global__ void __launch_bounds__(256) k_restrict_f4(LevelViewF F, LevelViewF Cv
     }
 }
 
+// BLACK = 1 when post-smoothing follows: its first half sweep overwrites the red
+// cells unread, so only the black fine cells take the correction (same bits)
+template <int BLACK>
 __global__ void k_prolong_f(LevelViewF Cv, LevelViewF F)
 {
     const int n = F.n, nc = Cv.n, half = n >> 1;
@@ -859,6 +862,7 @@ __global__ void k_prolong_f(LevelViewF Cv, LevelViewF F)
 #pragma unroll
     for (int odd = 0; odd < 2; ++odd) {
         const int i = 2 * ih + odd;
+        if (BLACK && ((i + j + k) & 1) == 0) continue;
         const int Is[2] = {ih, wrap1(odd ? ih + 1 : ih - 1, nc)};
         float s = 0.f;
 #pragma unroll
@@ -882,6 +886,7 @@ __global__ void k_prolong_f(LevelViewF Cv, LevelViewF F)
 // three of the other, loaded as a pair plus one.  Each fine cell sums its
 // eight weighted coarse values in e_prolong's order, so the results are the
 // scalar kernel's; the corrections go to two float4 of the fine arrays.
+template <int BLACK>
 __global__ void __launch_bounds__(256) k_prolong_f4(LevelViewF Cv, LevelViewF F)
 {
     const int n = F.n, nc = Cv.n;
@@ -935,11 +940,16 @@ __global__ void __launch_bounds__(256) k_prolong_f4(LevelViewF Cv, LevelViewF F)
     const bool even_fine_red = ((j + k) & 1) == 0;   // colour of fine i = 2 ih
     float4* fe = reinterpret_cast<float4*>(even_fine_red ? F.phi_r : F.phi_b) + (t >> 2);
     float4* fo = reinterpret_cast<float4*>(even_fine_red ? F.phi_b : F.phi_r) + (t >> 2);
-    float4 pe = *fe, po = *fo;
-    pe.x += s0[0]; pe.y += s0[1]; pe.z += s0[2]; pe.w += s0[3];
-    po.x += s1[0]; po.y += s1[1]; po.z += s1[2]; po.w += s1[3];
-    *fe = pe;
-    *fo = po;
+    if (!BLACK || !even_fine_red) {
+        float4 pe = *fe;
+        pe.x += s0[0]; pe.y += s0[1]; pe.z += s0[2]; pe.w += s0[3];
+        *fe = pe;
+    }
+    if (!BLACK || even_fine_red) {
+        float4 po = *fo;
+        po.x += s1[0]; po.y += s1[1]; po.z += s1[2]; po.w += s1[3];
+        *fo = po;
+    }
 }
 
 __global__ void k_bottom_f(int nb, const float* __restrict__ G, const float* __restrict__ beta, float* phi)
@@ -1184,12 +1194,15 @@ nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li)
     if ((st = vcycle_f(c, b, li + 1)) != NYXPM_OK) return st;
     {
         prof_begin(c);
+        const bool black = c.p.nu2 > 0;
         if (cl.split && (f.n / 2) % 4 == 0) {
             const Geo g = geo3(f.n / 8, f.n, f.n);
-            k_prolong_f4<<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+            if (black) k_prolong_f4<1><<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+            else k_prolong_f4<0><<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
         } else {
             const Geo g = geo3(f.n / 2, f.n, f.n);
-            k_prolong_f<<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+            if (black) k_prolong_f<1><<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+            else k_prolong_f<0><<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
         }
         prof_end(c, NYXPM_ST_PROLONG, 8.0 * ncf + 4.0 * ncc);
     }

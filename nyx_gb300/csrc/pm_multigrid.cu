@@ -237,6 +237,10 @@ __global__ void k_restrict(LevelView F, LevelView Cv)
 // half % 4 == 0: four compact columns (eight fine cells) per thread.  The six
 // coarse x-neighbours ih0-1 .. ih0+4 of each (J', K') row are a pair plus one
 // in each colour array.  Same weighted sums in the same order.
+// BLACK = 1 when post-smoothing follows (nu2 > 0): its first half sweep
+// overwrites every red cell without reading it, so only the black fine cells take
+// the correction -- the same bits as correcting all cells, for half the FP64 work
+template <int BLACK>
 __global__ void k_prolong4(LevelView Cv, LevelView F)
 {
     const int n = F.n, nc = Cv.n;
@@ -273,25 +277,40 @@ __global__ void k_prolong4(LevelView Cv, LevelView F)
     const bool even_fine_red = ((j + k) & 1) == 0;
     double* fe = (even_fine_red ? F.phi_r : F.phi_b) + t;
     double* fo = (even_fine_red ? F.phi_b : F.phi_r) + t;
+    if (!BLACK || !even_fine_red) {
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        double se = 0.0, so = 0.0;
+        for (int r = 0; r < 4; ++r) {
+            double se = 0.0;
 #pragma unroll
-        for (int b = 0; b < 2; ++b)
+            for (int b = 0; b < 2; ++b)
 #pragma unroll
-            for (int a = 0; a < 2; ++a) {
-                se = fma(kProlongW[0 + 2 * a + 4 * b], v[b][a][r + 1], se);
-                se = fma(kProlongW[1 + 2 * a + 4 * b], v[b][a][r], se);
-                so = fma(kProlongW[0 + 2 * a + 4 * b], v[b][a][r + 1], so);
-                so = fma(kProlongW[1 + 2 * a + 4 * b], v[b][a][r + 2], so);
-            }
-        fe[r] = fe[r] + se;
-        fo[r] = fo[r] + so;
+                for (int a = 0; a < 2; ++a) {
+                    se = fma(kProlongW[0 + 2 * a + 4 * b], v[b][a][r + 1], se);
+                    se = fma(kProlongW[1 + 2 * a + 4 * b], v[b][a][r], se);
+                }
+            fe[r] = fe[r] + se;
+        }
+    }
+    if (!BLACK || even_fine_red) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            double so = 0.0;
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    so = fma(kProlongW[0 + 2 * a + 4 * b], v[b][a][r + 1], so);
+                    so = fma(kProlongW[1 + 2 * a + 4 * b], v[b][a][r + 2], so);
+                }
+            fo[r] = fo[r] + so;
+        }
     }
 }
 
 // trilinear cell-centred prolongation of the coarse correction, added to the
-// fine phi; one thread per fine pair (2ih, 2ih+1) of a split level
+// fine phi; one thread per fine pair (2ih, 2ih+1) of a split level (BLACK: the
+// black cell of the pair only, as in k_prolong4)
+template <int BLACK>
 __global__ void k_prolong(LevelView Cv, LevelView F)
 {
     const int n = F.n, nc = Cv.n, half = n >> 1;
@@ -306,6 +325,7 @@ __global__ void k_prolong(LevelView Cv, LevelView F)
 #pragma unroll
     for (int odd = 0; odd < 2; ++odd) {
         const int i = 2 * ih + odd;
+        if (BLACK && ((i + j + k) & 1) == 0) continue;
         const int I = ih;
         const int Is[2] = {I, wrap1(odd ? I + 1 : I - 1, nc)};
         double s = 0.0;
@@ -444,12 +464,15 @@ nyxpm_status vcycle(Ctx& c, Box& b, size_t li)
     if ((st = vcycle(c, b, li + 1)) != NYXPM_OK) return st;
     {
         prof_begin(c);
+        const bool black = nu2 > 0;
         if (quads && cl.split) {
             const Geo g = geo3(f.n / 8, f.n, f.n);
-            k_prolong4<<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
+            if (black) k_prolong4<1><<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
+            else k_prolong4<0><<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
         } else {
             const Geo g = geo3(f.n / 2, f.n, f.n);
-            k_prolong<<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
+            if (black) k_prolong<1><<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
+            else k_prolong<0><<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
         }
         prof_end(c, NYXPM_ST_PROLONG, 16.0 * ncf + 8.0 * ncc);
     }

@@ -107,8 +107,10 @@ __device__ __forceinline__ void tail_restrict(const LevelViewF& F, const LevelVi
     }
 }
 
-// fine phi += trilinear interpolation of the coarse phi
-__device__ __forceinline__ void tail_prolong(const LevelViewF& Cv, const LevelViewF& F)
+// fine phi += trilinear interpolation of the coarse phi (black: the black fine
+// cells only -- the post-smoothing's first half sweep overwrites the red ones
+// unread)
+__device__ __forceinline__ void tail_prolong(const LevelViewF& Cv, const LevelViewF& F, bool black)
 {
     const int n = F.n, nc = Cv.n, half = n >> 1;
     const int total = half * n * n;
@@ -121,6 +123,7 @@ __device__ __forceinline__ void tail_prolong(const LevelViewF& Cv, const LevelVi
 #pragma unroll
         for (int odd = 0; odd < 2; ++odd) {
             const int i = 2 * ih + odd;
+            if (black && ((i + j + k) & 1) == 0) continue;
             const int Is[2] = {ih, tail_wrap(odd ? ih + 1 : ih - 1, nc)};
             float s = 0.f;
 #pragma unroll
@@ -182,7 +185,7 @@ __device__ __forceinline__ void vcycle_tail(const LevelViewF* lv, int nl, int nu
     tail_bottom(lv[nl - 1], Gf, nb, r, g);
     __syncthreads();
     for (int l = nl - 2; l >= 0; --l) {
-        tail_prolong(lv[l + 1], lv[l]);
+        tail_prolong(lv[l + 1], lv[l], nu2 > 0);
         __syncthreads();
         for (int sw = 0; sw < nu2; ++sw) {
             tail_gsrb(lv[l], 0);

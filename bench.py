@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--tuning", type=str, default="",
                     help="deposit_tile,smooth_rows,inner_vcycles for the ensemble instead of "
                          "the autotuner's choice")
+    ap.add_argument("--fused-edge", type=int, default=None,
+                    help="nyxpm_params.mg_fused_edge: FP32 V-cycle levels of at most this many "
+                         "cells per edge run as one CTA per box (default: the library's)")
     ap.add_argument("--quick", action="store_true",
                     help="headline timing only (no reuse-field pass, e2e or CPU baseline); "
                          "the command the ncu captures run")
@@ -487,7 +490,7 @@ def run_ours(args):
     ic = zeldovich_ics(n, 1.0, -2.0, replica_seed(rank), A_START, rms_disp_cells=0.2,
                        fraction=args.fraction)
     npart = len(ic.pos)
-    ctx = Context(device=local)
+    ctx = Context(device=local, mg_fused_edge=args.fused_edge)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     sched = schedule(ctx, W + K)
     box = Box(ctx, n, 1.0, npart, precision=args.precision)
@@ -745,7 +748,7 @@ def run_accuracy(args):
     ic = zeldovich_ics(n, L, -2.5, 3, A_START, rms_disp_cells=0.2)
     t_ic = time.perf_counter() - t0
     npart = len(ic.pos)
-    ctx = Context(device=0)
+    ctx = Context(device=0, mg_fused_edge=args.fused_edge)
     sched = ctx.step_schedule(A_START, A_END, NSTEPS_CFG)[:nsteps]
 
     def rel(a, b):
@@ -813,7 +816,7 @@ def run_ensemble_only(args):
     from nyx_gb300 import _lib
     _lib.load()
     from nyx_gb300.pm import Context
-    ctx = Context(device=0)
+    ctx = Context(device=0, mg_fused_edge=args.fused_edge)
     fixed = [int(v) for v in args.tuning.split(",")] if args.tuning else None
     out = run_ensemble_form(ctx, args.ensemble_boxes, args.ensemble_steps, fixed)
     ctx.close()

@@ -297,7 +297,7 @@ size_t nyxpm_box_bytes(int n, int64_t np, nyxpm_precision prec)
         per_cell = 4 + 4 + 4 + 4 + 8 + 24 + 8 + 16 + 4 + 16.0 * 8 / 7 + 8.0 * 8 / 7;
     } else {
         per_particle = 2.0 * (7 * 8 + 4) + 8 + 56 + 2;
-        per_cell = 4 + 4 + 4 + 8 + 24 + 8 + 64 + 16.0 * 8 / 7;
+        per_cell = 4 + 4 + 4 + 8 + 24 + 8 + 64 + 4 + 16.0 * 8 / 7;
     }
     return (size_t)(per_particle * (double)np + per_cell * nc + 8.0 * n * n + (1 << 20));
 }
@@ -395,6 +395,10 @@ nyxpm_status nyxpm_box_create(nyxpm_ctx* c, int n, double L, int64_t np, nyxpm_p
         if (nl == nbot) break;
     }
     b->nb = nbot;
+    if (prec == NYXPM_FP64 && b->levels[0].split) {
+        b->phi_r_alloc = b->levels[0].phi_r;
+        ALLOC(b->phi_r_spare, nc / 2);
+    }
     ALLOC(b->G, (size_t)nbot * nbot * nbot);
     ALLOC(b->Gf, (size_t)nbot * nbot * nbot);
 #undef ALLOC
@@ -432,7 +436,8 @@ nyxpm_status nyxpm_box_destroy(nyxpm_ctx* c, nyxpm_box* b)
     CHECK_BOX(c, b);
     cudaSetDevice(c->p.device);
     cudaStreamSynchronize(c->stream);
-    if (b->iter_graph.exec) cudaGraphExecDestroy(b->iter_graph.exec);
+    for (IterGraph& g : b->iter_graph)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     for (void* q : b->allocs) cudaFree(q);
     if (b->h_norms) cudaFreeHost(b->h_norms);
     delete b;

@@ -304,7 +304,10 @@ struct Box {
     double mscalar32_scale = 0;        // mixed: m / dx^3 applied to the FP32 deposit
     int nb = 0;
     std::vector<Level> levels;
-    IterGraph iter_graph;              // one solver iteration (V-cycle or defect correction)
+    IterGraph iter_graph[4];           // solver iterations: [0] mixed / plain FP64; FP64 with
+                                       // the fused norm: [opening 0 | later 2] + red array
+    double* phi_r_alloc = nullptr;     // FP64: level 0's own red array
+    double* phi_r_spare = nullptr;     // FP64: the other red array of level 0
 
     // host<->device staging: AoS pos (3 np), vel (3 np), mass (np) doubles
     double* staging = nullptr;

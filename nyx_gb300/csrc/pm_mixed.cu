@@ -1502,7 +1502,7 @@ nyxpm_status mixed_solve(Ctx& c, Box& b, int zero_guess, nyxpm_solve_info* info)
             return check_launch(c, "norm copy");
         };
         for (it = 1; it <= c.p.max_vcycles; ++it) {
-            if ((st = run_iteration(c, b.iter_graph, iteration)) != NYXPM_OK) return st;
+            if ((st = run_iteration(c, b.iter_graph[0], iteration)) != NYXPM_OK) return st;
             inner += c.p.mixed_inner_vcycles;
             if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "mixed sync");
             r = read_norm(b, 1);

@@ -169,6 +169,41 @@ __global__ void k_resnorm_red(int n, const double* __restrict__ phi_r, const dou
     block_umax_store(v, out);
 }
 
+// k_resnorm_red fused with the red half sweep that opens the next V-cycle: both
+// need the same neighbour sum s of each red cell, so one pass gives the norm of
+// beta - (s/6 - phi_red) and the next red value fma(s, 1/6, -beta), written to a
+// spare red array (adopted only if the solve goes on) -- the same bits as the
+// norm pass followed by the sweep
+__global__ void k_resnorm_red_sweep(int n, const double* __restrict__ phi_r,
+                                    const double* __restrict__ phi_b,
+                                    const double* __restrict__ beta_r, double* __restrict__ next_r,
+                                    unsigned long long* out)
+{
+    const int half = n >> 1;
+    const int ih = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    unsigned long long v = 0;
+    if (ih < half && j < n) {
+        const int q = (j + k) & 1;
+        const int ihm = q ? ih : (ih == 0 ? half - 1 : ih - 1);
+        const int ihp = q ? (ih == half - 1 ? 0 : ih + 1) : ih;
+        const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        const long long row = (long long)j + (long long)n * k;
+        const long long t = row * half + ih;
+        double s = phi_b[row * half + ihm] + phi_b[row * half + ihp];
+        s = s + phi_b[((long long)jm + (long long)n * k) * half + ih];
+        s = s + phi_b[((long long)jp + (long long)n * k) * half + ih];
+        s = s + phi_b[((long long)j + (long long)n * km) * half + ih];
+        s = s + phi_b[((long long)j + (long long)n * kp) * half + ih];
+        const double b = beta_r[t];
+        v = absbits(b - fma(s, kSixth, -phi_r[t]));
+        next_r[t] = fma(s, kSixth, -b);
+    }
+    block_umax_store(v, out);
+}
+
 __global__ void k_resnorm_nat(LevelView L, unsigned long long* out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -419,11 +454,11 @@ inline unsigned norm_blocks(Ctx& c, long long cnt)
     return (unsigned)std::max<long long>(1, std::min(b, cap));
 }
 
-nyxpm_status gsrb_sweep(Ctx& c, const Level& l, int fine)
+nyxpm_status gsrb_sweep(Ctx& c, const Level& l, int fine, int black_only = 0)
 {
     const long long half_cells = (long long)l.n * l.n * l.n / 2;
     const Geo g = geo3(l.n / 2, l.n, l.n);
-    for (int color = 0; color < 2; ++color) {
+    for (int color = black_only ? 1 : 0; color < 2; ++color) {
         double* mine = color ? l.phi_b : l.phi_r;
         const double* other = color ? l.phi_r : l.phi_b;
         const double* beta = color ? l.beta_b : l.beta_r;
@@ -434,7 +469,9 @@ nyxpm_status gsrb_sweep(Ctx& c, const Level& l, int fine)
     return check_launch(c, "gsrb");
 }
 
-nyxpm_status vcycle(Ctx& c, Box& b, size_t li)
+// red_done: the opening red half sweep of this level was already made (by
+// k_resnorm_red_sweep)
+nyxpm_status vcycle(Ctx& c, Box& b, size_t li, int red_done = 0)
 {
     nyxpm_status st;
     const Level& f = b.levels[li];
@@ -446,7 +483,7 @@ nyxpm_status vcycle(Ctx& c, Box& b, size_t li)
     }
     const int nu1 = c.p.nu1, nu2 = c.p.nu2;
     for (int s = 0; s < nu1; ++s)
-        if ((st = gsrb_sweep(c, f, li == 0)) != NYXPM_OK) return st;
+        if ((st = gsrb_sweep(c, f, li == 0, s == 0 && red_done)) != NYXPM_OK) return st;
     const Level& cl = b.levels[li + 1];
     const long long ncc = (long long)cl.n * cl.n * cl.n;
     const long long ncf = (long long)f.n * f.n * f.n;
@@ -580,17 +617,36 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
     int it = 0;
     nyxpm_status result = NYXPM_OK;
     const int red_only = (c.p.nu2 > 0 && b.levels.size() > 1) ? 1 : 0;
+    // The red-cell norm after a V-cycle and the red half sweep that opens the next
+    // one share their neighbour sums: k_resnorm_red_sweep makes both, the sweep into
+    // the spare red array, which becomes level 0's red array only if the solve
+    // goes on (the next V-cycle then starts at its black half sweep).
+    Level& L0 = b.levels[0];
+    const bool fuse = red_only && c.p.nu1 > 0 && L0.split && b.phi_r_spare;
     if (!(r0 <= target)) {
+        bool first = true;
         auto iteration = [&]() -> nyxpm_status {
             nyxpm_status s;
-            if ((s = vcycle(c, b, 0)) != NYXPM_OK) return s;
-            if ((s = launch_resnorm(c, b, 1, red_only)) != NYXPM_OK) return s;
+            if ((s = vcycle(c, b, 0, fuse && !first ? 1 : 0)) != NYXPM_OK) return s;
+            if (fuse) {
+                const Geo g = geo3(L0.n / 2, L0.n, L0.n);
+                prof_begin(c);
+                cudaMemsetAsync(b.norms + 1, 0, sizeof(unsigned long long), c.stream);
+                k_resnorm_red_sweep<<<g.grid, g.block, 0, c.stream>>>(L0.n, L0.phi_r, L0.phi_b, L0.beta_r,
+                                                                      b.phi_r_spare, b.norms + 1);
+                prof_end(c, NYXPM_ST_NORM, 16.0 * nc);
+                if ((s = check_launch(c, "red norm + sweep")) != NYXPM_OK) return s;
+            } else if ((s = launch_resnorm(c, b, 1, red_only)) != NYXPM_OK) {
+                return s;
+            }
             cudaMemcpyAsync(b.h_norms + 1, b.norms + 1, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, c.stream);
             return check_launch(c, "norm copy");
         };
         for (it = 1; it <= c.p.max_vcycles; ++it) {
-            if ((st = run_iteration(c, b.iter_graph, iteration)) != NYXPM_OK) return st;
+            // one graph per (opening or later iteration, physical red array)
+            const int gi = (first ? 0 : 2) + (L0.phi_r == b.phi_r_alloc ? 0 : 1);
+            if ((st = run_iteration(c, b.iter_graph[gi], iteration)) != NYXPM_OK) return st;
             if (cudaStreamSynchronize(c.stream) != cudaSuccess) return check_launch(c, "solve sync");
             r = read_norm(b, 1);
             if (r != r) {
@@ -598,6 +654,10 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
                 return NYXPM_NOT_CONVERGED;
             }
             if (r <= target) break;
+            if (fuse && it < c.p.max_vcycles) {
+                std::swap(L0.phi_r, b.phi_r_spare);
+                first = false;
+            }
         }
         if (it > c.p.max_vcycles) {
             it = c.p.max_vcycles;

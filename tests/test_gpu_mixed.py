@@ -131,3 +131,24 @@ def test_mixed_drift_rebinning_at_cell_origin(ctx):
     gpos, _ = b.download()
     err = np.abs(min_image(gpos - pos, L)).max() / (L / n)
     assert err < 1e-6, err
+
+
+@pytest.mark.parametrize("n", [64, 48])
+def test_mixed_zero_guess_solve_meets_the_fp64_tolerance(ctx, n):
+    """A zero-guess solve (its first correction is as large as phi, so the error
+    bound forces one FP64 recomputation of the residual): the residual of the
+    returned phi, recomputed by the oracle in FP64, meets the tolerance."""
+    L = 1.0
+    ic = config1_ics(n, seed=4)
+    b = Box(ctx, n, L, len(ic.pos), precision="mixed")
+    b.upload(ic.pos, ic.vel, ic.mass)
+    b.deposit(read_back=False)
+    info = b.solve_phi(0.05, zero_guess=True)
+    r_true, bnorm = true_resnorm(b, n, L, 0.05)
+    assert info["resnorm"] <= 1e-10 * max(info["bnorm"], info["resnorm0"]) * (1 + 1e-9)
+    assert r_true <= 1.05e-10 * max(bnorm, info["resnorm0"]), (r_true, bnorm, info)
+    # a second solve from that phi (no zero guess) stays within the tolerance too
+    info2 = b.solve_phi(0.05)
+    r2, _ = true_resnorm(b, n, L, 0.05)
+    assert r2 <= 1.05e-10 * max(bnorm, info2["resnorm0"]), (r2, info2)
+    b.close()

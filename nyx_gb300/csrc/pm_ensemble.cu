@@ -155,13 +155,14 @@ __global__ void e_load_step(int nbox, const EStep* __restrict__ st, const EDesc*
 // particle stages: item = (box, chunk of kPT particles)
 // ---------------------------------------------------------------------------
 // phase 0: kick-drift (a_old -> a_half, move); phase 1: kick (a_half -> a_new)
-__global__ void __launch_bounds__(kPT) e_kick(const Item* __restrict__ items, int nitems,
+__global__ void __launch_bounds__(kPT, 4) e_kick(const Item* __restrict__ items, int nitems,
                                                const EDesc* __restrict__ D, const EState* __restrict__ S,
                                                int phase)
 {
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
-        const EState st = S[it.box];
+        // by reference: a copy indexed by the runtime phase would live in local memory
+        const EState& st = S[it.box];
         if (!st.active) continue;
         const EDesc& d = D[it.box];
         const long long q = (long long)it.a * kPT + threadIdx.x;

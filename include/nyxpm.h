@@ -177,6 +177,19 @@ nyxpm_status nyxpm_kick(nyxpm_ctx* ctx, nyxpm_box* box, double dt, double a_new,
 nyxpm_status nyxpm_step(nyxpm_ctx* ctx, nyxpm_box* box, double a_old, double a_new, double dt,
                         unsigned flags, nyxpm_step_info* info);
 
+/* nyxpm_box_upload + nyxpm_step + nyxpm_box_download in one call, for callers
+ * whose particles live in host memory; pos and vel (np x 3, particle order) are
+ * read and overwritten with the stepped state.  The results are those of the
+ * three calls, bit for bit.  On FP64 boxes the transfers run on a second stream
+ * under the step: the velocities arrive during the sort, deposit and old-time
+ * solve, which read positions only, and the positions leave (wrapped, as the
+ * closing kick wraps them) during the new-time deposit and solve.  Pinned host
+ * buffers let the copies overlap.  No counterpart in the reference: Nyx keeps
+ * the particles in its own containers. */
+nyxpm_status nyxpm_step_host(nyxpm_ctx* ctx, nyxpm_box* box, double* pos, double* vel,
+                             const double* mass, double mass_scalar, double a_old, double a_new,
+                             double dt, unsigned flags, nyxpm_step_info* info);
+
 /* The post_init solve (Nyx::post_init, Source/Driver/Nyx.cpp:1957-2005):
  * redistribute, deposit, solve from phi = 0 at scale factor a. */
 nyxpm_status nyxpm_init_field(nyxpm_ctx* ctx, nyxpm_box* box, double a, nyxpm_solve_info* info);

@@ -28,7 +28,7 @@ EXPORTS = [
     "nyxpm_box_destroy", "nyxpm_box_bytes", "nyxpm_box_upload", "nyxpm_box_download",
     "nyxpm_set_mass_offset", "nyxpm_redistribute", "nyxpm_deposit", "nyxpm_solve_phi",
     "nyxpm_get_phi", "nyxpm_set_phi", "nyxpm_grav_vector", "nyxpm_kick_drift", "nyxpm_kick",
-    "nyxpm_step", "nyxpm_init_field", "nyxpm_integrate_a", "nyxpm_dt_for_da",
+    "nyxpm_step", "nyxpm_step_host", "nyxpm_init_field", "nyxpm_integrate_a", "nyxpm_dt_for_da",
     "nyxpm_set_profiling", "nyxpm_get_profile", "nyxpm_launch_count",
     "nyxpm_ensemble_create", "nyxpm_ensemble_destroy", "nyxpm_ensemble_box_bytes",
     "nyxpm_ensemble_arena_used", "nyxpm_ensemble_add", "nyxpm_ensemble_remove",
@@ -162,6 +162,7 @@ def load(path: str | None = None):
     L.nyxpm_kick_drift.argtypes = [vp, vp, d, d, d]
     L.nyxpm_kick.argtypes = [vp, vp, d, d, d]
     L.nyxpm_step.argtypes = [vp, vp, d, d, d, C.c_uint, C.POINTER(StepInfo)]
+    L.nyxpm_step_host.argtypes = [vp, vp, vp, vp, vp, d, d, d, d, C.c_uint, C.POINTER(StepInfo)]
     L.nyxpm_init_field.argtypes = [vp, vp, d, C.POINTER(SolveInfo)]
     L.nyxpm_integrate_a.argtypes = [C.POINTER(Params), d, d]
     L.nyxpm_integrate_a.restype = d

@@ -269,6 +269,12 @@ void nyxpm_destroy(nyxpm_ctx* c)
     cudaStreamSynchronize(c->stream);
     for (auto e : c->ev_a) cudaEventDestroy(e);
     for (auto e : c->ev_b) cudaEventDestroy(e);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaEventDestroy(c->ev_copy_in);
+        cudaEventDestroy(c->ev_copy_out);
+        cudaStreamDestroy(c->copy_stream);
+    }
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -652,6 +658,100 @@ nyxpm_status nyxpm_step(nyxpm_ctx* c, nyxpm_box* b, double a_old, double a_new, 
     st_new = do_solve(*c, *b, a_new, 0, &local.new_solve);
     if (st_new != NYXPM_OK && st_new != NYXPM_NOT_CONVERGED) return st_new;
     TRY(do_kick(*c, *b, dt, a_half, a_new, 0, 1));
+    if (info) *info = local;
+    return st_old != NYXPM_OK ? st_old : st_new;
+}
+
+nyxpm_status nyxpm_step_host(nyxpm_ctx* c, nyxpm_box* b, double* pos, double* vel,
+                             const double* mass, double mass_scalar, double a_old, double a_new,
+                             double dt, unsigned flags, nyxpm_step_info* info)
+{
+    CHECK_BOX(c, b);
+    if (!pos || !vel) return fail(c, NYXPM_INVALID_ARG, "null pos/vel");
+    if (!(a_old > 0) || !(a_new > 0) || !std::isfinite(dt)) return fail(c, NYXPM_INVALID_ARG, "bad a / dt");
+    const bool reuse = (flags & NYXPM_STEP_REUSE_FIELD) != 0;
+    if (b->prec != NYXPM_FP64) {
+        // the mixed form: the three calls one after another
+        TRY(nyxpm_box_upload(c, b, pos, vel, mass, mass_scalar));
+        const nyxpm_status st = nyxpm_step(c, b, a_old, a_new, dt, flags, info);
+        if (st != NYXPM_OK && st != NYXPM_NOT_CONVERGED) return st;
+        TRY(nyxpm_box_download(c, b, pos, vel));
+        return st;
+    }
+    if (reuse && !b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field to reuse: call nyxpm_init_field");
+    const int64_t np = b->np;
+    double total = 0.0;
+    if (mass) {
+        for (int64_t q = 0; q < np; ++q) {
+            if (!(mass[q] >= 0) || !std::isfinite(mass[q])) return fail(c, NYXPM_INVALID_ARG, "bad mass");
+            total = total + mass[q];
+        }
+    } else {
+        if (!(mass_scalar >= 0) || !std::isfinite(mass_scalar)) return fail(c, NYXPM_INVALID_ARG, "bad mass");
+        total = mass_scalar * (double)np;
+    }
+    if (!c->copy_stream) {
+        if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->ev_copy_in, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->ev_copy_out, cudaEventDisableTiming) != cudaSuccess)
+            return check_launch(*c, "copy stream");
+    }
+    b->uniform_mass = mass ? 0 : 1;
+    b->mscalar = mass ? 0.0 : mass_scalar;
+    b->mass_offset = total / (b->L * b->L * b->L);
+    double* s_pos = b->staging;
+    double* s_vel = b->staging + 3 * np;
+    double* s_mass = b->staging + 6 * np;
+    // positions (and masses) first, on the step's stream ...
+    cudaMemsetAsync(b->norms + 2, 0, sizeof(unsigned long long), c->stream);
+    cudaMemcpyAsync(s_pos, pos, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream);
+    if (mass) cudaMemcpyAsync(s_mass, mass, sizeof(double) * np, cudaMemcpyHostToDevice, c->stream);
+    TRY(launch_unpack_pos(*c, *b, s_pos, mass ? s_mass : nullptr));
+    // ... the velocities on the copy stream, under the sort, deposit and old-time solve
+    cudaMemcpyAsync(s_vel, vel, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->copy_stream);
+    cudaEventRecord(c->ev_copy_in, c->copy_stream);
+    TRY(check_launch(*c, "host step input copies"));
+    b->uploaded = 1;
+    b->sorted = 0;
+    const double a_half = 0.5 * (a_old + a_new);
+    nyxpm_step_info local;
+    std::memset(&local, 0, sizeof(local));
+    nyxpm_status st_old = NYXPM_OK, st_new;
+    bool sorted_since = false;
+    if (!reuse) {
+        // nyxpm_step's old-time part, the sort leaving the velocities for later
+        TRY(launch_sort(*c, *b, true));
+        sorted_since = true;
+        TRY(launch_deposit(*c, *b));
+        st_old = do_solve(*c, *b, a_old, 1, &local.old_solve);
+        if (st_old != NYXPM_OK && st_old != NYXPM_NOT_CONVERGED) return st_old;
+    }
+    cudaStreamWaitEvent(c->stream, c->ev_copy_in, 0);
+    TRY(launch_unpack_gather_vel(*c, *b, s_vel, sorted_since));
+    TRY(do_kick(*c, *b, dt, a_old, a_half, 1, 0));
+    // the positions are final now (the closing kick only wraps them): out on the
+    // copy stream, wrapped, under the new-time deposit and solve
+    TRY(launch_pack_pos_wrapped(*c, *b, s_pos));
+    cudaEventRecord(c->ev_copy_out, c->stream);
+    cudaStreamWaitEvent(c->copy_stream, c->ev_copy_out, 0);
+    cudaMemcpyAsync(pos, s_pos, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, c->copy_stream);
+    TRY(do_deposit(*c, *b));
+    st_new = do_solve(*c, *b, a_new, 0, &local.new_solve);
+    if (st_new != NYXPM_OK && st_new != NYXPM_NOT_CONVERGED) return st_new;
+    TRY(do_kick(*c, *b, dt, a_half, a_new, 0, 1));
+    TRY(launch_pack_vel(*c, *b, s_vel));
+    cudaMemcpyAsync(vel, s_vel, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(b->h_norms + 2, b->norms + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                    c->stream);
+    TRY(check_launch(*c, "host step output copies"));
+    const cudaError_t e1 = cudaStreamSynchronize(c->copy_stream);
+    const cudaError_t e2 = cudaStreamSynchronize(c->stream);
+    if (e1 != cudaSuccess || e2 != cudaSuccess)
+        return fail(c, NYXPM_CUDA_ERROR, cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+    if (b->h_norms[2] != 0) {
+        b->uploaded = 0;
+        return fail(c, NYXPM_INVALID_ARG, "non-finite particle position or velocity");
+    }
     if (info) *info = local;
     return st_old != NYXPM_OK ? st_old : st_new;
 }

@@ -327,6 +327,9 @@ struct Ctx {
     std::vector<ProfRec> recs;
     nyxpm_profile acc{};
     int sm_count = 0;
+    // second stream and events of the host-buffer step (created on first use)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy_in = nullptr, ev_copy_out = nullptr;
 };
 
 // launch bookkeeping: call prof_begin before and prof_end after each launch
@@ -344,7 +347,12 @@ nyxpm_status launch_unpack(Ctx& c, Box& b, const double* d_pos, const double* d_
                            const double* d_mass);
 nyxpm_status launch_pack(Ctx& c, Box& b, double* d_pos, double* d_vel);
 nyxpm_status launch_wrap(Ctx& c, Box& b);
-nyxpm_status launch_sort(Ctx& c, Box& b);
+nyxpm_status launch_sort(Ctx& c, Box& b, bool defer_vel = false);
+// the host-buffer step's split transfers (FP64 boxes)
+nyxpm_status launch_unpack_pos(Ctx& c, Box& b, const double* d_pos, const double* d_mass);
+nyxpm_status launch_unpack_gather_vel(Ctx& c, Box& b, const double* d_vel, bool sorted_since);
+nyxpm_status launch_pack_pos_wrapped(Ctx& c, Box& b, double* d_pos);
+nyxpm_status launch_pack_vel(Ctx& c, Box& b, double* d_vel);
 nyxpm_status launch_deposit(Ctx& c, Box& b);
 nyxpm_status launch_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move,
                          int do_wrap);

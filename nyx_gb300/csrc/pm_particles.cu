@@ -82,6 +82,73 @@ __device__ __forceinline__ double wrap_pos(double v, double L)
     return v;
 }
 
+// The host-buffer step's split upload and download (nyxpm_step_host): positions
+// (and masses) first, velocities later; positions out as soon as the drift made
+// them final, already wrapped as the step's closing kick wraps them.
+__global__ void k_unpack_pos(long long np, const double* __restrict__ pos,
+                             const double* __restrict__ mass, double* x, double* y, double* z,
+                             double* m, int* id, unsigned long long* bad)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const double px = pos[3 * q], py = pos[3 * q + 1], pz = pos[3 * q + 2];
+    if (!(isfinite(px) && isfinite(py) && isfinite(pz))) atomicAdd(bad, 1ULL);
+    x[q] = px;
+    y[q] = py;
+    z[q] = pz;
+    if (m) m[q] = mass[q];
+    id[q] = (int)q;
+}
+
+__global__ void k_unpack_vel(long long np, const double* __restrict__ vel, double* vx, double* vy,
+                             double* vz, unsigned long long* bad)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const double ux = vel[3 * q], uy = vel[3 * q + 1], uz = vel[3 * q + 2];
+    if (!(isfinite(ux) && isfinite(uy) && isfinite(uz))) atomicAdd(bad, 1ULL);
+    vx[q] = ux;
+    vy[q] = uy;
+    vz[q] = uz;
+}
+
+__global__ void k_pack_pos_wrapped(long long np, double L, const double* __restrict__ x,
+                                   const double* __restrict__ y, const double* __restrict__ z,
+                                   const int* __restrict__ id, double* pos)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const long long o = 3LL * id[q];
+    pos[o] = wrap_pos(x[q], L);
+    pos[o + 1] = wrap_pos(y[q], L);
+    pos[o + 2] = wrap_pos(z[q], L);
+}
+
+__global__ void k_pack_vel(long long np, const double* __restrict__ vx, const double* __restrict__ vy,
+                           const double* __restrict__ vz, const int* __restrict__ id, double* vel)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const long long o = 3LL * id[q];
+    vel[o] = vx[q];
+    vel[o + 1] = vy[q];
+    vel[o + 2] = vz[q];
+}
+
+// velocities permuted by the sort's perm (the position part of the sort ran
+// without them)
+__global__ void k_gather_vel(long long np, const int* __restrict__ perm,
+                             const double* __restrict__ vx, const double* __restrict__ vy,
+                             const double* __restrict__ vz, double* vx2, double* vy2, double* vz2)
+{
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= np) return;
+    const int q = perm[s];
+    vx2[s] = vx[q];
+    vy2[s] = vy[q];
+    vz2[s] = vz[q];
+}
+
 __global__ void k_wrap(long long np, double L, double* x, double* y, double* z)
 {
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -197,9 +264,11 @@ __global__ void k_gather(long long np, const int* __restrict__ perm, const doubl
     x2[s] = x[q];
     y2[s] = y[q];
     z2[s] = z[q];
-    vx2[s] = vx[q];
-    vy2[s] = vy[q];
-    vz2[s] = vz[q];
+    if (vx) {   // null: velocities follow later (k_gather_vel)
+        vx2[s] = vx[q];
+        vy2[s] = vy[q];
+        vz2[s] = vz[q];
+    }
     if (m) m2[s] = m[q];
     id2[s] = id[q];
 }
@@ -690,7 +759,7 @@ nyxpm_status sort_from_keys(Ctx& c, Box& b)
     return fix_segments(c, b);
 }
 
-nyxpm_status launch_sort(Ctx& c, Box& b)
+nyxpm_status launch_sort(Ctx& c, Box& b, bool defer_vel)
 {
     nyxpm_status st;
     // the scatter leaves the counts at zero, but an interrupted sort may not have
@@ -701,23 +770,73 @@ nyxpm_status launch_sort(Ctx& c, Box& b)
     prof_end(c, NYXPM_ST_KEYS, 32.0 * b.np);
     if ((st = check_launch(c, "keys")) != NYXPM_OK) return st;
     if ((st = sort_from_keys(c, b)) != NYXPM_OK) return st;
-    const int nvals = b.uniform_mass ? 6 : 7;
+    const int nvals = (b.uniform_mass ? 6 : 7) - (defer_vel ? 3 : 0);
     prof_begin(c);
+    // defer_vel: the velocities are not on the device yet; launch_gather_vel
+    // permutes them by the same perm once they are
     k_gather<<<blocks_for(b.np), kThreads, 0, c.stream>>>(
-        b.np, b.perm, b.x, b.y, b.z, b.vx, b.vy, b.vz, b.uniform_mass ? nullptr : b.m, b.id, b.x2,
-        b.y2, b.z2, b.vx2, b.vy2, b.vz2, b.uniform_mass ? nullptr : b.m2, b.id2);
+        b.np, b.perm, b.x, b.y, b.z, defer_vel ? nullptr : b.vx, b.vy, b.vz,
+        b.uniform_mass ? nullptr : b.m, b.id, b.x2, b.y2, b.z2, b.vx2, b.vy2, b.vz2,
+        b.uniform_mass ? nullptr : b.m2, b.id2);
     prof_end(c, NYXPM_ST_GATHER, (16.0 * nvals + 12.0) * b.np);
     if ((st = check_launch(c, "gather")) != NYXPM_OK) return st;
     std::swap(b.x, b.x2);
     std::swap(b.y, b.y2);
     std::swap(b.z, b.z2);
-    std::swap(b.vx, b.vx2);
-    std::swap(b.vy, b.vy2);
-    std::swap(b.vz, b.vz2);
+    if (!defer_vel) {
+        std::swap(b.vx, b.vx2);
+        std::swap(b.vy, b.vy2);
+        std::swap(b.vz, b.vz2);
+    }
     std::swap(b.m, b.m2);
     std::swap(b.id, b.id2);
     b.sorted = 1;
     return NYXPM_OK;
+}
+
+nyxpm_status launch_unpack_pos(Ctx& c, Box& b, const double* d_pos, const double* d_mass)
+{
+    prof_begin(c);
+    k_unpack_pos<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, d_pos, d_mass, b.x, b.y, b.z,
+                                                               d_mass ? b.m : nullptr, b.id, b.norms + 2);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "unpack positions");
+}
+
+// the velocities, in the order the particles had before the last (deferred) sort,
+// into the scratch arrays, then permuted into place by that sort's perm
+nyxpm_status launch_unpack_gather_vel(Ctx& c, Box& b, const double* d_vel, bool sorted_since)
+{
+    prof_begin(c);
+    if (sorted_since) {
+        k_unpack_vel<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, d_vel, b.vx2, b.vy2, b.vz2,
+                                                                   b.norms + 2);
+        k_gather_vel<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.perm, b.vx2, b.vy2, b.vz2,
+                                                                   b.vx, b.vy, b.vz);
+        c.launches += 1;
+    } else {
+        k_unpack_vel<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, d_vel, b.vx, b.vy, b.vz,
+                                                                   b.norms + 2);
+    }
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "unpack velocities");
+}
+
+nyxpm_status launch_pack_pos_wrapped(Ctx& c, Box& b, double* d_pos)
+{
+    prof_begin(c);
+    k_pack_pos_wrapped<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.L, b.x, b.y, b.z, b.id,
+                                                                     d_pos);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "pack positions");
+}
+
+nyxpm_status launch_pack_vel(Ctx& c, Box& b, double* d_vel)
+{
+    prof_begin(c);
+    k_pack_vel<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.vx, b.vy, b.vz, b.id, d_vel);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "pack velocities");
 }
 
 nyxpm_status launch_deposit(Ctx& c, Box& b)

@@ -289,6 +289,30 @@ class Box:
                 C.byref(info), what="step")
         return {"old_solve": info.old_solve.as_dict(), "new_solve": info.new_solve.as_dict()}
 
+    def step_host(self, pos, vel, mass, a_old, a_new, dt, reuse_field: bool = False) -> dict:
+        """upload + step + download in one call (nyxpm_step_host): pos and vel
+        (np x 3 float64, C order) are overwritten in place with the stepped state."""
+        for arr in (pos, vel):
+            if not (isinstance(arr, np.ndarray) and arr.dtype == np.float64 and arr.shape == (self.np, 3)
+                    and arr.flags.c_contiguous and arr.flags.writeable):
+                raise ValueError("pos and vel must be writeable C-contiguous float64 arrays of shape (np, 3)")
+        return self.step_host_ptr(pos.ctypes.data, vel.ctypes.data, mass, a_old, a_new, dt, reuse_field)
+
+    def step_host_ptr(self, pos_ptr: int, vel_ptr: int, mass, a_old, a_new, dt,
+                      reuse_field: bool = False) -> dict:
+        """step_host on raw host pointers (pinned buffers let the copies overlap the step)."""
+        info = _L.StepInfo()
+        flags = _L.NYXPM_STEP_REUSE_FIELD if reuse_field else 0
+        if np.ndim(mass) == 0:
+            mptr, ms = None, float(mass)
+        else:
+            m = _f64(mass, (self.np,))
+            mptr, ms = _ptr(m), 0.0
+        self._c(self.ctx.lib.nyxpm_step_host, C.c_void_p(pos_ptr), C.c_void_p(vel_ptr), mptr, ms,
+                float(a_old), float(a_new), float(dt), flags, C.byref(info), what="step_host")
+        self.mass = float(mass) if np.ndim(mass) == 0 else np.asarray(mass, dtype=np.float64).copy()
+        return {"old_solve": info.old_solve.as_dict(), "new_solve": info.new_solve.as_dict()}
+
     def close(self):
         if getattr(self, "handle", None) and self.ctx.handle:
             self.ctx.lib.nyxpm_box_destroy(self.ctx.handle, self.handle)

@@ -841,16 +841,18 @@ __global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items,
     }
 }
 
-// e = 0 on level 0 for the next inner solve (after e_correct), boxes still iterating
+// e = 0 on level 0 for the next inner solve (after e_correct), boxes still
+// iterating whose level 0 is cycled by e_tail
 __global__ void __launch_bounds__(256) e_zero_inner(const Item* __restrict__ items, int nitems,
                                                     const EDesc* __restrict__ D,
-                                                    const EState* __restrict__ S)
+                                                    const EState* __restrict__ S, int all)
 {
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
         const EState st = S[it.box];
         if (!(st.active && st.solve_active)) continue;
         const EDesc& d = D[it.box];
+        if (!all && d.tail_l != 0) continue;   // the others start with e_gsrb_zero
         const int n = d.n, half = n >> 1, k = it.b;
         const int j = it.c + threadIdx.y;
         if (j >= n) continue;
@@ -859,6 +861,29 @@ __global__ void __launch_bounds__(256) e_zero_inner(const Item* __restrict__ ite
             d.lv[0].phi_r[t] = 0.f;
             d.lv[0].phi_b[t] = 0.f;
         }
+    }
+}
+
+// The opening red half sweep of an inner solve on level 0, whose correction
+// starts at 0: fmaf(0, 1/6, -beta) per red cell (the general sweep's value with
+// every black neighbour 0), so e needs no zeroing between defect-correction
+// steps.  Boxes whose level 0 is cycled by e_tail are zeroed by e_zero_inner.
+__global__ void __launch_bounds__(256) e_gsrb_zero(const Item* __restrict__ items, int nitems,
+                                                   const EDesc* __restrict__ D,
+                                                   const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState& st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        if (d.tail_l == 0) continue;
+        const int n = d.n, half = n >> 1, k = it.b;
+        const int j = it.c + threadIdx.y;
+        if (j >= n) continue;
+        const long long row = ((long long)j + (long long)n * k) * half;
+        for (int ih = threadIdx.x; ih < half; ih += blockDim.x)
+            d.lv[0].phi_r[row + ih] = fmaf(0.f, kSixthF, -d.lv[0].beta_r[row + ih]);
     }
 }
 
@@ -1833,9 +1858,18 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
     const dim3 rb(32, E->tune.smooth_rows);
     // one red or black half sweep of level l over every box: the vectorised
     // kernel for the boxes whose level-l rows allow it, the row kernel for the rest
-    auto smooth = [&](int l, int color) {
+    auto smooth = [&](int l, int color, bool zero_start = false) {
         const auto& rv = E->r_smooth_march[l];
         const auto& rr = E->r_smooth_row[l];
+        if (zero_start) {
+            // the opening red half sweep of an inner solve on level 0
+            const auto& r0 = E->r_rows_split[0];
+            ep_begin(c);
+            e_gsrb_zero<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+            ep_end(c, NYXPM_ST_SMOOTH);
+            c->launches += 1;
+            return;
+        }
         ep_begin(c);
         if (rv.cnt) {
             e_gsrb4<<<pgrid(E, rv.cnt), rb, 0, s>>>(it + rv.off, rv.cnt, D, S, color);
@@ -1853,7 +1887,8 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
                 const auto& rs = E->r_rows_split[l];
                 if (rs.cnt == 0) continue;
                 for (int sw = 0; sw < c->p.nu1; ++sw)
-                    for (int color = 0; color < 2; ++color) smooth(l, color);
+                    for (int color = 0; color < 2; ++color)
+                        smooth(l, color, l == 0 && v == 0 && sw == 0 && color == 0);
                 const auto& qv = E->r_restrict_vec[l + 1];
                 const auto& qr = E->r_restrict_row[l + 1];
                 ep_begin(c);
@@ -1893,7 +1928,8 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
             const float c_hi = (float)(1.0 / 6.0);
             const float c_lo = (float)(1.0 / 6.0 - (double)c_hi);
             e_correct<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, c_hi, c_lo);
-            e_zero_inner<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+            e_zero_inner<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S,
+                                                          c->p.nu1 > 0 ? 0 : 1);
         }
         e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, (first && o == 0) ? 2 : 0);
         ep_end(c, NYXPM_ST_NORM);

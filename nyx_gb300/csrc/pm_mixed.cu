@@ -730,6 +730,16 @@ __global__ void __launch_bounds__(256) k_gsrb_f4(int n, int color, float* __rest
     }
 }
 
+// The opening red half sweep of an inner solve, whose correction starts at 0:
+// every black neighbour is 0, so each red cell gets fmaf(0, 1/6, -beta) -- the
+// general sweep's value, without the loads, and without zeroing e beforehand
+// (the black half sweep after it reads only the red cells it overwrote).
+__global__ void k_gsrb_f_zero(long long cnt, float* __restrict__ mine, const float* __restrict__ beta)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < cnt) mine[t] = fmaf(0.f, kSixthF, -beta[t]);
+}
+
 __device__ __forceinline__ float resid_f(const LevelViewF& L, int i, int j, int k)
 {
     const int n = L.n;
@@ -1105,7 +1115,9 @@ double read_norm(Box& b, int slot)
     return v;
 }
 
-nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine)
+// zero_start: the level's correction is 0 on entry (an inner solve's first sweep
+// on level 0): the red half sweep is k_gsrb_f_zero
+nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine, bool zero_start = false)
 {
     const long long half_cells = (long long)l.n * l.n * l.n / 2;
     const int half = l.n / 2;
@@ -1124,7 +1136,9 @@ nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine)
         const float* other = color ? l.fphi_r : l.fphi_b;
         const float* beta = color ? l.fbeta_b : l.fbeta_r;
         prof_begin(c);
-        if (march)
+        if (zero_start && color == 0)
+            k_gsrb_f_zero<<<blocks_for(half_cells), kThreads, 0, c.stream>>>(half_cells, mine, beta);
+        else if (march)
             k_gsrb_f4<kMarchZ><<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
         else if (vec)
             k_gsrb_f4<1><<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
@@ -1163,19 +1177,38 @@ bool tail_fits(const Ctx& c, const Box& b, size_t li)
            b.levels.size() - li <= (size_t)kMaxTail;
 }
 
-nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li)
+// fresh: level li's correction is 0 on entry without having been zeroed (the
+// first inner V-cycle of a defect-correction step)
+nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li, bool fresh = false)
 {
     nyxpm_status st;
-    if (tail_fits(c, b, li)) return vcycle_tail_f(c, b, li);
     const Level& f = b.levels[li];
+    if (fresh && (tail_fits(c, b, li) || !f.split)) {
+        // the fused tail and the bottom read the level as it is: zero it (a few
+        // thousand cells at most)
+        const size_t cnt = (size_t)f.n * f.n * f.n;
+        if (f.split) {
+            cudaMemsetAsync(f.fphi_r, 0, cnt / 2 * sizeof(float), c.stream);
+            cudaMemsetAsync(f.fphi_b, 0, cnt / 2 * sizeof(float), c.stream);
+        } else {
+            cudaMemsetAsync(f.fphi_r, 0, cnt * sizeof(float), c.stream);
+        }
+        fresh = false;
+    }
+    if (tail_fits(c, b, li)) return vcycle_tail_f(c, b, li);
     if (li + 1 == b.levels.size()) {
         prof_begin(c);
         k_bottom_f<<<1, 512, 0, c.stream>>>(b.nb, b.Gf, f.fbeta_r, f.fphi_r);
         prof_end(c, NYXPM_ST_BOTTOM, 8.0 * f.n * f.n * f.n);
         return check_launch(c, "bottom f32");
     }
+    if (fresh && c.p.nu1 == 0) {
+        const size_t half_bytes = (size_t)f.n * f.n * f.n / 2 * sizeof(float);
+        cudaMemsetAsync(f.fphi_r, 0, half_bytes, c.stream);
+        cudaMemsetAsync(f.fphi_b, 0, half_bytes, c.stream);
+    }
     for (int s = 0; s < c.p.nu1; ++s)
-        if ((st = gsrb_sweep_f(c, f, li == 0)) != NYXPM_OK) return st;
+        if ((st = gsrb_sweep_f(c, f, li == 0, fresh && s == 0)) != NYXPM_OK) return st;
     const Level& cl = b.levels[li + 1];
     const long long ncc = (long long)cl.n * cl.n * cl.n;
     const long long ncf = (long long)f.n * f.n * f.n;
@@ -1476,19 +1509,13 @@ nyxpm_status mixed_solve(Ctx& c, Box& b, int zero_guess, nyxpm_solve_info* info)
     double err = 0.0;   // bound on |tracked residual - residual of phi|
     int it = 0, inner = 0;
     nyxpm_status result = NYXPM_OK;
-    const size_t half_bytes = (size_t)nc / 2 * sizeof(float);
     if (!(r0 <= target)) {
         auto iteration = [&]() -> nyxpm_status {
             // inner FP32 solve of L e = r from e = 0, phi += e, the new residual
             nyxpm_status s;
-            if (l0.split) {
-                cudaMemsetAsync(l0.fphi_r, 0, half_bytes, c.stream);
-                cudaMemsetAsync(l0.fphi_b, 0, half_bytes, c.stream);
-            } else {
-                cudaMemsetAsync(l0.fphi_r, 0, (size_t)nc * sizeof(float), c.stream);
-            }
+            // e starts at 0: the first V-cycle's opening sweep does not read it
             for (int v = 0; v < c.p.mixed_inner_vcycles; ++v)
-                if ((s = vcycle_f(c, b, 0)) != NYXPM_OK) return s;
+                if ((s = vcycle_f(c, b, 0, v == 0)) != NYXPM_OK) return s;
             if (incremental) {
                 if ((s = launch_mx_correct(c, b)) != NYXPM_OK) return s;
                 cudaMemcpyAsync(b.h_norms + 4, b.norms + 4, sizeof(unsigned long long),

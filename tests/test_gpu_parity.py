@@ -283,3 +283,33 @@ def test_vcycle_cap_reports_not_converged(precision):
         assert rel_l2(mean_removed(b.get_phi()), mean_removed(phi_o)) <= TOL
     b.close()
     c2.close()
+
+
+@pytest.mark.parametrize("nu1,nu2", [(1, 1), (2, 0), (0, 2), (3, 1)])
+def test_smoothing_counts_match_oracle(nu1, nu2):
+    """Other pre/post-smoothing counts switch the exact shortcuts of the FP64
+    V-cycle on and off: the red-only restriction needs nu1 > 0, the black-only
+    prolongation and the red-cell norm nu2 > 0, the norm fused with the next
+    opening red sweep both.  Each combination equals the oracle run with the same
+    counts, bit for bit, over three steps."""
+    from nyx_gb300.pm import Context
+    n, L = 32, 1.0
+    ic = config1_ics(n, seed=9)
+    p = O.Particles(ic.pos, ic.vel, ic.mass)
+    pm = O.PMOracle(n, L, p, nu1=nu1, nu2=nu2)
+    c2 = Context(device=0, nu1=nu1, nu2=nu2)
+    try:
+        b = Box(c2, n, L, p.np)
+        b.upload(ic.pos, ic.vel, ic.mass)
+        for a0, a1, dt in equal_da_schedule(0.02, 0.04, 3):
+            info = b.step(a0, a1, dt)
+            pm.step(a0, a1, dt)
+            assert info["old_solve"]["vcycles"] == pm.cycles[0]
+            assert info["new_solve"]["vcycles"] == pm.cycles[1]
+            assert np.array_equal(mean_removed(b.get_phi()), mean_removed(pm.phi))
+        gpos, gvel = b.download()
+        opos, ovel = p.by_id()
+        assert np.array_equal(gpos, opos) and np.array_equal(gvel, ovel)
+        b.close()
+    finally:
+        c2.close()

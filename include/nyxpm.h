@@ -61,9 +61,10 @@ typedef struct nyxpm_params {
     int nu1, nu2;           /* red-black Gauss-Seidel sweeps before / after the coarse correction */
     int verbose;
     int mixed_inner_vcycles;/* NYXPM_MIXED: FP32 V-cycles per FP64 defect-correction iteration */
-    int mg_fused_edge;      /* NYXPM_MIXED: the FP32 V-cycle levels of at most this many cells
-                               per edge run as one launch (one CTA per box) per V-cycle, same
-                               results; 0: one launch per pass on every level (default 16) */
+    int mg_fused_edge;      /* the FP32 V-cycle levels of at most this many cells per edge
+                               (the FP64 ones of at most half as many, below the finest) run
+                               as one launch (one CTA per box) per V-cycle, same results;
+                               0: one launch per pass on every level (default 16) */
 } nyxpm_params;
 
 typedef struct nyxpm_ctx nyxpm_ctx;
@@ -301,6 +302,46 @@ nyxpm_status nyxpm_cosmo_ic_factors(const nyxpm_params* p, int source, int n, do
 nyxpm_status nyxpm_box_init_cosmo_1ppc(nyxpm_ctx* ctx, nyxpm_box* box, const double* disp,
                                        const double* vel, const double* disp_fac,
                                        const double* vel_fac, double particle_mass);
+
+/* ---- AMReX MultiFab files (VisMF, host I/O) ------------------------------------ */
+
+/* A cell-centred MultiFab stored as VisMF::Write stores it, header version 1:
+ * <name>_H (version, write mode, ncomp, ngrow, the BoxArray, one
+ * "FabOnDisk: <file> <offset>" per box, per-box per-component min and max) and
+ * data files holding each FAB as a text header (real descriptor, box, ncomp)
+ * and its values, component after component, x fastest.  This is the form of
+ * the IC MultiFab <cosmo.initDirName>/Level_0/Cell that Nyx::icReadAndPrepareFab
+ * reads with VisMF::Read (Source/Initialization/Nyx_initcosmo.cpp:15-96). */
+typedef struct nyxpm_multifab_info {
+    int ncomp;
+    int ngrow;
+    int nboxes;
+    int lo[3], hi[3];      /* bounding box of the BoxArray (cell indices) */
+    int has_minmax;        /* the header holds the min/max tables */
+} nyxpm_multifab_info;
+
+#define NYXPM_MF_REJECT_NAN 1u   /* a NaN is an error, as icReadAndPrepareFab's check */
+
+nyxpm_status nyxpm_multifab_info_read(const char* name, nyxpm_multifab_info* info, char* errbuf,
+                                      size_t errlen);
+/* boxes_out: nboxes x 6 ints (lo x y z, hi x y z) in header order; minmax_out:
+ * nboxes x ncomp x (min, max) from the header.  Either may be NULL. */
+nyxpm_status nyxpm_multifab_boxes(const char* name, int* boxes_out, double* minmax_out,
+                                  char* errbuf, size_t errlen);
+/* Components [comp0, comp0 + ncomp) of the valid cells in [lo, hi] into out
+ * (ncomp blocks of nx ny nz values, x fastest).  Every cell of [lo, hi] must lie
+ * in exactly one box.  FABs of IEEE float64 or float32 in either byte order. */
+nyxpm_status nyxpm_multifab_read(const char* name, int comp0, int ncomp, const int* lo,
+                                 const int* hi, unsigned flags, double* out, char* errbuf,
+                                 size_t errlen);
+/* Writes data (ncomp blocks over [lo, hi], x fastest) as a MultiFab with ngrow 0:
+ * the boxes given (nboxes x 6 ints that tile [lo, hi]) or, with boxes NULL, the
+ * region cut into boxes of at most max_grid_size cells per edge (x fastest,
+ * then y, then z).  One data file <name>_D_00000, float64 in the host's byte
+ * order.  The directory of name must exist. */
+nyxpm_status nyxpm_multifab_write(const char* name, int ncomp, const int* lo, const int* hi,
+                                  int max_grid_size, int nboxes, const int* boxes,
+                                  const double* data, char* errbuf, size_t errlen);
 
 /* ---- ensembles and serving ------------------------------------------------------ */
 

@@ -39,7 +39,21 @@ EXPORTS = [
     "nyxpm_compute_new_dt", "nyxpm_particle_file_count", "nyxpm_particle_file_read",
     "nyxpm_particle_file_write", "nyxpm_write_comoving_a", "nyxpm_read_comoving_a",
     "nyxpm_cosmo_1ppc_particles", "nyxpm_cosmo_ic_factors", "nyxpm_box_init_cosmo_1ppc",
+    "nyxpm_multifab_info_read", "nyxpm_multifab_boxes", "nyxpm_multifab_read",
+    "nyxpm_multifab_write",
 ]
+NYXPM_MF_REJECT_NAN = 1
+
+
+class MultiFabInfo(C.Structure):
+    _fields_ = [
+        ("ncomp", C.c_int),
+        ("ngrow", C.c_int),
+        ("nboxes", C.c_int),
+        ("lo", C.c_int * 3),
+        ("hi", C.c_int * 3),
+        ("has_minmax", C.c_int),
+    ]
 NYXPM_FILE_ASCII, NYXPM_FILE_BINARY, NYXPM_FILE_BINARY_META, NYXPM_FILE_BINARY_F64 = 0, 1, 2, 3
 
 
@@ -184,6 +198,10 @@ def load(path: str | None = None):
     L.nyxpm_cosmo_ic_factors.argtypes = [C.POINTER(Params), C.c_int, C.c_int, d, d, vp, vp,
                                          C.POINTER(d)]
     L.nyxpm_box_init_cosmo_1ppc.argtypes = [vp, vp, vp, vp, vp, vp, d]
+    L.nyxpm_multifab_info_read.argtypes = [cp, C.POINTER(MultiFabInfo), cp, sz]
+    L.nyxpm_multifab_boxes.argtypes = [cp, vp, vp, cp, sz]
+    L.nyxpm_multifab_read.argtypes = [cp, C.c_int, C.c_int, vp, vp, C.c_uint, vp, cp, sz]
+    L.nyxpm_multifab_write.argtypes = [cp, C.c_int, vp, vp, C.c_int, C.c_int, vp, vp, cp, sz]
     L.nyxpm_set_profiling.argtypes = [vp, C.c_int]
     L.nyxpm_get_profile.argtypes = [vp, C.POINTER(Profile), C.c_int]
     L.nyxpm_launch_count.argtypes = [vp]

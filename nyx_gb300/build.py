@@ -31,6 +31,7 @@ UNITS = {
     "pm_ensemble.cu": [],
     "pm_noalloc.cu": ["--fmad=false"],
     "pm_io.cpp": [],
+    "pm_vismf.cpp": [],
 }
 
 

@@ -1331,7 +1331,7 @@ __global__ void __launch_bounds__(kTailThreads) e_tail(int nbox, const EDesc* __
         const ELevel& e = d.lv[d.tail_l + l];
         lv[l] = LevelViewF{e.n, e.split, e.phi_r, e.phi_b, e.beta_r, e.beta_b};
     }
-    vcycle_tail(lv, nl, nu1, nu2, d.Gf, d.nb, r, g);
+    vcycle_tail<float>(lv, nl, nu1, nu2, d.Gf, d.nb, r, g, false);
 }
 
 // FP32 gravity vector from the FP64 phi (level-0 rows, natural coordinates)

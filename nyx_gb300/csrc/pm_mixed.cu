@@ -1000,7 +1000,7 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail_f(TailF A)
 {
     __shared__ float r[kMaxBottom * kMaxBottom * kMaxBottom];
     __shared__ float g[kMaxBottom * kMaxBottom * kMaxBottom];
-    vcycle_tail(A.lv, A.nl, A.nu1, A.nu2, A.Gf, A.nb, r, g);
+    vcycle_tail<float>(A.lv, A.nl, A.nu1, A.nu2, A.Gf, A.nb, r, g, false);
 }
 
 // FP32 gravity vector from the FP64 phi: the difference in FP64, the scaling in FP32

@@ -64,8 +64,10 @@ class RunConfig:
     absolute_max_change_a: float
     dt_binpow: float
     dt_cutoff: float
-    particle_file: str
-    particle_format: str       # ascii | binary | binary_meta
+    particle_file: str         # the particle file, or cosmo.initDirName for "cosmological"
+    particle_format: str       # ascii | binary | binary_meta | cosmological
+    ic_source: str             # cosmo.ic-source (MUSIC | nyx) for "cosmological"
+    n_particles: int           # nyx.n_particles per edge (the nyx source's particle mass)
     plot_int: int
     plot_file: str
     check_int: int
@@ -96,11 +98,30 @@ def run_config(d: dict[str, list[str]], base_dir: str = ".") -> RunConfig:
     if any(abs(s - sides[0]) > 1e-12 * sides[0] for s in sides) or any(v != 0.0 for v in lo):
         raise ValueError("the domain must be a cube with geometry.prob_lo = 0 0 0")
     init = _str(d, "nyx.particle_init_type", "AsciiFile")
-    fmt = {"AsciiFile": "ascii", "BinaryFile": "binary", "BinaryMetaFile": "binary_meta"}.get(init)
+    fmt = {"AsciiFile": "ascii", "BinaryFile": "binary", "BinaryMetaFile": "binary_meta",
+           "Cosmological": "cosmological"}.get(init)
     if fmt is None:
-        raise ValueError(f"nyx.particle_init_type {init} is not a particle file type "
-                         "(AsciiFile, BinaryFile, BinaryMetaFile)")
-    key = "nyx.ascii_particle_file" if fmt == "ascii" else "nyx.binary_particle_file"
+        raise ValueError(f"nyx.particle_init_type {init} is not supported "
+                         "(AsciiFile, BinaryFile, BinaryMetaFile, Cosmological)")
+    ic_source, n_part = "", ncell[0]
+    if fmt == "cosmological":
+        # Nyx::initcosmo (Source/Initialization/Nyx_initcosmo.cpp:100-427): the IC
+        # MultiFab <cosmo.initDirName>/Level_0/Cell, one particle per cell
+        key = "cosmo.initDirName"
+        ic_source = _str(d, "cosmo.ic-source", "")
+        if ic_source not in ("MUSIC", "nyx"):
+            raise ValueError("cosmo.ic-source must be MUSIC or nyx for particle_init_type Cosmological")
+        if _get(d, "nyx.initial_z", None) is None:
+            raise ValueError("nyx.initial_z is required for particle_init_type Cosmological")
+        npv = _get(d, "nyx.n_particles", None, int, 3)
+        if npv is None and ic_source == "nyx":
+            raise ValueError("nyx.n_particles is required for cosmo.ic-source nyx")
+        if npv is not None:
+            if len(set(npv)) != 1:
+                raise ValueError("nyx.n_particles must be the same on each axis")
+            n_part = npv[0]
+    else:
+        key = "nyx.ascii_particle_file" if fmt == "ascii" else "nyx.binary_particle_file"
     pfile = _str(d, key, "")
     if not pfile:
         raise ValueError(f"{key} is required for particle_init_type {init}")
@@ -121,7 +142,7 @@ def run_config(d: dict[str, list[str]], base_dir: str = ".") -> RunConfig:
         relative_max_change_a=_get(d, "nyx.relative_max_change_a", 0.01),
         absolute_max_change_a=_get(d, "nyx.absolute_max_change_a", -1.0),
         dt_binpow=_get(d, "nyx.dt_binpow", -1.0), dt_cutoff=_get(d, "nyx.dt_cutoff", 0.0),
-        particle_file=pfile, particle_format=fmt,
+        particle_file=pfile, particle_format=fmt, ic_source=ic_source, n_particles=n_part,
         plot_int=_get(d, "amr.plot_int", -1, int), plot_file=_str(d, "amr.plot_file", "plt"),
         check_int=_get(d, "amr.check_int", -1, int), check_file=_str(d, "amr.check_file", "chk"),
         data_log=_str(d, "amr.data_log", ""), restart=_str(d, "amr.restart", ""))

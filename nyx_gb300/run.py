@@ -3,7 +3,9 @@
     python -m nyx_gb300.run <inputs> [key=value ...] [--precision mixed]
 
 What it does, following Nyx's driver on one periodic level:
-1. It reads the particles named by ``nyx.particle_init_type``.
+1. It reads the particles named by ``nyx.particle_init_type``: a particle file,
+   or (Cosmological) one particle per cell from the IC MultiFab
+   ``<cosmo.initDirName>/Level_0/Cell`` as Nyx::initcosmo places them.
 2. It solves for the initial field at a = 1 / (1 + nyx.initial_z), as
    Nyx::post_init does.
 3. It takes PM steps, ``Nyx::advance_particles_only`` plus ``post_timestep``.
@@ -34,6 +36,7 @@ import time
 import numpy as np
 
 from . import inputs as _inputs
+from .multifab import read_ic_fields
 from .pm import (Box, Context, read_comoving_a, read_particle_file, uniform_mass,
                  write_comoving_a, write_particle_file)
 
@@ -76,9 +79,18 @@ def run(inputs_path: str, overrides: list[str] | None = None, precision: str = "
     else:
         step, t, dt_old = 0, 0.0, -1.0
         a = 1.0 / (1.0 + cfg.initial_z)
-        pos, vel, mass = read_particle_file(cfg.particle_file, cfg.particle_format)
-    box = Box(ctx, cfg.n, cfg.L, len(pos), precision=precision)
-    box.upload(pos, vel, uniform_mass(mass))
+        if cfg.particle_format != "cosmological":
+            pos, vel, mass = read_particle_file(cfg.particle_file, cfg.particle_format)
+    if not cfg.restart and cfg.particle_format == "cosmological":
+        disp, ivel = read_ic_fields(cfg.particle_file, cfg.ic_source, cfg.n)
+        # MUSIC: mass rho_m dx^3 of the grid; nyx: rho_m L^3 / n_particles^3
+        n_mass = cfg.n_particles if cfg.ic_source == "nyx" else cfg.n
+        dfac, vfac, pmass = ctx.cosmo_ic_factors(cfg.ic_source, n_mass, cfg.L, cfg.initial_z)
+        box = Box(ctx, cfg.n, cfg.L, cfg.n ** 3, precision=precision)
+        box.init_cosmo_1ppc(disp, ivel, dfac, vfac, pmass)
+    else:
+        box = Box(ctx, cfg.n, cfg.L, len(pos), precision=precision)
+        box.upload(pos, vel, uniform_mass(mass))
     if cfg.restart:
         # the checkpointed field, as Nyx restores PhiGrav_Type: the next dt
         # estimate then sees the same gravity as the uninterrupted run

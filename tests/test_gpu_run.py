@@ -91,3 +91,40 @@ def test_mixed_precision_run(tmp_path):
     disp = np.linalg.norm((fp["pos"] - ic.pos + 0.5) % 1.0 - 0.5)
     err = np.linalg.norm((mx["pos"] - fp["pos"] + 0.5) % 1.0 - 0.5)
     assert err <= 1e-5 * disp
+
+
+@pytest.mark.parametrize("source", ["MUSIC", "nyx"])
+def test_run_from_an_ic_multifab(ctx, tmp_path, source):
+    """particle_init_type = Cosmological: one particle per cell from the IC
+    MultiFab <cosmo.initDirName>/Level_0/Cell with Nyx::initcosmo's factors and
+    mass; the run equals the same fields placed by hand with init_cosmo_1ppc."""
+    from nyx_gb300 import multifab as M
+    n = 16
+    ic = config1_ics(n, seed=13, a_init=0.05)
+    disp = ((ic.pos - ic.lattice + 0.5) % 1.0 - 0.5).T.reshape(3, n, n, n)
+    vel = ic.vel.T.reshape(3, n, n, n)
+    fields = np.concatenate([disp, vel * 1e-3]) if source == "MUSIC" else disp
+    M.write(M.ic_multifab_name(str(tmp_path / "ics_mf")), fields, max_grid_size=8)
+    inp, _ = write_inputs(tmp_path, "amr.plot_int = -1\namr.check_int = -1\nmax_step = 3\n"
+                                    "nyx.particle_init_type = Cosmological\n"
+                                    "cosmo.initDirName = ics_mf\n"
+                                    f"cosmo.ic-source = {source}\n"
+                                    "nyx.n_particles = 16 16 16\n")
+    res = run(inp, ["amr.data_log="], out_dir=str(tmp_path), verbose=False)
+    assert res["steps"] == 3 and res["particles"] == n ** 3
+    d_ic, v_ic = M.read_ic_fields(str(tmp_path / "ics_mf"), source, n)
+    dfac, vfac, pmass = ctx.cosmo_ic_factors(source, n, 1.0, 19.0)
+    box = Box(ctx, n, 1.0, n ** 3)
+    box.init_cosmo_1ppc(d_ic, v_ic, dfac, vfac, pmass)
+    a, t, dt_old = 0.05, 0.0, -1.0
+    box.init_field(a)
+    for s in range(3):
+        dt, a_new = box.compute_new_dt(t, a, dt_old, cfl=0.5, relative_max_change_a=0.01, final_a=1.0)
+        if s == 0:
+            dt = dt * 0.5
+            a_new = ctx.integrate_comoving_a(a, dt)
+        box.step(a, a_new, dt)
+        t, a, dt_old = t + dt, a_new, dt
+    pos, v = box.download()
+    box.close()
+    assert np.array_equal(pos, res["pos"]) and np.array_equal(v, res["vel"])

@@ -34,9 +34,33 @@ def test_scope_is_enforced(tmp_path):
     for key, val, msg in (("nyx.do_hydro", ["1"], "do_hydro"), ("amr.max_level", ["1"], "max_level"),
                           ("amr.n_cell", ["16", "16", "32"], "cubic"),
                           ("geometry.is_periodic", ["1", "1", "0"], "periodic"),
-                          ("nyx.particle_init_type", ["Cosmological"], "particle file")):
+                          ("nyx.particle_init_type", ["Random"], "not supported"),
+                          ("nyx.particle_init_type", ["Cosmological"], "ic-source")):
         d = dict(base)
         d[key] = val
+        with pytest.raises(ValueError, match=msg):
+            run_config(d, str(tmp_path))
+
+
+def test_cosmological_init_type(tmp_path):
+    """particle_init_type = Cosmological reads cosmo.initDirName, cosmo.ic-source,
+    nyx.initial_z and nyx.n_particles, as Nyx::initcosmo does."""
+    base = {"amr.n_cell": ["16", "16", "16"], "geometry.prob_hi": ["1", "1", "1"],
+            "nyx.do_hydro": ["0"], "nyx.particle_init_type": ["Cosmological"],
+            "cosmo.initDirName": ["ics"], "cosmo.ic-source": ["MUSIC"], "nyx.initial_z": ["99"]}
+    cfg = run_config(dict(base), str(tmp_path))
+    assert cfg.particle_format == "cosmological" and cfg.ic_source == "MUSIC"
+    assert cfg.particle_file == os.path.join(str(tmp_path), "ics") and cfg.n_particles == 16
+    d = dict(base, **{"cosmo.ic-source": ["nyx"], "nyx.n_particles": ["8", "8", "8"]})
+    assert run_config(d, str(tmp_path)).n_particles == 8
+    for key, val, msg in (("cosmo.ic-source", ["nyx"], "n_particles"),
+                          ("cosmo.initDirName", [], "initDirName"),
+                          ("nyx.initial_z", None, "initial_z")):
+        d = dict(base)
+        if val is None:
+            del d[key]
+        else:
+            d[key] = val
         with pytest.raises(ValueError, match=msg):
             run_config(d, str(tmp_path))
 

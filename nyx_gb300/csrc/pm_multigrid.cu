@@ -13,6 +13,7 @@
 // --fmad=false: only the explicit fma() calls fuse, in the same places the CPU
 // oracle fuses, so both round identically.
 #include "pm_common.cuh"
+#include "pm_tail.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -404,6 +405,22 @@ __global__ void k_bottom(int nb, const double* __restrict__ G, const double* __r
     }
 }
 
+// the coarse end of an FP64 V-cycle by one CTA (pm_tail.cuh): the arithmetic of
+// k_gsrb, k_restrict, k_bottom and k_prolong in the same order, so the same bits
+struct TailD {
+    int nl;                  // levels in the tail; the last is the bottom (natural layout)
+    int nu1, nu2, nb;
+    const double* G;
+    LevelView lv[kMaxTail];
+};
+
+__global__ void __launch_bounds__(kTailThreadsD) k_vcycle_tail_d(TailD A)
+{
+    __shared__ double r[kMaxBottom * kMaxBottom * kMaxBottom];
+    __shared__ double g[kMaxBottom * kMaxBottom * kMaxBottom];
+    vcycle_tail<double>(A.lv, A.nl, A.nu1, A.nu2, A.G, A.nb, r, g, true);
+}
+
 // g_d(c) = 0.5*((phi_c - phi_{c-e_d})*dxi + (phi_{c+e_d} - phi_c)*dxi), second product fused;
 // component-major output
 __global__ void k_grav(LevelView L, double dxi, double* g)
@@ -469,12 +486,44 @@ nyxpm_status gsrb_sweep(Ctx& c, const Level& l, int fine, int black_only = 0)
     return check_launch(c, "gsrb");
 }
 
+// One SM issues FP64 at 1/64 of its FP32 rate, so the FP64 form fuses only the
+// levels of at most half the FP32 edge (8^3 cells at the default 16): there a
+// level's half sweep is a few hundred cells, cheaper on one SM than a launch.
+bool tail_fits_d(const Ctx& c, const Box& b, size_t li)
+{
+    const int edge = c.p.mg_fused_edge / 2;
+    return li > 0 && edge > 0 && b.levels[li].n <= edge && b.levels.size() - li >= 2 &&
+           b.levels.size() - li <= (size_t)kMaxTail;
+}
+
+nyxpm_status vcycle_tail_d(Ctx& c, Box& b, size_t li)
+{
+    TailD A;
+    A.nl = (int)(b.levels.size() - li);
+    A.nu1 = c.p.nu1;
+    A.nu2 = c.p.nu2;
+    A.nb = b.nb;
+    A.G = b.G;
+    double bytes = 0;
+    for (int l = 0; l < A.nl; ++l) {
+        const Level& lv = b.levels[li + l];
+        A.lv[l] = view(lv);
+        const double cells = (double)lv.n * lv.n * lv.n;
+        bytes += (l + 1 < A.nl) ? 12.0 * cells * 2 * (c.p.nu1 + c.p.nu2) + 32.0 * cells : 16.0 * cells;
+    }
+    prof_begin(c);
+    k_vcycle_tail_d<<<1, kTailThreadsD, 0, c.stream>>>(A);
+    prof_end(c, NYXPM_ST_SMOOTH, bytes);
+    return check_launch(c, "fused coarse V-cycle");
+}
+
 // red_done: the opening red half sweep of this level was already made (by
 // k_resnorm_red_sweep)
 nyxpm_status vcycle(Ctx& c, Box& b, size_t li, int red_done = 0)
 {
     nyxpm_status st;
     const Level& f = b.levels[li];
+    if (tail_fits_d(c, b, li)) return vcycle_tail_d(c, b, li);
     if (li + 1 == b.levels.size()) {
         prof_begin(c);
         k_bottom<<<1, 512, 0, c.stream>>>(b.nb, b.G, f.beta_r, f.phi_r);

@@ -63,3 +63,20 @@ def test_fused_coarse_vcycle_equals_one_launch_per_pass(ctx, n, edge):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
     assert a[3] == b[3]
     assert a[4] < b[4]                   # fewer launches
+
+
+@pytest.mark.parametrize("n", [32, 48, 64])
+def test_fused_fp64_coarse_vcycle_equals_one_launch_per_pass(ctx, n):
+    """The FP64 form fuses the levels of at most mg_fused_edge / 2 cells per edge
+    below the finest (8^3 and 4^3 at the default; n = 48: 6^3 and the 3^3
+    bottom).  Same bits as one launch per pass."""
+    from nyx_gb300.pm import Context
+    plain = Context(mg_fused_edge=0)
+    try:
+        a = run(ctx, "fp64", profiling=False, n=n, steps=2)
+        b = run(plain, "fp64", profiling=False, n=n, steps=2)
+    finally:
+        plain.close()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    assert a[3] == b[3]
+    assert a[4] < b[4]

@@ -72,6 +72,49 @@ __device__ inline void block_umax_store(unsigned long long v, unsigned long long
 }
 
 // warp max of bits into *out; the whole warp calls it (blocks of 32-wide rows)
+// Sorts a[s .. s+len) ascending, 2 <= len <= 32, values distinct and below
+// INT32_MAX: the counting sort's segment of one key, put back in particle order.
+// Up to 4 values (most segments at a particle per cell) go through a sorting
+// network in registers; longer ones through an insertion sort.
+__device__ __forceinline__ void sort_short_segment(int* a, int s, int len)
+{
+    if (len <= 4) {
+        int v0 = a[s], v1 = a[s + 1];
+        int v2 = len > 2 ? a[s + 2] : INT32_MAX, v3 = len > 3 ? a[s + 3] : INT32_MAX;
+        auto cs = [](int& x, int& y) {
+            const int lo = min(x, y), hi = max(x, y);
+            x = lo;
+            y = hi;
+        };
+        cs(v0, v1);
+        cs(v2, v3);
+        cs(v0, v2);
+        cs(v1, v3);
+        cs(v1, v2);
+        a[s] = v0;
+        a[s + 1] = v1;
+        if (len > 2) a[s + 2] = v2;
+        if (len > 3) a[s + 3] = v3;
+        return;
+    }
+    int v[32];
+#pragma unroll
+    for (int t = 0; t < 32; ++t)
+        if (t < len) v[t] = a[s + t];
+    for (int i = 1; i < len; ++i) {
+        const int cur = v[i];
+        int j = i - 1;
+        while (j >= 0 && v[j] > cur) {
+            v[j + 1] = v[j];
+            --j;
+        }
+        v[j + 1] = cur;
+    }
+#pragma unroll
+    for (int t = 0; t < 32; ++t)
+        if (t < len) a[s + t] = v[t];
+}
+
 __device__ inline void warp_umax_atomic(unsigned long long v, unsigned long long* out)
 {
 #pragma unroll

@@ -418,22 +418,7 @@ __global__ void __launch_bounds__(256) e_fix_short(const Item* __restrict__ item
             d.long_list[atomicAdd(d.long_count, 1)] = K;
             continue;
         }
-        int v[32];
-#pragma unroll
-        for (int t = 0; t < 32; ++t)
-            if (t < len) v[t] = d.perm[s + t];
-        for (int a = 1; a < len; ++a) {
-            int cur = v[a];
-            int bb = a - 1;
-            while (bb >= 0 && v[bb] > cur) {
-                v[bb + 1] = v[bb];
-                --bb;
-            }
-            v[bb + 1] = cur;
-        }
-#pragma unroll
-        for (int t = 0; t < 32; ++t)
-            if (t < len) d.perm[s + t] = v[t];
+        sort_short_segment(d.perm, s, len);
     }
 }
 

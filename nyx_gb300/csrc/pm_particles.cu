@@ -202,22 +202,7 @@ __global__ void k_fix_short(int nc, const int* __restrict__ start, int* perm, in
         long_list[atomicAdd(long_count, 1)] = K;
         return;
     }
-    int v[32];
-#pragma unroll
-    for (int t = 0; t < 32; ++t)
-        if (t < len) v[t] = perm[s + t];
-    for (int a = 1; a < len; ++a) {
-        int cur = v[a];
-        int b = a - 1;
-        while (b >= 0 && v[b] > cur) {
-            v[b + 1] = v[b];
-            --b;
-        }
-        v[b + 1] = cur;
-    }
-#pragma unroll
-    for (int t = 0; t < 32; ++t)
-        if (t < len) perm[s + t] = v[t];
+    sort_short_segment(perm, s, len);
 }
 
 // long segments: rank sort by one block per segment (values are distinct)

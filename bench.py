@@ -57,6 +57,7 @@ def parse():
                          "the autotuner's choice")
     ap.add_argument("--fused-edge", type=int, default=None,
                     help="nyxpm_params.mg_fused_edge: FP32 V-cycle levels of at most this many "
+                         "(FP64: half as many) "
                          "cells per edge run as one CTA per box (default: the library's)")
     ap.add_argument("--quick", action="store_true",
                     help="headline timing only (no reuse-field pass, e2e or CPU baseline); "

@@ -670,7 +670,10 @@ __global__ void __launch_bounds__(256) k_gsrb_f(int n, int color, float* __restr
 // loads three neighbour rows (y-1, y+1, z+1), the right-hand side and one edge
 // value for the x neighbours.  The sums are the scalar kernel's, term for term.
 // Needs half % 4 == 0 (rows start on 16 bytes).
-constexpr int kMarchZ = 4;
+// 2 planes: at 256^3 a block marching 4 planes leaves 2048 blocks, 2.25 waves
+// at 6 blocks per SM, and the last wave's tail costs a quarter of the launch
+// (measured 20.6 us per half sweep; 2 planes 19.1 us, 1 plane 19.4 us)
+constexpr int kMarchZ = 2;
 constexpr int kMarchMinEdge = 256;
 
 template <int MZ>

@@ -160,9 +160,24 @@ nyxpm_status nyxpm_set_phi(nyxpm_ctx* ctx, nyxpm_box* box, const double* phi);
  * on the device). */
 nyxpm_status nyxpm_grav_vector(nyxpm_ctx* ctx, nyxpm_box* box, double* g_out);
 
+/* The caller's acceleration for the next kicks: the `acc` MultiFab argument of
+ * DarkMatterParticleContainer::moveKickDrift / moveKick
+ * (Source/Particle/DarkMatterParticleContainer.cpp:76-112, 184-247;
+ * NyxParticleContainer.H:15-18), e.g. the grav_vec_old / grav_vec_new that Nyx's
+ * own Gravity object computed.  g holds 3 n^3 values, component-major, x fastest:
+ * the valid cells of a cell-centred 3-component field on the box's grid (the
+ * kicks wrap the CIC corners periodically, which is what the reference's
+ * periodic ghost fill of acc gives).  on_device = 0: g is host memory, copied
+ * before the call returns; 1: g is device memory on the context's device, copied
+ * on the context's stream.  The field replaces the box's own gravity vector until
+ * the next solve (nyxpm_solve_phi, nyxpm_step, nyxpm_init_field, nyxpm_set_phi);
+ * mixed boxes round it to FP32 as their kicks read it. */
+nyxpm_status nyxpm_set_grav_vector(nyxpm_ctx* ctx, nyxpm_box* box, const double* g, int on_device);
+
 /* DarkMatterParticleContainer::moveKickDrift (Source/Particle/DarkMatterParticleContainer.cpp:76-181):
- * the box's cell-centred gravity vector (kept in step with phi) interpolated to the
- * particle by CIC, v = (a_old v + dt/2 g)/a_half, x += dt/a_half v
+ * the box's cell-centred gravity vector (kept in step with phi, or the caller's
+ * from nyxpm_set_grav_vector) interpolated to the particle by CIC,
+ * v = (a_old v + dt/2 g)/a_half, x += dt/a_half v
  * (update_dm_particle_single, :250-306, do_move = 1). */
 nyxpm_status nyxpm_kick_drift(nyxpm_ctx* ctx, nyxpm_box* box, double dt, double a_old,
                               double a_half);

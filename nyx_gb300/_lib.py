@@ -27,7 +27,8 @@ EXPORTS = [
     "nyxpm_abi_version", "nyxpm_stream", "nyxpm_synchronize", "nyxpm_box_create",
     "nyxpm_box_destroy", "nyxpm_box_bytes", "nyxpm_box_upload", "nyxpm_box_download",
     "nyxpm_set_mass_offset", "nyxpm_redistribute", "nyxpm_deposit", "nyxpm_solve_phi",
-    "nyxpm_get_phi", "nyxpm_set_phi", "nyxpm_grav_vector", "nyxpm_kick_drift", "nyxpm_kick",
+    "nyxpm_get_phi", "nyxpm_set_phi", "nyxpm_grav_vector", "nyxpm_set_grav_vector",
+    "nyxpm_kick_drift", "nyxpm_kick",
     "nyxpm_step", "nyxpm_step_host", "nyxpm_init_field", "nyxpm_integrate_a", "nyxpm_dt_for_da",
     "nyxpm_set_profiling", "nyxpm_get_profile", "nyxpm_launch_count",
     "nyxpm_ensemble_create", "nyxpm_ensemble_destroy", "nyxpm_ensemble_box_bytes",
@@ -173,6 +174,7 @@ def load(path: str | None = None):
     L.nyxpm_get_phi.argtypes = [vp, vp, vp]
     L.nyxpm_set_phi.argtypes = [vp, vp, vp]
     L.nyxpm_grav_vector.argtypes = [vp, vp, vp]
+    L.nyxpm_set_grav_vector.argtypes = [vp, vp, vp, C.c_int]
     L.nyxpm_kick_drift.argtypes = [vp, vp, d, d, d]
     L.nyxpm_kick.argtypes = [vp, vp, d, d, d]
     L.nyxpm_step.argtypes = [vp, vp, d, d, d, C.c_uint, C.POINTER(StepInfo)]

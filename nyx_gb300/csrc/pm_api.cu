@@ -171,6 +171,7 @@ nyxpm_status do_solve(Ctx& c, Box& b, double a, int zero_guess, nyxpm_solve_info
     if (zero_guess && (st = launch_zero_phi(c, b)) != NYXPM_OK) return st;
     nyxpm_status solved = mixed ? mixed_solve(c, b, zero_guess, info) : mg_solve(c, b, info);
     if (solved != NYXPM_OK && solved != NYXPM_NOT_CONVERGED) return solved;
+    b.g_from_caller = 0;   // the gravity vector follows the new phi from here on
     // the mixed solve leaves its FP32 gravity vector in g32 itself
     if (!mixed && (st = launch_grav_vector(c, b)) != NYXPM_OK) return st;
     return solved;
@@ -587,14 +588,30 @@ nyxpm_status nyxpm_set_phi(nyxpm_ctx* c, nyxpm_box* b, const double* phi)
     TRY(launch_grav_vector(*c, *b));
     if (b->prec == NYXPM_MIXED) TRY(mixed_grav32(*c, *b));
     b->have_phi = 1;
+    b->g_from_caller = 0;
     return nyxpm_synchronize(c);
+}
+
+nyxpm_status nyxpm_set_grav_vector(nyxpm_ctx* c, nyxpm_box* b, const double* g, int on_device)
+{
+    CHECK_BOX(c, b);
+    if (!g) return fail(c, NYXPM_INVALID_ARG, "null g");
+    const size_t nc = (size_t)b->n * b->n * b->n;
+    cudaMemcpyAsync(b->g, g, sizeof(double) * 3 * nc,
+                    on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream);
+    TRY(check_launch(*c, "caller gravity copy"));
+    if (b->prec == NYXPM_MIXED) TRY(mixed_g32_from_g(*c, *b));
+    b->g_from_caller = 1;
+    // a host buffer may be reused as soon as the call returns
+    return on_device ? NYXPM_OK : nyxpm_synchronize(c);
 }
 
 nyxpm_status nyxpm_grav_vector(nyxpm_ctx* c, nyxpm_box* b, double* g_out)
 {
     CHECK_BOX(c, b);
-    if (!b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field: solve or set phi first");
-    if (b->prec == NYXPM_MIXED) TRY(launch_grav_vector(*c, *b));
+    if (!b->have_phi && !b->g_from_caller)
+        return fail(c, NYXPM_INVALID_ARG, "no field: solve, set phi or set the gravity vector first");
+    if (b->prec == NYXPM_MIXED && !b->g_from_caller) TRY(launch_grav_vector(*c, *b));
     if (g_out) {
         const size_t nc = (size_t)b->n * b->n * b->n;
         cudaMemcpyAsync(g_out, b->g, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream);
@@ -608,7 +625,8 @@ nyxpm_status nyxpm_kick_drift(nyxpm_ctx* c, nyxpm_box* b, double dt, double a_ol
 {
     CHECK_BOX(c, b);
     if (!b->uploaded) return fail(c, NYXPM_INVALID_ARG, "box has no particles");
-    if (!b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field: solve or set phi first");
+    if (!b->have_phi && !b->g_from_caller)
+        return fail(c, NYXPM_INVALID_ARG, "no field: solve, set phi or set the gravity vector first");
     if (!(a_half > 0) || !std::isfinite(dt)) return fail(c, NYXPM_INVALID_ARG, "bad dt / a");
     return do_kick(*c, *b, dt, a_old, a_half, 1, 0);
 }
@@ -617,7 +635,8 @@ nyxpm_status nyxpm_kick(nyxpm_ctx* c, nyxpm_box* b, double dt, double a_new, dou
 {
     CHECK_BOX(c, b);
     if (!b->uploaded) return fail(c, NYXPM_INVALID_ARG, "box has no particles");
-    if (!b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field: solve or set phi first");
+    if (!b->have_phi && !b->g_from_caller)
+        return fail(c, NYXPM_INVALID_ARG, "no field: solve, set phi or set the gravity vector first");
     if (!(a_new > 0) || !std::isfinite(dt)) return fail(c, NYXPM_INVALID_ARG, "bad dt / a");
     return do_kick(*c, *b, dt, a_half, a_new, 0, 0);
 }
@@ -827,7 +846,8 @@ nyxpm_status nyxpm_est_time_step(nyxpm_ctx* c, nyxpm_box* b, double cfl, double 
         *dt = -1.0e50;  // no particles at this level (NyxParticleContainer.H:455)
         return NYXPM_OK;
     }
-    if (!b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field: solve, step or set phi first");
+    if (!b->have_phi && !b->g_from_caller)
+        return fail(c, NYXPM_INVALID_ARG, "no field: solve, step, set phi or set the gravity vector first");
     TRY(b->prec == NYXPM_MIXED ? mixed_est_dt(*c, *b, cfl, a) : launch_est_dt(*c, *b, cfl, a));
     cudaMemcpyAsync(b->h_norms + 3, b->norms + 3, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                     c->stream);

@@ -296,6 +296,7 @@ struct Box {
     int sorted = 0;
     int uploaded = 0;
     int have_phi = 0;
+    int g_from_caller = 0;             // g (and g32) hold nyxpm_set_grav_vector's field
 
     // particles (FP64 form)
     double *x = nullptr, *y = nullptr, *z = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr,
@@ -422,6 +423,7 @@ nyxpm_status mixed_solve(Ctx& c, Box& b, int zero_guess, nyxpm_solve_info* info)
 
 nyxpm_status mixed_make_rhs(Ctx& c, Box& b, double a);
 nyxpm_status mixed_grav32(Ctx& c, Box& b);  // FP32 gravity vector of the FP64 phi
+nyxpm_status mixed_g32_from_g(Ctx& c, Box& b);  // FP32 gravity vector of the FP64 g
 nyxpm_status mixed_rho_to_double(Ctx& c, Box& b);
 
 // host-side helpers shared by the forms

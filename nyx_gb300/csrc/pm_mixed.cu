@@ -1027,6 +1027,15 @@ __global__ void k_mx_grav(LevelView L, float half_dxi, float* g)
                                                   (float)(P(i, j, kp) - P(i, j, km)) * half_dxi, 0.f);
 }
 
+// a caller's FP64 gravity vector (3 n^3, component-major) as the kicks' float4 per cell
+__global__ void k_mx_g32_from_g(long long nc, const double* __restrict__ g, float* g32)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    reinterpret_cast<float4*>(g32)[c] =
+        make_float4((float)g[c], (float)g[nc + c], (float)g[2 * nc + c], 0.f);
+}
+
 // ---------------------------------------------------------------------------
 // FP32 CIC interpolation + kick (+ drift in cell units with re-binning)
 // ---------------------------------------------------------------------------
@@ -1472,6 +1481,15 @@ nyxpm_status mixed_grav32(Ctx& c, Box& b)
     k_mx_grav<<<g.grid, g.block, 0, c.stream>>>(view(b.levels[0]), (float)(0.5 * b.dxi), b.g32);
     prof_end(c, NYXPM_ST_KICK, 20.0 * nc);
     return check_launch(c, "mixed grav");
+}
+
+nyxpm_status mixed_g32_from_g(Ctx& c, Box& b)
+{
+    const long long nc = (long long)b.n * b.n * b.n;
+    prof_begin(c);
+    k_mx_g32_from_g<<<blocks_for(nc), kThreads, 0, c.stream>>>(nc, b.g, b.g32);
+    prof_end(c, NYXPM_ST_KICK, 40.0 * nc);
+    return check_launch(c, "mixed caller gravity");
 }
 
 nyxpm_status mixed_solve(Ctx& c, Box& b, int zero_guess, nyxpm_solve_info* info)

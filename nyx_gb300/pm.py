@@ -255,6 +255,23 @@ class Box:
         self._c(self.ctx.lib.nyxpm_grav_vector, _ptr(g), what="grav_vector")
         return g
 
+    def set_grav_vector(self, g):
+        """The caller's acceleration for the next kicks (nyxpm_set_grav_vector): 3 n^3
+        values, component-major, x fastest -- a numpy array (host memory) or any object
+        with ``data_ptr()`` and ``is_cuda`` true (device memory on the context's device,
+        e.g. a torch tensor), float64 and contiguous."""
+        count = 3 * self.n ** 3
+        if getattr(g, "is_cuda", False) and hasattr(g, "data_ptr"):
+            if g.numel() != count or str(g.dtype) != "torch.float64" or not g.is_contiguous():
+                raise ValueError(f"device g must be {count} contiguous float64 values")
+            self._c(self.ctx.lib.nyxpm_set_grav_vector, C.c_void_p(g.data_ptr()), 1,
+                    what="set_grav_vector")
+            return
+        garr = _f64(np.asarray(g).reshape(-1))
+        if garr.size != count:
+            raise ValueError(f"g must hold {count} values (3 n^3)")
+        self._c(self.ctx.lib.nyxpm_set_grav_vector, _ptr(garr), 0, what="set_grav_vector")
+
     def kick_drift(self, dt, a_old, a_half):
         self._c(self.ctx.lib.nyxpm_kick_drift, float(dt), float(a_old), float(a_half), what="kick_drift")
 
@@ -433,21 +450,23 @@ class DarkMatterParticleContainer:
 
     def moveKickDrift(self, acceleration=None, lev: int = 0, dt: float = 0.0, a_old: float = 1.0,
                       a_half: float = 1.0, where_width: int = 0):
-        """Kick by dt/2 with the CIC-interpolated field of the current phi, then drift by dt.
-        ``acceleration`` is the box's own field (the gradient is fused); passing an array is
-        not supported because the field never leaves the device."""
-        if acceleration is not None:
-            raise NyxPMError(1, "moveKickDrift uses the box's own field; pass acceleration=None")
+        """Kick by dt/2 with the CIC-interpolated acceleration, then drift by dt.
+        ``acceleration`` is the caller's cell-centred field (3 n^3 values, component-major,
+        x fastest; host array or device tensor), as the reference's ``acc`` MultiFab; None
+        kicks with the box's own gravity vector, kept in step with phi on the device."""
         if lev != 0:
             raise NyxPMError(1, "single level only")
+        if acceleration is not None:
+            self.box.set_grav_vector(acceleration)
         self.box.kick_drift(dt, a_old, a_half)
 
     def moveKick(self, acceleration=None, lev: int = 0, dt: float = 0.0, a_new: float = 1.0,
                  a_half: float = 1.0):
-        if acceleration is not None:
-            raise NyxPMError(1, "moveKick uses the box's own field; pass acceleration=None")
+        """Kick by dt/2 with the CIC-interpolated acceleration (see moveKickDrift)."""
         if lev != 0:
             raise NyxPMError(1, "single level only")
+        if acceleration is not None:
+            self.box.set_grav_vector(acceleration)
         self.box.kick(dt, a_new, a_half)
 
     def AssignDensitySingleLevel(self, mf=None, lev: int = 0, ncomp: int = 1,
@@ -474,12 +493,12 @@ class DarkMatterParticleContainer:
         self.box.redistribute()
 
     def estTimestep(self, acceleration=None, a: float = 1.0, lev: int = 0, cfl: float = 0.5) -> float:
-        """NyxParticleContainer::estTimestep (NyxParticleContainer.H:329-465) with the box's
-        own gravity vector."""
-        if acceleration is not None:
-            raise NyxPMError(1, "estTimestep uses the box's own field; pass acceleration=None")
+        """NyxParticleContainer::estTimestep (NyxParticleContainer.H:329-465) with the
+        caller's acceleration (as in moveKickDrift) or, for None, the box's own gravity vector."""
         if lev != 0:
             raise NyxPMError(1, "single level only")
+        if acceleration is not None:
+            self.box.set_grav_vector(acceleration)
         return self.box.est_time_step(cfl, a)
 
     def sumParticleMass(self, lev: int = 0) -> float:

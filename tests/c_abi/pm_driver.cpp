@@ -3,11 +3,18 @@
 // particles, the post_init solve, then PM steps with dt from computeNewDt;
 // finally the particle state is written as an AsciiFile.
 //
+// A second mode kicks with an acceleration the caller computed, as a Nyx shim
+// hands moveKickDrift the acc MultiFab of its own Gravity object: upload, the
+// field from a raw float64 file (3 n^3 values, component-major, x fastest) by
+// nyxpm_set_grav_vector, one moveKickDrift, then the AsciiFile out.
+//
 // usage: pm_driver <in.ascii> <n> <L> <a0> <steps> <out.ascii>
+//        pm_driver kick <in.ascii> <n> <L> <acc.f64> <dt> <a_old> <a_half> <out.ascii>
 #include "nyxpm.h"
 
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <vector>
 
 static int check(nyxpm_ctx* c, nyxpm_status st, const char* what)
@@ -17,10 +24,71 @@ static int check(nyxpm_ctx* c, nyxpm_status st, const char* what)
     return 1;
 }
 
+static int read_particles(const char* in, std::vector<double>& pos, std::vector<double>& vel,
+                          std::vector<double>& mass, int64_t* np)
+{
+    char err[256];
+    if (nyxpm_particle_file_count(in, NYXPM_FILE_ASCII, np, err, sizeof(err)) != NYXPM_OK) {
+        std::fprintf(stderr, "%s\n", err);
+        return 1;
+    }
+    pos.resize(3 * *np);
+    vel.resize(3 * *np);
+    mass.resize(*np);
+    int64_t got = 0;
+    if (nyxpm_particle_file_read(in, NYXPM_FILE_ASCII, *np, pos.data(), vel.data(), mass.data(), &got,
+                                 err, sizeof(err)) != NYXPM_OK) {
+        std::fprintf(stderr, "%s\n", err);
+        return 1;
+    }
+    return 0;
+}
+
+static int kick_with_callers_field(char** argv)
+{
+    const int n = std::atoi(argv[3]);
+    const double L = std::atof(argv[4]);
+    const double dt = std::atof(argv[6]), a_old = std::atof(argv[7]), a_half = std::atof(argv[8]);
+    std::vector<double> pos, vel, mass;
+    int64_t np = 0;
+    if (read_particles(argv[2], pos, vel, mass, &np)) return 1;
+    const size_t count = 3 * (size_t)n * n * n;
+    std::vector<double> acc(count);
+    FILE* f = std::fopen(argv[5], "rb");
+    if (!f || std::fread(acc.data(), sizeof(double), count, f) != count) {
+        std::fprintf(stderr, "cannot read %zu doubles from %s\n", count, argv[5]);
+        if (f) std::fclose(f);
+        return 1;
+    }
+    std::fclose(f);
+    nyxpm_params p;
+    nyxpm_default_params(&p);
+    nyxpm_ctx* c = nullptr;
+    if (check(nullptr, nyxpm_create(&p, &c), "nyxpm_create")) return 1;
+    nyxpm_box* b = nullptr;
+    if (check(c, nyxpm_box_create(c, n, L, np, NYXPM_FP64, &b), "nyxpm_box_create")) return 1;
+    if (check(c, nyxpm_box_upload(c, b, pos.data(), vel.data(), nullptr, mass[0]), "upload")) return 1;
+    if (check(c, nyxpm_set_grav_vector(c, b, acc.data(), 0), "nyxpm_set_grav_vector")) return 1;
+    if (check(c, nyxpm_kick_drift(c, b, dt, a_old, a_half), "nyxpm_kick_drift")) return 1;
+    if (check(c, nyxpm_box_download(c, b, pos.data(), vel.data()), "download")) return 1;
+    char err[256];
+    if (nyxpm_particle_file_write(argv[9], NYXPM_FILE_ASCII, np, pos.data(), vel.data(), nullptr, mass[0],
+                                  err, sizeof(err)) != NYXPM_OK) {
+        std::fprintf(stderr, "%s\n", err);
+        return 1;
+    }
+    nyxpm_box_destroy(c, b);
+    nyxpm_destroy(c);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
+    if (argc == 10 && std::strcmp(argv[1], "kick") == 0) return kick_with_callers_field(argv);
     if (argc != 7) {
-        std::fprintf(stderr, "usage: %s in.ascii n L a0 steps out.ascii\n", argv[0]);
+        std::fprintf(stderr, "usage: %s in.ascii n L a0 steps out.ascii\n"
+                             "       %s kick in.ascii n L acc.f64 dt a_old a_half out.ascii\n",
+                     argv[0], argv[0]);
         return 2;
     }
     const char* in = argv[1];
@@ -30,17 +98,8 @@ int main(int argc, char** argv)
     const int steps = std::atoi(argv[5]);
     char err[256];
     int64_t np = 0;
-    if (nyxpm_particle_file_count(in, NYXPM_FILE_ASCII, &np, err, sizeof(err)) != NYXPM_OK) {
-        std::fprintf(stderr, "%s\n", err);
-        return 1;
-    }
-    std::vector<double> pos(3 * np), vel(3 * np), mass(np);
-    int64_t got = 0;
-    if (nyxpm_particle_file_read(in, NYXPM_FILE_ASCII, np, pos.data(), vel.data(), mass.data(), &got,
-                                 err, sizeof(err)) != NYXPM_OK) {
-        std::fprintf(stderr, "%s\n", err);
-        return 1;
-    }
+    std::vector<double> pos, vel, mass;
+    if (read_particles(in, pos, vel, mass, &np)) return 1;
     nyxpm_params p;
     nyxpm_default_params(&p);
     nyxpm_ctx* c = nullptr;

@@ -66,3 +66,31 @@ def test_driver_result_equals_python_path(ctx, tmp_path):
     ppos, pvel = box.download()
     assert np.array_equal(cpos, ppos) and np.array_equal(cvel, pvel)
     box.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no GPU")
+def test_driver_kicks_with_the_callers_acceleration(tmp_path):
+    """moveKickDrift with a caller-owned acc (DarkMatterParticleContainer.cpp:76-112):
+    the C++ caller hands the oracle's gravity vector over with nyxpm_set_grav_vector
+    and kicks; the result equals the oracle's update_dm_particle_single bit for bit."""
+    from oracle import oracle as O
+    exe = build_driver(str(tmp_path))
+    n, L = 16, 1.0
+    ic = config1_ics(n, seed=12)
+    rng = np.random.default_rng(3)
+    g = rng.standard_normal(3 * n ** 3) * 50.0
+    inp, out = str(tmp_path / "in.ascii"), str(tmp_path / "out.ascii")
+    accf = str(tmp_path / "acc.f64")
+    write_particle_file(inp, ic.pos, ic.vel, ic.mass)
+    g.astype("<f8").tofile(accf)
+    dt, a_old, a_half = 2.0e-4, 0.031, 0.0335
+    r = subprocess.run([exe, "kick", inp, str(n), str(L), accf, f"{dt:.17g}", f"{a_old:.17g}",
+                        f"{a_half:.17g}", out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    cpos, cvel, _ = read_particle_file(out)
+    pos, vel, _ = read_particle_file(inp)
+    p = O.Particles(pos, vel, ic.mass)
+    O.move(n, L, p, g, dt, a_old, a_half, 1)
+    opos, ovel = p.by_id()
+    assert np.array_equal(cpos, opos) and np.array_equal(cvel, ovel)

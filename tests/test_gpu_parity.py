@@ -89,6 +89,59 @@ def test_solve_grav_and_kicks_match_oracle(ctx):
     compare_particles(b, p, 1.0)
 
 
+def test_kicks_with_the_callers_acceleration(ctx):
+    """moveKickDrift / moveKick take a caller-owned acc MultiFab
+    (DarkMatterParticleContainer.cpp:76-112, 184-247): an acceleration computed
+    outside the box (here the oracle's gravity vector of a displaced state, and a
+    random field) is handed over from host memory and from device memory, and the
+    kicks equal the oracle's update_dm_particle_single bit for bit.  The mixed form
+    kicks with the same field rounded to FP32, within 1e-6."""
+    import torch
+    from nyx_gb300.pm import DarkMatterParticleContainer
+    n, L, a = 32, 1.0, 0.03
+    ic = config1_ics(n, seed=5)
+    # a field that is not the box's own: the oracle's from other particles
+    other = config1_ics(n, seed=6)
+    _, phi_o, _ = oracle_field(n, L, O.Particles(other.pos, other.vel, other.mass), a)
+    g_o = O.grav_vector(n, L, phi_o)
+    g_r = np.random.default_rng(7).standard_normal(3 * n ** 3) * float(np.abs(g_o).max())
+    dt, a_half, a_new = 2e-4, 0.0305, 0.031
+    for g, on_device in ((g_o, False), (g_r, True)):
+        b = make_box(ctx, n, L, ic.pos, ic.vel, ic.mass)
+        dm = DarkMatterParticleContainer(b)
+        acc = torch.from_numpy(g).cuda() if on_device else g.reshape(3, n, n, n)
+        dm.moveKickDrift(acc, 0, dt, a, a_half)
+        torch.cuda.synchronize()
+        p = O.Particles(ic.pos, ic.vel, ic.mass)
+        O.move(n, L, p, g, dt, a, a_half, 1)
+        gpos, gvel = b.download()
+        opos, ovel = p.by_id()
+        assert np.array_equal(gpos, opos) and np.array_equal(gvel, ovel)
+        dm.moveKick(None, 0, dt, a_new, a_half)   # the same field stays in place
+        O.move(n, L, p, g, dt, a_half, a_new, 0)
+        gpos, gvel = b.download()
+        opos, ovel = p.by_id()
+        assert np.array_equal(gpos, opos) and np.array_equal(gvel, ovel)
+        assert np.array_equal(b.grav_vector(), g)
+        # a solve replaces the caller's field by the box's own
+        b.deposit(read_back=False)
+        b.solve_phi(a, zero_guess=True)
+        assert not np.array_equal(b.grav_vector(), g)
+        b.close()
+    bm = Box(ctx, n, L, len(ic.pos), precision="mixed")
+    bm.upload(ic.pos, ic.vel, ic.mass)
+    bm.set_grav_vector(g_o)
+    bm.kick_drift(dt, a, a_half)
+    p = O.Particles(ic.pos, ic.vel, ic.mass)
+    O.move(n, L, p, g_o, dt, a, a_half, 1)
+    gpos, gvel = bm.download()
+    opos, ovel = p.by_id()
+    dv = rel_l2(gvel, ovel)
+    dx_cells = float(np.abs(min_image(gpos - opos, L)).max()) * n / L
+    assert dv <= 1e-6 and dx_cells <= 1e-6, (dv, dx_cells)
+    bm.close()
+
+
 @pytest.mark.parametrize("reuse", [False, True])
 def test_config1_step_by_step(ctx, reuse):
     """Plain PM 64^3, a 0.02 -> 0.05 in 10 equal-da steps; every GPU step starts

@@ -425,12 +425,16 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* ctx, nyxpm_ensemble* ens, const doub
  * counting-sort scratch is a file-scope device array of about 10 MiB that every
  * GPU loading this library holds until the process exits.  Limits: n <= 64 and
  * np <= 262,144; larger problems return NYXPM_INVALID_ARG (use nyxpm_deposit).
- * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU (other
- * streams, other host threads) race and must be ordered by the caller.  The
- * result equals nyxpm_deposit's for the same particles in the same order, bit
- * for bit.  errbuf (may be NULL) receives a message on failure. */
+ * Each call on a stream that is not capturing looks up the array's device
+ * address on the current device (a device reset may move it); a call on a
+ * capturing stream uses the address the last such call found, so make one call
+ * on the device before any stream capture.  The call returns once the stream has
+ * finished the deposit: it reads back a count of non-finite positions, and
+ * refuses such input with NYXPM_INVALID_ARG (rho then holds no valid density),
+ * as nyxpm_deposit does.  All calls share the one array: calls that overlap on
+ * the GPU (other streams, other host threads) race and must be ordered by the
+ * caller.  The result equals nyxpm_deposit's for the same particles in the same
+ * order, bit for bit.  errbuf (may be NULL) receives a message on failure. */
 nyxpm_status nyxpm_deposit_noalloc(const double* x, const double* y, const double* z, int64_t np,
                                    double mass, int n, double L, double* rho, void* stream,
                                    char* errbuf, size_t errlen);

@@ -15,6 +15,8 @@
 //
 // The arithmetic (key, sort order, per-key partial sums, cell sums) is that of
 // nyxpm_deposit for uniform masses, so both give the same density bit for bit.
+// Like nyxpm_deposit it refuses non-finite positions: the key pass counts them,
+// and the call reads the count back before it returns.
 // Built with --fmad=false like the other FP64 units.
 #include "pm_common.cuh"
 
@@ -53,10 +55,14 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 unsigned char* g_scratch_addr[kMaxDevices] = {};
+int g_sm_count[kMaxDevices] = {};
 
-// the device address of the scratch on the current device; looked up once per
-// device (the host-side name of the array is not a device address)
-nyxpm_status scratch_address(unsigned char** out, char* errbuf, size_t errlen)
+// The device address of the scratch on the current device (the host-side name
+// of the array is not a device address).  It is looked up again on every call
+// whose stream is not capturing -- a device reset reloads the module and may
+// move the array -- and the last address found is used while a capture runs.
+nyxpm_status scratch_address(cudaStream_t stream, unsigned char** out, int* sm_count,
+                             char* errbuf, size_t errlen)
 {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
@@ -64,8 +70,13 @@ nyxpm_status scratch_address(unsigned char** out, char* errbuf, size_t errlen)
         if (errbuf && errlen) std::snprintf(errbuf, errlen, "no current CUDA device");
         return NYXPM_NO_DEVICE;
     }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusNone;
+    }
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
+    if (!g_scratch_addr[dev] || cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -76,8 +87,15 @@ nyxpm_status scratch_address(unsigned char** out, char* errbuf, size_t errlen)
             return NYXPM_CUDA_ERROR;
         }
         g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            sms = 1;
+        }
+        g_sm_count[dev] = sms > 0 ? sms : 1;
     }
     *out = g_scratch_addr[dev];
+    *sm_count = g_sm_count[dev];
     return NYXPM_OK;
 }
 
@@ -95,15 +113,21 @@ __global__ void na_zero(int* a, long long cnt)
     if (t < cnt) a[t] = 0;
 }
 
+// A non-finite coordinate is counted in *bad (the call then refuses the input);
+// its key is still a valid cell (the float-to-int conversion saturates and a NaN
+// converts to 0), so no access leaves the arrays.
 __global__ void na_keys(long long np, int n, double dxi, const double* __restrict__ x,
-                        const double* __restrict__ y, const double* __restrict__ z, int* key, int* count)
+                        const double* __restrict__ y, const double* __restrict__ z, int* key, int* count,
+                        int* bad)
 {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
+    const double px = x[q], py = y[q], pz = z[q];
+    if (!(isfinite(px) && isfinite(py) && isfinite(pz))) atomicAdd(bad, 1);
     double f;
-    const int i = na_key1(x[q], dxi, n, &f);
-    const int j = na_key1(y[q], dxi, n, &f);
-    const int k = na_key1(z[q], dxi, n, &f);
+    const int i = na_key1(px, dxi, n, &f);
+    const int j = na_key1(py, dxi, n, &f);
+    const int k = na_key1(pz, dxi, n, &f);
     const int K = (int)cidx(i, j, k, n);
     key[q] = K;
     atomicAdd(count + K, 1);
@@ -207,36 +231,35 @@ __global__ void na_fix_short(int nc, const int* __restrict__ start, int* perm, i
         long_list[atomicAdd(long_count, 1)] = K;
         return;
     }
-    int v[32];
-#pragma unroll
-    for (int t = 0; t < 32; ++t)
-        if (t < len) v[t] = perm[s + t];
-    for (int a = 1; a < len; ++a) {
-        const int cur = v[a];
-        int b = a - 1;
-        while (b >= 0 && v[b] > cur) {
-            v[b + 1] = v[b];
-            --b;
-        }
-        v[b + 1] = cur;
-    }
-#pragma unroll
-    for (int t = 0; t < 32; ++t)
-        if (t < len) perm[s + t] = v[t];
+    sort_short_segment(perm, s, len);
 }
+
+// Long segments: a rank sort by one block per segment (the values are distinct).
+// A segment of up to kNaLongSmem entries is ranked from shared memory; a longer
+// one (every particle in a few cells) from global memory.
+constexpr int kNaLongSmem = 12288;
 
 __global__ void na_fix_long(const int* __restrict__ start, const int* __restrict__ long_list,
                             const int* __restrict__ long_count, int* perm, int* tmp)
 {
+    __shared__ int sv[kNaLongSmem];
     const int total = *long_count;
     for (int li = blockIdx.x; li < total; li += gridDim.x) {
         const int K = long_list[li];
         const int s = start[K], len = start[K + 1] - s;
+        const bool in_smem = len <= kNaLongSmem;
+        __syncthreads();
+        if (in_smem)
+            for (int t = threadIdx.x; t < len; t += blockDim.x) sv[t] = perm[s + t];
         __syncthreads();
         for (int t = threadIdx.x; t < len; t += blockDim.x) {
-            const int v = perm[s + t];
+            const int v = in_smem ? sv[t] : perm[s + t];
             int rank = 0;
-            for (int u = 0; u < len; ++u) rank += perm[s + u] < v;
+            if (in_smem) {
+                for (int u = 0; u < len; ++u) rank += sv[u] < v;
+            } else {
+                for (int u = 0; u < len; ++u) rank += perm[s + u] < v;
+            }
             tmp[s + rank] = v;
         }
         __syncthreads();
@@ -372,13 +395,15 @@ extern "C" nyxpm_status nyxpm_deposit_noalloc(const double* d_x, const double* d
     if (!(L > 0) || !std::isfinite(L)) return fail(NYXPM_INVALID_ARG, "box length must be positive");
     if (!(mass >= 0) || !std::isfinite(mass)) return fail(NYXPM_INVALID_ARG, "mass must be finite, >= 0");
     unsigned char* base = nullptr;
-    const nyxpm_status st = scratch_address(&base, errbuf, errlen);
-    if (st != NYXPM_OK) return st;
+    int sm_count = 1;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const nyxpm_status st = scratch_address(s, &base, &sm_count, errbuf, errlen);
+    if (st != NYXPM_OK) return st;
     int* count = reinterpret_cast<int*>(base + kOffCount);
     int* start = reinterpret_cast<int*>(base + kOffStart);
     int* tiles = reinterpret_cast<int*>(base + kOffTiles);
     int* long_count = reinterpret_cast<int*>(base + kOffLongCount);
+    int* bad = long_count + 1;   // non-finite positions seen
     int* long_list = reinterpret_cast<int*>(base + kOffLongList);
     int* key = reinterpret_cast<int*>(base + kOffKey);
     int* perm = reinterpret_cast<int*>(base + kOffPerm);
@@ -392,17 +417,17 @@ extern "C" nyxpm_status nyxpm_deposit_noalloc(const double* d_x, const double* d
     const unsigned pb = (unsigned)((np + 255) / 256);
     const unsigned cb = (unsigned)((nc + 255) / 256);
     const int ntiles = (nc + kNaScanTile - 1) / kNaScanTile;
-    // the counts and the long-segment counter must start at zero: the array keeps
-    // whatever the previous call (or an interrupted one) left in it
+    // the counts, the long-segment counter and the non-finite count must start at
+    // zero: the array keeps whatever the previous call (or an interrupted one) left
     na_zero<<<cb, 256, 0, s>>>(count, nc);
-    na_zero<<<1, 32, 0, s>>>(long_count, 1);
-    na_keys<<<pb, 256, 0, s>>>(np, n, dxi, d_x, d_y, d_z, key, count);
+    na_zero<<<1, 32, 0, s>>>(long_count, 2);
+    na_keys<<<pb, 256, 0, s>>>(np, n, dxi, d_x, d_y, d_z, key, count, bad);
     na_scan_reduce<<<ntiles, kNaScanT, 0, s>>>(count, nc, tiles);
     na_scan_top<<<1, 1024, 0, s>>>(tiles, ntiles);
     na_scan_down<<<ntiles, kNaScanT, 0, s>>>(count, nc, tiles, start);
     na_scatter<<<pb, 256, 0, s>>>(np, key, start, count, perm);
     na_fix_short<<<cb, 256, 0, s>>>(nc, start, perm, long_list, long_count);
-    na_fix_long<<<64, 256, 0, s>>>(start, long_list, long_count, perm, key);
+    na_fix_long<<<2 * sm_count, 512, 0, s>>>(start, long_list, long_count, perm, key);
     na_gather<<<pb, 256, 0, s>>>(np, perm, d_x, d_y, d_z, xs, ys, zs);
     const dim3 grid((n + kTx - 1) / kTx, (n + kTy - 1) / kTy, (n + kTz - 1) / kTz);
     na_deposit<<<grid, 256, 0, s>>>(n, dxi, scale, xs, ys, zs, start, d_rho);
@@ -411,5 +436,17 @@ extern "C" nyxpm_status nyxpm_deposit_noalloc(const double* d_x, const double* d
         if (errbuf && errlen) std::snprintf(errbuf, errlen, "kernel launch failed: %s", cudaGetErrorString(e));
         return NYXPM_CUDA_ERROR;
     }
+    // refuse non-finite positions as nyxpm_deposit does: read the count back
+    // (into a host variable, no allocation), which waits for the stream
+    int h_bad = 0;
+    const cudaError_t ec = cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    const cudaError_t es = ec == cudaSuccess ? cudaStreamSynchronize(s) : ec;
+    if (es != cudaSuccess) {
+        cudaGetLastError();
+        if (errbuf && errlen) std::snprintf(errbuf, errlen, "deposit failed: %s", cudaGetErrorString(es));
+        return NYXPM_CUDA_ERROR;
+    }
+    if (h_bad != 0)
+        return fail(NYXPM_INVALID_ARG, "non-finite particle position (rho holds no valid density)");
     return NYXPM_OK;
 }

@@ -4,14 +4,15 @@ on a 1 x 32 x 32 slice) into tests/golden/vismf_slice_00340/.  They are AMReX Vi
 files written by AMReX itself: the golden input of the MultiFab reader and writer
 tests.  Run from the repository root:
 
-    python tests/golden/make_vismf_fixture.py [reference root]
+    python tests/golden/make_vismf_fixture.py <Nyx source tree>
 """
 import os
 import shutil
 import sys
 
-SRC = os.path.join(sys.argv[1] if len(sys.argv) > 1 else "/root/reference",
-                   "Util", "SliceUtils", "slice_00340")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_vismf_fixture.py <Nyx source tree>")
+SRC = os.path.join(sys.argv[1], "Util", "SliceUtils", "slice_00340")
 DST = os.path.join(os.path.dirname(os.path.abspath(__file__)), "vismf_slice_00340")
 
 os.makedirs(DST, exist_ok=True)

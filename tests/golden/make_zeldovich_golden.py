@@ -11,9 +11,9 @@ Two reference artefacts are used, both from Nyx's Zel'dovich pancake test
    parameter file and the first particles it writes are stored so that the
    tests can check their own IC construction against the reference generator.
 
-Run here (where the reference tree is mounted):
+Run with NYX_REFERENCE set to the Nyx source tree:
 
-    make -C oracle ref && python tests/golden/make_zeldovich_golden.py
+    make -C oracle ref REF=$NYX_REFERENCE && python tests/golden/make_zeldovich_golden.py
 """
 from __future__ import annotations
 
@@ -27,7 +27,9 @@ import tempfile
 
 import numpy as np
 
-REF = os.environ.get("NYX_REFERENCE", "/root/reference")
+REF = os.environ.get("NYX_REFERENCE", "")
+if not REF:
+    sys.exit("set NYX_REFERENCE to the Nyx source tree")
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 GEN = os.path.join(REPO, "oracle", "_ref", "generate_zeldovich_ics")

@@ -7,8 +7,9 @@ import pytest
 
 from nyx_gb300.inputs import read_inputs, run_config
 
-REF = os.environ.get("NYX_REFERENCE", "/root/reference")
-NOHYDRO = os.path.join(REF, "Exec", "LyA", "inputs_nohydro.rt")
+from tests.conftest import reference_file
+
+NOHYDRO = reference_file("Exec", "LyA", "inputs_nohydro.rt")
 
 
 def test_syntax_comments_quotes_and_overrides(tmp_path):
@@ -65,7 +66,7 @@ def test_cosmological_init_type(tmp_path):
             run_config(d, str(tmp_path))
 
 
-@pytest.mark.skipif(not os.path.exists(NOHYDRO), reason="reference tree not mounted")
+@pytest.mark.skipif(NOHYDRO is None, reason="NYX_REFERENCE (the Nyx source tree) not set")
 def test_the_references_dm_only_inputs():
     cfg = run_config(read_inputs(NOHYDRO), os.path.dirname(NOHYDRO))
     assert (cfg.n, cfg.L) == (32, 8.0)
@@ -75,4 +76,5 @@ def test_the_references_dm_only_inputs():
     assert os.path.exists(cfg.particle_file)
     assert (cfg.rel_tol, cfg.cfl, cfg.change_max, cfg.relative_max_change_a) == (1e-12, 0.5, 1.1, 0.01)
     with pytest.raises(ValueError, match="do_hydro"):
-        run_config(read_inputs(os.path.join(REF, "Exec", "LyA", "inputs")), REF)
+        run_config(read_inputs(os.path.join(os.path.dirname(NOHYDRO), "inputs")),
+                   os.path.dirname(NOHYDRO))

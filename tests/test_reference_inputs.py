@@ -1,5 +1,5 @@
-"""The reference's own particle input files, read where the reference tree is
-mounted (skipped elsewhere):
+"""The reference's own particle input files, read from the Nyx source tree that
+NYX_REFERENCE names (skipped without it):
 
 * Exec/LyA/32.nyx, the BinaryFile IC of Exec/LyA/inputs_nohydro.rt (32^3
   particles in an 8 Mpc box at z = 100).  It holds float64 records, and the
@@ -23,11 +23,13 @@ import pytest
 from nyx_gb300.pm import read_particle_file, uniform_mass
 from oracle import oracle as O
 
-REF = os.environ.get("NYX_REFERENCE", "/root/reference")
-LYA_IC = os.path.join(REF, "Exec", "LyA", "32.nyx")
-POT = os.path.join(REF, "Exec", "ParticleOnlyTest")
+from tests.conftest import reference_file
 
-needs_ref = pytest.mark.skipif(not os.path.exists(LYA_IC), reason="reference tree not mounted")
+LYA_IC = reference_file("Exec", "LyA", "32.nyx")
+POT = os.path.dirname(reference_file("Exec", "ParticleOnlyTest", "particle_file.mass") or "")
+
+needs_ref = pytest.mark.skipif(LYA_IC is None or not POT,
+                               reason="NYX_REFERENCE (the Nyx source tree) not set")
 
 
 def numpy_binary(path):

@@ -68,3 +68,51 @@ def test_noalloc_deposit_equals_allocating_deposit_twice():
                                    C.c_void_p(rho.data_ptr()), C.c_void_p(stream), err, len(err))
     assert st == 1 and b"64" in err.value
     ctx.close()
+
+
+@pytest.mark.skipif(not gpu_available(), reason="no GPU")
+def test_noalloc_deposit_other_length_own_stream_no_device_memory_taken():
+    """A box of side 7.5 (dx and the density scale not powers of two) on a stream
+    the caller created: equal to the allocating deposit bit for bit on two calls
+    in a row, and the calls after the first take no device memory (free bytes
+    unchanged).  A non-finite position is refused, as nyxpm_deposit refuses it."""
+    import torch
+    from nyx_gb300 import _lib
+    from nyx_gb300.ics import zeldovich_ics
+    from nyx_gb300.pm import Box, Context
+
+    lib = _lib.load()
+    ctx = Context(device=0)
+    err = C.create_string_buffer(256)
+    L, n, mass = 7.5, 40, 1.7e10
+    pos = zeldovich_ics(n, L, -2.0, 21, 0.05, rms_disp_cells=0.5).pos
+    box = Box(ctx, n, L, len(pos))
+    box.upload(pos, np.zeros_like(pos), mass)
+    expect = box.deposit()
+    box.close()
+    x, y, z, rho = _device_arrays(torch, pos, n)
+    side = torch.cuda.Stream(device=0)
+    torch.cuda.synchronize()
+
+    def call(xp=x):
+        return lib.nyxpm_deposit_noalloc(C.c_void_p(xp.data_ptr()), C.c_void_p(y.data_ptr()),
+                                         C.c_void_p(z.data_ptr()), len(pos), mass, n, L,
+                                         C.c_void_p(rho.data_ptr()), C.c_void_p(side.cuda_stream),
+                                         err, len(err))
+
+    assert call() == 0, err.value.decode()        # the first call sets up the device
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    for _ in range(2):
+        rho.fill_(float("nan"))
+        torch.cuda.synchronize()
+        assert call() == 0, err.value.decode()
+        side.synchronize()
+        assert np.array_equal(rho.cpu().numpy(), expect)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(0)[0] == free0
+    bad = x.clone()
+    bad[len(pos) // 2] = float("nan")
+    torch.cuda.synchronize()
+    assert call(bad) == 1 and b"non-finite" in err.value
+    ctx.close()

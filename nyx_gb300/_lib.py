@@ -30,7 +30,7 @@ EXPORTS = [
     "nyxpm_get_phi", "nyxpm_set_phi", "nyxpm_grav_vector", "nyxpm_set_grav_vector",
     "nyxpm_kick_drift", "nyxpm_kick",
     "nyxpm_step", "nyxpm_step_host", "nyxpm_init_field", "nyxpm_integrate_a", "nyxpm_dt_for_da",
-    "nyxpm_set_profiling", "nyxpm_get_profile", "nyxpm_launch_count",
+    "nyxpm_set_profiling", "nyxpm_get_profile", "nyxpm_launch_count", "nyxpm_measure_fp64_peak",
     "nyxpm_ensemble_create", "nyxpm_ensemble_destroy", "nyxpm_ensemble_box_bytes",
     "nyxpm_ensemble_arena_used", "nyxpm_ensemble_add", "nyxpm_ensemble_remove",
     "nyxpm_ensemble_upload", "nyxpm_ensemble_download", "nyxpm_ensemble_get_phi",
@@ -208,6 +208,7 @@ def load(path: str | None = None):
     L.nyxpm_get_profile.argtypes = [vp, C.POINTER(Profile), C.c_int]
     L.nyxpm_launch_count.argtypes = [vp]
     L.nyxpm_launch_count.restype = i64
+    L.nyxpm_measure_fp64_peak.argtypes = [vp, C.POINTER(d)]
     dp = C.POINTER(C.c_double)
     L.nyxpm_ensemble_create.argtypes = [vp, C.c_size_t, C.POINTER(vp)]
     L.nyxpm_ensemble_destroy.argtypes = [vp, vp]

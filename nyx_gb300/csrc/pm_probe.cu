@@ -1,0 +1,84 @@
+// Measured FP64 issue rate of this GPU, the denominator of the FP64 roofline.
+//
+// The FP64 form of the PM step is bound by the FP64 pipe, not by HBM: GB300
+// issues FP64 at a small fraction of its FP32 rate.  Its achieved FP64 rate is
+// reported against the rate this probe measures on the same GPU: every thread
+// runs eight independent chains of dependent FP64 fused multiply-adds, enough
+// threads to fill every SM, timed with CUDA events on the context's stream.
+// The chains converge (a -> a b + c with 0 < b < 1), so no value overflows or
+// turns subnormal; the sum is stored only if it equals a value it never takes,
+// which keeps the compiler from removing the work without a store per thread.
+#include "pm_common.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace nyxpm {
+
+namespace {
+
+constexpr int kProbeChains = 8;
+constexpr int kProbeThreads = 256;
+constexpr int kProbeBlocksPerSm = 4;
+
+__device__ double g_probe_sink;
+
+__global__ void __launch_bounds__(kProbeThreads) k_fp64_fma_probe(int iters, double b, double c,
+                                                                   double never)
+{
+    double a[kProbeChains];
+#pragma unroll
+    for (int t = 0; t < kProbeChains; ++t) a[t] = 1e-3 * (threadIdx.x + t);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int t = 0; t < kProbeChains; ++t) a[t] = fma(a[t], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int t = 0; t < kProbeChains; ++t) s = s + a[t];
+    if (s == never) g_probe_sink = s;
+}
+
+}  // namespace
+
+}  // namespace nyxpm
+
+using namespace nyxpm;
+
+extern "C" nyxpm_status nyxpm_measure_fp64_peak(nyxpm_ctx* c, double* tflops)
+{
+    if (!c || !tflops) return NYXPM_INVALID_ARG;
+    cudaSetDevice(c->p.device);
+    const int blocks = std::max(1, c->sm_count) * kProbeBlocksPerSm;
+    const int iters = 8192;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        cudaGetLastError();
+        if (e0) cudaEventDestroy(e0);
+        c->err = "cudaEventCreate";
+        return NYXPM_CUDA_ERROR;
+    }
+    float best = 0.f;
+    nyxpm_status st = NYXPM_OK;
+    for (int rep = 0; rep < 4 && st == NYXPM_OK; ++rep) {   // the first run warms up
+        cudaEventRecord(e0, c->stream);
+        k_fp64_fma_probe<<<blocks, kProbeThreads, 0, c->stream>>>(iters, 0.999999, 1e-7, -1.0);
+        cudaEventRecord(e1, c->stream);
+        c->launches += 1;
+        st = check_launch(*c, "fp64 probe");
+        if (st == NYXPM_OK && cudaEventSynchronize(e1) != cudaSuccess) st = check_launch(*c, "fp64 probe");
+        float ms = 0.f;
+        if (st == NYXPM_OK && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0)
+            best = best == 0.f ? ms : std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != NYXPM_OK) return st;
+    if (!(best > 0)) {
+        c->err = "fp64 probe: no timing";
+        return NYXPM_CUDA_ERROR;
+    }
+    const double flops = 2.0 * kProbeChains * (double)iters * (double)blocks * kProbeThreads;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return NYXPM_OK;
+}

@@ -86,6 +86,12 @@ class Context:
     def launch_count(self) -> int:
         return int(self.lib.nyxpm_launch_count(self.handle))
 
+    def measure_fp64_peak(self) -> float:
+        """FP64 TFLOP/s this GPU sustains on FMA chains (nyxpm_measure_fp64_peak)."""
+        v = C.c_double(0)
+        self.check(self.lib.nyxpm_measure_fp64_peak(self.handle, C.byref(v)), "measure_fp64_peak")
+        return v.value
+
     def set_profiling(self, on: bool):
         self.check(self.lib.nyxpm_set_profiling(self.handle, 1 if on else 0), "set_profiling")
 

@@ -34,8 +34,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 GEN = os.path.join(REPO, "oracle", "_ref", "generate_zeldovich_ics")
 
-# lattice of the tests: n cells per dimension, one particle per cell centre
+# lattices of the tests: n cells per dimension, one particle per cell centre
+# (the 64 lattice is the resolution check's finer grid)
 N_LATTICE = 32
+N_LATTICE_FINE = 64
 Z_STOPS = [100.0, 50.0, 30.0, 20.0]
 N_SAMPLE = 256
 
@@ -72,14 +74,19 @@ def main():
     offset = params["offset"]
     H0 = params["H_0"]
     z_c = params["caustic_z"]
-    q = (np.arange(N_LATTICE) + 0.5) * (L / N_LATTICE)
-    stops = []
-    for z in Z_STOPS:
-        qq = q + offset
-        x = zel.perturbed_x(qq, z, z_c, k) - offset
-        v = zel.perturbed_v_x(qq, z, z_c, k, H0)
-        stops.append({"z": z, "a": float(zel.get_scale_factor(z)), "x": list(map(float, x)),
-                      "xdot": list(map(float, v))})
+    def lattice_stops(nl):
+        q = (np.arange(nl) + 0.5) * (L / nl)
+        stops = []
+        for z in Z_STOPS:
+            qq = q + offset
+            x = zel.perturbed_x(qq, z, z_c, k) - offset
+            v = zel.perturbed_v_x(qq, z, z_c, k, H0)
+            stops.append({"z": z, "a": float(zel.get_scale_factor(z)), "x": list(map(float, x)),
+                          "xdot": list(map(float, v))})
+        return q, stops
+
+    q, stops = lattice_stops(N_LATTICE)
+    q_fine, stops_fine = lattice_stops(N_LATTICE_FINE)
     out = {
         "source": "Exec/GravityTests/zeldovich_dm analysis/zeldovich.py + ics/generate_zeldovich_ics.cpp",
         "params": params,
@@ -88,6 +95,8 @@ def main():
         "n_lattice": N_LATTICE,
         "q": list(map(float, q)),
         "stops": stops,
+        "lattice_fine": {"n_lattice": N_LATTICE_FINE, "q": list(map(float, q_fine)),
+                         "stops": stops_fine},
     }
     with open(os.path.join(HERE, "zeldovich_pancake.json"), "w") as f:
         json.dump(out, f, indent=1)

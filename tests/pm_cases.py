@@ -70,14 +70,21 @@ def load_zeldovich():
         return json.load(f)
 
 
-def zeldovich_particles(d):
+def zeldovich_lattice(d, fine=False):
+    """(n, stops) of the golden's 32-lattice, or of its 64-lattice when fine."""
+    if fine:
+        return d["lattice_fine"]["n_lattice"], d["lattice_fine"]["stops"]
+    return d["n_lattice"], d["stops"]
+
+
+def zeldovich_particles(d, fine=False):
     """Particles of the pancake on the golden's lattice at its first stop (z=100):
     x from the reference's perturbed_x, velocity = perturbed_v_x * a (the
     generator's proper-velocity convention), mass from the critical density."""
     P = d["params"]
     L = P["box_length"]
-    n = d["n_lattice"]
-    s0 = d["stops"][0]
+    n, stops = zeldovich_lattice(d, fine)
+    s0 = stops[0]
     idx = np.arange(n)
     Z, Y, X = np.meshgrid(idx, idx, idx, indexing="ij")
     X, Y, Z = X.ravel(), Y.ravel(), Z.ravel()

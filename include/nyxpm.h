@@ -468,8 +468,8 @@ nyxpm_status nyxpm_get_profile(nyxpm_ctx* ctx, nyxpm_profile* out, int reset);
 int64_t nyxpm_launch_count(const nyxpm_ctx* ctx);
 /* The FP64 rate this GPU sustains, in TFLOP/s (a fused multiply-add counts as two
  * operations): chains of dependent FP64 FMAs filling every SM, timed with CUDA
- * events on the context's stream (best of three runs of about 10 ms after one
- * warm-up).  The denominator of the FP64 roofline of the FP64 form, whose
+ * events on the context's stream (the best over four launch shapes of three runs
+ * of about 10 ms, each shape after one warm-up run).  The denominator of the FP64 roofline of the FP64 form, whose
  * kernels are bound by the FP64 pipe.  No counterpart in the reference. */
 nyxpm_status nyxpm_measure_fp64_peak(nyxpm_ctx* ctx, double* tflops);
 

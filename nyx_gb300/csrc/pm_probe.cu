@@ -3,8 +3,9 @@
 // The FP64 form of the PM step is bound by the FP64 pipe, not by HBM: GB300
 // issues FP64 at a small fraction of its FP32 rate.  Its achieved FP64 rate is
 // reported against the rate this probe measures on the same GPU: every thread
-// runs eight independent chains of dependent FP64 fused multiply-adds, enough
-// threads to fill every SM, timed with CUDA events on the context's stream.
+// runs independent chains of dependent FP64 fused multiply-adds (8 or 16 chains,
+// 4 or 8 blocks of 256 threads per SM: the best of the four shapes), timed with
+// CUDA events on the context's stream.
 // The chains converge (a -> a b + c with 0 < b < 1), so no value overflows or
 // turns subnormal; the sum is stored only if it equals a value it never takes,
 // which keeps the compiler from removing the work without a store per thread.
@@ -17,25 +18,24 @@ namespace nyxpm {
 
 namespace {
 
-constexpr int kProbeChains = 8;
 constexpr int kProbeThreads = 256;
-constexpr int kProbeBlocksPerSm = 4;
 
 __device__ double g_probe_sink;
 
+template <int CHAINS>
 __global__ void __launch_bounds__(kProbeThreads) k_fp64_fma_probe(int iters, double b, double c,
                                                                    double never)
 {
-    double a[kProbeChains];
+    double a[CHAINS];
 #pragma unroll
-    for (int t = 0; t < kProbeChains; ++t) a[t] = 1e-3 * (threadIdx.x + t);
+    for (int t = 0; t < CHAINS; ++t) a[t] = 1e-3 * (threadIdx.x + t);
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
-        for (int t = 0; t < kProbeChains; ++t) a[t] = fma(a[t], b, c);
+        for (int t = 0; t < CHAINS; ++t) a[t] = fma(a[t], b, c);
     }
     double s = 0.0;
 #pragma unroll
-    for (int t = 0; t < kProbeChains; ++t) s = s + a[t];
+    for (int t = 0; t < CHAINS; ++t) s = s + a[t];
     if (s == never) g_probe_sink = s;
 }
 
@@ -49,8 +49,6 @@ extern "C" nyxpm_status nyxpm_measure_fp64_peak(nyxpm_ctx* c, double* tflops)
 {
     if (!c || !tflops) return NYXPM_INVALID_ARG;
     cudaSetDevice(c->p.device);
-    const int blocks = std::max(1, c->sm_count) * kProbeBlocksPerSm;
-    const int iters = 8192;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
         cudaGetLastError();
@@ -58,27 +56,37 @@ extern "C" nyxpm_status nyxpm_measure_fp64_peak(nyxpm_ctx* c, double* tflops)
         c->err = "cudaEventCreate";
         return NYXPM_CUDA_ERROR;
     }
-    float best = 0.f;
+    double best_rate = 0.0;
     nyxpm_status st = NYXPM_OK;
-    for (int rep = 0; rep < 4 && st == NYXPM_OK; ++rep) {   // the first run warms up
-        cudaEventRecord(e0, c->stream);
-        k_fp64_fma_probe<<<blocks, kProbeThreads, 0, c->stream>>>(iters, 0.999999, 1e-7, -1.0);
-        cudaEventRecord(e1, c->stream);
-        c->launches += 1;
-        st = check_launch(*c, "fp64 probe");
-        if (st == NYXPM_OK && cudaEventSynchronize(e1) != cudaSuccess) st = check_launch(*c, "fp64 probe");
-        float ms = 0.f;
-        if (st == NYXPM_OK && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0)
-            best = best == 0.f ? ms : std::min(best, ms);
+    for (int shape = 0; shape < 4 && st == NYXPM_OK; ++shape) {
+        const int chains = shape & 1 ? 16 : 8;
+        const int blocks = std::max(1, c->sm_count) * (shape & 2 ? 8 : 4);
+        // about the same work per shape (~10 ms at 1 TFLOP/s)
+        const int iters = (shape & 1 ? 4096 : 8192) / (shape & 2 ? 2 : 1);
+        for (int rep = 0; rep < 4 && st == NYXPM_OK; ++rep) {   // the first run warms up
+            cudaEventRecord(e0, c->stream);
+            if (chains == 16)
+                k_fp64_fma_probe<16><<<blocks, kProbeThreads, 0, c->stream>>>(iters, 0.999999, 1e-7, -1.0);
+            else
+                k_fp64_fma_probe<8><<<blocks, kProbeThreads, 0, c->stream>>>(iters, 0.999999, 1e-7, -1.0);
+            cudaEventRecord(e1, c->stream);
+            c->launches += 1;
+            st = check_launch(*c, "fp64 probe");
+            if (st == NYXPM_OK && cudaEventSynchronize(e1) != cudaSuccess) st = check_launch(*c, "fp64 probe");
+            float ms = 0.f;
+            if (st == NYXPM_OK && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0) {
+                const double flops = 2.0 * chains * (double)iters * (double)blocks * kProbeThreads;
+                best_rate = std::max(best_rate, flops / (ms * 1e-3) / 1e12);
+            }
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st != NYXPM_OK) return st;
-    if (!(best > 0)) {
+    if (!(best_rate > 0)) {
         c->err = "fp64 probe: no timing";
         return NYXPM_CUDA_ERROR;
     }
-    const double flops = 2.0 * kProbeChains * (double)iters * (double)blocks * kProbeThreads;
-    *tflops = flops / (best * 1e-3) / 1e12;
+    *tflops = best_rate;
     return NYXPM_OK;
 }

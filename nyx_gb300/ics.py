@@ -79,16 +79,64 @@ def displacement_field(n: int, L: float, slope: float, seed: int) -> np.ndarray:
     return psi
 
 
+def _zeldovich_ics_on_device(n, L, slope, seed, a_init, rms_disp_cells, cosmo, device):
+    """zeldovich_ics with the FFTs and the lattice arithmetic on a CUDA device
+    (torch), for the large grids of the benchmark: the same white noise (numpy's
+    generator, same seed) and the same steps, so the field equals the host
+    path's up to the rounding of the FFTs."""
+    import torch
+    dev = torch.device(device)
+    f64 = torch.float64
+    rng = np.random.default_rng(seed)
+    wk = torch.fft.rfftn(torch.from_numpy(rng.standard_normal((n, n, n))).to(dev))
+    kf = 2.0 * np.pi / L
+    kx = torch.fft.fftfreq(n, d=1.0 / n, dtype=f64, device=dev) * kf
+    kz = torch.fft.rfftfreq(n, d=1.0 / n, dtype=f64, device=dev) * kf
+    KX, KY, KZ = kx[:, None, None], kx[None, :, None], kz[None, None, :]
+    k2 = KX * KX + KY * KY + KZ * KZ
+    k2[0, 0, 0] = 1.0
+    amp = torch.pow(torch.sqrt(k2), 0.5 * slope)
+    amp[0, 0, 0] = 0.0
+    dk = wk * amp
+    del wk, amp
+    psi = torch.empty((3, n, n, n), dtype=f64, device=dev)
+    for d, K in enumerate((KX, KY, KZ)):
+        psi[d] = torch.fft.irfftn(1j * K / k2 * dk, s=(n, n, n), dim=(0, 1, 2))
+    del dk, k2
+    rms = float(torch.sqrt(torch.mean(torch.sum(psi * psi, dim=0))))
+    if rms > 0:
+        psi *= (rms_disp_cells * L / n) / rms
+    # array axes are (x, y, z); particles are x-fastest (z, y, x order of the axes)
+    disp = psi.permute(0, 3, 2, 1).reshape(3, -1).t()
+    del psi
+    idx = (torch.arange(n, dtype=f64, device=dev) + 0.5) * (L / n)
+    lattice = torch.stack(torch.meshgrid(idx, idx, idx, indexing="ij")[::-1], dim=-1).reshape(-1, 3)
+    pos = torch.remainder(lattice + disp, L)
+    pos[pos >= L] = 0.0
+    vel = disp * (a_init * cosmo.hubble(a_init))
+    mass = cosmo.OmM * cosmo.rho_crit() * L ** 3 / pos.shape[0]
+    out = InitialConditions(pos=pos.cpu().numpy(), vel=vel.cpu().numpy(), mass=mass, n=n, L=L,
+                            a=a_init, lattice=lattice.cpu().numpy())
+    del pos, vel, lattice, disp
+    torch.cuda.empty_cache()
+    return out
+
+
 def zeldovich_ics(n: int, L: float = 1.0, slope: float = -2.0, seed: int = 1,
                   a_init: float = 0.02, rms_disp_cells: float = 0.2,
                   cosmo: Cosmology | None = None, fraction: float = 1.0,
-                  npart_1d: int | None = None) -> InitialConditions:
+                  npart_1d: int | None = None, device: str | None = None) -> InitialConditions:
     """Zel'dovich ICs on an n^3 grid with rms displacement rms_disp_cells * dx.
 
     fraction < 1 keeps a seeded random subset of ceil(fraction * n^3) lattice
-    sites; the particle mass rises so the mean density is unchanged.
+    sites; the particle mass rises so the mean density is unchanged.  device (a
+    CUDA device, e.g. "cuda:0") runs the FFTs there (one particle per cell only).
     """
     cosmo = cosmo or Cosmology()
+    if device is not None:
+        if fraction != 1.0 or npart_1d not in (None, n):
+            raise ValueError("the device path makes one particle per cell")
+        return _zeldovich_ics_on_device(n, L, slope, seed, a_init, rms_disp_cells, cosmo, device)
     m = npart_1d or n
     psi = displacement_field(m, L, slope, seed) * (rms_disp_cells * L / n)
     dxp = L / m

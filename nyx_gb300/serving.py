@@ -12,7 +12,9 @@ the arena at once, so requests that arrive while others are on the GPU join as
 memory frees up.
 
 ``serve_sequential`` is the comparison: the same stream served by the plain
-FP64 drop-in one run at a time, in arrival order.
+FP64 drop-in one run at a time, in arrival order, on the same step schedule as
+the server (the old-time field reused: one deposit and one solve per step) or,
+with ``reuse_field=False``, on Nyx's own two-solve schedule.
 
 Each run uses equal-delta-a steps from a = 0.02 with delta a = 0.009 (the
 ensemble configuration's 0.02 -> 0.2 in 20 steps).
@@ -61,6 +63,7 @@ class Result:
     done: float
     pos: np.ndarray | None = None
     vel: np.ndarray | None = None
+    g: np.ndarray | None = None          # the gravity vector the run ended with
 
     @property
     def latency(self) -> float:
@@ -118,9 +121,17 @@ class ServeStats:
                 "particle_steps_per_s": self.particle_steps / self.wall if self.wall else 0.0}
 
 
+def _keeps(keep, rid: int) -> bool:
+    """keep: False, True (every run) or a set of request ids."""
+    return bool(keep) and (keep is True or rid in keep)
+
+
 class ContinuousBatchingServer:
+    """keep_results: False, True or a set of request ids whose final particle
+    state and gravity vector are downloaded into their Result."""
+
     def __init__(self, ctx: Context, budget_bytes: int, ic_provider, tuning: dict | None = None,
-                 keep_results: bool = False, max_skip: int = 64):
+                 keep_results=False, max_skip: int = 64):
         self.ctx = ctx
         self.ens = Ensemble(ctx, budget_bytes)
         if tuning:
@@ -179,13 +190,14 @@ class ContinuousBatchingServer:
                 run.k += 1
                 st.particle_steps += run.req.np
                 if run.k == len(run.sched):
-                    pos = vel = None
-                    if self.keep:
+                    pos = vel = g = None
+                    if _keeps(self.keep, run.req.rid):
                         pos, vel = self.ens.download(s)
+                        g = self.ens.grav_vector(s)
                     self.ens.remove(s)
                     del active[s]
                     st.results.append(Result(run.req.rid, run.req.arrival if realtime else 0.0,
-                                             run.start, time.perf_counter() - t0, pos, vel))
+                                             run.start, time.perf_counter() - t0, pos, vel, g))
         st.wall = time.perf_counter() - t0
         return st
 
@@ -194,8 +206,11 @@ class ContinuousBatchingServer:
 
 
 def serve_sequential(ctx: Context, requests: list[Request], ic_provider, realtime: bool = True,
-                     max_requests: int | None = None) -> ServeStats:
-    """The same stream served by the plain FP64 drop-in, one run at a time."""
+                     max_requests: int | None = None, reuse_field: bool = True,
+                     keep_results=False) -> ServeStats:
+    """The same stream served by the plain FP64 drop-in, one run at a time.
+    reuse_field: the server's schedule (post_init solve, then one deposit and one
+    solve per step); False: the reference's two solves per step."""
     st = ServeStats()
     reqs = sorted(requests, key=lambda r: r.arrival)
     if max_requests is not None:
@@ -210,12 +225,19 @@ def serve_sequential(ctx: Context, requests: list[Request], ic_provider, realtim
         ic = ic_provider(r)
         box = Box(ctx, r.n, r.L, r.np)
         box.upload(ic.pos, ic.vel, ic.mass)
-        for a0, a1, dt in schedule(ctx, r.nsteps):
-            box.step(a0, a1, dt)
-        box.download()
+        sched = schedule(ctx, r.nsteps)
+        if reuse_field:
+            box.init_field(sched[0][0])
+        for a0, a1, dt in sched:
+            box.step(a0, a1, dt, reuse_field=reuse_field)
+        pos, vel = box.download()
+        g = box.grav_vector() if _keeps(keep_results, r.rid) else None
+        if not _keeps(keep_results, r.rid):
+            pos = vel = None
         box.close()
         st.particle_steps += r.np * r.nsteps
-        st.results.append(Result(r.rid, r.arrival if realtime else 0.0, start, time.perf_counter() - t0))
+        st.results.append(Result(r.rid, r.arrival if realtime else 0.0, start, time.perf_counter() - t0,
+                                 pos, vel, g))
         st.max_active = 1
     st.wall = time.perf_counter() - t0
     return st

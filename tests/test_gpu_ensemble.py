@@ -2,7 +2,10 @@
 stage over all boxes, captured step graphs).
 
 * every box of an ensemble tracks the FP64 oracle run on its own
-  (old-time field reused) to <= 1e-5 relative L2 after several steps;
+  (old-time field reused): after several steps the force (gravity vector) to
+  <= 1e-6 relative L2 and particle state to <= 1e-5, on boxes of every size the
+  ensemble configuration draws (32 .. 128 cells, one and half a particle per
+  cell);
 * a box's result is bitwise the same alone and inside a mix of other boxes;
 * the deposit tile and smoother row shapes do not change results;
 * the memory budget is enforced and freed memory is reused.
@@ -42,12 +45,17 @@ SPECS = [BoxSpec(32, 1.0, 11, -2.0), BoxSpec(48, 0.5, 12, -1.6), BoxSpec(16, 1.0
          BoxSpec(64, 0.5, 14, -2.2)]
 
 
+# the sizes and particle fractions of the ensemble configuration's draws
+ORACLE_SPECS = SPECS + [BoxSpec(96, 0.5, 15, -1.8), BoxSpec(128, 1.0, 16, -2.5),
+                        BoxSpec(128, 0.5, 17, -1.5), BoxSpec(32, 0.5, 18, -2.1)]
+
+
 def test_ensemble_matches_oracle_per_box(ctx):
-    ics = [box_ics(s, 0.05) for s in SPECS]
+    ics = [box_ics(s, 0.05) for s in ORACLE_SPECS]
     sched = equal_da_schedule(0.05, 0.08, 4)
-    out, g, infos = run_ensemble(ctx, SPECS, ics, sched)
-    assert all(i["boxes"] == len(SPECS) for i in infos)
-    for s, ic, (pos, vel), gg in zip(SPECS, ics, out, g):
+    out, g, infos = run_ensemble(ctx, ORACLE_SPECS, ics, sched)
+    assert all(i["boxes"] == len(ORACLE_SPECS) for i in infos)
+    for s, ic, (pos, vel), gg in zip(ORACLE_SPECS, ics, out, g):
         p = O.Particles(ic.pos, ic.vel, ic.mass)
         pm = O.PMOracle(s.n, s.L, p, reuse_field=True)
         pm.init_field(0.05)
@@ -58,7 +66,7 @@ def test_ensemble_matches_oracle_per_box(ctx):
         ex = np.linalg.norm(min_image(pos - opos, s.L)) / np.linalg.norm(disp)
         ev = rel_l2(vel, ovel)
         eg = rel_l2(gg, pm.g)
-        assert max(ex, ev, eg) <= 1e-5, (s, ex, ev, eg)
+        assert eg <= 1e-6 and max(ex, ev) <= 1e-5, (s, ex, ev, eg)
 
 
 def test_alone_equals_in_mix(ctx):

@@ -629,7 +629,7 @@ def run_ours(args):
 
     # ---- the FP64 issue rate of this GPU (outside the timed region): the
     #      denominator of the FP64 form's roofline ----
-    fp64_peak = ctx.measure_fp64_peak() if args.precision == "fp64" else None
+    fp64_peak, fp64_add = ctx.measure_fp64_peak() if args.precision == "fp64" else (None, None)
 
     # ---- device-resident run: warm-up, then K timed steps (solver iterations
     #      replayed from the box's CUDA graphs) ----
@@ -700,20 +700,24 @@ def run_ours(args):
     if args.precision == "fp64" and dom == "smooth" and prof["fine_smooth"]["launches"]:
         # the finest FP64 half sweep updates n^3/2 cells with 6 FP64 operations each
         # (5 additions of the neighbour sum and one fused multiply-add), 24 algorithmic
-        # bytes per cell; the FP64 pipe issues an add, a multiply or an FMA at one rate,
-        # so the pipe's bound is the probe's FMA rate (TFLOP/s / 2) in operations/s
+        # bytes per cell.  The bound is the time the FP64 pipe needs for that mix at the
+        # rates measured on this GPU: 5 / add rate + 1 / FMA rate per cell, i.e. a peak
+        # of 6 / (5 / R_add + 1 / R_fma) operations per second
         cells = per_launch / 24.0
         ops = 6.0 * cells / (avg_ms * 1e-3) / 1e12
-        peak_ops = fp64_peak / 2.0
+        r_fma = fp64_peak / 2.0
+        peak_ops = 6.0 / (5.0 / fp64_add + 1.0 / r_fma)
         roofline = {"bound": "fp64", "kernel": kname,
                     "achieved": round(ops, 4), "peak": round(peak_ops, 4),
-                    "peak_source": "measured: nyxpm_measure_fp64_peak on this GPU (FMA chains, "
-                                   "CUDA events)",
-                    "unit": "T FP64 op/s (an add, multiply or FMA is one op)",
+                    "peak_source": "measured: nyxpm_measure_fp64_peak on this GPU (chains of FP64 "
+                                   "additions and of FMAs, CUDA events), weighted 5 adds : 1 FMA",
+                    "unit": "T FP64 op/s (an add or an FMA is one op)",
                     "frac": round(ops / peak_ops, 4), "traffic": traffic_launch,
+                    "fp64_rates_measured": {"fma_T_per_s": round(r_fma, 4),
+                                            "add_T_per_s": round(fp64_add, 4)},
                     "flops": {"achieved_TFLOPs": round(7.0 * cells / (avg_ms * 1e-3) / 1e12, 4),
                               "peak_TFLOPs": round(fp64_peak, 4),
-                              "note": "FMA = 2 flops: 7 flops per updated cell"},
+                              "note": "FMA = 2 flops: 7 flops per updated cell; peak = FMA chains"},
                     "hbm": hbm,
                     "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms,
                     "fp64_pipe_active_ncu": traffic.get("k_gsrb_fine_fp64_pipe_active"),

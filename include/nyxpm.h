@@ -196,12 +196,12 @@ nyxpm_status nyxpm_step(nyxpm_ctx* ctx, nyxpm_box* box, double a_old, double a_n
 /* nyxpm_box_upload + nyxpm_step + nyxpm_box_download in one call, for callers
  * whose particles live in host memory; pos and vel (np x 3, particle order) are
  * read and overwritten with the stepped state.  The results are those of the
- * three calls, bit for bit.  On FP64 boxes the transfers run on a second stream
- * under the step: the velocities arrive during the sort, deposit and old-time
- * solve, which read positions only, and the positions leave (wrapped, as the
- * closing kick wraps them) during the new-time deposit and solve.  Pinned host
- * buffers let the copies overlap.  No counterpart in the reference: Nyx keeps
- * the particles in its own containers. */
+ * three calls, bit for bit.  The transfers run on a second stream under the
+ * step (both precisions): the velocities arrive during the sort, deposit and
+ * old-time solve, which read positions only, and the positions leave (wrapped,
+ * as the closing kick wraps them) during the new-time deposit and solve.
+ * Pinned host buffers let the copies overlap.  No counterpart in the
+ * reference: Nyx keeps the particles in its own containers. */
 nyxpm_status nyxpm_step_host(nyxpm_ctx* ctx, nyxpm_box* box, double* pos, double* vel,
                              const double* mass, double mass_scalar, double a_old, double a_new,
                              double dt, unsigned flags, nyxpm_step_info* info);
@@ -317,6 +317,49 @@ nyxpm_status nyxpm_cosmo_ic_factors(const nyxpm_params* p, int source, int n, do
 nyxpm_status nyxpm_box_init_cosmo_1ppc(nyxpm_ctx* ctx, nyxpm_box* box, const double* disp,
                                        const double* vel, const double* disp_fac,
                                        const double* vel_fac, double particle_mass);
+
+/* ---- checkpoint and plotfile particle directories (host I/O) ---------------------- */
+
+/* The "DM" directory of a Nyx checkpoint (chkNNNNN/DM, written by NyxCheckpoint,
+ * Source/Particle/NyxParticleContainer.H:510-517, from Nyx::particle_check_point,
+ * Source/IO/Nyx_output.cpp:726-750) or plotfile (pltNNNNN/DM, WriteNyxPlotFile,
+ * NyxParticleContainer.H:499-505): the AMReX particle container layout
+ * Version_Two_Dot_Zero -- a text Header (version and real precision, dimension,
+ * the names of the real and int components, checkpoint flag, particle count,
+ * next id, finest level, grids per level, one "file count offset" line per
+ * grid), binary Level_<l>/DATA_<nnnnn> files (per grid: a checkpoint's int32 id
+ * and cpu, then x y z and the real components per particle, native byte order)
+ * and Level_<l>/Particle_H (the level's BoxArray).  Nyx reads it back with
+ * Restart (Source/Particle/NyxParticles.cpp:584-586, 928-934). */
+typedef struct nyxpm_particle_header {
+    int single_precision;   /* Version_Two_Dot_Zero_single: float32 reals; 0: float64 */
+    int dim;                /* 3 */
+    int n_real_extra;       /* real components after the position (Nyx DM: 4) */
+    int n_int_extra;        /* int components after id and cpu */
+    int is_checkpoint;      /* 1: ids and cpus stored (checkpoint); 0: plotfile */
+    int finest_level;
+    int64_t num_particles;
+    int64_t max_next_id;
+    int ngrids;             /* grids over all levels */
+    int pad;
+} nyxpm_particle_header;
+
+nyxpm_status nyxpm_particles_info(const char* dir, nyxpm_particle_header* h, char* errbuf,
+                                  size_t errlen);
+/* Every grid of every level in header order into pos[3 np], vel[3 np], mass[np]
+ * (the arrays nyxpm_box_upload takes); mass and velocity are the components named
+ * mass, xvel, yvel, zvel (else the first four); ids (may be NULL; checkpoints
+ * only) receives the AMReX particle ids. */
+nyxpm_status nyxpm_particles_read(const char* dir, int64_t capacity, double* pos, double* vel,
+                                  double* mass, int64_t* ids, int64_t* np_read, char* errbuf,
+                                  size_t errlen);
+/* Writes dir (created if absent) as one level with one grid covering the n^3
+ * periodic domain: ids 1..np, cpu 0, components mass xvel yvel zvel; float32
+ * reals with single_precision, float64 otherwise; mass NULL writes mass_scalar. */
+nyxpm_status nyxpm_particles_write(const char* dir, int n, int64_t np, const double* pos,
+                                   const double* vel, const double* mass, double mass_scalar,
+                                   int is_checkpoint, int single_precision, char* errbuf,
+                                   size_t errlen);
 
 /* ---- AMReX MultiFab files (VisMF, host I/O) ------------------------------------ */
 
@@ -469,9 +512,11 @@ int64_t nyxpm_launch_count(const nyxpm_ctx* ctx);
 /* The FP64 rate this GPU sustains, in TFLOP/s (a fused multiply-add counts as two
  * operations): chains of dependent FP64 FMAs filling every SM, timed with CUDA
  * events on the context's stream (the best over four launch shapes of three runs
- * of about 10 ms, each shape after one warm-up run).  The denominator of the FP64 roofline of the FP64 form, whose
- * kernels are bound by the FP64 pipe.  No counterpart in the reference. */
-nyxpm_status nyxpm_measure_fp64_peak(nyxpm_ctx* ctx, double* tflops);
+ * of about 10 ms, each shape after one warm-up run); add_tops (may be NULL)
+ * receives the rate of FP64 additions measured the same way, in T additions/s.
+ * The denominators of the FP64 roofline of the FP64 form, whose kernels are bound
+ * by the FP64 pipe.  No counterpart in the reference. */
+nyxpm_status nyxpm_measure_fp64_peak(nyxpm_ctx* ctx, double* tflops, double* add_tops);
 
 #ifdef __cplusplus
 }

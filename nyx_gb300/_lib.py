@@ -41,7 +41,7 @@ EXPORTS = [
     "nyxpm_particle_file_write", "nyxpm_write_comoving_a", "nyxpm_read_comoving_a",
     "nyxpm_cosmo_1ppc_particles", "nyxpm_cosmo_ic_factors", "nyxpm_box_init_cosmo_1ppc",
     "nyxpm_multifab_info_read", "nyxpm_multifab_boxes", "nyxpm_multifab_read",
-    "nyxpm_multifab_write",
+    "nyxpm_multifab_write", "nyxpm_particles_info", "nyxpm_particles_read", "nyxpm_particles_write",
 ]
 NYXPM_MF_REJECT_NAN = 1
 
@@ -56,6 +56,24 @@ class MultiFabInfo(C.Structure):
         ("has_minmax", C.c_int),
     ]
 NYXPM_FILE_ASCII, NYXPM_FILE_BINARY, NYXPM_FILE_BINARY_META, NYXPM_FILE_BINARY_F64 = 0, 1, 2, 3
+
+
+class ParticleHeader(C.Structure):
+    _fields_ = [
+        ("single_precision", C.c_int),
+        ("dim", C.c_int),
+        ("n_real_extra", C.c_int),
+        ("n_int_extra", C.c_int),
+        ("is_checkpoint", C.c_int),
+        ("finest_level", C.c_int),
+        ("num_particles", C.c_int64),
+        ("max_next_id", C.c_int64),
+        ("ngrids", C.c_int),
+        ("pad", C.c_int),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
 
 
 class Params(C.Structure):
@@ -204,11 +222,14 @@ def load(path: str | None = None):
     L.nyxpm_multifab_boxes.argtypes = [cp, vp, vp, cp, sz]
     L.nyxpm_multifab_read.argtypes = [cp, C.c_int, C.c_int, vp, vp, C.c_uint, vp, cp, sz]
     L.nyxpm_multifab_write.argtypes = [cp, C.c_int, vp, vp, C.c_int, C.c_int, vp, vp, cp, sz]
+    L.nyxpm_particles_info.argtypes = [cp, C.POINTER(ParticleHeader), cp, sz]
+    L.nyxpm_particles_read.argtypes = [cp, i64, vp, vp, vp, vp, C.POINTER(i64), cp, sz]
+    L.nyxpm_particles_write.argtypes = [cp, C.c_int, i64, vp, vp, vp, d, C.c_int, C.c_int, cp, sz]
     L.nyxpm_set_profiling.argtypes = [vp, C.c_int]
     L.nyxpm_get_profile.argtypes = [vp, C.POINTER(Profile), C.c_int]
     L.nyxpm_launch_count.argtypes = [vp]
     L.nyxpm_launch_count.restype = i64
-    L.nyxpm_measure_fp64_peak.argtypes = [vp, C.POINTER(d)]
+    L.nyxpm_measure_fp64_peak.argtypes = [vp, C.POINTER(d), C.POINTER(d)]
     dp = C.POINTER(C.c_double)
     L.nyxpm_ensemble_create.argtypes = [vp, C.c_size_t, C.POINTER(vp)]
     L.nyxpm_ensemble_destroy.argtypes = [vp, vp]

@@ -33,6 +33,7 @@ UNITS = {
     "pm_probe.cu": [],
     "pm_io.cpp": [],
     "pm_vismf.cpp": [],
+    "pm_particle_io.cpp": [],
 }
 
 

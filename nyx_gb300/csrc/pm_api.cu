@@ -689,14 +689,7 @@ nyxpm_status nyxpm_step_host(nyxpm_ctx* c, nyxpm_box* b, double* pos, double* ve
     if (!pos || !vel) return fail(c, NYXPM_INVALID_ARG, "null pos/vel");
     if (!(a_old > 0) || !(a_new > 0) || !std::isfinite(dt)) return fail(c, NYXPM_INVALID_ARG, "bad a / dt");
     const bool reuse = (flags & NYXPM_STEP_REUSE_FIELD) != 0;
-    if (b->prec != NYXPM_FP64) {
-        // the mixed form: the three calls one after another
-        TRY(nyxpm_box_upload(c, b, pos, vel, mass, mass_scalar));
-        const nyxpm_status st = nyxpm_step(c, b, a_old, a_new, dt, flags, info);
-        if (st != NYXPM_OK && st != NYXPM_NOT_CONVERGED) return st;
-        TRY(nyxpm_box_download(c, b, pos, vel));
-        return st;
-    }
+    const bool mixed = b->prec == NYXPM_MIXED;
     if (reuse && !b->have_phi) return fail(c, NYXPM_INVALID_ARG, "no field to reuse: call nyxpm_init_field");
     const int64_t np = b->np;
     double total = 0.0;
@@ -725,7 +718,8 @@ nyxpm_status nyxpm_step_host(nyxpm_ctx* c, nyxpm_box* b, double* pos, double* ve
     cudaMemsetAsync(b->norms + 2, 0, sizeof(unsigned long long), c->stream);
     cudaMemcpyAsync(s_pos, pos, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream);
     if (mass) cudaMemcpyAsync(s_mass, mass, sizeof(double) * np, cudaMemcpyHostToDevice, c->stream);
-    TRY(launch_unpack_pos(*c, *b, s_pos, mass ? s_mass : nullptr));
+    TRY(mixed ? mixed_unpack_pos(*c, *b, s_pos, mass ? s_mass : nullptr)
+              : launch_unpack_pos(*c, *b, s_pos, mass ? s_mass : nullptr));
     // ... the velocities on the copy stream, under the sort, deposit and old-time solve
     cudaMemcpyAsync(s_vel, vel, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->copy_stream);
     cudaEventRecord(c->ev_copy_in, c->copy_stream);
@@ -739,18 +733,20 @@ nyxpm_status nyxpm_step_host(nyxpm_ctx* c, nyxpm_box* b, double* pos, double* ve
     bool sorted_since = false;
     if (!reuse) {
         // nyxpm_step's old-time part, the sort leaving the velocities for later
-        TRY(launch_sort(*c, *b, true));
+        TRY(mixed ? mixed_sort(*c, *b, true) : launch_sort(*c, *b, true));
         sorted_since = true;
-        TRY(launch_deposit(*c, *b));
+        TRY(mixed ? mixed_deposit(*c, *b) : launch_deposit(*c, *b));
         st_old = do_solve(*c, *b, a_old, 1, &local.old_solve);
         if (st_old != NYXPM_OK && st_old != NYXPM_NOT_CONVERGED) return st_old;
     }
     cudaStreamWaitEvent(c->stream, c->ev_copy_in, 0);
-    TRY(launch_unpack_gather_vel(*c, *b, s_vel, sorted_since));
+    TRY(mixed ? mixed_unpack_vel(*c, *b, s_vel, sorted_since)
+              : launch_unpack_gather_vel(*c, *b, s_vel, sorted_since));
     TRY(do_kick(*c, *b, dt, a_old, a_half, 1, 0));
-    // the positions are final now (the closing kick only wraps them): out on the
-    // copy stream, wrapped, under the new-time deposit and solve
-    TRY(launch_pack_pos_wrapped(*c, *b, s_pos));
+    // the positions are final now (the closing kick only wraps them, and not at
+    // all in the mixed form): out on the copy stream under the new-time deposit
+    // and solve
+    TRY(mixed ? mixed_pack_pos(*c, *b, s_pos) : launch_pack_pos_wrapped(*c, *b, s_pos));
     cudaEventRecord(c->ev_copy_out, c->stream);
     cudaStreamWaitEvent(c->copy_stream, c->ev_copy_out, 0);
     cudaMemcpyAsync(pos, s_pos, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, c->copy_stream);
@@ -758,7 +754,7 @@ nyxpm_status nyxpm_step_host(nyxpm_ctx* c, nyxpm_box* b, double* pos, double* ve
     st_new = do_solve(*c, *b, a_new, 0, &local.new_solve);
     if (st_new != NYXPM_OK && st_new != NYXPM_NOT_CONVERGED) return st_new;
     TRY(do_kick(*c, *b, dt, a_half, a_new, 0, 1));
-    TRY(launch_pack_vel(*c, *b, s_vel));
+    TRY(mixed ? mixed_pack_vel(*c, *b, s_vel) : launch_pack_vel(*c, *b, s_vel));
     cudaMemcpyAsync(vel, s_vel, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, c->stream);
     cudaMemcpyAsync(b->h_norms + 2, b->norms + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                     c->stream);

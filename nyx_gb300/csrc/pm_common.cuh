@@ -416,7 +416,12 @@ nyxpm_status launch_phi_from_natural(Ctx& c, Box& b, const double* d_in);
 nyxpm_status mixed_unpack(Ctx& c, Box& b, const double* d_pos, const double* d_vel,
                           const double* d_mass);
 nyxpm_status mixed_pack(Ctx& c, Box& b, double* d_pos, double* d_vel);
-nyxpm_status mixed_sort(Ctx& c, Box& b);
+nyxpm_status mixed_sort(Ctx& c, Box& b, bool defer_vel = false);
+// the host-buffer step's split transfers (mixed boxes)
+nyxpm_status mixed_unpack_pos(Ctx& c, Box& b, const double* d_pos, const double* d_mass);
+nyxpm_status mixed_unpack_vel(Ctx& c, Box& b, const double* d_vel, bool sorted_since);
+nyxpm_status mixed_pack_pos(Ctx& c, Box& b, double* d_pos);
+nyxpm_status mixed_pack_vel(Ctx& c, Box& b, double* d_vel);
 nyxpm_status mixed_deposit(Ctx& c, Box& b);
 nyxpm_status mixed_kick(Ctx& c, Box& b, double dt, double a_prev, double a_cur, int do_move);
 nyxpm_status mixed_solve(Ctx& c, Box& b, int zero_guess, nyxpm_solve_info* info);

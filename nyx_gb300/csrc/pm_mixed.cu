@@ -105,6 +105,80 @@ __global__ void k_mx_unpack(long long np, int n, double dxi, const double* __res
     id[q] = (int)q;
 }
 
+// The host-buffer step's split transfers (nyxpm_step_host): positions (and
+// masses) first, velocities later; positions out as soon as the drift made them
+// final (the mixed closing kick does not move particles).  Together these give
+// exactly what k_mx_unpack and k_mx_pack give.
+__global__ void k_mx_unpack_pos(long long np, int n, double dxi, const double* __restrict__ pos,
+                                const double* __restrict__ mass, int* cell, float* ox, float* oy,
+                                float* oz, float* m, int* id, unsigned long long* bad)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    id[q] = (int)q;
+    if (m) m[q] = (float)mass[q];
+    const double px = pos[3 * q], py = pos[3 * q + 1], pz = pos[3 * q + 2];
+    if (!(isfinite(px) && isfinite(py) && isfinite(pz))) {
+        atomicAdd(bad, 1ULL);
+        cell[q] = 0;
+        ox[q] = oy[q] = oz[q] = 0.f;
+        return;
+    }
+    int i, j, k;
+    float a, b, c;
+    to_cell(px, dxi, n, &i, &a);
+    to_cell(py, dxi, n, &j, &b);
+    to_cell(pz, dxi, n, &k, &c);
+    cell[q] = pack_cell(i, j, k);
+    ox[q] = a;
+    oy[q] = b;
+    oz[q] = c;
+}
+
+// velocities in upload order; with perm, permuted by the sort that ran without
+// them (vx[s] = vel[perm[s]]), else in place (vx[q] = vel[q])
+__global__ void k_mx_unpack_vel(long long np, const double* __restrict__ vel,
+                                const int* __restrict__ perm, float* vx, float* vy, float* vz,
+                                unsigned long long* bad)
+{
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= np) return;
+    const long long q = perm ? (long long)perm[s] : s;
+    const double ux = vel[3 * q], uy = vel[3 * q + 1], uz = vel[3 * q + 2];
+    if (!(isfinite(ux) && isfinite(uy) && isfinite(uz))) {
+        atomicAdd(bad, 1ULL);
+        vx[s] = vy[s] = vz[s] = 0.f;
+        return;
+    }
+    vx[s] = (float)ux;
+    vy[s] = (float)uy;
+    vz[s] = (float)uz;
+}
+
+__global__ void k_mx_pack_pos(long long np, double dx, const int* __restrict__ cell,
+                              const float* __restrict__ ox, const float* __restrict__ oy,
+                              const float* __restrict__ oz, const int* __restrict__ id, double* pos)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const int c = cell[q];
+    const long long o = 3LL * id[q];
+    pos[o] = ((double)cell_i(c) + (double)ox[q]) * dx;
+    pos[o + 1] = ((double)cell_j(c) + (double)oy[q]) * dx;
+    pos[o + 2] = ((double)cell_k(c) + (double)oz[q]) * dx;
+}
+
+__global__ void k_mx_pack_vel(long long np, const float* __restrict__ vx, const float* __restrict__ vy,
+                              const float* __restrict__ vz, const int* __restrict__ id, double* vel)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const long long o = 3LL * id[q];
+    vel[o] = vx[q];
+    vel[o + 1] = vy[q];
+    vel[o + 2] = vz[q];
+}
+
 __global__ void k_mx_pack(long long np, double dx, const int* __restrict__ cell,
                           const float* __restrict__ ox, const float* __restrict__ oy,
                           const float* __restrict__ oz, const float* __restrict__ vx,
@@ -157,9 +231,11 @@ __global__ void k_mx_gather(long long np, const int* __restrict__ perm, const in
     ox2[s] = ox[q];
     oy2[s] = oy[q];
     oz2[s] = oz[q];
-    vx2[s] = vx[q];
-    vy2[s] = vy[q];
-    vz2[s] = vz[q];
+    if (vx) {   // null: the velocities follow later (k_mx_unpack_vel with perm)
+        vx2[s] = vx[q];
+        vy2[s] = vy[q];
+        vz2[s] = vz[q];
+    }
     if (m) m2[s] = m[q];
     id2[s] = id[q];
 }
@@ -168,9 +244,6 @@ __global__ void k_mx_gather(long long np, const int* __restrict__ perm, const in
 // FP32 deposit (same tiling as the FP64 form: per-key partials in shared
 // memory, cells add their 8 key partials in a fixed order)
 // ---------------------------------------------------------------------------
-constexpr int kTx = 8, kTy = 8, kTz = 8;
-constexpr int kKx = kTx + 1, kKy = kTy + 1, kKz = kTz + 1;
-constexpr int kNKeys = kKx * kKy * kKz;
 
 // adds particle q's eight CIC weights (times its mass, if m) to s
 __device__ __forceinline__ void mx_add_weights(int q, int n, const int* __restrict__ cell,
@@ -234,51 +307,175 @@ __global__ void __launch_bounds__(256) k_mx_deposit_heavy(int n, const int* __re
     }
 }
 
-__global__ void __launch_bounds__(256) k_mx_deposit(int n, float scale, const int* __restrict__ cell,
-                                                    const float* __restrict__ ox,
-                                                    const float* __restrict__ oy,
-                                                    const float* __restrict__ oz,
-                                                    const float* __restrict__ m,
-                                                    const int* __restrict__ start,
-                                                    const int* __restrict__ key_slot,
-                                                    const float* __restrict__ heavy_part, float* rho)
+// One CTA per tile of 16 x 8 x 8 cells; its density needs the 17 x 9 x 9 keys
+// (cells of floor(x/dx + 1/2)) from the tile's own corner to one past its far
+// corner.  The keys' particles are contiguous runs of the sorted arrays (one
+// run per row of 17 keys, cut only where a row wraps), so the CTA
+// 1. reads cell_start for its keys and numbers their particles densely (a block
+//    scan of the per-key counts; keys longer than a warp count 0, their sums come
+//    from k_mx_deposit_heavy);
+// 2. in chunks of up to kDepChunk particles, every thread loads particles of
+//    consecutive numbers -- consecutive addresses within a row, so every warp's
+//    loads are coalesced -- and writes their 8 CIC weights to shared memory;
+// 3. each thread adds the weights of its own keys' particles in sorted order
+//    (the per-key sums of one thread per key, in registers across chunks);
+// 4. each cell adds its 8 keys' corner sums in a fixed (dk, dj, di) order.
+// No atomics: the order of every sum is fixed, so the density is bitwise
+// reproducible, and equals a thread-per-key walk of the same keys.
+constexpr int kDepTx = 16, kDepTy = 8, kDepTz = 8;
+constexpr int kDepKx = kDepTx + 1, kDepKy = kDepTy + 1, kDepKz = kDepTz + 1;
+constexpr int kDepKeys = kDepKx * kDepKy * kDepKz;           // 1377
+constexpr int kDepThreads = 512;
+constexpr int kDepKpt = (kDepKeys + kDepThreads - 1) / kDepThreads;   // keys per thread: 3
+constexpr int kDepChunk = 2048;                              // particles per chunk
+static_assert(kDepKeys < 65536, "key numbers are kept in 16 bits");
+// dynamic shared memory: offsets and bases of the keys, then the chunk buffers
+// (weights + owners), which the keys' corner sums reuse at the end
+constexpr size_t kDepChunkBytes = sizeof(float) * 8 * kDepChunk + sizeof(unsigned short) * kDepChunk;
+constexpr size_t kDepPartBytes = sizeof(float) * 8 * kDepKeys;
+constexpr size_t kDepSmem = sizeof(int) * (2 * kDepKeys + 1) +
+                            (kDepChunkBytes > kDepPartBytes ? kDepChunkBytes : kDepPartBytes);
+
+__device__ __forceinline__ int wrap_up(int i, int n)
 {
-    // corner-major: a warp's 32 consecutive keys (or cells) touch 32 banks
-    __shared__ float part[8 * kNKeys];
-    const int i0 = blockIdx.x * kTx, j0 = blockIdx.y * kTy, k0 = blockIdx.z * kTz;
-    for (int kl = threadIdx.x; kl < kNKeys; kl += blockDim.x) {
-        const int ki = kl % kKx, kj = (kl / kKx) % kKy, kk = kl / (kKx * kKy);
-        const long long K = cidx(wrapi(i0 + ki, n), wrapi(j0 + kj, n), wrapi(k0 + kk, n), n);
-        float s[8];
-        const int b0 = start[K], e = start[K + 1];
-        if (e - b0 > kDepositLanes) {
-            const float* hp = heavy_part + 8LL * key_slot[K];
+    while (i >= n) i -= n;   // i < n + 17: at most one pass unless n < 17
+    return i;
+}
+
+__global__ void __launch_bounds__(kDepThreads, 2) k_mx_deposit(
+    int n, float scale, const int* __restrict__ cell, const float* __restrict__ ox,
+    const float* __restrict__ oy, const float* __restrict__ oz, const float* __restrict__ m,
+    const int* __restrict__ start, const int* __restrict__ key_slot,
+    const float* __restrict__ heavy_part, float* rho)
+{
+    extern __shared__ __align__(16) unsigned char dep_smem[];
+    __shared__ int s_warp[kDepThreads / 32];
+    int* s_off = reinterpret_cast<int*>(dep_smem);          // first particle number of each key
+    int* s_base = s_off + kDepKeys + 1;                      // first sorted particle of each key
+    float* w = reinterpret_cast<float*>(s_base + kDepKeys); // a chunk's weights, corner-major
+    unsigned short* owner = reinterpret_cast<unsigned short*>(w + 8 * kDepChunk);  // key of each
+    float* part = w;                                         // at the end: the keys' corner sums
+    const int tid = threadIdx.x;
+    const int i0 = blockIdx.x * kDepTx, j0 = blockIdx.y * kDepTy, k0 = blockIdx.z * kDepTz;
+    // 1. this thread's keys kl = kDepKpt*tid + r: start, count (heavy: 0), heavy sums
+    float acc[kDepKpt][8];
+    int cnt[kDepKpt];
+    int local = 0;
 #pragma unroll
-            for (int c = 0; c < 8; ++c) s[c] = hp[c];
-        } else {
+    for (int r = 0; r < kDepKpt; ++r) {
+        const int kl = kDepKpt * tid + r;
+        cnt[r] = 0;
 #pragma unroll
-            for (int c = 0; c < 8; ++c) s[c] = 0.f;
-            for (int q = b0; q < e; ++q) mx_add_weights(q, n, cell, ox, oy, oz, m, s);
+        for (int c = 0; c < 8; ++c) acc[r][c] = 0.f;
+        if (kl < kDepKeys) {
+            const int ki = kl % kDepKx, kj = (kl / kDepKx) % kDepKy, kk = kl / (kDepKx * kDepKy);
+            const long long K = cidx(wrap_up(i0 + ki, n), wrap_up(j0 + kj, n), wrap_up(k0 + kk, n), n);
+            const int b0 = start[K], len = start[K + 1] - b0;
+            s_base[kl] = b0;
+            if (len > kDepositLanes) {
+                const float* hp = heavy_part + 8LL * key_slot[K];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) acc[r][c] = hp[c];
+            } else {
+                cnt[r] = len;
+            }
+            local += cnt[r];
         }
+    }
+    // block exclusive scan of the per-thread counts (keys in kl order)
+    const int lane = tid & 31, wid = tid >> 5;
+    int inc = local;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) part[c * kNKeys + kl] = s[c];
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) s_warp[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int v = lane < kDepThreads / 32 ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += t;
+        }
+        if (lane < kDepThreads / 32) s_warp[lane] = v;
     }
     __syncthreads();
-    for (int cl = threadIdx.x; cl < kTx * kTy * kTz; cl += blockDim.x) {
-        const int ci = cl % kTx, cj = (cl / kTx) % kTy, ck = cl / (kTx * kTy);
+    int run = (wid > 0 ? s_warp[wid - 1] : 0) + inc - local;
+    const int total = s_warp[kDepThreads / 32 - 1];
+    int off[kDepKpt];
+#pragma unroll
+    for (int r = 0; r < kDepKpt; ++r) {
+        const int kl = kDepKpt * tid + r;
+        off[r] = run;
+        if (kl < kDepKeys) s_off[kl] = run;
+        run += cnt[r];
+    }
+    __syncthreads();
+    // 2.-3. the particles in chunks
+    for (int c0 = 0; c0 < total; c0 += kDepChunk) {
+        const int c1 = min(total, c0 + kDepChunk);
+#pragma unroll
+        for (int r = 0; r < kDepKpt; ++r) {
+            const int lo = max(off[r], c0), hi = min(off[r] + cnt[r], c1);
+            for (int p = lo; p < hi; ++p) owner[p - c0] = (unsigned short)(kDepKpt * tid + r);
+        }
+        __syncthreads();
+        for (int p = c0 + tid; p < c1; p += kDepThreads) {
+            const int kl = owner[p - c0];
+            const int q = s_base[kl] + (p - s_off[kl]);
+            const int cq = cell[q];
+            float fx, fy, fz;
+            key_frac(cell_i(cq), ox[q], n, &fx);
+            key_frac(cell_j(cq), oy[q], n, &fy);
+            key_frac(cell_k(cq), oz[q], n, &fz);
+            const float sx[2] = {1.f - fx, fx};
+            const float sy[2] = {1.f - fy, fy};
+            const float sz[2] = {1.f - fz, fz};
+            const float mq = m ? m[q] : 1.f;
+#pragma unroll
+            for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+                for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                    for (int cx = 0; cx < 2; ++cx)
+                        w[(cx + 2 * cy + 4 * cz) * kDepChunk + p - c0] = __fmul_rn(__fmul_rn(__fmul_rn(sx[cx], sy[cy]), sz[cz]), mq);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kDepKpt; ++r) {
+            const int lo = max(off[r], c0), hi = min(off[r] + cnt[r], c1);
+            for (int p = lo; p < hi; ++p)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) acc[r][c] = __fadd_rn(acc[r][c], w[c * kDepChunk + p - c0]);
+        }
+        __syncthreads();
+    }
+    // 4. the cells: each adds its 8 keys' corners in the fixed (dk, dj, di) order
+#pragma unroll
+    for (int r = 0; r < kDepKpt; ++r) {
+        const int kl = kDepKpt * tid + r;
+        if (kl < kDepKeys)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) part[c * kDepKeys + kl] = acc[r][c];
+    }
+    __syncthreads();
+    for (int cl = tid; cl < kDepTx * kDepTy * kDepTz; cl += kDepThreads) {
+        const int ci = cl % kDepTx, cj = (cl / kDepTx) % kDepTy, ck = cl / (kDepTx * kDepTy);
         const int i = i0 + ci, j = j0 + cj, k = k0 + ck;
         if (i >= n || j >= n || k >= n) continue;
-        float acc = 0.f;
+        float a = 0.f;
 #pragma unroll
         for (int dk = 0; dk < 2; ++dk)
 #pragma unroll
             for (int dj = 0; dj < 2; ++dj)
 #pragma unroll
                 for (int di = 0; di < 2; ++di) {
-                    const int kl = (ci + di) + kKx * ((cj + dj) + kKy * (ck + dk));
-                    acc += part[((1 - di) + 2 * (1 - dj) + 4 * (1 - dk)) * kNKeys + kl];
+                    const int kl = (ci + di) + kDepKx * ((cj + dj) + kDepKy * (ck + dk));
+                    a = __fadd_rn(a, part[((1 - di) + 2 * (1 - dj) + 4 * (1 - dk)) * kDepKeys + kl]);
                 }
-        rho[cidx(i, j, k, n)] = acc * scale;
+        rho[cidx(i, j, k, n)] = a * scale;
     }
 }
 
@@ -1384,6 +1581,42 @@ nyxpm_status mixed_unpack(Ctx& c, Box& b, const double* d_pos, const double* d_v
     return check_launch(c, "mixed unpack");
 }
 
+nyxpm_status mixed_unpack_pos(Ctx& c, Box& b, const double* d_pos, const double* d_mass)
+{
+    prof_begin(c);
+    k_mx_unpack_pos<<<blocks_for(b.np), kThreads, 0, c.stream>>>(
+        b.np, b.n, b.dxi, d_pos, d_mass, b.cell, b.ox, b.oy, b.oz, d_mass ? b.fm : nullptr, b.id,
+        b.norms + 2);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "mixed unpack positions");
+}
+
+nyxpm_status mixed_unpack_vel(Ctx& c, Box& b, const double* d_vel, bool sorted_since)
+{
+    prof_begin(c);
+    k_mx_unpack_vel<<<blocks_for(b.np), kThreads, 0, c.stream>>>(
+        b.np, d_vel, sorted_since ? b.perm : nullptr, b.fvx, b.fvy, b.fvz, b.norms + 2);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "mixed unpack velocities");
+}
+
+nyxpm_status mixed_pack_pos(Ctx& c, Box& b, double* d_pos)
+{
+    prof_begin(c);
+    k_mx_pack_pos<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.dx, b.cell, b.ox, b.oy, b.oz,
+                                                                b.id, d_pos);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "mixed pack positions");
+}
+
+nyxpm_status mixed_pack_vel(Ctx& c, Box& b, double* d_vel)
+{
+    prof_begin(c);
+    k_mx_pack_vel<<<blocks_for(b.np), kThreads, 0, c.stream>>>(b.np, b.fvx, b.fvy, b.fvz, b.id, d_vel);
+    prof_end(c, NYXPM_ST_GATHER, 0);
+    return check_launch(c, "mixed pack velocities");
+}
+
 nyxpm_status mixed_pack(Ctx& c, Box& b, double* d_pos, double* d_vel)
 {
     prof_begin(c);
@@ -1393,7 +1626,7 @@ nyxpm_status mixed_pack(Ctx& c, Box& b, double* d_pos, double* d_vel)
     return check_launch(c, "mixed pack");
 }
 
-nyxpm_status mixed_sort(Ctx& c, Box& b)
+nyxpm_status mixed_sort(Ctx& c, Box& b, bool defer_vel)
 {
     nyxpm_status st;
     cudaMemsetAsync(b.cell_count, 0, sizeof(int) * (size_t)b.n * b.n * b.n, c.stream);
@@ -1406,17 +1639,20 @@ nyxpm_status mixed_sort(Ctx& c, Box& b)
     const bool pm = !b.uniform_mass;
     prof_begin(c);
     k_mx_gather<<<blocks_for(b.np), kThreads, 0, c.stream>>>(
-        b.np, b.perm, b.cell, b.ox, b.oy, b.oz, b.fvx, b.fvy, b.fvz, pm ? b.fm : nullptr, b.id,
-        b.cell2, b.ox2, b.oy2, b.oz2, b.fvx2, b.fvy2, b.fvz2, pm ? b.fm2 : nullptr, b.id2);
-    prof_end(c, NYXPM_ST_GATHER, (pm ? 76.0 : 68.0) * b.np);
+        b.np, b.perm, b.cell, b.ox, b.oy, b.oz, defer_vel ? nullptr : b.fvx, b.fvy, b.fvz,
+        pm ? b.fm : nullptr, b.id, b.cell2, b.ox2, b.oy2, b.oz2, b.fvx2, b.fvy2, b.fvz2,
+        pm ? b.fm2 : nullptr, b.id2);
+    prof_end(c, NYXPM_ST_GATHER, ((pm ? 76.0 : 68.0) - (defer_vel ? 24.0 : 0.0)) * b.np);
     if ((st = check_launch(c, "mixed gather")) != NYXPM_OK) return st;
     std::swap(b.cell, b.cell2);
     std::swap(b.ox, b.ox2);
     std::swap(b.oy, b.oy2);
     std::swap(b.oz, b.oz2);
-    std::swap(b.fvx, b.fvx2);
-    std::swap(b.fvy, b.fvy2);
-    std::swap(b.fvz, b.fvz2);
+    if (!defer_vel) {
+        std::swap(b.fvx, b.fvx2);
+        std::swap(b.fvy, b.fvy2);
+        std::swap(b.fvz, b.fvz2);
+    }
     std::swap(b.fm, b.fm2);
     std::swap(b.id, b.id2);
     b.sorted = 1;
@@ -1426,7 +1662,7 @@ nyxpm_status mixed_sort(Ctx& c, Box& b)
 nyxpm_status mixed_deposit(Ctx& c, Box& b)
 {
     const int n = b.n;
-    dim3 grid((n + kTx - 1) / kTx, (n + kTy - 1) / kTy, (n + kTz - 1) / kTz);
+    dim3 grid((n + kDepTx - 1) / kDepTx, (n + kDepTy - 1) / kDepTy, (n + kDepTz - 1) / kDepTz);
     const double dx = b.L / n;
     const double inv_vol = 1.0 / (dx * dx * dx);
     const float scale = (float)(b.uniform_mass ? b.mscalar * inv_vol : inv_vol);
@@ -1439,8 +1675,11 @@ nyxpm_status mixed_deposit(Ctx& c, Box& b)
     k_mx_deposit_heavy<<<c.sm_count * 4, 256, 0, c.stream>>>(n, b.cell, b.ox, b.oy, b.oz, mq,
                                                              b.cell_start, b.long_list, b.long_count,
                                                              b.key_slot, heavy);
-    k_mx_deposit<<<grid, 256, 0, c.stream>>>(n, scale, b.cell, b.ox, b.oy, b.oz, mq, b.cell_start,
-                                             b.key_slot, heavy, b.frho);
+    // more than the default 48 KB of dynamic shared memory (set on every call: the
+    // attribute belongs to the current device)
+    cudaFuncSetAttribute(k_mx_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDepSmem);
+    k_mx_deposit<<<grid, kDepThreads, kDepSmem, c.stream>>>(n, scale, b.cell, b.ox, b.oy, b.oz, mq,
+                                                            b.cell_start, b.key_slot, heavy, b.frho);
     c.launches += 1;
     prof_end(c, NYXPM_ST_DEPOSIT, (b.uniform_mass ? 16.0 : 20.0) * b.np + 8.0 * nc);
     return check_launch(c, "mixed deposit");

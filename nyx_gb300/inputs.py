@@ -64,8 +64,9 @@ class RunConfig:
     absolute_max_change_a: float
     dt_binpow: float
     dt_cutoff: float
-    particle_file: str         # the particle file, or cosmo.initDirName for "cosmological"
-    particle_format: str       # ascii | binary | binary_meta | cosmological
+    particle_file: str         # the particle file, cosmo.initDirName for "cosmological",
+                               # <restart_particle_file>/DM for "restart"
+    particle_format: str       # ascii | binary | binary_meta | cosmological | restart
     ic_source: str             # cosmo.ic-source (MUSIC | nyx) for "cosmological"
     n_particles: int           # nyx.n_particles per edge (the nyx source's particle mass)
     plot_int: int
@@ -74,6 +75,7 @@ class RunConfig:
     check_file: str
     data_log: str
     restart: str
+    ascii_output: bool = False  # particles.dm_particle_output_ascii: plotfiles add particles.ascii
 
 
 def run_config(d: dict[str, list[str]], base_dir: str = ".") -> RunConfig:
@@ -99,10 +101,10 @@ def run_config(d: dict[str, list[str]], base_dir: str = ".") -> RunConfig:
         raise ValueError("the domain must be a cube with geometry.prob_lo = 0 0 0")
     init = _str(d, "nyx.particle_init_type", "AsciiFile")
     fmt = {"AsciiFile": "ascii", "BinaryFile": "binary", "BinaryMetaFile": "binary_meta",
-           "Cosmological": "cosmological"}.get(init)
+           "Cosmological": "cosmological", "Restart": "restart"}.get(init)
     if fmt is None:
         raise ValueError(f"nyx.particle_init_type {init} is not supported "
-                         "(AsciiFile, BinaryFile, BinaryMetaFile, Cosmological)")
+                         "(AsciiFile, BinaryFile, BinaryMetaFile, Cosmological, Restart)")
     ic_source, n_part = "", ncell[0]
     if fmt == "cosmological":
         # Nyx::initcosmo (Source/Initialization/Nyx_initcosmo.cpp:100-427): the IC
@@ -120,6 +122,9 @@ def run_config(d: dict[str, list[str]], base_dir: str = ".") -> RunConfig:
             if len(set(npv)) != 1:
                 raise ValueError("nyx.n_particles must be the same on each axis")
             n_part = npv[0]
+    elif fmt == "restart":
+        # the DM directory of a plotfile or checkpoint (NyxParticles.cpp:584-586)
+        key = "nyx.restart_particle_file"
     else:
         key = "nyx.ascii_particle_file" if fmt == "ascii" else "nyx.binary_particle_file"
     pfile = _str(d, key, "")
@@ -127,6 +132,8 @@ def run_config(d: dict[str, list[str]], base_dir: str = ".") -> RunConfig:
         raise ValueError(f"{key} is required for particle_init_type {init}")
     if not os.path.isabs(pfile):
         pfile = os.path.join(base_dir, pfile)
+    if fmt == "restart":
+        pfile = os.path.join(pfile, "DM")
     final_a = _get(d, "nyx.final_a", -1.0)
     final_z = _get(d, "nyx.final_z", -1.0)
     if final_a <= 0 and final_z >= 0:
@@ -145,4 +152,5 @@ def run_config(d: dict[str, list[str]], base_dir: str = ".") -> RunConfig:
         particle_file=pfile, particle_format=fmt, ic_source=ic_source, n_particles=n_part,
         plot_int=_get(d, "amr.plot_int", -1, int), plot_file=_str(d, "amr.plot_file", "plt"),
         check_int=_get(d, "amr.check_int", -1, int), check_file=_str(d, "amr.check_file", "chk"),
-        data_log=_str(d, "amr.data_log", ""), restart=_str(d, "amr.restart", ""))
+        data_log=_str(d, "amr.data_log", ""), restart=_str(d, "amr.restart", ""),
+        ascii_output=_get(d, "particles.dm_particle_output_ascii", 0, int) != 0)

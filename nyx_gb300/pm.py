@@ -86,11 +86,13 @@ class Context:
     def launch_count(self) -> int:
         return int(self.lib.nyxpm_launch_count(self.handle))
 
-    def measure_fp64_peak(self) -> float:
-        """FP64 TFLOP/s this GPU sustains on FMA chains (nyxpm_measure_fp64_peak)."""
-        v = C.c_double(0)
-        self.check(self.lib.nyxpm_measure_fp64_peak(self.handle, C.byref(v)), "measure_fp64_peak")
-        return v.value
+    def measure_fp64_peak(self) -> tuple[float, float]:
+        """(FP64 TFLOP/s on FMA chains, T FP64 additions/s) this GPU sustains
+        (nyxpm_measure_fp64_peak)."""
+        v, a = C.c_double(0), C.c_double(0)
+        self.check(self.lib.nyxpm_measure_fp64_peak(self.handle, C.byref(v), C.byref(a)),
+                   "measure_fp64_peak")
+        return v.value, a.value
 
     def set_profiling(self, on: bool):
         self.check(self.lib.nyxpm_set_profiling(self.handle, 1 if on else 0), "set_profiling")
@@ -406,6 +408,39 @@ def cosmo_1ppc_particles(n: int, L: float, disp, vel, disp_fac, vel_fac):
     if st != _L.NYXPM_OK:
         raise NyxPMError(st, "cosmo_1ppc_particles: bad arguments")
     return pos, v
+
+
+def particles_info(directory: str) -> dict:
+    """Header of an AMReX particle directory (a checkpoint's or plotfile's "DM")."""
+    lib = _L.load()
+    h = _L.ParticleHeader()
+    _io_call(lib.nyxpm_particles_info, str(directory).encode(), C.byref(h))
+    return h.as_dict()
+
+
+def read_particles_dir(directory: str, with_ids: bool = False):
+    """The particles of an AMReX particle directory -> (pos, vel, mass[, ids])."""
+    lib = _L.load()
+    n = particles_info(directory)["num_particles"]
+    pos, vel, mass = np.empty((n, 3)), np.empty((n, 3)), np.empty(n)
+    ids = np.empty(n, dtype=np.int64) if with_ids else None
+    got = C.c_int64(0)
+    _io_call(lib.nyxpm_particles_read, str(directory).encode(), n, _ptr(pos), _ptr(vel), _ptr(mass),
+             _ptr(ids), C.byref(got))
+    out = (pos[:got.value], vel[:got.value], mass[:got.value])
+    return out + (ids[:got.value],) if with_ids else out
+
+
+def write_particles_dir(directory: str, n: int, pos, vel, mass, checkpoint: bool = True,
+                        single_precision: bool = False):
+    """Write particles as an AMReX particle directory (Version_Two_Dot_Zero), one grid
+    over the n^3 domain; mass is an array or a scalar."""
+    lib = _L.load()
+    pos, vel = _f64(pos), _f64(vel)
+    marr = None if np.ndim(mass) == 0 else _f64(mass)
+    _io_call(lib.nyxpm_particles_write, str(directory).encode(), int(n), len(pos), _ptr(pos), _ptr(vel),
+             _ptr(marr), float(mass) if marr is None else 0.0, 1 if checkpoint else 0,
+             1 if single_precision else 0)
 
 
 def write_comoving_a(directory: str, a: float):

@@ -18,12 +18,18 @@ What it does, following Nyx's driver on one periodic level:
 Output:
 - ``amr.data_log``: the runlog, one line of nstep, time, dt, z, a per step
   (Source/IO/write_info.cpp:46-60).
-- ``amr.plot_file`` directories every ``amr.plot_int`` steps: the particles as an
-  AsciiFile and the ``comoving_a`` file.
-- ``amr.check_file`` directories every ``amr.check_int`` steps: the particles as
-  a float64 BinaryFile, the potential (``phi.f64``), ``comoving_a`` and the
-  exact step, time, dt and a.  ``amr.restart = <dir>`` resumes from one bit for
-  bit (FP64 path).
+- ``amr.plot_file`` directories every ``amr.plot_int`` steps: the particles in
+  ``DM/`` as Nyx's plotfile writes them (the AMReX particle layout
+  Version_Two_Dot_Zero, float64, no ids, with the ``precision`` file of
+  Source/IO/Nyx_output.cpp:677-688), ``particles.ascii`` when
+  ``particles.dm_particle_output_ascii = 1``, and the ``comoving_a`` file.
+- ``amr.check_file`` directories every ``amr.check_int`` steps: the particles in
+  ``DM/`` as Nyx's checkpoint writes them (the same layout with ids, float64:
+  a Nyx restart with ``nyx.particle_init_type = Restart`` reads them), the
+  potential (``phi.f64``), ``comoving_a`` and the exact step, time, dt and a.
+  ``amr.restart = <dir>`` resumes from one bit for bit (FP64 path).
+- ``nyx.particle_init_type = Restart`` starts from the ``DM/`` particles of a
+  Nyx plotfile or checkpoint named by ``nyx.restart_particle_file``.
 """
 from __future__ import annotations
 
@@ -37,23 +43,27 @@ import numpy as np
 
 from . import inputs as _inputs
 from .multifab import read_ic_fields
-from .pm import (Box, Context, read_comoving_a, read_particle_file, uniform_mass,
-                 write_comoving_a, write_particle_file)
+from .pm import (Box, Context, read_comoving_a, read_particle_file, read_particles_dir,
+                 uniform_mass, write_comoving_a, write_particle_file, write_particles_dir)
 
 STATE_FILE = "run_state.json"
 PHI_FILE = "phi.f64"            # PhiGrav_Type, n^3 float64, x fastest
 
 
-def _write_dir(path, box, step, t, dt, a, exact):
+def _write_dir(path, box, step, t, dt, a, exact, ascii_output=False):
     os.makedirs(path, exist_ok=True)
     pos, vel = box.download()
+    # the DM directory as Nyx writes it (particle_check_point / particle_plot_file)
+    write_particles_dir(os.path.join(path, "DM"), box.n, pos, vel, box.mass, checkpoint=exact)
     if exact:
-        write_particle_file(os.path.join(path, "particles.bin"), pos, vel, box.mass, "binary64")
         box.get_phi().tofile(os.path.join(path, PHI_FILE))
         with open(os.path.join(path, STATE_FILE), "w") as f:
             json.dump({"step": step, "time": t.hex(), "dt": dt.hex(), "a": a.hex()}, f)
     else:
-        write_particle_file(os.path.join(path, "particles.ascii"), pos, vel, box.mass, "ascii")
+        with open(os.path.join(path, "DM", "precision"), "w") as f:
+            f.write("NATIVE\n")
+        if ascii_output:
+            write_particle_file(os.path.join(path, "particles.ascii"), pos, vel, box.mass, "ascii")
     write_comoving_a(path, a)
 
 
@@ -73,13 +83,15 @@ def run(inputs_path: str, overrides: list[str] | None = None, precision: str = "
             st = json.load(f)
         step, t, dt_old, a = (st["step"], float.fromhex(st["time"]), float.fromhex(st["dt"]),
                               float.fromhex(st["a"]))
-        pos, vel, mass = read_particle_file(os.path.join(rdir, "particles.bin"), "binary")
+        pos, vel, mass = read_particles_dir(os.path.join(rdir, "DM"))
         if abs(read_comoving_a(rdir) - a) > 1e-14 * a:
             raise ValueError(f"{rdir}: comoving_a does not match the run state")
     else:
         step, t, dt_old = 0, 0.0, -1.0
         a = 1.0 / (1.0 + cfg.initial_z)
-        if cfg.particle_format != "cosmological":
+        if cfg.particle_format == "restart":
+            pos, vel, mass = read_particles_dir(cfg.particle_file)
+        elif cfg.particle_format != "cosmological":
             pos, vel, mass = read_particle_file(cfg.particle_file, cfg.particle_format)
     if not cfg.restart and cfg.particle_format == "cosmological":
         disp, ivel = read_ic_fields(cfg.particle_file, cfg.ic_source, cfg.n)
@@ -124,7 +136,8 @@ def run(inputs_path: str, overrides: list[str] | None = None, precision: str = "
         if verbose:
             print(f"step {step:6d}  a {a:.8f}  z {1.0 / a - 1.0:9.4f}  dt {dt:.4e}", file=sys.stderr)
         if cfg.plot_int > 0 and step % cfg.plot_int == 0:
-            _write_dir(os.path.join(out_dir, f"{cfg.plot_file}{step:05d}"), box, step, t, dt, a, False)
+            _write_dir(os.path.join(out_dir, f"{cfg.plot_file}{step:05d}"), box, step, t, dt, a, False,
+                       cfg.ascii_output)
         if cfg.check_int > 0 and step % cfg.check_int == 0:
             _write_dir(os.path.join(out_dir, f"{cfg.check_file}{step:05d}"), box, step, t, dt, a, True)
     wall = time.perf_counter() - t0

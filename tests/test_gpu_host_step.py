@@ -1,6 +1,7 @@
-"""nyxpm_step_host (upload + step + download in one call, the transfers of an FP64
-box overlapped with the step on a second stream) gives the results of the three
-calls, bit for bit; a non-finite input is reported as an error."""
+"""nyxpm_step_host (upload + step + download in one call, the transfers
+overlapped with the step on a second stream, FP64 and mixed boxes) gives the
+results of the three calls, bit for bit; a non-finite input is reported as an
+error."""
 from __future__ import annotations
 
 import numpy as np
@@ -14,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("precision,reuse,per_particle_mass",
                          [("fp64", False, False), ("fp64", True, False), ("fp64", False, True),
-                          ("mixed", False, False)])
+                          ("mixed", False, False), ("mixed", True, False), ("mixed", False, True)])
 def test_host_step_equals_upload_step_download(ctx, precision, reuse, per_particle_mass):
     n = 32
     ic = config1_ics(n, seed=7)
@@ -41,14 +42,16 @@ def test_host_step_equals_upload_step_download(ctx, precision, reuse, per_partic
     b2.close()
 
 
-def test_host_step_reports_non_finite_input(ctx):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_host_step_reports_non_finite_input(ctx, precision):
     n = 16
     ic = config1_ics(n, seed=8)
-    b = Box(ctx, n, 1.0, len(ic.pos))
+    b = Box(ctx, n, 1.0, len(ic.pos), precision=precision)
     b.upload(ic.pos, ic.vel, ic.mass)
-    p, v = ic.pos.copy(), ic.vel.copy()
-    v[5, 1] = np.nan
-    with pytest.raises(NyxPMError) as e:
-        b.step_host(p, v, ic.mass, 0.02, 0.021, 1e-3)
-    assert "non-finite" in str(e.value)
+    for which in ("vel", "pos"):
+        p, v = ic.pos.copy(), ic.vel.copy()
+        (v if which == "vel" else p)[5, 1] = np.nan
+        with pytest.raises(NyxPMError) as e:
+            b.step_host(p, v, ic.mass, 0.02, 0.021, 1e-3)
+        assert "non-finite" in str(e.value)
     b.close()

@@ -152,3 +152,29 @@ def test_mixed_zero_guess_solve_meets_the_fp64_tolerance(ctx, n):
     r2, _ = true_resnorm(b, n, L, 0.05)
     assert r2 <= 1.05e-10 * max(bnorm, info2["resnorm0"]), (r2, info2)
     b.close()
+
+
+def test_mixed_deposit_clustered_vs_oracle(ctx):
+    """The FP32 deposit on clustered particles: windows of a tile holding many
+    chunks of particles, keys of up to a warp's worth (summed in order by one
+    thread) and keys longer than a warp (summed by the warp pass), against the
+    FP64 oracle's density; deterministic run to run."""
+    n, L = 32, 1.0
+    rng = np.random.default_rng(21)
+    pos = np.concatenate([rng.random((20000, 3)),                      # background
+                          0.40 + 0.03 * rng.random((6000, 3)),         # keys of ~5-40
+                          0.71 + 0.004 * rng.random((1500, 3)),        # keys of hundreds
+                          0.1 + 0.5 * rng.random((4000, 3)) * [1, 0.05, 0.05]])
+    mass = 3.0e9
+    p = O.Particles(pos, np.zeros_like(pos), mass)
+    rho_o = O.deposit(n, L, p, O.sort(n, L, p))
+    b = Box(ctx, n, L, len(pos), precision="mixed")
+    b.upload(pos, np.zeros_like(pos), mass)
+    r1 = b.deposit()
+    b.redistribute()
+    r2 = b.deposit()
+    assert np.array_equal(r1, r2)
+    assert rel_l2(r1, rho_o) <= 2e-6, rel_l2(r1, rho_o)
+    big = rho_o > 0.1 * rho_o.max()
+    assert np.abs(r1[big] / rho_o[big] - 1).max() <= 1e-5
+    b.close()

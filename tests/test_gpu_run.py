@@ -13,7 +13,8 @@ import os
 import numpy as np
 import pytest
 
-from nyx_gb300.pm import Box, read_comoving_a, write_particle_file
+from nyx_gb300.pm import (Box, particles_info, read_comoving_a, read_particles_dir,
+                          write_particle_file)
 from nyx_gb300.run import run
 from tests.pm_cases import config1_ics
 
@@ -73,6 +74,12 @@ def test_run_matches_the_library_calls_and_restarts_exactly(ctx, tmp_path):
     assert len(log) == 7 and log[0].startswith("#")
     for d in ("plt00002", "plt00004", "plt00006", "chk00003", "chk00006"):
         assert (tmp_path / d / "comoving_a").exists(), d
+        assert (tmp_path / d / "DM" / "Header").exists(), d
+    # the checkpoint's DM directory holds the particles of step 3 with their ids
+    assert particles_info(str(tmp_path / "chk00003" / "DM"))["is_checkpoint"] == 1
+    assert particles_info(str(tmp_path / "plt00006" / "DM"))["is_checkpoint"] == 0
+    ppos, pvel, _ = read_particles_dir(str(tmp_path / "plt00006" / "DM"))
+    assert np.array_equal(ppos, res["pos"]) and np.array_equal(pvel, res["vel"])
     assert abs(read_comoving_a(str(tmp_path / "chk00006")) - a) <= 1e-14 * a
     assert (tmp_path / "chk00003" / "phi.f64").stat().st_size == 8 * 16 ** 3
     # restart from step 3 and finish: the uninterrupted result, bit for bit
@@ -82,6 +89,11 @@ def test_run_matches_the_library_calls_and_restarts_exactly(ctx, tmp_path):
                out_dir=str(out2), verbose=False)
     assert res2["steps"] == 3 and res2["last_step"] == 6
     assert np.array_equal(res2["pos"], res["pos"]) and np.array_equal(res2["vel"], res["vel"])
+    # a run that starts from the plotfile's particles (nyx.particle_init_type = Restart)
+    res3 = run(inp, ["nyx.particle_init_type=Restart", "nyx.restart_particle_file=plt00006",
+                     "max_step=1", "amr.data_log=", "amr.plot_int=-1", "amr.check_int=-1"],
+               out_dir=str(tmp_path), verbose=False)
+    assert res3["steps"] == 1 and res3["particles"] == len(res["pos"])
 
 
 def test_mixed_precision_run(tmp_path):

@@ -78,3 +78,18 @@ def test_the_references_dm_only_inputs():
     with pytest.raises(ValueError, match="do_hydro"):
         run_config(read_inputs(os.path.join(os.path.dirname(NOHYDRO), "inputs")),
                    os.path.dirname(NOHYDRO))
+
+
+def test_restart_init_type(tmp_path):
+    """particle_init_type = Restart takes the DM directory of the plotfile or
+    checkpoint that nyx.restart_particle_file names (NyxParticles.cpp:584-586)."""
+    base = {"amr.n_cell": ["16", "16", "16"], "geometry.prob_hi": ["1", "1", "1"],
+            "nyx.do_hydro": ["0"], "nyx.particle_init_type": ["Restart"],
+            "nyx.restart_particle_file": ["plt00100"], "particles.dm_particle_output_ascii": ["1"]}
+    cfg = run_config(dict(base), str(tmp_path))
+    assert cfg.particle_format == "restart" and cfg.ascii_output
+    assert cfg.particle_file == os.path.join(str(tmp_path), "plt00100", "DM")
+    d = dict(base)
+    del d["nyx.restart_particle_file"]
+    with pytest.raises(ValueError, match="restart_particle_file"):
+        run_config(d, str(tmp_path))

@@ -418,6 +418,7 @@ typedef struct nyxpm_tuning {
     int smooth_rows;        /* plane rows per multigrid work item: 1, 2, 4 or 8 */
     int inner_vcycles;      /* FP32 V-cycles per FP64 defect-correction iteration */
     int max_outer;          /* defect-correction iterations inside the step graph */
+    int sort_bucket;        /* particles per work item of the sort and the kicks: 256, 512 or 1024 */
 } nyxpm_tuning;
 
 typedef struct nyxpm_ensemble_info {

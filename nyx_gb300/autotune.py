@@ -1,9 +1,10 @@
 """Autotuner for the batched ensemble step.
 
 The knobs are the shapes the batched kernels take from nyxpm_tuning: the CIC
-deposit tile (8x8x8, 8x8x4 or 16x8x4 cells per work item), the number of plane
-rows per multigrid work item (the smoother block height) and the number of
-FP32 V-cycles per FP64 defect-correction iteration.  The tuner runs coordinate
+deposit tile (8x8x8, 8x8x4 or 16x8x4 cells per work item), the sort bucket (256,
+512 or 1024 particles per work item of the counting sort and the kicks), the
+number of plane rows per multigrid work item (the smoother block height) and the
+number of FP32 V-cycles per FP64 defect-correction iteration.  The tuner runs coordinate
 descent on a scratch ensemble built from a size-stratified sample of the real
 boxes: for each knob in turn it times a few steps per candidate value (CUDA
 events inside nyxpm_ensemble_step, after a warm-up step that captures the new
@@ -23,6 +24,7 @@ from .ensemble import Ensemble, box_ics
 
 CANDIDATES = {
     "deposit_tile": (0, 1, 2),
+    "sort_bucket": (256, 512, 1024),
     "smooth_rows": (2, 4, 8),
     "inner_vcycles": (1, 2, 3),
 }

@@ -34,7 +34,9 @@ namespace nyxpm {
 namespace {
 
 constexpr int kMaxLev = 9;
-constexpr int kPT = 256;             // particles per particle work item
+constexpr int kPT = 256;             // threads of the particle kernels' blocks
+// particles per particle work item (the sort's and the kicks' bucket): the
+// nyxpm_tuning knob sort_bucket, a multiple of kPT
 constexpr int kScanT = 512, kScanIPT = 8, kScanTile = kScanT * kScanIPT;
 constexpr float kSixthF = 1.0f / 6.0f;
 constexpr double kSixth = 1.0 / 6.0;
@@ -152,12 +154,13 @@ __global__ void e_load_step(int nbox, const EStep* __restrict__ st, const EDesc*
 }
 
 // ---------------------------------------------------------------------------
-// particle stages: item = (box, chunk of kPT particles)
+// particle stages: item = (box, bucket of `bucket` consecutive particles), a
+// block of kPT threads striding through the bucket
 // ---------------------------------------------------------------------------
 // phase 0: kick-drift (a_old -> a_half, move); phase 1: kick (a_half -> a_new)
 __global__ void __launch_bounds__(kPT, 4) e_kick(const Item* __restrict__ items, int nitems,
                                                const EDesc* __restrict__ D, const EState* __restrict__ S,
-                                               int phase)
+                                               int phase, int bucket)
 {
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
@@ -165,8 +168,9 @@ __global__ void __launch_bounds__(kPT, 4) e_kick(const Item* __restrict__ items,
         const EState& st = S[it.box];
         if (!st.active) continue;
         const EDesc& d = D[it.box];
-        const long long q = (long long)it.a * kPT + threadIdx.x;
-        if (q >= d.np) continue;
+      for (int t = threadIdx.x; t < bucket; t += kPT) {
+        const long long q = (long long)it.a * bucket + t;
+        if (q >= d.np) break;
         const PArr P = parr(d, st.parity);
         const int n = d.n;
         const float a_prev = st.kick[phase][0];
@@ -231,65 +235,75 @@ __global__ void __launch_bounds__(kPT, 4) e_kick(const Item* __restrict__ items,
             P.oy[q] = o[1];
             P.oz[q] = o[2];
         }
+      }
     }
 }
 
 __global__ void __launch_bounds__(kPT) e_keys(const Item* __restrict__ items, int nitems,
-                                               const EDesc* __restrict__ D, const EState* __restrict__ S)
+                                               const EDesc* __restrict__ D, const EState* __restrict__ S,
+                                               int bucket)
 {
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
         const EState st = S[it.box];
         if (!st.active) continue;
         const EDesc& d = D[it.box];
-        const long long q = (long long)it.a * kPT + threadIdx.x;
-        if (q >= d.np) continue;
         const PArr P = parr(d, st.parity);
-        const int c = P.cell[q];
-        float f;
-        const int i = key_frac(cell_i(c), P.ox[q], d.n, &f);
-        const int j = key_frac(cell_j(c), P.oy[q], d.n, &f);
-        const int k = key_frac(cell_k(c), P.oz[q], d.n, &f);
-        const int K = (int)cidx(i, j, k, d.n);
-        d.key[q] = K;
-        atomicAdd(d.cell_count + K, 1);
+        for (int t = threadIdx.x; t < bucket; t += kPT) {
+            const long long q = (long long)it.a * bucket + t;
+            if (q >= d.np) break;
+            const int c = P.cell[q];
+            float f;
+            const int i = key_frac(cell_i(c), P.ox[q], d.n, &f);
+            const int j = key_frac(cell_j(c), P.oy[q], d.n, &f);
+            const int k = key_frac(cell_k(c), P.oz[q], d.n, &f);
+            const int K = (int)cidx(i, j, k, d.n);
+            d.key[q] = K;
+            atomicAdd(d.cell_count + K, 1);
+        }
     }
 }
 
 __global__ void __launch_bounds__(kPT) e_scatter(const Item* __restrict__ items, int nitems,
-                                                  const EDesc* __restrict__ D, const EState* __restrict__ S)
+                                                  const EDesc* __restrict__ D, const EState* __restrict__ S,
+                                                  int bucket)
 {
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
         if (!S[it.box].active) continue;
         const EDesc& d = D[it.box];
-        const long long q = (long long)it.a * kPT + threadIdx.x;
-        if (q >= d.np) continue;
-        const int K = d.key[q];
-        d.perm[d.cell_start[K] + atomicSub(d.cell_count + K, 1) - 1] = (int)q;
+        for (int t = threadIdx.x; t < bucket; t += kPT) {
+            const long long q = (long long)it.a * bucket + t;
+            if (q >= d.np) break;
+            const int K = d.key[q];
+            d.perm[d.cell_start[K] + atomicSub(d.cell_count + K, 1) - 1] = (int)q;
+        }
     }
 }
 
 __global__ void __launch_bounds__(kPT) e_gather(const Item* __restrict__ items, int nitems,
-                                                 const EDesc* __restrict__ D, const EState* __restrict__ S)
+                                                 const EDesc* __restrict__ D, const EState* __restrict__ S,
+                                                 int bucket)
 {
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
         const EState st = S[it.box];
         if (!st.active) continue;
         const EDesc& d = D[it.box];
-        const long long s = (long long)it.a * kPT + threadIdx.x;
-        if (s >= d.np) continue;
         const PArr A = parr(d, st.parity), B = parr(d, st.parity ^ 1);
-        const int q = d.perm[s];
-        B.cell[s] = A.cell[q];
-        B.ox[s] = A.ox[q];
-        B.oy[s] = A.oy[q];
-        B.oz[s] = A.oz[q];
-        B.vx[s] = A.vx[q];
-        B.vy[s] = A.vy[q];
-        B.vz[s] = A.vz[q];
-        B.id[s] = A.id[q];
+        for (int t = threadIdx.x; t < bucket; t += kPT) {
+            const long long s = (long long)it.a * bucket + t;
+            if (s >= d.np) break;
+            const int q = d.perm[s];
+            B.cell[s] = A.cell[q];
+            B.ox[s] = A.ox[q];
+            B.oy[s] = A.oy[q];
+            B.oz[s] = A.oz[q];
+            B.vx[s] = A.vx[q];
+            B.vy[s] = A.vy[q];
+            B.vz[s] = A.vz[q];
+            B.id[s] = A.id[q];
+        }
     }
 }
 
@@ -1579,7 +1593,8 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
     for (int b = 0; b < nbox; ++b) {
         const EnsSlot& s = E->slots[b];
         if (!s.used) continue;
-        for (long long ch = 0; ch < (s.desc.np + kPT - 1) / kPT; ++ch) items.push_back(Item{b, (int)ch, 0, 0});
+        const long long bk = E->tune.sort_bucket;
+        for (long long ch = 0; ch < (s.desc.np + bk - 1) / bk; ++ch) items.push_back(Item{b, (int)ch, 0, 0});
     }
     end(E->r_part);
     begin(E->r_scan);
@@ -1789,7 +1804,8 @@ void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
     const unsigned bb = (unsigned)((nbox + 127) / 128);
     ep_begin(c);
     e_sort_reset<<<bb, 128, 0, s>>>(nbox, D, S);
-    e_keys<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S);
+    e_keys<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S,
+                                                   E->tune.sort_bucket);
     ep_end(c, NYXPM_ST_KEYS);
     ep_begin(c);
     e_scan_reduce<<<pgrid(E, E->r_scan.cnt), kScanT, 0, s>>>(it + E->r_scan.off, E->r_scan.cnt, D, S);
@@ -1797,12 +1813,14 @@ void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
     e_scan_down<<<pgrid(E, E->r_scan.cnt), kScanT, 0, s>>>(it + E->r_scan.off, E->r_scan.cnt, D, S);
     ep_end(c, NYXPM_ST_SCAN);
     ep_begin(c);
-    e_scatter<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S);
+    e_scatter<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S,
+                                                      E->tune.sort_bucket);
     e_fix_short<<<pgrid(E, E->r_keys.cnt), 256, 0, s>>>(it + E->r_keys.off, E->r_keys.cnt, D, S);
     e_fix_long<<<E->sm * 2, 512, 0, s>>>(nbox, D, S);
     ep_end(c, NYXPM_ST_SCATTER);
     ep_begin(c);
-    e_gather<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S);
+    e_gather<<<pgrid(E, E->r_part.cnt), kPT, 0, s>>>(it + E->r_part.off, E->r_part.cnt, D, S,
+                                                     E->tune.sort_bucket);
     e_flip<<<bb, 128, 0, s>>>(nbox, S);
     ep_end(c, NYXPM_ST_GATHER);
     ep_begin(c);
@@ -1936,7 +1954,8 @@ void enqueue_kick(nyxpm_ctx* c, nyxpm_ensemble* E, int phase)
 {
     ep_begin(c);
     e_kick<<<pgrid(E, E->r_part.cnt), kPT, 0, c->stream>>>(E->d_items + E->r_part.off, E->r_part.cnt,
-                                                            E->d_desc, E->d_state, phase);
+                                                            E->d_desc, E->d_state, phase,
+                                                            E->tune.sort_bucket);
     ep_end(c, NYXPM_ST_KICK);
     c->launches += 1;
 }
@@ -2033,6 +2052,7 @@ nyxpm_status nyxpm_ensemble_create(nyxpm_ctx* c, size_t arena_bytes, nyxpm_ensem
     E->tune.smooth_rows = 8;
     E->tune.inner_vcycles = c->p.mixed_inner_vcycles;
     E->tune.max_outer = 6;
+    E->tune.sort_bucket = 256;
     E->sm = c->sm_count;
     *out = E;
     return NYXPM_OK;
@@ -2310,7 +2330,8 @@ nyxpm_status nyxpm_ensemble_set_tuning(nyxpm_ctx* c, nyxpm_ensemble* E, const ny
     if (!c || !E || !t) return NYXPM_INVALID_ARG;
     if (t->deposit_tile < 0 || t->deposit_tile > 2 ||
         (t->smooth_rows != 1 && t->smooth_rows != 2 && t->smooth_rows != 4 && t->smooth_rows != 8) ||
-        t->inner_vcycles < 1 || t->inner_vcycles > 8 || t->max_outer < 1 || t->max_outer > 64)
+        t->inner_vcycles < 1 || t->inner_vcycles > 8 || t->max_outer < 1 || t->max_outer > 64 ||
+        (t->sort_bucket != 256 && t->sort_bucket != 512 && t->sort_bucket != 1024))
         return efail(c, NYXPM_INVALID_ARG, "bad tuning");
     E->tune = *t;
     E->dirty = 1;

@@ -136,7 +136,8 @@ class ContinuousBatchingServer:
         self.ens = Ensemble(ctx, budget_bytes)
         if tuning:
             self.ens.set_tuning(**{k: v for k, v in tuning.items()
-                                   if k in ("deposit_tile", "smooth_rows", "inner_vcycles", "max_outer")})
+                                   if k in ("deposit_tile", "smooth_rows", "inner_vcycles", "max_outer",
+                                            "sort_bucket")})
         self.ic_provider = ic_provider
         self.keep = keep_results
         self.max_skip = max_skip

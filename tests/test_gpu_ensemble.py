@@ -7,7 +7,7 @@ stage over all boxes, captured step graphs).
   ensemble configuration draws (32 .. 128 cells, one and half a particle per
   cell);
 * a box's result is bitwise the same alone and inside a mix of other boxes;
-* the deposit tile and smoother row shapes do not change results;
+* the deposit tile, sort bucket and smoother row shapes do not change results;
 * the memory budget is enforced and freed memory is reused.
 """
 from __future__ import annotations
@@ -83,7 +83,8 @@ def test_shapes_do_not_change_results(ctx):
     ics = [box_ics(s, 0.05) for s in SPECS[:2]]
     sched = equal_da_schedule(0.05, 0.06, 2)
     base, _, _ = run_ensemble(ctx, SPECS[:2], ics, sched)
-    for tuning in ({"deposit_tile": 1, "smooth_rows": 2}, {"deposit_tile": 2, "smooth_rows": 4}):
+    for tuning in ({"deposit_tile": 1, "smooth_rows": 2, "sort_bucket": 512},
+                   {"deposit_tile": 2, "smooth_rows": 4, "sort_bucket": 1024}):
         other, _, _ = run_ensemble(ctx, SPECS[:2], ics, sched, tuning)
         for (p0, v0), (p1, v1) in zip(base, other):
             assert np.array_equal(p0, p1) and np.array_equal(v0, v1)

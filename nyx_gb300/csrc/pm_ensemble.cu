@@ -15,10 +15,13 @@
 // The arithmetic per box is that of the single-box mixed form (FP32
 // cell-relative particles, FP32 deposit and V-cycles, FP64 defect correction to
 // the context's relative tolerance, compensated FP64 mean, FP64 a(t) on the
-// host).  Convergence is per box: the solve graph runs max_outer
-// defect-correction iterations, a box that has met its tolerance skips the rest,
-// and boxes still above tolerance get further iterations before the gravity +
-// kick graph runs.
+// host).  Convergence is per box: a step is ONE graph -- the opening kick, the
+// deposit and max_outer defect-correction iterations, then a conditional WHILE
+// node that repeats one more iteration (the residual recomputed with the FP64
+// stencil) while any box is above its tolerance, up to max_vcycles, then the
+// gravity vector and the closing kick.  A box that has met its tolerance skips
+// the remaining iterations' work, so a slow box never changes another box's
+// result.
 #include "pm_common.cuh"
 #include "pm_tail.cuh"
 
@@ -730,6 +733,25 @@ __global__ void e_flags(int nbox, const EDesc* __restrict__ D, EState* S, double
     }
     d.norms[1] = 0ULL;
     d.norms[3] = 0ULL;
+}
+
+// The condition of the step graph's WHILE node: repeat while any active box is
+// above its tolerance and fewer than `limit` extra iterations ran.  One block;
+// inc: a loop body just ran (count it); else: the loop is about to start.
+__global__ void e_loop_cond(int nbox, const EState* __restrict__ S, int* loop, int limit, int inc,
+                            cudaGraphConditionalHandle h)
+{
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbox; b += blockDim.x)
+        if (S[b].active && S[b].solve_active) any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int it = inc ? loop[0] + 1 : 0;
+        loop[0] = it;
+        cudaGraphSetConditional(h, (any && it < limit) ? 1u : 0u);
+    }
 }
 
 __global__ void e_count_inner(int nbox, EState* S, int cycles)
@@ -1521,6 +1543,13 @@ struct nyxpm_ensemble {
     cudaGraphExec_t exec_solve = nullptr, exec_finish = nullptr;
     int sm = 0;
     int64_t graph_launches_solve = 0, graph_launches_finish = 0;
+    // the whole step as one graph (conditional WHILE node for the extra iterations)
+    cudaGraphExec_t exec_step = nullptr;
+    int64_t graph_launches_step = 0;   // launches of the graph without the loop body's
+    int64_t graph_launches_body = 0;   // launches of one loop body
+    int single_graph_failed = 0;       // the runtime refused it: the two graphs from then on
+    cudaStream_t body_stream = nullptr;// captures the loop body
+    int* d_loop = nullptr;             // [0] loop iterations of the last step
 };
 
 using namespace nyxpm;
@@ -1557,7 +1586,8 @@ void invalidate_graphs(nyxpm_ensemble* E)
 {
     if (E->exec_solve) cudaGraphExecDestroy(E->exec_solve);
     if (E->exec_finish) cudaGraphExecDestroy(E->exec_finish);
-    E->exec_solve = E->exec_finish = nullptr;
+    if (E->exec_step) cudaGraphExecDestroy(E->exec_step);
+    E->exec_solve = E->exec_finish = E->exec_step = nullptr;
 }
 
 bool slot_ok(nyxpm_ensemble* E, int slot)
@@ -1980,11 +2010,95 @@ nyxpm_status finish_unconverged(nyxpm_ctx* c, nyxpm_ensemble* E, int* extra)
             if (E->slots[b].used && E->h_state[b].active && E->h_state[b].solve_active) any = true;
         if (!any) return NYXPM_OK;
         if (guard == c->p.max_vcycles) break;
-        enqueue_iterations(c, E, 1, guard == 0 ? 1 : 0);
+        // each extra iteration refreshes the residual with the FP64 stencil, as
+        // the step graph's loop body does
+        enqueue_iterations(c, E, 1, 1);
         ETRY(echeck(c, "ensemble iterations"));
         *extra += 1;
     }
     return efail(c, NYXPM_NOT_CONVERGED, "ensemble: a box did not converge");
+}
+
+// The whole step as one graph: load, kick-drift, deposit and solve head,
+// max_outer iterations, then a WHILE node whose body is one more iteration (FP64
+// residual refresh) and the loop condition, then gravity and the closing kick.
+// The WHILE node is added to the graph under capture and its body captured on a
+// second stream; any refusal by the runtime returns an error and the caller
+// falls back to two graphs with the loop on the host.
+nyxpm_status capture_step(nyxpm_ctx* c, nyxpm_ensemble* E)
+{
+    if (c->prof_on) return efail(c, NYXPM_INVALID_ARG, "ensemble graphs are not captured while profiling");
+    const int nbox = (int)E->slots.size();
+    const int64_t l0 = c->launches;
+    cudaGraph_t g = nullptr;
+    cudaStream_t main = c->stream;
+    if (cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return echeck(c, "ensemble capture begin");
+    bool ok = true;
+    enqueue_load(c, E, E->h_step);
+    enqueue_kick(c, E, 0);
+    enqueue_solve_head(c, E);
+    enqueue_iterations(c, E, E->tune.max_outer, 0);
+    cudaGraph_t cg = nullptr;
+    cudaStreamCaptureStatus cs;
+    cudaGraphConditionalHandle h = 0;
+    ok = cudaStreamGetCaptureInfo(main, &cs, nullptr, &cg, nullptr, nullptr, nullptr) == cudaSuccess &&
+         cs == cudaStreamCaptureStatusActive &&
+         cudaGraphConditionalHandleCreate(&h, cg, 0, 0) == cudaSuccess;
+    int64_t body_launches = 0;
+    if (ok) {
+        e_loop_cond<<<1, 128, 0, main>>>(nbox, E->d_state, E->d_loop, c->p.max_vcycles, 0, h);
+        c->launches += 1;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        ok = cudaStreamGetCaptureInfo(main, &cs, nullptr, &cg, &deps, nullptr, &ndeps) == cudaSuccess;
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t wn = nullptr;
+        ok = ok && cudaGraphAddNode(&wn, cg, deps, nullptr, ndeps, &p) == cudaSuccess &&
+             cudaStreamUpdateCaptureDependencies(main, &wn, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+                 cudaSuccess;
+        if (ok) {
+            // the loop body, captured into the WHILE node's graph on the second stream
+            ok = cudaStreamBeginCaptureToGraph(E->body_stream, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (ok) {
+                const int64_t lb = c->launches;
+                c->stream = E->body_stream;
+                enqueue_iterations(c, E, 1, 1);
+                e_loop_cond<<<1, 128, 0, E->body_stream>>>(nbox, E->d_state, E->d_loop, c->p.max_vcycles, 1, h);
+                c->launches += 1;
+                c->stream = main;
+                body_launches = c->launches - lb;
+                c->launches = lb;
+                cudaGraph_t bg = nullptr;
+                ok = cudaStreamEndCapture(E->body_stream, &bg) == cudaSuccess;
+            }
+        }
+    }
+    if (ok) {
+        enqueue_grav(c, E);
+        enqueue_kick(c, E, 1);
+    }
+    const cudaError_t ce = cudaStreamEndCapture(main, &g);
+    cudaError_t ie = cudaErrorUnknown;
+    cudaGraphExec_t exec = nullptr;
+    if (ok && ce == cudaSuccess && g) ie = cudaGraphInstantiate(&exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    const int64_t n = c->launches - l0;
+    c->launches = l0;
+    if (!ok || ce != cudaSuccess || ie != cudaSuccess) {
+        cudaGetLastError();
+        if (exec) cudaGraphExecDestroy(exec);
+        return efail(c, NYXPM_CUDA_ERROR, "ensemble: the one-graph step was refused by the runtime");
+    }
+    E->exec_step = exec;
+    E->graph_launches_step = n;
+    E->graph_launches_body = body_launches;
+    return NYXPM_OK;
 }
 
 nyxpm_status capture(nyxpm_ctx* c, nyxpm_ensemble* E, cudaGraphExec_t* exec, int which)
@@ -2042,12 +2156,16 @@ nyxpm_status nyxpm_ensemble_create(nyxpm_ctx* c, size_t arena_bytes, nyxpm_ensem
         delete E;
         return efail(c, NYXPM_OOM, "ensemble arena (memory budget) could not be allocated");
     }
-    if (cudaMallocHost(&E->h_scratch, 64) != cudaSuccess) {
+    if (cudaMallocHost(&E->h_scratch, 64) != cudaSuccess || cudaMalloc(&E->d_loop, 64) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&E->body_stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
+        if (E->h_scratch) cudaFreeHost(E->h_scratch);
+        if (E->d_loop) cudaFree(E->d_loop);
         E->arena.destroy();
         delete E;
         return efail(c, NYXPM_OOM, "ensemble pinned scratch");
     }
+    cudaMemset(E->d_loop, 0, 64);
     E->tune.deposit_tile = 0;
     E->tune.smooth_rows = 8;
     E->tune.inner_vcycles = c->p.mixed_inner_vcycles;
@@ -2071,6 +2189,8 @@ nyxpm_status nyxpm_ensemble_destroy(nyxpm_ctx* c, nyxpm_ensemble* E)
     if (E->h_init) cudaFreeHost(E->h_init);
     if (E->h_state) cudaFreeHost(E->h_state);
     if (E->h_scratch) cudaFreeHost(E->h_scratch);
+    if (E->d_loop) cudaFree(E->d_loop);
+    if (E->body_stream) cudaStreamDestroy(E->body_stream);
     E->arena.destroy();
     delete E;
     return NYXPM_OK;
@@ -2359,6 +2479,7 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* c, nyxpm_ensemble* E, const double* 
     cudaEventCreate(&ev1);
     cudaEventRecord(ev0, c->stream);
     int extra = 0;
+    bool one_graph = false;
     // initial fields of boxes uploaded since their last step (an eager pass with
     // only those boxes active; the RHS of the init solve uses a_new = a_old)
     bool any_init = false;
@@ -2404,15 +2525,26 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* c, nyxpm_ensemble* E, const double* 
         enqueue_grav(c, E);
         enqueue_kick(c, E, 1);
     } else {
-        if (!E->exec_solve) ETRY(capture(c, E, &E->exec_solve, 0));
-        if (!E->exec_finish) ETRY(capture(c, E, &E->exec_finish, 1));
-        if (cudaGraphLaunch(E->exec_solve, c->stream) != cudaSuccess) return echeck(c, "ensemble solve graph");
-        c->launches += E->graph_launches_solve;
-        int more = 0;
-        ETRY(finish_unconverged(c, E, &more));
-        extra += more;
-        if (cudaGraphLaunch(E->exec_finish, c->stream) != cudaSuccess) return echeck(c, "ensemble finish graph");
-        c->launches += E->graph_launches_finish;
+        if (!E->exec_step && !E->single_graph_failed && capture_step(c, E) != NYXPM_OK)
+            E->single_graph_failed = 1;
+        if (E->exec_step) {
+            // the whole step: one graph launch
+            if (cudaGraphLaunch(E->exec_step, c->stream) != cudaSuccess) return echeck(c, "ensemble step graph");
+            cudaMemcpyAsync(E->h_scratch, E->d_loop, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+            one_graph = true;
+        } else {
+            if (!E->exec_solve) ETRY(capture(c, E, &E->exec_solve, 0));
+            if (!E->exec_finish) ETRY(capture(c, E, &E->exec_finish, 1));
+            if (cudaGraphLaunch(E->exec_solve, c->stream) != cudaSuccess)
+                return echeck(c, "ensemble solve graph");
+            c->launches += E->graph_launches_solve;
+            int more = 0;
+            ETRY(finish_unconverged(c, E, &more));
+            extra += more;
+            if (cudaGraphLaunch(E->exec_finish, c->stream) != cudaSuccess)
+                return echeck(c, "ensemble finish graph");
+            c->launches += E->graph_launches_finish;
+        }
     }
     cudaEventRecord(ev1, c->stream);
     if (cudaEventSynchronize(ev1) != cudaSuccess) return echeck(c, "ensemble step");
@@ -2421,6 +2553,15 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* c, nyxpm_ensemble* E, const double* 
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
     ETRY(pull_state(c, E));
+    bool unconverged = false;
+    if (one_graph) {
+        int loops = 0;
+        std::memcpy(&loops, E->h_scratch, sizeof(int));
+        extra += loops;
+        c->launches += E->graph_launches_step + loops * E->graph_launches_body;
+        for (int b = 0; b < nbox; ++b)
+            if (E->slots[b].used && E->h_state[b].active && E->h_state[b].solve_active) unconverged = true;
+    }
     if (info) {
         int mx = 0, inner = 0, boxes = 0;
         for (int b = 0; b < nbox; ++b)
@@ -2436,6 +2577,7 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* c, nyxpm_ensemble* E, const double* 
         info->launches = (int)(c->launches - launches0);
         info->ms = ms;
     }
+    if (unconverged) return efail(c, NYXPM_NOT_CONVERGED, "ensemble: a box did not converge");
     return NYXPM_OK;
 }
 

@@ -90,6 +90,27 @@ def test_shapes_do_not_change_results(ctx):
             assert np.array_equal(p0, p1) and np.array_equal(v0, v1)
 
 
+def test_one_graph_step_loops_on_the_device(ctx):
+    """With max_outer = 1 every box needs more defect-correction iterations than
+    the graph's fixed ones: the step graph's WHILE node runs them on the device,
+    one graph launch per step, and the result equals the eager step's (profiling
+    mode: the same kernels launched one by one, the extra iterations driven by the
+    host), bit for bit."""
+    ics = [box_ics(s, 0.05) for s in SPECS]
+    sched = equal_da_schedule(0.05, 0.07, 3)
+    graph, g_graph, infos = run_ensemble(ctx, SPECS, ics, sched, {"max_outer": 1})
+    assert all(i["fallback_iters"] > 0 for i in infos), infos
+    ctx.set_profiling(True)
+    try:
+        eager, g_eager, infos_e = run_ensemble(ctx, SPECS, ics, sched, {"max_outer": 1})
+    finally:
+        ctx.set_profiling(False)
+        ctx.profile(reset=True)
+    assert [i["fallback_iters"] for i in infos] == [i["fallback_iters"] for i in infos_e]
+    for (p0, v0), (p1, v1), ga, gb in zip(graph, eager, g_graph, g_eager):
+        assert np.array_equal(p0, p1) and np.array_equal(v0, v1) and np.array_equal(ga, gb)
+
+
 def test_budget_and_reuse(ctx):
     one = Ensemble.box_bytes(32, 32 ** 3)
     ens = Ensemble(ctx, int(one * 2.2))

@@ -309,32 +309,32 @@ __global__ void __launch_bounds__(256) k_mx_deposit_heavy(int n, const int* __re
 
 // One CTA per tile of 16 x 8 x 8 cells; its density needs the 17 x 9 x 9 keys
 // (cells of floor(x/dx + 1/2)) from the tile's own corner to one past its far
-// corner.  The keys' particles are contiguous runs of the sorted arrays (one
-// run per row of 17 keys, cut only where a row wraps), so the CTA
-// 1. reads cell_start for its keys and numbers their particles densely (a block
-//    scan of the per-key counts; keys longer than a warp count 0, their sums come
-//    from k_mx_deposit_heavy);
-// 2. in chunks of up to kDepChunk particles, every thread loads particles of
-//    consecutive numbers -- consecutive addresses within a row, so every warp's
-//    loads are coalesced -- and writes their 8 CIC weights to shared memory;
-// 3. each thread adds the weights of its own keys' particles in sorted order
-//    (the per-key sums of one thread per key, in registers across chunks);
-// 4. each cell adds its 8 keys' corner sums in a fixed (dk, dj, di) order.
-// No atomics: the order of every sum is fixed, so the density is bitwise
-// reproducible, and equals a thread-per-key walk of the same keys.
+// corner, whose particles are contiguous runs of the sorted arrays.
+// 1. The CTA reads cell_start for its keys and numbers their particles densely
+//    (a block scan of the per-key counts); keys longer than a warp count 0 and
+//    their corner sums come from k_mx_deposit_heavy.
+// 2. Each warp takes 32 consecutive particle numbers at a time -- consecutive
+//    addresses within a row of keys, so its loads are coalesced -- finds each
+//    lane's key by a binary search of the numbering, and puts the 8 CIC weights
+//    in its own slice of shared memory.  The first lane of every key's run in
+//    the 32 adds the run's weights in sorted order and adds the 8 sums to the
+//    key's corner sums in shared memory.  A key of at most 32 particles spans at
+//    most two such runs, so its corner sums get at most two adds onto zero, and
+//    two floating-point adds commute: the sums do not depend on which warp comes
+//    first.  No block-wide barrier until the cells are summed.
+// 3. Each cell adds its 8 keys' corner sums in a fixed (dk, dj, di) order.
+// The density is therefore bitwise reproducible run to run.
 constexpr int kDepTx = 16, kDepTy = 8, kDepTz = 8;
 constexpr int kDepKx = kDepTx + 1, kDepKy = kDepTy + 1, kDepKz = kDepTz + 1;
 constexpr int kDepKeys = kDepKx * kDepKy * kDepKz;           // 1377
 constexpr int kDepThreads = 512;
+constexpr int kDepWarps = kDepThreads / 32;
 constexpr int kDepKpt = (kDepKeys + kDepThreads - 1) / kDepThreads;   // keys per thread: 3
-constexpr int kDepChunk = 2048;                              // particles per chunk
-static_assert(kDepKeys < 65536, "key numbers are kept in 16 bits");
-// dynamic shared memory: offsets and bases of the keys, then the chunk buffers
-// (weights + owners), which the keys' corner sums reuse at the end
-constexpr size_t kDepChunkBytes = sizeof(float) * 8 * kDepChunk + sizeof(unsigned short) * kDepChunk;
-constexpr size_t kDepPartBytes = sizeof(float) * 8 * kDepKeys;
-constexpr size_t kDepSmem = sizeof(int) * (2 * kDepKeys + 1) +
-                            (kDepChunkBytes > kDepPartBytes ? kDepChunkBytes : kDepPartBytes);
+static_assert(kDepositLanes == 32, "a light key spans at most two 32-particle runs");
+// dynamic shared memory: the keys' particle numbering and corner sums, and one
+// slice of 8 x 32 weights per warp
+constexpr size_t kDepSmem = sizeof(int) * (2 * kDepKeys + 1) + sizeof(float) * 8 * kDepKeys +
+                            sizeof(float) * 8 * 32 * kDepWarps;
 
 __device__ __forceinline__ int wrap_up(int i, int n)
 {
@@ -342,31 +342,27 @@ __device__ __forceinline__ int wrap_up(int i, int n)
     return i;
 }
 
-__global__ void __launch_bounds__(kDepThreads, 2) k_mx_deposit(
+__global__ void __launch_bounds__(kDepThreads) k_mx_deposit(
     int n, float scale, const int* __restrict__ cell, const float* __restrict__ ox,
     const float* __restrict__ oy, const float* __restrict__ oz, const float* __restrict__ m,
     const int* __restrict__ start, const int* __restrict__ key_slot,
     const float* __restrict__ heavy_part, float* rho)
 {
     extern __shared__ __align__(16) unsigned char dep_smem[];
-    __shared__ int s_warp[kDepThreads / 32];
-    int* s_off = reinterpret_cast<int*>(dep_smem);          // first particle number of each key
-    int* s_base = s_off + kDepKeys + 1;                      // first sorted particle of each key
-    float* w = reinterpret_cast<float*>(s_base + kDepKeys); // a chunk's weights, corner-major
-    unsigned short* owner = reinterpret_cast<unsigned short*>(w + 8 * kDepChunk);  // key of each
-    float* part = w;                                         // at the end: the keys' corner sums
-    const int tid = threadIdx.x;
+    __shared__ int s_warp[kDepWarps];
+    int* s_off = reinterpret_cast<int*>(dep_smem);            // first particle number of each key
+    int* s_base = s_off + kDepKeys + 1;                        // first sorted particle of each key
+    float* part = reinterpret_cast<float*>(s_base + kDepKeys); // the keys' corner sums, corner-major
+    float* wslice = part + 8 * kDepKeys;                       // per warp: 8 x 32 weights
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int i0 = blockIdx.x * kDepTx, j0 = blockIdx.y * kDepTy, k0 = blockIdx.z * kDepTz;
-    // 1. this thread's keys kl = kDepKpt*tid + r: start, count (heavy: 0), heavy sums
-    float acc[kDepKpt][8];
+    // 1. this thread's keys kl = kDepKpt*tid + r: start, count (heavy: 0), initial sums
     int cnt[kDepKpt];
     int local = 0;
 #pragma unroll
     for (int r = 0; r < kDepKpt; ++r) {
         const int kl = kDepKpt * tid + r;
         cnt[r] = 0;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) acc[r][c] = 0.f;
         if (kl < kDepKeys) {
             const int ki = kl % kDepKx, kj = (kl / kDepKx) % kDepKy, kk = kl / (kDepKx * kDepKy);
             const long long K = cidx(wrap_up(i0 + ki, n), wrap_up(j0 + kj, n), wrap_up(k0 + kk, n), n);
@@ -375,15 +371,15 @@ __global__ void __launch_bounds__(kDepThreads, 2) k_mx_deposit(
             if (len > kDepositLanes) {
                 const float* hp = heavy_part + 8LL * key_slot[K];
 #pragma unroll
-                for (int c = 0; c < 8; ++c) acc[r][c] = hp[c];
+                for (int c = 0; c < 8; ++c) part[c * kDepKeys + kl] = hp[c];
             } else {
                 cnt[r] = len;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) part[c * kDepKeys + kl] = 0.f;
             }
             local += cnt[r];
         }
     }
-    // block exclusive scan of the per-thread counts (keys in kl order)
-    const int lane = tid & 31, wid = tid >> 5;
     int inc = local;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -393,38 +389,44 @@ __global__ void __launch_bounds__(kDepThreads, 2) k_mx_deposit(
     if (lane == 31) s_warp[wid] = inc;
     __syncthreads();
     if (wid == 0) {
-        int v = lane < kDepThreads / 32 ? s_warp[lane] : 0;
+        int v = lane < kDepWarps ? s_warp[lane] : 0;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int t = __shfl_up_sync(0xffffffffu, v, o);
             if (lane >= o) v += t;
         }
-        if (lane < kDepThreads / 32) s_warp[lane] = v;
+        if (lane < kDepWarps) s_warp[lane] = v;
     }
     __syncthreads();
     int run = (wid > 0 ? s_warp[wid - 1] : 0) + inc - local;
-    const int total = s_warp[kDepThreads / 32 - 1];
-    int off[kDepKpt];
+    const int total = s_warp[kDepWarps - 1];
 #pragma unroll
     for (int r = 0; r < kDepKpt; ++r) {
         const int kl = kDepKpt * tid + r;
-        off[r] = run;
         if (kl < kDepKeys) s_off[kl] = run;
         run += cnt[r];
     }
+    if (tid == 0) s_off[kDepKeys] = total;
     __syncthreads();
-    // 2.-3. the particles in chunks
-    for (int c0 = 0; c0 < total; c0 += kDepChunk) {
-        const int c1 = min(total, c0 + kDepChunk);
-#pragma unroll
-        for (int r = 0; r < kDepKpt; ++r) {
-            const int lo = max(off[r], c0), hi = min(off[r] + cnt[r], c1);
-            for (int p = lo; p < hi; ++p) owner[p - c0] = (unsigned short)(kDepKpt * tid + r);
+    // 2. 32 particle numbers per warp at a time
+    float* w = wslice + wid * (8 * 32);
+    for (int p0 = wid * 32; p0 < total; p0 += kDepThreads) {
+        const int p = p0 + lane;
+        const bool live = p < total;
+        // the key of number p: the last kl with s_off[kl] <= p (keys of count 0 share
+        // their offset with the next key; the search lands on the one that holds p)
+        int lo = 0, hi = kDepKeys;   // s_off[lo] <= p < s_off[hi]
+        if (live) {
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (s_off[mid] <= p) lo = mid;
+                else hi = mid;
+            }
         }
-        __syncthreads();
-        for (int p = c0 + tid; p < c1; p += kDepThreads) {
-            const int kl = owner[p - c0];
-            const int q = s_base[kl] + (p - s_off[kl]);
+        const int kl = lo;
+        const int first = live ? s_off[kl] : 0;
+        if (live) {
+            const int q = s_base[kl] + (p - first);
             const int cq = cell[q];
             float fx, fy, fz;
             key_frac(cell_i(cq), ox[q], n, &fx);
@@ -440,27 +442,26 @@ __global__ void __launch_bounds__(kDepThreads, 2) k_mx_deposit(
                 for (int cy = 0; cy < 2; ++cy)
 #pragma unroll
                     for (int cx = 0; cx < 2; ++cx)
-                        w[(cx + 2 * cy + 4 * cz) * kDepChunk + p - c0] = __fmul_rn(__fmul_rn(__fmul_rn(sx[cx], sy[cy]), sz[cz]), mq);
+                        w[(cx + 2 * cy + 4 * cz) * 32 + lane] =
+                            __fmul_rn(__fmul_rn(__fmul_rn(sx[cx], sy[cy]), sz[cz]), mq);
         }
-        __syncthreads();
+        __syncwarp();
+        // the first lane of each key's run within these 32 sums the run in order
+        if (live && (p == first || lane == 0)) {
+            const int end = min(s_off[kl + 1], p0 + 32);
+            float acc[8];
 #pragma unroll
-        for (int r = 0; r < kDepKpt; ++r) {
-            const int lo = max(off[r], c0), hi = min(off[r] + cnt[r], c1);
-            for (int p = lo; p < hi; ++p)
+            for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+            for (int t = lane; t < end - p0; ++t)
 #pragma unroll
-                for (int c = 0; c < 8; ++c) acc[r][c] = __fadd_rn(acc[r][c], w[c * kDepChunk + p - c0]);
+                for (int c = 0; c < 8; ++c) acc[c] = __fadd_rn(acc[c], w[c * 32 + t]);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) atomicAdd(part + c * kDepKeys + kl, acc[c]);
         }
-        __syncthreads();
-    }
-    // 4. the cells: each adds its 8 keys' corners in the fixed (dk, dj, di) order
-#pragma unroll
-    for (int r = 0; r < kDepKpt; ++r) {
-        const int kl = kDepKpt * tid + r;
-        if (kl < kDepKeys)
-#pragma unroll
-            for (int c = 0; c < 8; ++c) part[c * kDepKeys + kl] = acc[r][c];
+        __syncwarp();
     }
     __syncthreads();
+    // 3. the cells: each adds its 8 keys' corners in the fixed (dk, dj, di) order
     for (int cl = tid; cl < kDepTx * kDepTy * kDepTz; cl += kDepThreads) {
         const int ci = cl % kDepTx, cj = (cl / kDepTx) % kDepTy, ck = cl / (kDepTx * kDepTy);
         const int i = i0 + ci, j = j0 + cj, k = k0 + ck;

@@ -2434,15 +2434,23 @@ nyxpm_status nyxpm_ensemble_grav_vector(nyxpm_ctx* c, nyxpm_ensemble* E, int slo
 {
     if (!c || !E || !slot_ok(E, slot) || !g_out) return NYXPM_INVALID_ARG;
     const EDesc& d = E->slots[slot].desc;
-    const long long cnt = 3LL * d.n * d.n * d.n;
+    const long long ncell = (long long)d.n * d.n * d.n;
+    const long long cnt = 3 * ncell;
     void* tmp = E->arena.alloc(8 * cnt);
-    if (!tmp) return efail(c, NYXPM_OOM, "ensemble g staging");
-    const long long ncell = cnt / 3;
-    e_g32_to_double<<<(unsigned)((ncell + 255) / 256), 256, 0, c->stream>>>(ncell, d.g32, (double*)tmp);
-    cudaMemcpyAsync(g_out, tmp, 8 * cnt, cudaMemcpyDeviceToHost, c->stream);
-    const cudaError_t e = cudaStreamSynchronize(c->stream);
-    E->arena.release(tmp);
-    return e == cudaSuccess ? NYXPM_OK : echeck(c, "ensemble grav");
+    if (tmp) {
+        e_g32_to_double<<<(unsigned)((ncell + 255) / 256), 256, 0, c->stream>>>(ncell, d.g32, (double*)tmp);
+        cudaMemcpyAsync(g_out, tmp, 8 * cnt, cudaMemcpyDeviceToHost, c->stream);
+        const cudaError_t e = cudaStreamSynchronize(c->stream);
+        E->arena.release(tmp);
+        return e == cudaSuccess ? NYXPM_OK : echeck(c, "ensemble grav");
+    }
+    // the arena is full: the FP32 float4 field to the host and widened there
+    std::vector<float> h(4 * (size_t)ncell);
+    cudaMemcpyAsync(h.data(), d.g32, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return echeck(c, "ensemble grav");
+    for (long long t = 0; t < ncell; ++t)
+        for (int comp = 0; comp < 3; ++comp) g_out[comp * ncell + t] = h[4 * t + comp];
+    return NYXPM_OK;
 }
 
 nyxpm_status nyxpm_ensemble_set_tuning(nyxpm_ctx* c, nyxpm_ensemble* E, const nyxpm_tuning* t)

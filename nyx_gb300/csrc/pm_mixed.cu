@@ -1029,6 +1029,73 @@ __device__ __forceinline__ void fine_row_resid(const LevelViewF& F, int j, int k
     }
 }
 
+// The red cells' residuals of one fine row segment (cells 4t .. 4t+3 of row (j, k)):
+// r[u] for the red cell of the pair (4t + 2u, 4t + 2u + 1).  After pre-smoothing,
+// which ends with a black half sweep, the black cells' residuals are round-off,
+// so the restriction takes the red children only: the red values of this row
+// (phi and beta at red[2t], red[2t+1]), three black values of this row around
+// them and the black values of the four neighbour rows at the same x.  The
+// neighbour sum is formed in the order of fine_row_resid (x-, x+, y-, y+, z-, z+).
+__device__ __forceinline__ void fine_row_resid_red(const LevelViewF& F, int j, int k, unsigned t,
+                                                   float r[2])
+{
+    const int n = F.n;
+    const unsigned half = (unsigned)n >> 1;
+    const int p = (j + k) & 1;                    // 0: red cells at even i
+    auto row = [&](int jj, int kk) -> unsigned { return ((unsigned)jj + (unsigned)n * (unsigned)kk) * half; };
+    const unsigned r0 = row(j, k), c2 = 2 * t;
+    const float2 self = __ldg(reinterpret_cast<const float2*>(F.phi_r + r0 + c2));
+    const float2 beta = __ldg(reinterpret_cast<const float2*>(F.beta_r + r0 + c2));
+    const float2 bl = __ldg(reinterpret_cast<const float2*>(F.phi_b + r0 + c2));   // black 2t, 2t+1
+    // the black value one beyond the pair: 2t-1 (p = 0) or 2t+2 (p = 1), periodic
+    const float edge = p ? __ldg(F.phi_b + r0 + (c2 + 2 == half ? 0u : c2 + 2))
+                         : __ldg(F.phi_b + r0 + (c2 == 0 ? half - 1 : c2 - 1));
+    const float xm[2] = {p ? bl.x : edge, p ? bl.y : bl.x};
+    const float xp[2] = {p ? bl.y : bl.x, p ? edge : bl.y};
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+    const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+    const unsigned nr[4] = {row(jm, k), row(jp, k), row(j, km), row(j, kp)};
+    float2 nb[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) nb[a] = __ldg(reinterpret_cast<const float2*>(F.phi_b + nr[a] + c2));
+    const float sv[2] = {self.x, self.y}, bv[2] = {beta.x, beta.y};
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        float s = xm[u] + xp[u];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) s += u ? nb[a].y : nb[a].x;
+        r[u] = bv[u] - fmaf(s, kSixthF, -sv[u]);
+    }
+}
+
+// The restriction after pre-smoothing: the coarse right-hand side from the red
+// children only (the black ones' residuals are round-off), summed in (dk, dj)
+// order; half the loads of k_restrict_f4.
+__global__ void __launch_bounds__(256) k_restrict_f4_red(LevelViewF F, LevelViewF Cv)
+{
+    const int nc = Cv.n;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // coarse cells 2t, 2t+1
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z;
+    if (t >= (unsigned)nc / 2 || J >= nc) return;
+    float r[2][2][2];
+#pragma unroll
+    for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj) fine_row_resid_red(F, 2 * J + dj, 2 * K + dk, t, r[dk][dj]);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        float s = 0.f;
+#pragma unroll
+        for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+            for (int dj = 0; dj < 2; ++dj) s += r[dk][dj][u];
+        const int I = 2 * (int)t + u;
+        *lv_ptr<float>(Cv.beta_r, Cv.beta_b, nc, Cv.split, I, J, K) = s * 0.5f;
+        *lv_ptr<float>(Cv.phi_r, Cv.phi_b, nc, Cv.split, I, J, K) = 0.f;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_restrict_f4(LevelViewF F, LevelViewF Cv)
 {
     const int nc = Cv.n;
@@ -1426,12 +1493,16 @@ nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li, bool fresh = false)
         prof_begin(c);
         if ((f.n / 2) % 4 == 0) {
             const Geo g = geo3(cl.n / 2, cl.n, cl.n);
-            k_restrict_f4<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+            if (c.p.nu1 > 0) k_restrict_f4_red<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+            else k_restrict_f4<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
         } else {
             const Geo g = geo3(cl.n, cl.n, cl.n);
             k_restrict_f<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
         }
-        prof_end(c, NYXPM_ST_RESTRICT, 8.0 * ncf + 8.0 * ncc);
+        // phi and beta read once, coarse beta and phi written; the red-only form reads
+        // the black cells' beta not at all
+        const bool red = c.p.nu1 > 0 && (f.n / 2) % 4 == 0;
+        prof_end(c, NYXPM_ST_RESTRICT, (red ? 6.0 : 8.0) * ncf + 8.0 * ncc);
     }
     if ((st = check_launch(c, "restrict f32")) != NYXPM_OK) return st;
     if ((st = vcycle_f(c, b, li + 1)) != NYXPM_OK) return st;

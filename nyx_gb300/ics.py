@@ -115,8 +115,10 @@ def _zeldovich_ics_on_device(n, L, slope, seed, a_init, rms_disp_cells, cosmo, d
     pos[pos >= L] = 0.0
     vel = disp * (a_init * cosmo.hubble(a_init))
     mass = cosmo.OmM * cosmo.rho_crit() * L ** 3 / pos.shape[0]
-    out = InitialConditions(pos=pos.cpu().numpy(), vel=vel.cpu().numpy(), mass=mass, n=n, L=L,
-                            a=a_init, lattice=lattice.cpu().numpy())
+    # (np, 3) arrays in row-major order, as the host path returns them
+    out = InitialConditions(pos=np.ascontiguousarray(pos.cpu().numpy()),
+                            vel=np.ascontiguousarray(vel.cpu().numpy()), mass=mass, n=n, L=L,
+                            a=a_init, lattice=np.ascontiguousarray(lattice.cpu().numpy()))
     del pos, vel, lattice, disp
     torch.cuda.empty_cache()
     return out

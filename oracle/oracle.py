@@ -111,22 +111,24 @@ class Particles:
     """FP64 SoA particle state (AMReX Particle<4,0>: pos + mass, vx, vy, vz)."""
 
     def __init__(self, pos, vel, mass, ids=None):
+        # always copies: the oracle steps its arrays in place, and a column of a
+        # column-major (np, 3) array would otherwise be the caller's own memory
         pos = np.asarray(pos, dtype=np.float64)
         vel = np.asarray(vel, dtype=np.float64)
-        self.x = np.ascontiguousarray(pos[:, 0])
-        self.y = np.ascontiguousarray(pos[:, 1])
-        self.z = np.ascontiguousarray(pos[:, 2])
-        self.vx = np.ascontiguousarray(vel[:, 0])
-        self.vy = np.ascontiguousarray(vel[:, 1])
-        self.vz = np.ascontiguousarray(vel[:, 2])
+        self.x = np.array(pos[:, 0], dtype=np.float64, order="C", copy=True)
+        self.y = np.array(pos[:, 1], dtype=np.float64, order="C", copy=True)
+        self.z = np.array(pos[:, 2], dtype=np.float64, order="C", copy=True)
+        self.vx = np.array(vel[:, 0], dtype=np.float64, order="C", copy=True)
+        self.vy = np.array(vel[:, 1], dtype=np.float64, order="C", copy=True)
+        self.vz = np.array(vel[:, 2], dtype=np.float64, order="C", copy=True)
         if np.ndim(mass) == 0:
             self.m = None
             self.mscalar = float(mass)
         else:
-            self.m = np.ascontiguousarray(mass, dtype=np.float64)
+            self.m = np.array(mass, dtype=np.float64, order="C", copy=True)
             self.mscalar = 0.0
         self.id = (np.arange(len(self.x), dtype=np.int32) if ids is None
-                   else np.ascontiguousarray(ids, dtype=np.int32))
+                   else np.array(ids, dtype=np.int32, order="C", copy=True))
 
     @property
     def np(self) -> int:

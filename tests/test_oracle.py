@@ -300,3 +300,18 @@ def test_particle_time_step_limit():
     assert O.est_time_step(n, L, p0, g, cfl, a) == 1.0 / math.sqrt(5.0 / dx)
     empty = O.Particles(np.zeros((0, 3)), np.zeros((0, 3)), 1.0)
     assert O.est_time_step(n, L, empty, g, cfl, a) == -1e50
+
+
+def test_particles_copy_the_callers_arrays():
+    """The oracle steps its particle arrays in place; it must never step the
+    caller's: a column of a column-major (np, 3) array is contiguous and would
+    otherwise be the caller's own memory."""
+    rng = np.random.default_rng(1)
+    pos = np.asfortranarray(rng.random((4096, 3)))
+    vel = np.asfortranarray(rng.standard_normal((4096, 3)))
+    mass = rng.random(4096) + 1.0
+    keep = (pos.copy(), vel.copy(), mass.copy())
+    p = O.Particles(pos, vel, mass)
+    pm = O.PMOracle(16, 1.0, p)
+    pm.step(0.02, 0.021, 1e-4)
+    assert np.array_equal(pos, keep[0]) and np.array_equal(vel, keep[1]) and np.array_equal(mass, keep[2])

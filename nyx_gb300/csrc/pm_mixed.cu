@@ -307,38 +307,25 @@ __global__ void __launch_bounds__(256) k_mx_deposit_heavy(int n, const int* __re
     }
 }
 
-// One CTA per tile of 16 x 8 x 8 cells; its density needs the 17 x 9 x 9 keys
-// (cells of floor(x/dx + 1/2)) from the tile's own corner to one past its far
-// corner, whose particles are contiguous runs of the sorted arrays.
-// 1. The CTA reads cell_start for its keys and numbers their particles densely
-//    (a block scan of the per-key counts); keys longer than a warp count 0 and
-//    their corner sums come from k_mx_deposit_heavy.
-// 2. Each warp takes 32 consecutive particle numbers at a time -- consecutive
-//    addresses within a row of keys, so its loads are coalesced -- finds each
-//    lane's key by a binary search of the numbering, and puts the 8 CIC weights
-//    in its own slice of shared memory.  The first lane of every key's run in
-//    the 32 adds the run's weights in sorted order and adds the 8 sums to the
-//    key's corner sums in shared memory.  A key of at most 32 particles spans at
-//    most two such runs, so its corner sums get at most two adds onto zero, and
-//    two floating-point adds commute: the sums do not depend on which warp comes
-//    first.  No block-wide barrier until the cells are summed.
-// 3. Each cell adds its 8 keys' corner sums in a fixed (dk, dj, di) order.
-// The density is therefore bitwise reproducible run to run.
-constexpr int kDepTx = 16, kDepTy = 8, kDepTz = 8;
+// One CTA per tile of 8 x 8 x 8 cells.  Phase 1: one thread per key of the
+// 9 x 9 x 9 key window (cells of floor(x/dx + 1/2), from the tile's corner to one
+// past its far corner) sums its segment's 8 corner weights in sorted order (keys
+// longer than a warp take their sums from k_mx_deposit_heavy).  Phase 2: each
+// cell adds the 8 corner sums of its keys in a fixed (dk, dj, di) order.  No
+// atomics: the order of every sum is fixed, so the density is bitwise
+// reproducible.  (Measured against it at 256^3, one particle per cell, on
+// GB300, and slower: a 16 x 8 x 8 tile whose warps number the window's particles
+// densely and stage their weights in shared memory, 382-384 us against 233 us;
+// cell sums by shared-memory fixed-point atomics, 270 us with 32-bit and 464 us
+// and more with 64-bit accumulators.)
+constexpr int kDepTx = 8, kDepTy = 8, kDepTz = 8;
 constexpr int kDepKx = kDepTx + 1, kDepKy = kDepTy + 1, kDepKz = kDepTz + 1;
-constexpr int kDepKeys = kDepKx * kDepKy * kDepKz;           // 1377
-constexpr int kDepThreads = 512;
-constexpr int kDepWarps = kDepThreads / 32;
-constexpr int kDepKpt = (kDepKeys + kDepThreads - 1) / kDepThreads;   // keys per thread: 3
-static_assert(kDepositLanes == 32, "a light key spans at most two 32-particle runs");
-// dynamic shared memory: the keys' particle numbering and corner sums, and one
-// slice of 8 x 32 weights per warp
-constexpr size_t kDepSmem = sizeof(int) * (2 * kDepKeys + 1) + sizeof(float) * 8 * kDepKeys +
-                            sizeof(float) * 8 * 32 * kDepWarps;
+constexpr int kDepKeys = kDepKx * kDepKy * kDepKz;   // 729
+constexpr int kDepThreads = 256;
 
 __device__ __forceinline__ int wrap_up(int i, int n)
 {
-    while (i >= n) i -= n;   // i < n + 17: at most one pass unless n < 17
+    while (i >= n) i -= n;   // i < n + 9: at most one pass unless n < 9
     return i;
 }
 
@@ -348,125 +335,32 @@ __global__ void __launch_bounds__(kDepThreads) k_mx_deposit(
     const int* __restrict__ start, const int* __restrict__ key_slot,
     const float* __restrict__ heavy_part, float* rho)
 {
-    extern __shared__ __align__(16) unsigned char dep_smem[];
-    __shared__ int s_warp[kDepWarps];
-    int* s_off = reinterpret_cast<int*>(dep_smem);            // first particle number of each key
-    int* s_base = s_off + kDepKeys + 1;                        // first sorted particle of each key
-    float* part = reinterpret_cast<float*>(s_base + kDepKeys); // the keys' corner sums, corner-major
-    float* wslice = part + 8 * kDepKeys;                       // per warp: 8 x 32 weights
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    // corner-major: a warp's 32 consecutive keys (or cells) touch 32 banks
+    __shared__ float part[8 * kDepKeys];
     const int i0 = blockIdx.x * kDepTx, j0 = blockIdx.y * kDepTy, k0 = blockIdx.z * kDepTz;
-    // 1. this thread's keys kl = kDepKpt*tid + r: start, count (heavy: 0), initial sums
-    int cnt[kDepKpt];
-    int local = 0;
+    for (int kl = threadIdx.x; kl < kDepKeys; kl += blockDim.x) {
+        const int ki = kl % kDepKx, kj = (kl / kDepKx) % kDepKy, kk = kl / (kDepKx * kDepKy);
+        const long long K = cidx(wrap_up(i0 + ki, n), wrap_up(j0 + kj, n), wrap_up(k0 + kk, n), n);
+        float s[8];
+        const int b0 = start[K], e = start[K + 1];
+        if (e - b0 > kDepositLanes) {
+            const float* hp = heavy_part + 8LL * key_slot[K];
 #pragma unroll
-    for (int r = 0; r < kDepKpt; ++r) {
-        const int kl = kDepKpt * tid + r;
-        cnt[r] = 0;
-        if (kl < kDepKeys) {
-            const int ki = kl % kDepKx, kj = (kl / kDepKx) % kDepKy, kk = kl / (kDepKx * kDepKy);
-            const long long K = cidx(wrap_up(i0 + ki, n), wrap_up(j0 + kj, n), wrap_up(k0 + kk, n), n);
-            const int b0 = start[K], len = start[K + 1] - b0;
-            s_base[kl] = b0;
-            if (len > kDepositLanes) {
-                const float* hp = heavy_part + 8LL * key_slot[K];
+            for (int c = 0; c < 8; ++c) s[c] = hp[c];
+        } else {
 #pragma unroll
-                for (int c = 0; c < 8; ++c) part[c * kDepKeys + kl] = hp[c];
-            } else {
-                cnt[r] = len;
-#pragma unroll
-                for (int c = 0; c < 8; ++c) part[c * kDepKeys + kl] = 0.f;
-            }
-            local += cnt[r];
+            for (int c = 0; c < 8; ++c) s[c] = 0.f;
+            for (int q = b0; q < e; ++q) mx_add_weights(q, n, cell, ox, oy, oz, m, s);
         }
-    }
-    int inc = local;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
-    }
-    if (lane == 31) s_warp[wid] = inc;
-    __syncthreads();
-    if (wid == 0) {
-        int v = lane < kDepWarps ? s_warp[lane] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, v, o);
-            if (lane >= o) v += t;
-        }
-        if (lane < kDepWarps) s_warp[lane] = v;
+        for (int c = 0; c < 8; ++c) part[c * kDepKeys + kl] = s[c];
     }
     __syncthreads();
-    int run = (wid > 0 ? s_warp[wid - 1] : 0) + inc - local;
-    const int total = s_warp[kDepWarps - 1];
-#pragma unroll
-    for (int r = 0; r < kDepKpt; ++r) {
-        const int kl = kDepKpt * tid + r;
-        if (kl < kDepKeys) s_off[kl] = run;
-        run += cnt[r];
-    }
-    if (tid == 0) s_off[kDepKeys] = total;
-    __syncthreads();
-    // 2. 32 particle numbers per warp at a time
-    float* w = wslice + wid * (8 * 32);
-    for (int p0 = wid * 32; p0 < total; p0 += kDepThreads) {
-        const int p = p0 + lane;
-        const bool live = p < total;
-        // the key of number p: the last kl with s_off[kl] <= p (keys of count 0 share
-        // their offset with the next key; the search lands on the one that holds p)
-        int lo = 0, hi = kDepKeys;   // s_off[lo] <= p < s_off[hi]
-        if (live) {
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (s_off[mid] <= p) lo = mid;
-                else hi = mid;
-            }
-        }
-        const int kl = lo;
-        const int first = live ? s_off[kl] : 0;
-        if (live) {
-            const int q = s_base[kl] + (p - first);
-            const int cq = cell[q];
-            float fx, fy, fz;
-            key_frac(cell_i(cq), ox[q], n, &fx);
-            key_frac(cell_j(cq), oy[q], n, &fy);
-            key_frac(cell_k(cq), oz[q], n, &fz);
-            const float sx[2] = {1.f - fx, fx};
-            const float sy[2] = {1.f - fy, fy};
-            const float sz[2] = {1.f - fz, fz};
-            const float mq = m ? m[q] : 1.f;
-#pragma unroll
-            for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-                for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-                    for (int cx = 0; cx < 2; ++cx)
-                        w[(cx + 2 * cy + 4 * cz) * 32 + lane] =
-                            __fmul_rn(__fmul_rn(__fmul_rn(sx[cx], sy[cy]), sz[cz]), mq);
-        }
-        __syncwarp();
-        // the first lane of each key's run within these 32 sums the run in order
-        if (live && (p == first || lane == 0)) {
-            const int end = min(s_off[kl + 1], p0 + 32);
-            float acc[8];
-#pragma unroll
-            for (int c = 0; c < 8; ++c) acc[c] = 0.f;
-            for (int t = lane; t < end - p0; ++t)
-#pragma unroll
-                for (int c = 0; c < 8; ++c) acc[c] = __fadd_rn(acc[c], w[c * 32 + t]);
-#pragma unroll
-            for (int c = 0; c < 8; ++c) atomicAdd(part + c * kDepKeys + kl, acc[c]);
-        }
-        __syncwarp();
-    }
-    __syncthreads();
-    // 3. the cells: each adds its 8 keys' corners in the fixed (dk, dj, di) order
-    for (int cl = tid; cl < kDepTx * kDepTy * kDepTz; cl += kDepThreads) {
+    for (int cl = threadIdx.x; cl < kDepTx * kDepTy * kDepTz; cl += blockDim.x) {
         const int ci = cl % kDepTx, cj = (cl / kDepTx) % kDepTy, ck = cl / (kDepTx * kDepTy);
         const int i = i0 + ci, j = j0 + cj, k = k0 + ck;
         if (i >= n || j >= n || k >= n) continue;
-        float a = 0.f;
+        float acc = 0.f;
 #pragma unroll
         for (int dk = 0; dk < 2; ++dk)
 #pragma unroll
@@ -474,9 +368,9 @@ __global__ void __launch_bounds__(kDepThreads) k_mx_deposit(
 #pragma unroll
                 for (int di = 0; di < 2; ++di) {
                     const int kl = (ci + di) + kDepKx * ((cj + dj) + kDepKy * (ck + dk));
-                    a = __fadd_rn(a, part[((1 - di) + 2 * (1 - dj) + 4 * (1 - dk)) * kDepKeys + kl]);
+                    acc += part[((1 - di) + 2 * (1 - dj) + 4 * (1 - dk)) * kDepKeys + kl];
                 }
-        rho[cidx(i, j, k, n)] = a * scale;
+        rho[cidx(i, j, k, n)] = acc * scale;
     }
 }
 
@@ -957,6 +851,9 @@ __device__ __forceinline__ float resid_f(const LevelViewF& L, int i, int j, int 
     return *lv_ptr<float>(L.beta_r, L.beta_b, n, L.split, i, j, k) - fmaf(s, kSixthF, -c);
 }
 
+// RED = 1 after pre-smoothing (it ends with a black half sweep): the red
+// children only, as k_restrict_f4_red and the fused coarse V-cycle take them
+template <int RED>
 __global__ void k_restrict_f(LevelViewF F, LevelViewF Cv)
 {
     const int nc = Cv.n;
@@ -970,7 +867,8 @@ __global__ void k_restrict_f(LevelViewF F, LevelViewF Cv)
 #pragma unroll
         for (int dj = 0; dj < 2; ++dj)
 #pragma unroll
-            for (int di = 0; di < 2; ++di) s += resid_f(F, 2 * I + di, 2 * J + dj, 2 * K + dk);
+            for (int di = 0; di < 2; ++di)
+                if (!RED || ((di + dj + dk) & 1) == 0) s += resid_f(F, 2 * I + di, 2 * J + dj, 2 * K + dk);
     *lv_ptr<float>(Cv.beta_r, Cv.beta_b, nc, Cv.split, I, J, K) = s * 0.5f;
     *lv_ptr<float>(Cv.phi_r, Cv.phi_b, nc, Cv.split, I, J, K) = 0.f;
 }
@@ -1268,7 +1166,7 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail_f(TailF A)
 {
     __shared__ float r[kMaxBottom * kMaxBottom * kMaxBottom];
     __shared__ float g[kMaxBottom * kMaxBottom * kMaxBottom];
-    vcycle_tail<float>(A.lv, A.nl, A.nu1, A.nu2, A.Gf, A.nb, r, g, false);
+    vcycle_tail<float>(A.lv, A.nl, A.nu1, A.nu2, A.Gf, A.nb, r, g, true);
 }
 
 // FP32 gravity vector from the FP64 phi: the difference in FP64, the scaling in FP32
@@ -1497,11 +1395,12 @@ nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li, bool fresh = false)
             else k_restrict_f4<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
         } else {
             const Geo g = geo3(cl.n, cl.n, cl.n);
-            k_restrict_f<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+            if (c.p.nu1 > 0) k_restrict_f<1><<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+            else k_restrict_f<0><<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
         }
         // phi and beta read once, coarse beta and phi written; the red-only form reads
         // the black cells' beta not at all
-        const bool red = c.p.nu1 > 0 && (f.n / 2) % 4 == 0;
+        const bool red = c.p.nu1 > 0;
         prof_end(c, NYXPM_ST_RESTRICT, (red ? 6.0 : 8.0) * ncf + 8.0 * ncc);
     }
     if ((st = check_launch(c, "restrict f32")) != NYXPM_OK) return st;
@@ -1747,11 +1646,8 @@ nyxpm_status mixed_deposit(Ctx& c, Box& b)
     k_mx_deposit_heavy<<<c.sm_count * 4, 256, 0, c.stream>>>(n, b.cell, b.ox, b.oy, b.oz, mq,
                                                              b.cell_start, b.long_list, b.long_count,
                                                              b.key_slot, heavy);
-    // more than the default 48 KB of dynamic shared memory (set on every call: the
-    // attribute belongs to the current device)
-    cudaFuncSetAttribute(k_mx_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDepSmem);
-    k_mx_deposit<<<grid, kDepThreads, kDepSmem, c.stream>>>(n, scale, b.cell, b.ox, b.oy, b.oz, mq,
-                                                            b.cell_start, b.key_slot, heavy, b.frho);
+    k_mx_deposit<<<grid, kDepThreads, 0, c.stream>>>(n, scale, b.cell, b.ox, b.oy, b.oz, mq,
+                                                     b.cell_start, b.key_slot, heavy, b.frho);
     c.launches += 1;
     prof_end(c, NYXPM_ST_DEPOSIT, (b.uniform_mass ? 16.0 : 20.0) * b.np + 8.0 * nc);
     return check_launch(c, "mixed deposit");

@@ -472,10 +472,12 @@ nyxpm_status nyxpm_ensemble_step(nyxpm_ctx* ctx, nyxpm_ensemble* ens, const doub
  * Each call on a stream that is not capturing looks up the array's device
  * address on the current device (a device reset may move it); a call on a
  * capturing stream uses the address the last such call found, so make one call
- * on the device before any stream capture.  The call returns once the stream has
- * finished the deposit: it reads back a count of non-finite positions, and
- * refuses such input with NYXPM_INVALID_ARG (rho then holds no valid density),
- * as nyxpm_deposit does.  All calls share the one array: calls that overlap on
+ * on the device before any stream capture.  On a stream that is not capturing
+ * the call returns once the stream has finished the deposit: it reads back a
+ * count of non-finite positions, and refuses such input with NYXPM_INVALID_ARG
+ * (rho then holds no valid density), as nyxpm_deposit does.  On a capturing
+ * stream it only enqueues the deposit (a capture cannot be waited for): finite
+ * positions at every replay are then the caller's to ensure.  All calls share the one array: calls that overlap on
  * the GPU (other streams, other host threads) race and must be ordered by the
  * caller.  The result equals nyxpm_deposit's for the same particles in the same
  * order, bit for bit.  errbuf (may be NULL) receives a message on failure. */

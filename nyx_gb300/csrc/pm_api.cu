@@ -718,9 +718,14 @@ nyxpm_status nyxpm_step_host(nyxpm_ctx* c, nyxpm_box* b, double* pos, double* ve
     cudaMemsetAsync(b->norms + 2, 0, sizeof(unsigned long long), c->stream);
     cudaMemcpyAsync(s_pos, pos, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream);
     if (mass) cudaMemcpyAsync(s_mass, mass, sizeof(double) * np, cudaMemcpyHostToDevice, c->stream);
+    // (the velocity copy starts after them: run at the same time, the two would
+    // share the host link and the positions, on the critical path, would take
+    // twice as long)
+    cudaEventRecord(c->ev_copy_out, c->stream);
     TRY(mixed ? mixed_unpack_pos(*c, *b, s_pos, mass ? s_mass : nullptr)
               : launch_unpack_pos(*c, *b, s_pos, mass ? s_mass : nullptr));
     // ... the velocities on the copy stream, under the sort, deposit and old-time solve
+    cudaStreamWaitEvent(c->copy_stream, c->ev_copy_out, 0);
     cudaMemcpyAsync(s_vel, vel, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->copy_stream);
     cudaEventRecord(c->ev_copy_in, c->copy_stream);
     TRY(check_launch(*c, "host step input copies"));

@@ -61,7 +61,7 @@ int g_sm_count[kMaxDevices] = {};
 // of the array is not a device address).  It is looked up again on every call
 // whose stream is not capturing -- a device reset reloads the module and may
 // move the array -- and the last address found is used while a capture runs.
-nyxpm_status scratch_address(cudaStream_t stream, unsigned char** out, int* sm_count,
+nyxpm_status scratch_address(cudaStream_t stream, unsigned char** out, int* sm_count, bool* capturing,
                              char* errbuf, size_t errlen)
 {
     int dev = -1;
@@ -96,6 +96,7 @@ nyxpm_status scratch_address(cudaStream_t stream, unsigned char** out, int* sm_c
     }
     *out = g_scratch_addr[dev];
     *sm_count = g_sm_count[dev];
+    *capturing = cap != cudaStreamCaptureStatusNone;
     return NYXPM_OK;
 }
 
@@ -397,7 +398,8 @@ extern "C" nyxpm_status nyxpm_deposit_noalloc(const double* d_x, const double* d
     unsigned char* base = nullptr;
     int sm_count = 1;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const nyxpm_status st = scratch_address(s, &base, &sm_count, errbuf, errlen);
+    bool capturing = false;
+    const nyxpm_status st = scratch_address(s, &base, &sm_count, &capturing, errbuf, errlen);
     if (st != NYXPM_OK) return st;
     int* count = reinterpret_cast<int*>(base + kOffCount);
     int* start = reinterpret_cast<int*>(base + kOffStart);
@@ -437,7 +439,10 @@ extern "C" nyxpm_status nyxpm_deposit_noalloc(const double* d_x, const double* d
         return NYXPM_CUDA_ERROR;
     }
     // refuse non-finite positions as nyxpm_deposit does: read the count back
-    // (into a host variable, no allocation), which waits for the stream
+    // (into a host variable, no allocation), which waits for the stream.  A
+    // stream under capture cannot be waited for: the graph holds the deposit
+    // alone, and the check is the caller's (every replay's positions finite).
+    if (capturing) return NYXPM_OK;
     int h_bad = 0;
     const cudaError_t ec = cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
     const cudaError_t es = ec == cudaSuccess ? cudaStreamSynchronize(s) : ec;

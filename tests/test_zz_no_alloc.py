@@ -116,3 +116,45 @@ def test_noalloc_deposit_other_length_own_stream_no_device_memory_taken():
     torch.cuda.synchronize()
     assert call(bad) == 1 and b"non-finite" in err.value
     ctx.close()
+
+
+@pytest.mark.skipif(not gpu_available(), reason="no GPU")
+def test_noalloc_deposit_captured_in_a_cuda_graph():
+    """After one call on the device, the call can be captured into a CUDA graph
+    (it then only enqueues: no read-back, no wait) and every replay writes the
+    allocating deposit's density, bit for bit."""
+    import torch
+    from nyx_gb300 import _lib
+    from nyx_gb300.ics import zeldovich_ics
+    from nyx_gb300.pm import Box, Context
+
+    lib = _lib.load()
+    ctx = Context(device=0)
+    err = C.create_string_buffer(256)
+    L, n, mass = 2.0, 32, 4e9
+    pos = zeldovich_ics(n, L, -2.0, 8, 0.05, rms_disp_cells=0.5).pos
+    box = Box(ctx, n, L, len(pos))
+    box.upload(pos, np.zeros_like(pos), mass)
+    expect = box.deposit()
+    box.close()
+    x, y, z, rho = _device_arrays(torch, pos, n)
+
+    def call(stream):
+        return lib.nyxpm_deposit_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                                         C.c_void_p(z.data_ptr()), len(pos), mass, n, L,
+                                         C.c_void_p(rho.data_ptr()), C.c_void_p(stream), err, len(err))
+
+    assert call(torch.cuda.current_stream(0).cuda_stream) == 0, err.value.decode()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream(device=0)
+    with torch.cuda.graph(graph, stream=side, capture_error_mode="thread_local"):
+        st = call(torch.cuda.current_stream(0).cuda_stream)
+    assert st == 0, err.value.decode()
+    for _ in range(2):
+        rho.fill_(float("nan"))
+        graph.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(rho.cpu().numpy(), expect)
+    del graph
+    ctx.close()

@@ -867,8 +867,10 @@ def run_ours(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e0.record(stream)
+        vc_e = []
         for a0, a1, dt in sched[W:W + K]:
-            box.step_host_ptr(hpos.data_ptr(), hvel.data_ptr(), ic.mass, a0, a1, dt)
+            inf = box.step_host_ptr(hpos.data_ptr(), hvel.data_ptr(), ic.mass, a0, a1, dt)
+            vc_e.append((inf["old_solve"]["vcycles"], inf["new_solve"]["vcycles"]))
         e1.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
@@ -879,6 +881,8 @@ def run_ours(args):
                        "h2d_bytes_per_step": int(hpos.numel() * 8 + hvel.numel() * 8),
                        "d2h_bytes_per_step": int(hpos.numel() * 8 + hvel.numel() * 8),
                        "ms_per_step": ms_e / K, "wall_ms_per_step": 1e3 * wall / K,
+                       "vcycles_per_step": {"old_mean": float(np.mean([v[0] for v in vc_e])),
+                                            "new_mean": float(np.mean([v[1] for v in vc_e]))},
                        "api": "nyxpm_step_host per step (upload + step + download in one call; "
                               "the transfers overlap the step on a second stream; pinned host "
                               "buffers)"}

@@ -75,7 +75,7 @@ def tune(ctx, specs, a_start=0.02, da=0.009, steps=2, max_boxes=48, cache_path=N
     sample = _sample(specs, max_boxes)
     arena = int(sum(Ensemble.box_bytes(s.n, s.np) for s in sample) * 1.3) + (256 << 20)
     ens = Ensemble(ctx, arena)
-    slots = []
+    slots, ics = [], []
     for s in sample:
         if ic_provider is not None:
             pos, vel, mass = ic_provider(s)
@@ -85,8 +85,17 @@ def tune(ctx, specs, a_start=0.02, da=0.009, steps=2, max_boxes=48, cache_path=N
         slot = ens.add(s.n, s.L, s.np)
         ens.upload(slot, pos, vel, mass)
         slots.append(slot)
+        ics.append((pos, vel, mass))
     best = ens.tuning()
     a = [a_start]
+
+    def restart():
+        # every candidate starts from the same ICs at the same a: the solve's
+        # cost changes with a, and a candidate timed later in the run would
+        # otherwise be timed on a different state
+        for slot, (pos, vel, mass) in zip(slots, ics):
+            ens.upload(slot, pos, vel, mass)
+        a[0] = a_start
 
     def run(n_steps):
         ms = 0.0
@@ -107,7 +116,8 @@ def tune(ctx, specs, a_start=0.02, da=0.009, steps=2, max_boxes=48, cache_path=N
         res = {}
         for v in values:
             ens.set_tuning(**dict(best, **{knob: v}))
-            run(1)                      # graph capture + warm-up
+            restart()
+            run(1)                      # the initial solve, graph capture, warm-up
             res[v] = run(steps) / steps
         timings[knob] = res
         best[knob] = min(res, key=res.get)

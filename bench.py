@@ -55,7 +55,7 @@ def parse():
                          "the ensemble's ncu captures run)")
     ap.add_argument("--ensemble-steps", type=int, default=20)
     ap.add_argument("--tuning", type=str, default="",
-                    help="deposit_tile,smooth_rows,inner_vcycles,sort_bucket for the ensemble "
+                    help="deposit_tile,smooth_rows,inner_vcycles,sort_bucket[,prolong_quad] for the ensemble "
                          "instead of the autotuner's choice")
     ap.add_argument("--fused-edge", type=int, default=None,
                     help="nyxpm_params.mg_fused_edge: FP32 V-cycle levels of at most this many "
@@ -334,7 +334,8 @@ def run_ensemble_form(ctx, nboxes, steps=20, fixed_tuning=None, stream=None):
     t_ic = time.perf_counter() - t0
     by_id = {id(s): ic for s, ic in zip(specs, ics)}
     if fixed_tuning:
-        tune = dict(dict(zip(("deposit_tile", "smooth_rows", "inner_vcycles", "sort_bucket"), fixed_tuning)),
+        tune = dict(dict(zip(("deposit_tile", "smooth_rows", "inner_vcycles", "sort_bucket", "prolong_quad"),
+                             fixed_tuning)),
                     cached=True)
     else:
         tune = autotune.tune(ctx, specs,
@@ -343,7 +344,9 @@ def run_ensemble_form(ctx, nboxes, steps=20, fixed_tuning=None, stream=None):
     arena = int(sum(Ensemble.box_bytes(s.n, s.np) for s in specs) * 1.05) + (256 << 20)
     ens = Ensemble(ctx, arena)
     tune.setdefault("sort_bucket", 256)
-    ens.set_tuning(**{k: tune[k] for k in ("deposit_tile", "smooth_rows", "inner_vcycles", "sort_bucket")})
+    tune.setdefault("prolong_quad", 1)
+    knobs = ("deposit_tile", "smooth_rows", "inner_vcycles", "sort_bucket", "prolong_quad")
+    ens.set_tuning(**{k: tune[k] for k in knobs})
     slots = []
     for s, (pos, vel, mass) in zip(specs, ics):
         slot = ens.add(s.n, s.L, s.np)
@@ -392,7 +395,7 @@ def run_ensemble_form(ctx, nboxes, steps=20, fixed_tuning=None, stream=None):
         "max_outer_iters": max(i["max_outer_used"] for i in infos),
         "fallback_iters": sum(i["fallback_iters"] for i in infos),
         "launches_per_step": launches / steps,
-        "tuning": {k: tune[k] for k in ("deposit_tile", "smooth_rows", "inner_vcycles", "sort_bucket")},
+        "tuning": {k: tune[k] for k in knobs},
         "tuning_cached": tune.get("cached", False),
         "plain_fp64_same_schedule": {
             "value": psteps / (plain_ms / 1e3), "unit": UNIT, "total_s": plain_ms / 1e3,

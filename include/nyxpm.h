@@ -419,6 +419,8 @@ typedef struct nyxpm_tuning {
     int inner_vcycles;      /* FP32 V-cycles per FP64 defect-correction iteration */
     int max_outer;          /* defect-correction iterations inside the step graph */
     int sort_bucket;        /* particles per work item of the sort and the kicks: 256, 512 or 1024 */
+    int prolong_quad;       /* 1: the black-only prolongation covers four fine rows (2 x 2) per
+                               task, sharing the coarse rows; 0: one fine row per task */
 } nyxpm_tuning;
 
 typedef struct nyxpm_ensemble_info {

@@ -136,7 +136,7 @@ class Profile(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("deposit_tile", C.c_int), ("smooth_rows", C.c_int), ("inner_vcycles", C.c_int),
-                ("max_outer", C.c_int), ("sort_bucket", C.c_int)]
+                ("max_outer", C.c_int), ("sort_bucket", C.c_int), ("prolong_quad", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

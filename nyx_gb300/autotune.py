@@ -3,12 +3,14 @@
 The knobs are the shapes the batched kernels take from nyxpm_tuning: the CIC
 deposit tile (8x8x8, 8x8x4 or 16x8x4 cells per work item), the sort bucket (256,
 512 or 1024 particles per work item of the counting sort and the kicks), the
-number of plane rows per multigrid work item (the smoother block height) and the
-number of FP32 V-cycles per FP64 defect-correction iteration.  The tuner runs coordinate
+number of plane rows per multigrid work item (the smoother block height), the
+number of FP32 V-cycles per FP64 defect-correction iteration, and whether the
+black-only prolongation covers four fine rows per task.  The tuner runs coordinate
 descent on a scratch ensemble built from a size-stratified sample of the real
 boxes: for each knob in turn it times a few steps per candidate value (CUDA
 events inside nyxpm_ensemble_step, after a warm-up step that captures the new
-graphs) with the other knobs at their best so far.  Results are cached in a
+graphs) with the other knobs at their best so far, every candidate from the
+same ICs and a.  Results are cached in a
 JSON file keyed by GPU name and the ensemble's size mix, so a serving process
 tunes once per workload shape.
 """
@@ -27,6 +29,7 @@ CANDIDATES = {
     "sort_bucket": (256, 512, 1024),
     "smooth_rows": (2, 4, 8),
     "inner_vcycles": (1, 2, 3),
+    "prolong_quad": (1, 0),
 }
 
 

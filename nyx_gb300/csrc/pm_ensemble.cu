@@ -23,6 +23,7 @@
 // the remaining iterations' work, so a slow box never changes another box's
 // result.
 #include "pm_common.cuh"
+#include "pm_prolong.cuh"
 #include "pm_tail.cuh"
 
 #include <algorithm>
@@ -1335,6 +1336,39 @@ __global__ void __launch_bounds__(256) e_prolong4(const Item* __restrict__ items
     }
 }
 
+// coarse rows per item of e_prolong4_black: rows x h4 tasks fill a 256-thread block
+__host__ __device__ inline int quad_rows(int n)
+{
+    const int h4 = n >> 3;
+    const int r = 256 / h4;
+    return r < 1 ? 1 : (r > (n >> 1) ? (n >> 1) : r);
+}
+
+// The black-only prolongation (post-smoothing follows) with four fine rows per
+// task (pm_prolong.cuh), on items {box, fine level a, coarse plane K = b, first
+// coarse row J0 = c}: fine levels whose compact rows hold a multiple of four
+// cells, over a split coarse level.  The same bits as e_prolong4.
+__global__ void __launch_bounds__(256, 4) e_prolong4_black(const Item* __restrict__ items, int nitems,
+                                                          const EDesc* __restrict__ D,
+                                                          const EState* __restrict__ S)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const ELevel F = D[it.box].lv[it.a];
+        const ELevel C = D[it.box].lv[it.a + 1];
+        const int h4 = F.n >> 3, nc = C.n;
+        const int rows = quad_rows(F.n);
+        for (int task = threadIdx.x; task < rows * h4; task += blockDim.x) {
+            const int r = task / h4, t4 = task - r * h4;
+            const int J = it.c + r;
+            if (J >= nc) continue;
+            prolong_black_quad(C, F, J, it.b, (unsigned)t4);
+        }
+    }
+}
+
 // the coarse end of every box's V-cycle (levels tail_l .. bottom), one CTA per
 // box: the per-pass kernels' arithmetic (pm_tail.cuh), so the same bits
 __global__ void __launch_bounds__(kTailThreads) e_tail(int nbox, const EDesc* __restrict__ D,
@@ -1530,6 +1564,10 @@ struct nyxpm_ensemble {
     // the restriction's coarse-row items, split the same way by the fine level
     Range r_restrict_vec[nyxpm::kMaxLev];
     Range r_restrict_row[nyxpm::kMaxLev];
+    // the black-only prolongation's items (nyxpm_tuning.prolong_quad): four fine
+    // rows per task where the coarse level is split, e_prolong4's items elsewhere
+    Range r_prolong_quad[nyxpm::kMaxLev];
+    Range r_prolong_rest[nyxpm::kMaxLev];
     nyxpm::EDesc* d_desc = nullptr;
     nyxpm::EState* d_state = nullptr;
     nyxpm::EStep* d_step = nullptr;
@@ -1709,6 +1747,28 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
                 for (int j0 = 0; j0 < nl; j0 += R) items.push_back(Item{b, l, k, j0});
         }
         end(E->r_smooth_row[l]);
+        begin(E->r_prolong_quad[l]);
+        for (int b = 0; b < nbox; ++b) {
+            const EnsSlot& s = E->slots[b];
+            if (!s.used || l >= s.desc.tail_l) continue;
+            const int nl = s.desc.lv[l].n;
+            if ((nl / 2) % 4 != 0 || !s.desc.lv[l + 1].split) continue;
+            const int rq = quad_rows(nl);
+            for (int K = 0; K < nl / 2; ++K)
+                for (int J0 = 0; J0 < nl / 2; J0 += rq) items.push_back(Item{b, l, K, J0});
+        }
+        end(E->r_prolong_quad[l]);
+        begin(E->r_prolong_rest[l]);
+        for (int b = 0; b < nbox; ++b) {
+            const EnsSlot& s = E->slots[b];
+            if (!s.used || l >= s.desc.tail_l) continue;
+            const int nl = s.desc.lv[l].n;
+            if ((nl / 2) % 4 != 0 || s.desc.lv[l + 1].split) continue;
+            const int rv = vec_rows(nl, 32 * R);
+            for (int k = 0; k < nl; ++k)
+                for (int j0 = 0; j0 < nl; j0 += rv) items.push_back(Item{b, l, k, j0});
+        }
+        end(E->r_prolong_rest[l]);
         for (int vec = 1; vec >= 0; --vec) {
             auto& rg = vec ? E->r_restrict_vec[l] : E->r_restrict_row[l];
             begin(rg);
@@ -1942,10 +2002,20 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
                 const auto& pr = E->r_smooth_row[l];
                 ep_begin(c);
                 const int black = c->p.nu2 > 0 ? 1 : 0;
-                if (pv.cnt) e_prolong4<<<pgrid(E, pv.cnt), rb, 0, s>>>(it + pv.off, pv.cnt, D, S, black);
+                int nk = 0;
+                if (black && E->tune.prolong_quad) {
+                    const auto& pq = E->r_prolong_quad[l];
+                    const auto& pe = E->r_prolong_rest[l];
+                    if (pq.cnt) e_prolong4_black<<<pgrid(E, pq.cnt, 4), 256, 0, s>>>(it + pq.off, pq.cnt, D, S);
+                    if (pe.cnt) e_prolong4<<<pgrid(E, pe.cnt), rb, 0, s>>>(it + pe.off, pe.cnt, D, S, black);
+                    nk += (pq.cnt ? 1 : 0) + (pe.cnt ? 1 : 0);
+                } else {
+                    if (pv.cnt) e_prolong4<<<pgrid(E, pv.cnt), rb, 0, s>>>(it + pv.off, pv.cnt, D, S, black);
+                    nk += pv.cnt ? 1 : 0;
+                }
                 if (pr.cnt) e_prolong<<<pgrid(E, pr.cnt), rb, 0, s>>>(it + pr.off, pr.cnt, D, S, black);
                 ep_end(c, NYXPM_ST_PROLONG);
-                c->launches += (pv.cnt ? 1 : 0) + (pr.cnt ? 1 : 0) - 1;
+                c->launches += nk + (pr.cnt ? 1 : 0) - 1;
                 for (int sw = 0; sw < c->p.nu2; ++sw)
                     for (int color = 0; color < 2; ++color) smooth(l, color);
                 c->launches += 1;
@@ -2171,6 +2241,7 @@ nyxpm_status nyxpm_ensemble_create(nyxpm_ctx* c, size_t arena_bytes, nyxpm_ensem
     E->tune.inner_vcycles = c->p.mixed_inner_vcycles;
     E->tune.max_outer = 6;
     E->tune.sort_bucket = 256;
+    E->tune.prolong_quad = 1;
     E->sm = c->sm_count;
     *out = E;
     return NYXPM_OK;
@@ -2459,7 +2530,8 @@ nyxpm_status nyxpm_ensemble_set_tuning(nyxpm_ctx* c, nyxpm_ensemble* E, const ny
     if (t->deposit_tile < 0 || t->deposit_tile > 2 ||
         (t->smooth_rows != 1 && t->smooth_rows != 2 && t->smooth_rows != 4 && t->smooth_rows != 8) ||
         t->inner_vcycles < 1 || t->inner_vcycles > 8 || t->max_outer < 1 || t->max_outer > 64 ||
-        (t->sort_bucket != 256 && t->sort_bucket != 512 && t->sort_bucket != 1024))
+        (t->sort_bucket != 256 && t->sort_bucket != 512 && t->sort_bucket != 1024) ||
+        (t->prolong_quad != 0 && t->prolong_quad != 1))
         return efail(c, NYXPM_INVALID_ARG, "bad tuning");
     E->tune = *t;
     E->dirty = 1;

@@ -13,6 +13,7 @@
 // FP32 arithmetic is compiled with multiply-add contraction (the default): this
 // form is checked against the FP64 oracle by a stated tolerance, not bitwise.
 #include "pm_common.cuh"
+#include "pm_prolong.cuh"
 #include "pm_tail.cuh"
 
 #include <algorithm>
@@ -1128,91 +1129,17 @@ __global__ void __launch_bounds__(256) k_prolong_f4(LevelViewF Cv, LevelViewF F)
     }
 }
 
-// loads the six coarse values at I = ih0-1 .. ih0+4 of coarse row (J, K) of the
-// split coarse level (c2 = the compact index of the even I = ih0)
-__device__ __forceinline__ void prolong_row6(const LevelViewF& Cv, int J, int K, unsigned c2, float v[6])
-{
-    const unsigned chalf = (unsigned)Cv.n >> 1;
-    const unsigned row = ((unsigned)J + (unsigned)Cv.n * (unsigned)K) * chalf;
-    const bool even_red = ((J + K) & 1) == 0;   // colour of an even I
-    const float* ev = even_red ? Cv.phi_r : Cv.phi_b;
-    const float* od = even_red ? Cv.phi_b : Cv.phi_r;
-    const float2 e01 = __ldg(reinterpret_cast<const float2*>(ev + row + c2));
-    const float e2 = __ldg(ev + row + (c2 + 2 == chalf ? 0u : c2 + 2));
-    const float2 o01 = __ldg(reinterpret_cast<const float2*>(od + row + c2));
-    const float om = __ldg(od + row + (c2 == 0 ? chalf - 1 : c2 - 1));
-    v[0] = om;
-    v[1] = e01.x;
-    v[2] = o01.x;
-    v[3] = e01.y;
-    v[4] = o01.y;
-    v[5] = e2;
-}
-
-// the black corrections of fine row (2J + dj, 2K + DK) from the coarse rows
-// v[kk][jj] = (J - 1 + jj, K - 1 + kk): Js = {J, dj ? J + 1 : J - 1}, Ks likewise;
-// the row's even cells are red iff dj + DK is even, and then its black cells are
-// the odd ones (k_prolong_f4's s1), else the even ones (s0)
-template <int DK>
-__device__ __forceinline__ void prolong_black_rows(const float (&v)[3][3][6], const LevelViewF& F, int J,
-                                                  int K, unsigned t4)
-{
-    const unsigned half = (unsigned)F.n >> 1;
-#pragma unroll
-    for (int dj = 0; dj < 2; ++dj) {
-        const bool odd_black = ((dj + DK) & 1) == 0;
-        float s[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            float acc = 0.f;
-#pragma unroll
-            for (int b = 0; b < 2; ++b)
-#pragma unroll
-                for (int a = 0; a < 2; ++a) {
-                    const float* w = v[b ? (DK ? 2 : 0) : 1][a ? (dj ? 2 : 0) : 1];
-                    acc = fmaf(kProlongWF[0 + 2 * a + 4 * b], w[r + 1], acc);
-                    acc = fmaf(kProlongWF[1 + 2 * a + 4 * b], odd_black ? w[r + 2] : w[r], acc);
-                }
-            s[r] = acc;
-        }
-        const unsigned j = 2u * J + dj, k = 2u * K + DK;
-        const unsigned t = (j + (unsigned)F.n * k) * half + 4 * t4;
-        float4* fb = reinterpret_cast<float4*>(F.phi_b) + (t >> 2);
-        float4 p = *fb;
-        p.x += s[0]; p.y += s[1]; p.z += s[2]; p.w += s[3];
-        *fb = p;
-    }
-}
-
 // The black-only prolongation (post-smoothing follows) with four fine rows per
-// thread: the rows j = 2J, 2J + 1 of the planes k = 2K, 2K + 1 all draw on the
-// coarse rows J - 1 .. J + 1 of the planes K - 1 .. K + 1, so nine coarse row
-// segments are loaded instead of sixteen (the plane K + 1 only after the rows of
-// plane 2K are done, which keeps the kernel at five CTAs per SM).  Each fine
-// row computes only its four black cells; in the split layout they are one
-// float4 of the black array whichever colour the row starts with.  Every black
-// cell sums its eight weighted coarse values in k_prolong_f4's order, so the
-// bits are the same.
+// thread (pm_prolong.cuh): nine coarse row segments for four fine rows, the same
+// bits as k_prolong_f4<1>.
 __global__ void __launch_bounds__(256, 5) k_prolong_f4_black(LevelViewF Cv, LevelViewF F)
 {
-    const int n = F.n, nc = Cv.n;
-    const unsigned h4 = (unsigned)n >> 3;
+    const unsigned h4 = (unsigned)F.n >> 3;
     const unsigned t4 = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int K = blockIdx.z;
-    if (t4 >= h4 || J >= nc) return;
-    const int Jr[3] = {wrap1(J - 1, nc), J, wrap1(J + 1, nc)};
-    const unsigned c2 = 2 * t4;
-    float v[3][3][6];
-#pragma unroll
-    for (int jj = 0; jj < 3; ++jj) {
-        prolong_row6(Cv, Jr[jj], wrap1(K - 1, nc), c2, v[0][jj]);
-        prolong_row6(Cv, Jr[jj], K, c2, v[1][jj]);
-    }
-    prolong_black_rows<0>(v, F, J, K, t4);
-#pragma unroll
-    for (int jj = 0; jj < 3; ++jj) prolong_row6(Cv, Jr[jj], wrap1(K + 1, nc), c2, v[2][jj]);
-    prolong_black_rows<1>(v, F, J, K, t4);
+    if (t4 >= h4 || J >= Cv.n) return;
+    prolong_black_quad(Cv, F, J, K, t4);
 }
 
 __global__ void k_bottom_f(int nb, const float* __restrict__ G, const float* __restrict__ beta, float* phi)

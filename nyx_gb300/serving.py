@@ -137,7 +137,7 @@ class ContinuousBatchingServer:
         if tuning:
             self.ens.set_tuning(**{k: v for k, v in tuning.items()
                                    if k in ("deposit_tile", "smooth_rows", "inner_vcycles", "max_outer",
-                                            "sort_bucket")})
+                                            "sort_bucket", "prolong_quad")})
         self.ic_provider = ic_provider
         self.keep = keep_results
         self.max_skip = max_skip

@@ -83,7 +83,7 @@ def test_shapes_do_not_change_results(ctx):
     ics = [box_ics(s, 0.05) for s in SPECS[:2]]
     sched = equal_da_schedule(0.05, 0.06, 2)
     base, _, _ = run_ensemble(ctx, SPECS[:2], ics, sched)
-    for tuning in ({"deposit_tile": 1, "smooth_rows": 2, "sort_bucket": 512},
+    for tuning in ({"deposit_tile": 1, "smooth_rows": 2, "sort_bucket": 512, "prolong_quad": 0},
                    {"deposit_tile": 2, "smooth_rows": 4, "sort_bucket": 1024}):
         other, _, _ = run_ensemble(ctx, SPECS[:2], ics, sched, tuning)
         for (p0, v0), (p1, v1) in zip(base, other):

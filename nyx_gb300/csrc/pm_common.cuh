@@ -34,6 +34,47 @@ constexpr int kCoarsenAbove = 4;       // levels halve while the edge is even an
 // |v| as ordered bits: for non-negative doubles the bit patterns order like the
 // values and a NaN orders above every number, so max reductions run on the
 // integer pipe (FP64 compares would take FP64 issue slots)
+// Conversions between FP64 and FP32 on the integer pipes.  On GB300 the FP64
+// pipe issues at a small fraction of the FP32 rate, and the hardware conversion
+// instructions between the two formats run on it; the FP32 kernels of the mixed
+// form that round FP64 values to FP32 use these instead.  Both follow IEEE 754
+// directly: a double whose float rounding is a normal float (exponent
+// -126 .. 127) keeps its sign, its exponent rebiased (1023 -> 127) and the top 23
+// of its 52 fraction bits, and the 29 dropped bits round to nearest, ties to
+// even (a carry out of the fraction steps the exponent, up to infinity, as the
+// rounding demands).  Zeros, values that round into the float subnormal range,
+// and infinities and NaNs go to the hardware conversion.  The results are the
+// hardware's, bit for bit.  The hardware paths are calls, not inlined, so that
+// the compiler branches around them instead of converting every value and
+// selecting.
+static __device__ __noinline__ float f64_to_f32_hw(double x) { return (float)x; }
+static __device__ __noinline__ double f32_to_f64_hw(float f) { return (double)f; }
+
+__device__ __forceinline__ float f64_to_f32_rn(double x)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+    const unsigned e = (hi >> 20) & 0x7ffu;                // biased FP64 exponent
+    if (e - 897u > 253u) return f64_to_f32_hw(x);           // outside 2^-126 .. 2^127
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 fraction bits
+    const unsigned rest = lo & 0x1fffffffu;                  // the 29 dropped bits
+    unsigned bits = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
+    bits += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(bits);
+}
+
+// a normal float, exactly, as a double (zeros, subnormals, infinities and NaNs:
+// the hardware conversion)
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned ef = (b >> 23) & 0xffu;
+    if (ef - 1u > 253u) return f32_to_f64_hw(f);
+    const unsigned hi = (b & 0x80000000u) | ((ef + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    const unsigned lo = b << 29;
+    return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
+}
+
 __host__ __device__ inline unsigned long long absbits(double v)
 {
 #ifdef __CUDA_ARCH__

@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(256) e_rowsum(const Item* __restrict__ items, 
             df_two_sum(sh, r[i], sh, err);
             sl = __fadd_rn(sl, err);
         }
-        double s = (double)sh + (double)sl;
+        double s = f32_to_f64(sh) + f32_to_f64(sl);
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
         if (lane == 0) d.rows[row] = s - (double)n * d.mass_offset;
@@ -633,7 +633,7 @@ __global__ void __launch_bounds__(256) e_make_beta(const Item* __restrict__ item
 #pragma unroll
                 for (int odd = 0; odd < 2; ++odd) {
                     const int i = 2 * ih + odd;
-                    const double v = (double)d.frho[cidx(i, j, k, n)];
+                    const double v = f32_to_f64(d.frho[cidx(i, j, k, n)]);
                     const double bt = (v - off) * scale;
                     (((i + j + k) & 1) ? d.beta_b : d.beta_r)[t] = bt;
                     const unsigned long long u = absbits(bt);
@@ -687,9 +687,9 @@ __global__ void __launch_bounds__(256) e_resid(const Item* __restrict__ items, i
                     const double* beta = color ? d.beta_b : d.beta_r;
                     const double s = nbr_sum_split<double>(other, n, half, ih, j, k, q);
                     const double r = beta[t] - fma(s, kSixth, -mine[t]);
-                    const float h = (float)r;
+                    const float h = f64_to_f32_rn(r);
                     (color ? d.lv[0].beta_b : d.lv[0].beta_r)[t] = h;
-                    if (low_words) d.r_lo[(color ? (long long)n * n * half : 0LL) + t] = (float)(r - (double)h);
+                    if (low_words) d.r_lo[(color ? (long long)n * n * half : 0LL) + t] = f64_to_f32_rn(r - f32_to_f64(h));
                     (color ? d.lv[0].phi_b : d.lv[0].phi_r)[t] = 0.f;
                     const unsigned long long u = absbits(r);
                     vmax = u > vmax ? u : vmax;
@@ -826,8 +826,8 @@ __global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items,
                     *rl_p = rlo;
                     double2* pp = reinterpret_cast<double2*>((color ? p_b : p_r) + t);
                     double2 ph = *pp;
-                    ph.x = ph.x + (double)em.x;
-                    ph.y = ph.y + (double)em.y;
+                    ph.x = ph.x + f32_to_f64(em.x);
+                    ph.y = ph.y + f32_to_f64(em.y);
                     *pp = ph;
                     vmax = fmaxf(vmax, fmaxf(fabsf(rh.x), fabsf(rh.y)));
                     emax = fmaxf(emax, fmaxf(fabsf(em.x), fabsf(em.y)));
@@ -852,14 +852,14 @@ __global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items,
                     *rh_p = rh;
                     *rl_p = rlo;
                     double* pp = (color ? p_b : p_r) + t;
-                    *pp = *pp + (double)em;
+                    *pp = *pp + f32_to_f64(em);
                     vmax = fmaxf(vmax, fabsf(rh));
                     emax = fmaxf(emax, fabsf(em));
                 }
             }
         }
-        warp_umax_atomic(absbits((double)vmax), d.norms + 1);
-        warp_umax_atomic(absbits((double)emax), d.norms + 3);
+        warp_umax_atomic(absbits(f32_to_f64(vmax)), d.norms + 1);
+        warp_umax_atomic(absbits(f32_to_f64(emax)), d.norms + 3);
     }
 }
 
@@ -923,8 +923,8 @@ __global__ void __launch_bounds__(256) e_update(const Item* __restrict__ items, 
         if (j >= n) continue;
         for (int ih = threadIdx.x; ih < half; ih += blockDim.x) {
             const long long t = ((long long)j + (long long)n * k) * half + ih;
-            d.phi_r[t] = d.phi_r[t] + (double)d.lv[0].phi_r[t];
-            d.phi_b[t] = d.phi_b[t] + (double)d.lv[0].phi_b[t];
+            d.phi_r[t] = d.phi_r[t] + f32_to_f64(d.lv[0].phi_r[t]);
+            d.phi_b[t] = d.phi_b[t] + f32_to_f64(d.lv[0].phi_b[t]);
         }
     }
 }
@@ -1411,9 +1411,9 @@ __global__ void __launch_bounds__(256) e_grav(const Item* __restrict__ items, in
             };
             const long long c = cidx(i, j, k, n);
             reinterpret_cast<float4*>(d.g32)[c] =
-                make_float4((float)(P(ip, j, k) - P(im, j, k)) * hdxi,
-                            (float)(P(i, jp, k) - P(i, jm, k)) * hdxi,
-                            (float)(P(i, j, kp) - P(i, j, km)) * hdxi, 0.f);
+                make_float4(f64_to_f32_rn(P(ip, j, k) - P(im, j, k)) * hdxi,
+                            f64_to_f32_rn(P(i, jp, k) - P(i, jm, k)) * hdxi,
+                            f64_to_f32_rn(P(i, j, kp) - P(i, j, km)) * hdxi, 0.f);
         }
     }
 }

@@ -49,7 +49,7 @@ __device__ __forceinline__ void to_cell(double x, double dxi, int n, int* i, flo
 {
     const double l = x * dxi;
     double fl = floor(l);
-    float f = (float)(l - fl);
+    float f = f64_to_f32_rn(l - fl);
     if (f >= 1.0f) {  // rounding up to 1 moves the particle to the next cell's origin
         f = 0.0f;
         fl += 1.0;
@@ -99,10 +99,10 @@ __global__ void k_mx_unpack(long long np, int n, double dxi, const double* __res
     ox[q] = a;
     oy[q] = b;
     oz[q] = c;
-    vx[q] = (float)vel[3 * q];
-    vy[q] = (float)vel[3 * q + 1];
-    vz[q] = (float)vel[3 * q + 2];
-    if (m) m[q] = (float)mass[q];
+    vx[q] = f64_to_f32_rn(vel[3 * q]);
+    vy[q] = f64_to_f32_rn(vel[3 * q + 1]);
+    vz[q] = f64_to_f32_rn(vel[3 * q + 2]);
+    if (m) m[q] = f64_to_f32_rn(mass[q]);
     id[q] = (int)q;
 }
 
@@ -117,7 +117,7 @@ __global__ void k_mx_unpack_pos(long long np, int n, double dxi, const double* _
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
     id[q] = (int)q;
-    if (m) m[q] = (float)mass[q];
+    if (m) m[q] = f64_to_f32_rn(mass[q]);
     const double px = pos[3 * q], py = pos[3 * q + 1], pz = pos[3 * q + 2];
     if (!(isfinite(px) && isfinite(py) && isfinite(pz))) {
         atomicAdd(bad, 1ULL);
@@ -151,9 +151,9 @@ __global__ void k_mx_unpack_vel(long long np, const double* __restrict__ vel,
         vx[s] = vy[s] = vz[s] = 0.f;
         return;
     }
-    vx[s] = (float)ux;
-    vy[s] = (float)uy;
-    vz[s] = (float)uz;
+    vx[s] = f64_to_f32_rn(ux);
+    vy[s] = f64_to_f32_rn(uy);
+    vz[s] = f64_to_f32_rn(uz);
 }
 
 __global__ void k_mx_pack_pos(long long np, double dx, const int* __restrict__ cell,
@@ -164,9 +164,9 @@ __global__ void k_mx_pack_pos(long long np, double dx, const int* __restrict__ c
     if (q >= np) return;
     const int c = cell[q];
     const long long o = 3LL * id[q];
-    pos[o] = ((double)cell_i(c) + (double)ox[q]) * dx;
-    pos[o + 1] = ((double)cell_j(c) + (double)oy[q]) * dx;
-    pos[o + 2] = ((double)cell_k(c) + (double)oz[q]) * dx;
+    pos[o] = ((double)cell_i(c) + f32_to_f64(ox[q])) * dx;
+    pos[o + 1] = ((double)cell_j(c) + f32_to_f64(oy[q])) * dx;
+    pos[o + 2] = ((double)cell_k(c) + f32_to_f64(oz[q])) * dx;
 }
 
 __global__ void k_mx_pack_vel(long long np, const float* __restrict__ vx, const float* __restrict__ vy,
@@ -175,9 +175,9 @@ __global__ void k_mx_pack_vel(long long np, const float* __restrict__ vx, const 
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= np) return;
     const long long o = 3LL * id[q];
-    vel[o] = vx[q];
-    vel[o + 1] = vy[q];
-    vel[o + 2] = vz[q];
+    vel[o] = f32_to_f64(vx[q]);
+    vel[o + 1] = f32_to_f64(vy[q]);
+    vel[o + 2] = f32_to_f64(vz[q]);
 }
 
 __global__ void k_mx_pack(long long np, double dx, const int* __restrict__ cell,
@@ -190,12 +190,12 @@ __global__ void k_mx_pack(long long np, double dx, const int* __restrict__ cell,
     if (q >= np) return;
     const int c = cell[q];
     const long long o = 3LL * id[q];
-    pos[o] = ((double)cell_i(c) + (double)ox[q]) * dx;
-    pos[o + 1] = ((double)cell_j(c) + (double)oy[q]) * dx;
-    pos[o + 2] = ((double)cell_k(c) + (double)oz[q]) * dx;
-    vel[o] = vx[q];
-    vel[o + 1] = vy[q];
-    vel[o + 2] = vz[q];
+    pos[o] = ((double)cell_i(c) + f32_to_f64(ox[q])) * dx;
+    pos[o + 1] = ((double)cell_j(c) + f32_to_f64(oy[q])) * dx;
+    pos[o + 2] = ((double)cell_k(c) + f32_to_f64(oz[q])) * dx;
+    vel[o] = f32_to_f64(vx[q]);
+    vel[o + 1] = f32_to_f64(vy[q]);
+    vel[o + 2] = f32_to_f64(vz[q]);
 }
 
 // ---------------------------------------------------------------------------
@@ -407,7 +407,7 @@ __global__ void k_mx_rowsum(int n, const float* __restrict__ rho, double mo, dou
         df_two_sum(sh, r[i], sh, err);
         sl = __fadd_rn(sl, err);
     }
-    double s = (double)sh + (double)sl;
+    double s = f32_to_f64(sh) + f32_to_f64(sl);
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
         const double t = __shfl_down_sync(0xffffffffu, s, off);
@@ -447,7 +447,7 @@ __global__ void k_mx_make_beta(int n, int split, const float* __restrict__ rho, 
     const int k = blockIdx.z;
     if (i >= n || j >= n) return;
     const double off = mo + scal[0];
-    const double v = (double)rho[cidx(i, j, k, n)];
+    const double v = f32_to_f64(rho[cidx(i, j, k, n)]);
     *lv_ptr<double>(beta_r, beta_b, n, split, i, j, k) = (v - off) * scale;
 }
 
@@ -506,9 +506,9 @@ __global__ void k_mx_resid(int n, const double* __restrict__ phi_r, const double
             const double* beta = color ? beta_b : beta_r;
             const double s = nbr_sum_split<double>(other, n, half, ih, j, k, q);
             const double r = beta[t] - fma(s, kSixth, -mine[t]);
-            const float h = (float)r;
+            const float h = f64_to_f32_rn(r);
             (color ? r_b : r_r)[t] = h;
-            if (rl_r) (color ? rl_b : rl_r)[t] = (float)(r - (double)h);
+            if (rl_r) (color ? rl_b : rl_r)[t] = f64_to_f32_rn(r - f32_to_f64(h));
             const unsigned long long u = absbits(r);
             v = u > v ? u : v;
         }
@@ -569,11 +569,11 @@ __global__ void k_mx_resid2(int n, const double* __restrict__ phi_r, const doubl
             s1 = s1 + zp.y;
             const double r0v = b.x - fma(s0, kSixth, -m.x);
             const double r1v = b.y - fma(s1, kSixth, -m.y);
-            const float h0 = (float)r0v, h1 = (float)r1v;
+            const float h0 = f64_to_f32_rn(r0v), h1 = f64_to_f32_rn(r1v);
             reinterpret_cast<float2*>(color ? r_b : r_r)[t >> 1] = make_float2(h0, h1);
             if (rl_r)
                 reinterpret_cast<float2*>(color ? rl_b : rl_r)[t >> 1] =
-                    make_float2((float)(r0v - (double)h0), (float)(r1v - (double)h1));
+                    make_float2(f64_to_f32_rn(r0v - f32_to_f64(h0)), f64_to_f32_rn(r1v - f32_to_f64(h1)));
             const unsigned long long u0 = absbits(r0v), u1 = absbits(r1v);
             v = u0 > v ? u0 : v;
             v = u1 > v ? u1 : v;
@@ -600,7 +600,7 @@ __global__ void k_mx_resid_nat(int n, const double* __restrict__ phi, const doub
         s = s + phi[cidx(i, j, kp, n)];
         const long long c = cidx(i, j, k, n);
         const double rr = beta[c] - fma(s, kSixth, -phi[c]);
-        r[c] = (float)rr;
+        r[c] = f64_to_f32_rn(rr);
         v = absbits(rr);
     }
     block_umax_store(v, norm);
@@ -610,7 +610,7 @@ __global__ void k_mx_resid_nat(int n, const double* __restrict__ phi, const doub
 __global__ void k_mx_update(long long cnt, double* phi, const float* __restrict__ e)
 {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < cnt) phi[t] = phi[t] + (double)e[t];
+    if (t < cnt) phi[t] = phi[t] + f32_to_f64(e[t]);
 }
 
 // Defect-correction step without an FP64 stencil: phi += e (FP64) and the
@@ -655,13 +655,13 @@ __global__ void k_mx_correct(int n, float c_hi, float c_lo, const float* __restr
             rh_p[t] = rh;
             rl_p[t] = rl;
             double* pp = color ? phi_b : phi_r;
-            pp[t] = pp[t] + (double)em;
+            pp[t] = pp[t] + f32_to_f64(em);
             vmax = fmaxf(vmax, fabsf(rh));
             emax = fmaxf(emax, fabsf(em));
         }
     }
-    block_umax_store(absbits((double)vmax), norm);
-    block_umax_store(absbits((double)emax), enorm);
+    block_umax_store(absbits(f32_to_f64(vmax)), norm);
+    block_umax_store(absbits(f32_to_f64(emax)), enorm);
 }
 
 // k_mx_correct with two compact cells of each colour per thread (8- and 16-byte
@@ -713,15 +713,15 @@ __global__ void k_mx_correct2(int n, float c_hi, float c_lo, const float* __rest
             *rl_p = rl;
             double2* pp = reinterpret_cast<double2*>((color ? phi_b : phi_r) + t);
             double2 ph = *pp;
-            ph.x = ph.x + (double)em.x;
-            ph.y = ph.y + (double)em.y;
+            ph.x = ph.x + f32_to_f64(em.x);
+            ph.y = ph.y + f32_to_f64(em.y);
             *pp = ph;
             vmax = fmaxf(vmax, fmaxf(fabsf(rh.x), fabsf(rh.y)));
             emax = fmaxf(emax, fmaxf(fabsf(em.x), fabsf(em.y)));
         }
     }
-    block_umax_store(absbits((double)vmax), norm);
-    block_umax_store(absbits((double)emax), enorm);
+    block_umax_store(absbits(f32_to_f64(vmax)), norm);
+    block_umax_store(absbits(f32_to_f64(emax)), enorm);
 }
 
 // r0 = beta of a split level 0 as its two words (the residual of phi = 0)
@@ -732,11 +732,11 @@ __global__ void k_mx_split_beta(long long cnt, const double* __restrict__ beta_r
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cnt) return;
     const double br = beta_r[t], bb = beta_b[t];
-    const float hr = (float)br, hb = (float)bb;
+    const float hr = f64_to_f32_rn(br), hb = f64_to_f32_rn(bb);
     r_r[t] = hr;
     r_b[t] = hb;
-    rl_r[t] = (float)(br - (double)hr);
-    rl_b[t] = (float)(bb - (double)hb);
+    rl_r[t] = f64_to_f32_rn(br - f32_to_f64(hr));
+    rl_b[t] = f64_to_f32_rn(bb - f32_to_f64(hb));
 }
 
 // ---------------------------------------------------------------------------
@@ -1199,9 +1199,9 @@ __global__ void k_mx_grav(LevelView L, float half_dxi, float* g)
     const int im = i == 0 ? n - 1 : i - 1, ip = i == n - 1 ? 0 : i + 1;
     const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
     const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
-    reinterpret_cast<float4*>(g)[c] = make_float4((float)(P(ip, j, k) - P(im, j, k)) * half_dxi,
-                                                  (float)(P(i, jp, k) - P(i, jm, k)) * half_dxi,
-                                                  (float)(P(i, j, kp) - P(i, j, km)) * half_dxi, 0.f);
+    reinterpret_cast<float4*>(g)[c] = make_float4(f64_to_f32_rn(P(ip, j, k) - P(im, j, k)) * half_dxi,
+                                                  f64_to_f32_rn(P(i, jp, k) - P(i, jm, k)) * half_dxi,
+                                                  f64_to_f32_rn(P(i, j, kp) - P(i, j, km)) * half_dxi, 0.f);
 }
 
 // a caller's FP64 gravity vector (3 n^3, component-major) as the kicks' float4 per cell
@@ -1210,7 +1210,7 @@ __global__ void k_mx_g32_from_g(long long nc, const double* __restrict__ g, floa
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     reinterpret_cast<float4*>(g32)[c] =
-        make_float4((float)g[c], (float)g[nc + c], (float)g[2 * nc + c], 0.f);
+        make_float4(f64_to_f32_rn(g[c]), f64_to_f32_rn(g[nc + c]), f64_to_f32_rn(g[2 * nc + c]), 0.f);
 }
 
 // ---------------------------------------------------------------------------

@@ -75,6 +75,43 @@ __device__ __forceinline__ double f32_to_f64(float f)
     return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
 }
 
+// floor(l) as a double and as an int, on the integer pipes (floor and the
+// double -> int conversion run on the FP64 pipe): for l in [0, 2^31) the
+// fraction bits below the binary point are cleared; (-1, 0) gives -1 and -0.0
+// gives -0.0, as floor does.  Anything else (l <= -1, l >= 2^31, NaN) goes to
+// floor itself.  The same values as floor and (int)floor, bit for bit.
+static __device__ __noinline__ double floor_hw(double l, int* i)
+{
+    const double f = floor(l);
+    *i = (int)f;
+    return f;
+}
+
+__device__ __forceinline__ double floor_int(double l, int* i)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(l);
+    const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+    if ((u >> 63) == 0) {
+        if (e < 1023u) {   // [+0, 1)
+            *i = 0;
+            return 0.0;
+        }
+        if (e < 1054u) {   // [1, 2^31): 1075 - e = 22 .. 52 fraction bits below the point
+            const unsigned sh = 1075u - e;
+            *i = (int)(((u & 0xfffffffffffffULL) | (1ULL << 52)) >> sh);
+            return __longlong_as_double((long long)(u & (~0ULL << sh)));
+        }
+    } else if (e < 1023u) {   // (-1, -0]
+        if ((u << 1) == 0) {
+            *i = 0;
+            return l;   // -0.0
+        }
+        *i = -1;
+        return -1.0;
+    }
+    return floor_hw(l, i);
+}
+
 __host__ __device__ inline unsigned long long absbits(double v)
 {
 #ifdef __CUDA_ARCH__

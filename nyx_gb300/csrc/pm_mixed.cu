@@ -48,13 +48,14 @@ __device__ __forceinline__ int cell_k(int c) { return (c >> 20) & 1023; }
 __device__ __forceinline__ void to_cell(double x, double dxi, int n, int* i, float* o)
 {
     const double l = x * dxi;
-    double fl = floor(l);
+    int il;
+    const double fl = floor_int(l, &il);
     float f = f64_to_f32_rn(l - fl);
     if (f >= 1.0f) {  // rounding up to 1 moves the particle to the next cell's origin
         f = 0.0f;
-        fl += 1.0;
+        il += 1;
     }
-    *i = wrapi((int)fl, n);
+    *i = wrapi(il, n);
     *o = f;
 }
 

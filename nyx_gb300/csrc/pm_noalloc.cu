@@ -103,9 +103,10 @@ nyxpm_status scratch_address(cudaStream_t stream, unsigned char** out, int* sm_c
 __device__ __forceinline__ int na_key1(double x, double dxi, int n, double* frac)
 {
     const double l = fma(x, dxi, 0.5);
-    const double fl = floor(l);
+    int il;
+    const double fl = floor_int(l, &il);
     *frac = l - fl;
-    return wrapi((int)fl, n);
+    return wrapi(il, n);
 }
 
 __global__ void na_zero(int* a, long long cnt)

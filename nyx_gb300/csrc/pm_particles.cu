@@ -30,9 +30,10 @@ inline unsigned blocks_for(long long n, int t = kThreads)
 __device__ __forceinline__ int key1(double x, double dxi, int n, double* frac)
 {
     const double l = fma(x, dxi, 0.5);
-    const double fl = floor(l);
+    int il;
+    const double fl = floor_int(l, &il);
     *frac = l - fl;
-    return wrapi((int)fl, n);
+    return wrapi(il, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -74,11 +75,27 @@ __global__ void k_pack(long long np, const double* __restrict__ x, const double*
     vel[o + 2] = vz[q];
 }
 
-__device__ __forceinline__ double wrap_pos(double v, double L)
+static __device__ __noinline__ double wrap_pos_hw(double v, double L)
 {
     if (v >= L) v = v - L;
     else if (v < 0.0) v = v + L;
     if (v >= L) v = 0.0;
+    return v;
+}
+
+// the periodic shift into [0, L) (L > 0).  For a finite v the comparisons are
+// integer comparisons of the bit patterns (for L > 0, v >= L exactly when v's
+// pattern, read as a signed integer, is not below L's; v < 0 when the sign bit
+// is set and v is not -0.0), off the FP64 pipe; infinities and NaNs take the
+// floating-point comparisons.  The same results, bit for bit.
+__device__ __forceinline__ double wrap_pos(double v, double L)
+{
+    const long long bv = __double_as_longlong(v), bL = __double_as_longlong(L);
+    const unsigned long long uv = (unsigned long long)bv;
+    if (((uv >> 52) & 0x7ffULL) == 0x7ffULL) return wrap_pos_hw(v, L);
+    if (bv >= bL) v = v - L;
+    else if (bv < 0 && (uv << 1) != 0) v = v + L;
+    if (__double_as_longlong(v) >= bL) v = 0.0;
     return v;
 }
 
@@ -583,8 +600,8 @@ __global__ void __launch_bounds__(256) k_kick(long long np, KickArgs A, double* 
     const double lx = fma(x[q], A.dxi, 0.5);
     const double ly = fma(y[q], A.dxi, 0.5);
     const double lz = fma(z[q], A.dxi, 0.5);
-    const double fi = floor(lx), fj = floor(ly), fk = floor(lz);
-    const int i = (int)fi, j = (int)fj, k = (int)fk;
+    int i, j, k;
+    const double fi = floor_int(lx, &i), fj = floor_int(ly, &j), fk = floor_int(lz, &k);
     const double xint = lx - fi, yint = ly - fj, zint = lz - fk;
     const double sx[2] = {1.0 - xint, xint};
     const double sy[2] = {1.0 - yint, yint};
@@ -657,9 +674,13 @@ __global__ void __launch_bounds__(256) k_est_dt(long long np, int n, double dxi,
     double best = 1.0e50;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < np;
          q += (long long)gridDim.x * blockDim.x) {
-        const int i = wrapi((int)floor(x[q] * dxi), n);
-        const int j = wrapi((int)floor(y[q] * dxi), n);
-        const int k = wrapi((int)floor(z[q] * dxi), n);
+        int i, j, k;
+        floor_int(x[q] * dxi, &i);
+        floor_int(y[q] * dxi, &j);
+        floor_int(z[q] * dxi, &k);
+        i = wrapi(i, n);
+        j = wrapi(j, n);
+        k = wrapi(k, n);
         const double ux = fabs(vx[q]) * adxi, uy = fabs(vy[q]) * adxi, uz = fabs(vz[q]) * adxi;
         const double um = fmax(fmax(ux, uy), uz);
         double dtp = um > 0 ? cfl / um : 1.0e50;

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -259,6 +260,8 @@ nyxpm_status nyxpm_create(const nyxpm_params* p, nyxpm_ctx** out)
         c->own_stream = 1;
     }
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, p->device);
+    const char* no_pdl = std::getenv("NYXPM_NO_PDL");
+    c->pdl = (no_pdl && no_pdl[0] && no_pdl[0] != '0') ? 0 : 1;
     *out = c;
     return NYXPM_OK;
 }

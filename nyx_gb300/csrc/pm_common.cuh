@@ -452,7 +452,37 @@ struct Ctx {
     // second stream and events of the host-buffer step (created on first use)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copy_in = nullptr, ev_copy_out = nullptr;
+    // multigrid kernels launched with programmatic dependent launch (off with
+    // the environment variable NYXPM_NO_PDL set, for comparison)
+    int pdl = 1;
 };
+
+// Programmatic dependent launch: a kernel launched by launch_pdl may be scheduled
+// while the kernel before it in the stream finishes its last blocks, hiding the
+// launch gap between the short multigrid kernels (inside the solver graphs too).
+// Every kernel launched this way starts with pdl_wait(), which returns once the
+// previous kernel has completed and its writes are visible, before it reads or
+// writes global memory; then pdl_trigger() lets the next kernel be scheduled once
+// all of this kernel's blocks have started.  Launched without the attribute, both
+// are no-ops, so the kernels are correct on every path.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(const Ctx& c, void (*kernel)(KArgs...), dim3 grid, dim3 block, Args... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = c.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = c.pdl ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 
 // launch bookkeeping: call prof_begin before and prof_end after each launch
 void prof_begin(Ctx& c);

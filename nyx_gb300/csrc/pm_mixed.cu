@@ -747,6 +747,8 @@ __global__ void __launch_bounds__(256) k_gsrb_f(int n, int color, float* __restr
                                                 const float* __restrict__ other,
                                                 const float* __restrict__ beta)
 {
+    pdl_wait();
+    pdl_trigger();
     const int half = n >> 1;
     const int ih = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -775,6 +777,8 @@ __global__ void __launch_bounds__(256) k_gsrb_f4(int n, int color, float* __rest
                                                  const float* __restrict__ other,
                                                  const float* __restrict__ beta)
 {
+    pdl_wait();
+    pdl_trigger();
     // 32-bit offsets: a level holds at most 1024^3 / 2 cells of a colour
     const unsigned half = (unsigned)n >> 1, h4 = half >> 2;
     const unsigned t4 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -833,6 +837,8 @@ __global__ void __launch_bounds__(256) k_gsrb_f4(int n, int color, float* __rest
 // (the black half sweep after it reads only the red cells it overwrote).
 __global__ void k_gsrb_f_zero(long long cnt, float* __restrict__ mine, const float* __restrict__ beta)
 {
+    pdl_wait();
+    pdl_trigger();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < cnt) mine[t] = fmaf(0.f, kSixthF, -beta[t]);
 }
@@ -858,6 +864,8 @@ __device__ __forceinline__ float resid_f(const LevelViewF& L, int i, int j, int 
 template <int RED>
 __global__ void k_restrict_f(LevelViewF F, LevelViewF Cv)
 {
+    pdl_wait();
+    pdl_trigger();
     const int nc = Cv.n;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -973,6 +981,8 @@ __device__ __forceinline__ void fine_row_resid_red(const LevelViewF& F, int j, i
 // order; half the loads of k_restrict_f4.
 __global__ void __launch_bounds__(256) k_restrict_f4_red(LevelViewF F, LevelViewF Cv)
 {
+    pdl_wait();
+    pdl_trigger();
     const int nc = Cv.n;
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // coarse cells 2t, 2t+1
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -998,6 +1008,8 @@ __global__ void __launch_bounds__(256) k_restrict_f4_red(LevelViewF F, LevelView
 
 __global__ void __launch_bounds__(256) k_restrict_f4(LevelViewF F, LevelViewF Cv)
 {
+    pdl_wait();
+    pdl_trigger();
     const int nc = Cv.n;
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // coarse cells 2t, 2t+1
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -1028,6 +1040,8 @@ __global__ void __launch_bounds__(256) k_restrict_f4(LevelViewF F, LevelViewF Cv
 template <int BLACK>
 __global__ void k_prolong_f(LevelViewF Cv, LevelViewF F)
 {
+    pdl_wait();
+    pdl_trigger();
     const int n = F.n, nc = Cv.n, half = n >> 1;
     const int ih = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -1067,6 +1081,8 @@ __global__ void k_prolong_f(LevelViewF Cv, LevelViewF F)
 template <int BLACK>
 __global__ void __launch_bounds__(256) k_prolong_f4(LevelViewF Cv, LevelViewF F)
 {
+    pdl_wait();
+    pdl_trigger();
     const int n = F.n, nc = Cv.n;
     const unsigned half = (unsigned)n >> 1, chalf = (unsigned)nc >> 1, h4 = half >> 2;
     const unsigned t4 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1135,6 +1151,8 @@ __global__ void __launch_bounds__(256) k_prolong_f4(LevelViewF Cv, LevelViewF F)
 // bits as k_prolong_f4<1>.
 __global__ void __launch_bounds__(256, 5) k_prolong_f4_black(LevelViewF Cv, LevelViewF F)
 {
+    pdl_wait();
+    pdl_trigger();
     const unsigned h4 = (unsigned)F.n >> 3;
     const unsigned t4 = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -1145,6 +1163,8 @@ __global__ void __launch_bounds__(256, 5) k_prolong_f4_black(LevelViewF Cv, Leve
 
 __global__ void k_bottom_f(int nb, const float* __restrict__ G, const float* __restrict__ beta, float* phi)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ float r[kMaxBottom * kMaxBottom * kMaxBottom];
     __shared__ float g[kMaxBottom * kMaxBottom * kMaxBottom];
     const int nc = nb * nb * nb;
@@ -1179,6 +1199,8 @@ struct TailF {
 
 __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail_f(TailF A)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ float r[kMaxBottom * kMaxBottom * kMaxBottom];
     __shared__ float g[kMaxBottom * kMaxBottom * kMaxBottom];
     vcycle_tail<float>(A.lv, A.nl, A.nu1, A.nu2, A.Gf, A.nb, r, g, true);
@@ -1327,13 +1349,13 @@ nyxpm_status gsrb_sweep_f(Ctx& c, const Level& l, int fine, bool zero_start = fa
         const float* beta = color ? l.fbeta_b : l.fbeta_r;
         prof_begin(c);
         if (zero_start && color == 0)
-            k_gsrb_f_zero<<<blocks_for(half_cells), kThreads, 0, c.stream>>>(half_cells, mine, beta);
+            launch_pdl(c, k_gsrb_f_zero, dim3(blocks_for(half_cells)), dim3(kThreads), half_cells, mine, beta);
         else if (march)
-            k_gsrb_f4<kMarchZ><<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
+            launch_pdl(c, k_gsrb_f4<kMarchZ>, dim3(g.grid), dim3(g.block), l.n, color, mine, other, beta);
         else if (vec)
-            k_gsrb_f4<1><<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
+            launch_pdl(c, k_gsrb_f4<1>, dim3(g.grid), dim3(g.block), l.n, color, mine, other, beta);
         else
-            k_gsrb_f<<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
+            launch_pdl(c, k_gsrb_f, dim3(g.grid), dim3(g.block), l.n, color, mine, other, beta);
         prof_end(c, NYXPM_ST_SMOOTH, 12.0 * half_cells, fine);
     }
     return check_launch(c, "gsrb f32");
@@ -1356,7 +1378,7 @@ nyxpm_status vcycle_tail_f(Ctx& c, Box& b, size_t li)
         bytes += (l + 1 < A.nl) ? 6.0 * cells * 2 * (c.p.nu1 + c.p.nu2) + 16.0 * cells : 8.0 * cells;
     }
     prof_begin(c);
-    k_vcycle_tail_f<<<1, kTailThreads, 0, c.stream>>>(A);
+    launch_pdl(c, k_vcycle_tail_f, dim3(1), dim3(kTailThreads), A);
     prof_end(c, NYXPM_ST_SMOOTH, bytes);
     return check_launch(c, "fused coarse V-cycle f32");
 }
@@ -1388,7 +1410,7 @@ nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li, bool fresh = false)
     if (tail_fits(c, b, li)) return vcycle_tail_f(c, b, li);
     if (li + 1 == b.levels.size()) {
         prof_begin(c);
-        k_bottom_f<<<1, 512, 0, c.stream>>>(b.nb, b.Gf, f.fbeta_r, f.fphi_r);
+        launch_pdl(c, k_bottom_f, dim3(1), dim3(512), b.nb, b.Gf, f.fbeta_r, f.fphi_r);
         prof_end(c, NYXPM_ST_BOTTOM, 8.0 * f.n * f.n * f.n);
         return check_launch(c, "bottom f32");
     }
@@ -1406,12 +1428,12 @@ nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li, bool fresh = false)
         prof_begin(c);
         if ((f.n / 2) % 4 == 0) {
             const Geo g = geo3(cl.n / 2, cl.n, cl.n);
-            if (c.p.nu1 > 0) k_restrict_f4_red<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
-            else k_restrict_f4<<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+            if (c.p.nu1 > 0) launch_pdl(c, k_restrict_f4_red, dim3(g.grid), dim3(g.block), viewf(f), viewf(cl));
+            else launch_pdl(c, k_restrict_f4, dim3(g.grid), dim3(g.block), viewf(f), viewf(cl));
         } else {
             const Geo g = geo3(cl.n, cl.n, cl.n);
-            if (c.p.nu1 > 0) k_restrict_f<1><<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
-            else k_restrict_f<0><<<g.grid, g.block, 0, c.stream>>>(viewf(f), viewf(cl));
+            if (c.p.nu1 > 0) launch_pdl(c, k_restrict_f<1>, dim3(g.grid), dim3(g.block), viewf(f), viewf(cl));
+            else launch_pdl(c, k_restrict_f<0>, dim3(g.grid), dim3(g.block), viewf(f), viewf(cl));
         }
         // phi and beta read once, coarse beta and phi written; the red-only form reads
         // the black cells' beta not at all
@@ -1425,14 +1447,14 @@ nyxpm_status vcycle_f(Ctx& c, Box& b, size_t li, bool fresh = false)
         const bool black = c.p.nu2 > 0;
         if (cl.split && (f.n / 2) % 4 == 0 && black) {
             const Geo g = geo3(f.n / 8, cl.n, cl.n);
-            k_prolong_f4_black<<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+            launch_pdl(c, k_prolong_f4_black, dim3(g.grid), dim3(g.block), viewf(cl), viewf(f));
         } else if (cl.split && (f.n / 2) % 4 == 0) {
             const Geo g = geo3(f.n / 8, f.n, f.n);
-            k_prolong_f4<0><<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+            launch_pdl(c, k_prolong_f4<0>, dim3(g.grid), dim3(g.block), viewf(cl), viewf(f));
         } else {
             const Geo g = geo3(f.n / 2, f.n, f.n);
-            if (black) k_prolong_f<1><<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
-            else k_prolong_f<0><<<g.grid, g.block, 0, c.stream>>>(viewf(cl), viewf(f));
+            if (black) launch_pdl(c, k_prolong_f<1>, dim3(g.grid), dim3(g.block), viewf(cl), viewf(f));
+            else launch_pdl(c, k_prolong_f<0>, dim3(g.grid), dim3(g.block), viewf(cl), viewf(f));
         }
         // the fine corrections read and written (black cells only when post-smoothing
         // follows), the coarse level read once

@@ -1246,7 +1246,7 @@ struct MxKickArgs {
     int do_move;
 };
 
-__global__ void __launch_bounds__(256) k_mx_kick(long long np, MxKickArgs A, int* cell, float* ox,
+__global__ void __launch_bounds__(256, 6) k_mx_kick(long long np, MxKickArgs A, int* cell, float* ox,
                                                  float* oy, float* oz, float* vx, float* vy, float* vz)
 {
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1263,7 +1263,13 @@ __global__ void __launch_bounds__(256) k_mx_kick(long long np, MxKickArgs A, int
     const float sy[2] = {1.f - fy, fy};
     const float sz[2] = {1.f - fz, fz};
     float w[8];
-    long long cc[8];
+    // 32-bit cell offsets (n <= 1024): the eight corners are a row pair, a plane
+    // pair and a column pair around (i, j, k)
+    const unsigned xs[2] = {(unsigned)i, (unsigned)wrap1(i - 1, n)};
+    const unsigned ys[2] = {(unsigned)j * (unsigned)n, (unsigned)wrap1(j - 1, n) * (unsigned)n};
+    const unsigned nn = (unsigned)n * (unsigned)n;
+    const unsigned zs[2] = {(unsigned)k * nn, (unsigned)wrap1(k - 1, n) * nn};
+    unsigned cc[8];
 #pragma unroll
     for (int kk = 0; kk <= 1; ++kk)
 #pragma unroll
@@ -1272,7 +1278,7 @@ __global__ void __launch_bounds__(256) k_mx_kick(long long np, MxKickArgs A, int
             for (int ii = 0; ii <= 1; ++ii) {
                 const int t = ii + 2 * jj + 4 * kk;
                 w[t] = (sx[1 - ii] * sy[1 - jj]) * sz[1 - kk];
-                cc[t] = cidx(wrap1(i - ii, n), wrap1(j - jj, n), wrap1(k - kk, n), n);
+                cc[t] = xs[ii] + ys[jj] + zs[kk];
             }
     float v[3] = {vx[q], vy[q], vz[q]};
     float val[3] = {0.f, 0.f, 0.f};
@@ -1301,8 +1307,12 @@ __global__ void __launch_bounds__(256) k_mx_kick(long long np, MxKickArgs A, int
                 fl += 1.f;
             }
             int idx = ic[d] + (int)fl;
-            idx %= n;
-            if (idx < 0) idx += n;
+            if (idx >= n) idx -= n;       // a move of less than n cells: one step
+            else if (idx < 0) idx += n;
+            if ((unsigned)idx >= (unsigned)n) {   // further: the general wrap
+                idx %= n;
+                if (idx < 0) idx += n;
+            }
             ic[d] = idx;
             o[d] = p;
         }

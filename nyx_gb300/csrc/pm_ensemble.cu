@@ -192,7 +192,12 @@ __global__ void __launch_bounds__(kPT, 4) e_kick(const Item* __restrict__ items,
         const float sy[2] = {1.f - fy, fy};
         const float sz[2] = {1.f - fz, fz};
         float wgt[8];
-        long long cc[8];
+        // 32-bit cell offsets (n <= 1024), as in k_mx_kick
+        const unsigned xs[2] = {(unsigned)i, (unsigned)wrap1(i - 1, n)};
+        const unsigned ys[2] = {(unsigned)j * (unsigned)n, (unsigned)wrap1(j - 1, n) * (unsigned)n};
+        const unsigned nn = (unsigned)n * (unsigned)n;
+        const unsigned zs[2] = {(unsigned)k * nn, (unsigned)wrap1(k - 1, n) * nn};
+        unsigned cc[8];
 #pragma unroll
         for (int kk = 0; kk <= 1; ++kk)
 #pragma unroll
@@ -201,7 +206,7 @@ __global__ void __launch_bounds__(kPT, 4) e_kick(const Item* __restrict__ items,
                 for (int ii = 0; ii <= 1; ++ii) {
                     const int t = ii + 2 * jj + 4 * kk;
                     wgt[t] = (sx[1 - ii] * sy[1 - jj]) * sz[1 - kk];
-                    cc[t] = cidx(wrap1(i - ii, n), wrap1(j - jj, n), wrap1(k - kk, n), n);
+                    cc[t] = xs[ii] + ys[jj] + zs[kk];
                 }
         float v[3] = {P.vx[q], P.vy[q], P.vz[q]};
         float val[3] = {0.f, 0.f, 0.f};
@@ -229,8 +234,13 @@ __global__ void __launch_bounds__(kPT, 4) e_kick(const Item* __restrict__ items,
                     p = 0.f;
                     fl += 1.f;
                 }
-                int idx = (ic[dd] + (int)fl) % n;
-                if (idx < 0) idx += n;
+                int idx = ic[dd] + (int)fl;
+                if (idx >= n) idx -= n;       // a move of less than n cells: one step
+                else if (idx < 0) idx += n;
+                if ((unsigned)idx >= (unsigned)n) {   // further: the general wrap
+                    idx %= n;
+                    if (idx < 0) idx += n;
+                }
                 ic[dd] = idx;
                 o[dd] = p;
             }

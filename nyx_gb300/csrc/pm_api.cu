@@ -36,6 +36,8 @@ void prof_end(Ctx& c, int stage, double bytes, int fine)
 nyxpm_status check_launch(Ctx& c, const char* what)
 {
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = c.launch_error;
+    c.launch_error = cudaSuccess;
     if (e == cudaSuccess) return NYXPM_OK;
     c.err = std::string(what) + ": " + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? NYXPM_OOM : NYXPM_CUDA_ERROR;

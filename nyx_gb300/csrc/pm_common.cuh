@@ -455,6 +455,8 @@ struct Ctx {
     // multigrid kernels launched with programmatic dependent launch (off with
     // the environment variable NYXPM_NO_PDL set, for comparison)
     int pdl = 1;
+    // the first error a launch_pdl returned since the last check_launch
+    cudaError_t launch_error = cudaSuccess;
 };
 
 // Programmatic dependent launch: a kernel launched by launch_pdl may be scheduled
@@ -469,7 +471,7 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 template <typename... KArgs, typename... Args>
-inline cudaError_t launch_pdl(const Ctx& c, void (*kernel)(KArgs...), dim3 grid, dim3 block, Args... args)
+inline void launch_pdl(Ctx& c, void (*kernel)(KArgs...), dim3 grid, dim3 block, Args... args)
 {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = grid;
@@ -481,7 +483,8 @@ inline cudaError_t launch_pdl(const Ctx& c, void (*kernel)(KArgs...), dim3 grid,
     attr[0].val.programmaticStreamSerializationAllowed = c.pdl ? 1 : 0;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    if (e != cudaSuccess && c.launch_error == cudaSuccess) c.launch_error = e;   // check_launch reports it
 }
 
 // launch bookkeeping: call prof_begin before and prof_end after each launch

@@ -180,6 +180,8 @@ __global__ void k_resnorm_red_sweep(int n, const double* __restrict__ phi_r,
                                     const double* __restrict__ beta_r, double* __restrict__ next_r,
                                     unsigned long long* out)
 {
+    pdl_wait();
+    pdl_trigger();
     const int half = n >> 1;
     const int ih = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -223,6 +225,8 @@ __global__ void __launch_bounds__(256) k_gsrb(int n, int color, double* __restri
                                               const double* __restrict__ other,
                                               const double* __restrict__ beta)
 {
+    pdl_wait();
+    pdl_trigger();
     const int half = n >> 1;
     const int ih = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -251,6 +255,8 @@ __global__ void __launch_bounds__(256) k_gsrb(int n, int color, double* __restri
 template <int RED>
 __global__ void k_restrict(LevelView F, LevelView Cv)
 {
+    pdl_wait();
+    pdl_trigger();
     const int nc = Cv.n;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -279,6 +285,8 @@ __global__ void k_restrict(LevelView F, LevelView Cv)
 template <int BLACK>
 __global__ void k_prolong4(LevelView Cv, LevelView F)
 {
+    pdl_wait();
+    pdl_trigger();
     const int n = F.n, nc = Cv.n;
     const unsigned half = (unsigned)n >> 1, chalf = (unsigned)nc >> 1, h4 = half >> 2;
     const unsigned t4 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -349,6 +357,8 @@ __global__ void k_prolong4(LevelView Cv, LevelView F)
 template <int BLACK>
 __global__ void k_prolong(LevelView Cv, LevelView F)
 {
+    pdl_wait();
+    pdl_trigger();
     const int n = F.n, nc = Cv.n, half = n >> 1;
     const int ih = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -382,6 +392,8 @@ __global__ void k_prolong(LevelView Cv, LevelView F)
 __global__ void k_bottom(int nb, const double* __restrict__ G, const double* __restrict__ beta,
                          double* phi)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double r[kMaxBottom * kMaxBottom * kMaxBottom];
     __shared__ double g[kMaxBottom * kMaxBottom * kMaxBottom];
     const int nc = nb * nb * nb;
@@ -416,6 +428,8 @@ struct TailD {
 
 __global__ void __launch_bounds__(kTailThreadsD) k_vcycle_tail_d(TailD A)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double r[kMaxBottom * kMaxBottom * kMaxBottom];
     __shared__ double g[kMaxBottom * kMaxBottom * kMaxBottom];
     vcycle_tail<double>(A.lv, A.nl, A.nu1, A.nu2, A.G, A.nb, r, g, true);
@@ -480,7 +494,7 @@ nyxpm_status gsrb_sweep(Ctx& c, const Level& l, int fine, int black_only = 0)
         const double* other = color ? l.phi_r : l.phi_b;
         const double* beta = color ? l.beta_b : l.beta_r;
         prof_begin(c);
-        k_gsrb<<<g.grid, g.block, 0, c.stream>>>(l.n, color, mine, other, beta);
+        launch_pdl(c, k_gsrb, dim3(g.grid), dim3(g.block), l.n, color, mine, other, beta);
         prof_end(c, NYXPM_ST_SMOOTH, 24.0 * half_cells, fine);
     }
     return check_launch(c, "gsrb");
@@ -512,7 +526,7 @@ nyxpm_status vcycle_tail_d(Ctx& c, Box& b, size_t li)
         bytes += (l + 1 < A.nl) ? 12.0 * cells * 2 * (c.p.nu1 + c.p.nu2) + 32.0 * cells : 16.0 * cells;
     }
     prof_begin(c);
-    k_vcycle_tail_d<<<1, kTailThreadsD, 0, c.stream>>>(A);
+    launch_pdl(c, k_vcycle_tail_d, dim3(1), dim3(kTailThreadsD), A);
     prof_end(c, NYXPM_ST_SMOOTH, bytes);
     return check_launch(c, "fused coarse V-cycle");
 }
@@ -526,7 +540,7 @@ nyxpm_status vcycle(Ctx& c, Box& b, size_t li, int red_done = 0)
     if (tail_fits_d(c, b, li)) return vcycle_tail_d(c, b, li);
     if (li + 1 == b.levels.size()) {
         prof_begin(c);
-        k_bottom<<<1, 512, 0, c.stream>>>(b.nb, b.G, f.beta_r, f.phi_r);
+        launch_pdl(c, k_bottom, dim3(1), dim3(512), b.nb, b.G, f.beta_r, f.phi_r);
         prof_end(c, NYXPM_ST_BOTTOM, 16.0 * f.n * f.n * f.n);
         return check_launch(c, "bottom");
     }
@@ -541,9 +555,9 @@ nyxpm_status vcycle(Ctx& c, Box& b, size_t li, int red_done = 0)
         const Geo g = geo3(cl.n, cl.n, cl.n);
         prof_begin(c);
         if (c.p.nu1 > 0)
-            k_restrict<1><<<g.grid, g.block, 0, c.stream>>>(view(f), view(cl));
+            launch_pdl(c, k_restrict<1>, dim3(g.grid), dim3(g.block), view(f), view(cl));
         else
-            k_restrict<0><<<g.grid, g.block, 0, c.stream>>>(view(f), view(cl));
+            launch_pdl(c, k_restrict<0>, dim3(g.grid), dim3(g.block), view(f), view(cl));
         prof_end(c, NYXPM_ST_RESTRICT, 16.0 * ncf + 16.0 * ncc);
     }
     if ((st = check_launch(c, "restrict")) != NYXPM_OK) return st;
@@ -553,12 +567,12 @@ nyxpm_status vcycle(Ctx& c, Box& b, size_t li, int red_done = 0)
         const bool black = nu2 > 0;
         if (quads && cl.split) {
             const Geo g = geo3(f.n / 8, f.n, f.n);
-            if (black) k_prolong4<1><<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
-            else k_prolong4<0><<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
+            if (black) launch_pdl(c, k_prolong4<1>, dim3(g.grid), dim3(g.block), view(cl), view(f));
+            else launch_pdl(c, k_prolong4<0>, dim3(g.grid), dim3(g.block), view(cl), view(f));
         } else {
             const Geo g = geo3(f.n / 2, f.n, f.n);
-            if (black) k_prolong<1><<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
-            else k_prolong<0><<<g.grid, g.block, 0, c.stream>>>(view(cl), view(f));
+            if (black) launch_pdl(c, k_prolong<1>, dim3(g.grid), dim3(g.block), view(cl), view(f));
+            else launch_pdl(c, k_prolong<0>, dim3(g.grid), dim3(g.block), view(cl), view(f));
         }
         prof_end(c, NYXPM_ST_PROLONG, 16.0 * ncf + 8.0 * ncc);
     }
@@ -681,7 +695,7 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info)
                 const Geo g = geo3(L0.n / 2, L0.n, L0.n);
                 prof_begin(c);
                 cudaMemsetAsync(b.norms + 1, 0, sizeof(unsigned long long), c.stream);
-                k_resnorm_red_sweep<<<g.grid, g.block, 0, c.stream>>>(L0.n, L0.phi_r, L0.phi_b, L0.beta_r,
+                launch_pdl(c, k_resnorm_red_sweep, dim3(g.grid), dim3(g.block), L0.n, L0.phi_r, L0.phi_b, L0.beta_r,
                                                                       b.phi_r_spare, b.norms + 1);
                 prof_end(c, NYXPM_ST_NORM, 16.0 * nc);
                 if ((s = check_launch(c, "red norm + sweep")) != NYXPM_OK) return s;

@@ -112,6 +112,30 @@ __device__ __forceinline__ double floor_int(double l, int* i)
     return floor_hw(l, i);
 }
 
+static __device__ __noinline__ double wrap_pos_hw(double v, double L)
+{
+    if (v >= L) v = v - L;
+    else if (v < 0.0) v = v + L;
+    if (v >= L) v = 0.0;
+    return v;
+}
+
+// the periodic shift into [0, L) (L > 0).  For a finite v the comparisons are
+// integer comparisons of the bit patterns (for L > 0, v >= L exactly when v's
+// pattern, read as a signed integer, is not below L's; v < 0 when the sign bit
+// is set and v is not -0.0), off the FP64 pipe; infinities and NaNs take the
+// floating-point comparisons.  The same results, bit for bit.
+__device__ __forceinline__ double wrap_pos(double v, double L)
+{
+    const long long bv = __double_as_longlong(v), bL = __double_as_longlong(L);
+    const unsigned long long uv = (unsigned long long)bv;
+    if (((uv >> 52) & 0x7ffULL) == 0x7ffULL) return wrap_pos_hw(v, L);
+    if (bv >= bL) v = v - L;
+    else if (bv < 0 && (uv << 1) != 0) v = v + L;
+    if (__double_as_longlong(v) >= bL) v = 0.0;
+    return v;
+}
+
 __host__ __device__ inline unsigned long long absbits(double v)
 {
 #ifdef __CUDA_ARCH__

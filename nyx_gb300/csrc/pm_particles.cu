@@ -75,29 +75,6 @@ __global__ void k_pack(long long np, const double* __restrict__ x, const double*
     vel[o + 2] = vz[q];
 }
 
-static __device__ __noinline__ double wrap_pos_hw(double v, double L)
-{
-    if (v >= L) v = v - L;
-    else if (v < 0.0) v = v + L;
-    if (v >= L) v = 0.0;
-    return v;
-}
-
-// the periodic shift into [0, L) (L > 0).  For a finite v the comparisons are
-// integer comparisons of the bit patterns (for L > 0, v >= L exactly when v's
-// pattern, read as a signed integer, is not below L's; v < 0 when the sign bit
-// is set and v is not -0.0), off the FP64 pipe; infinities and NaNs take the
-// floating-point comparisons.  The same results, bit for bit.
-__device__ __forceinline__ double wrap_pos(double v, double L)
-{
-    const long long bv = __double_as_longlong(v), bL = __double_as_longlong(L);
-    const unsigned long long uv = (unsigned long long)bv;
-    if (((uv >> 52) & 0x7ffULL) == 0x7ffULL) return wrap_pos_hw(v, L);
-    if (bv >= bL) v = v - L;
-    else if (bv < 0 && (uv << 1) != 0) v = v + L;
-    if (__double_as_longlong(v) >= bL) v = 0.0;
-    return v;
-}
 
 // The host-buffer step's split upload and download (nyxpm_step_host): positions
 // (and masses) first, velocities later; positions out as soon as the drift made

@@ -24,6 +24,7 @@
 // result.
 #include "pm_common.cuh"
 #include "pm_prolong.cuh"
+#include "pm_restrict.cuh"
 #include "pm_tail.cuh"
 
 #include <algorithm>
@@ -1190,6 +1191,50 @@ __global__ void __launch_bounds__(256) e_restrict4(const Item* __restrict__ item
     }
 }
 
+// e_restrict4 after pre-smoothing (the last half sweep black): the coarse
+// right-hand side from the 4 red children of each coarse cell, whose residuals
+// are the only ones above round-off (pm_restrict.cuh, as k_restrict_f4_red),
+// summed in (dk, dj) order; half the loads and residual arithmetic.
+__global__ void __launch_bounds__(256) e_restrict4_red(const Item* __restrict__ items, int nitems,
+                                                       const EDesc* __restrict__ D,
+                                                       const EState* __restrict__ S)
+{
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int R = blockDim.y;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        const ELevel& F = d.lv[it.a - 1];
+        const ELevel& C = d.lv[it.a];
+        const int nc = C.n, K = it.b;
+        const int npair = nc >> 1;
+        for (int task = tid; task < R * npair; task += nthreads) {
+            const int rr = task / npair, t = task - rr * npair;
+            const int J = it.c + rr;
+            if (J >= nc) continue;
+            float r[2][2][2];
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+                for (int dj = 0; dj < 2; ++dj) fine_row_resid_red(F, 2 * J + dj, 2 * K + dk, (unsigned)t, r[dk][dj]);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                float s = 0.f;
+#pragma unroll
+                for (int dk = 0; dk < 2; ++dk)
+#pragma unroll
+                    for (int dj = 0; dj < 2; ++dj) s += r[dk][dj][u];
+                const int I = 2 * t + u;
+                *lv_ptr<float>(C.beta_r, C.beta_b, nc, C.split, I, J, K) = s * 0.5f;
+                *lv_ptr<float>(C.phi_r, C.phi_b, nc, C.split, I, J, K) = 0.f;
+            }
+        }
+    }
+}
+
 // item level = the fine level (split); rows of the fine level
 // black: only the black fine cells take the correction (post-smoothing follows
 // and overwrites the red ones unread; the same bits)
@@ -1396,7 +1441,7 @@ __global__ void __launch_bounds__(kTailThreads) e_tail(int nbox, const EDesc* __
         const ELevel& e = d.lv[d.tail_l + l];
         lv[l] = LevelViewF{e.n, e.split, e.phi_r, e.phi_b, e.beta_r, e.beta_b};
     }
-    vcycle_tail<float>(lv, nl, nu1, nu2, d.Gf, d.nb, r, g, false);
+    vcycle_tail<float>(lv, nl, nu1, nu2, d.Gf, d.nb, r, g, nu1 > 0);
 }
 
 // FP32 gravity vector from the FP64 phi (level-0 rows, natural coordinates)
@@ -1995,7 +2040,10 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
                 const auto& qv = E->r_restrict_vec[l + 1];
                 const auto& qr = E->r_restrict_row[l + 1];
                 ep_begin(c);
-                if (qv.cnt) e_restrict4<<<pgrid(E, qv.cnt), rb, 0, s>>>(it + qv.off, qv.cnt, D, S);
+                if (qv.cnt && c->p.nu1 > 0)
+                    e_restrict4_red<<<pgrid(E, qv.cnt), rb, 0, s>>>(it + qv.off, qv.cnt, D, S);
+                else if (qv.cnt)
+                    e_restrict4<<<pgrid(E, qv.cnt), rb, 0, s>>>(it + qv.off, qv.cnt, D, S);
                 if (qr.cnt) e_restrict<<<pgrid(E, qr.cnt), rb, 0, s>>>(it + qr.off, qr.cnt, D, S);
                 ep_end(c, NYXPM_ST_RESTRICT);
                 c->launches += (qv.cnt ? 1 : 0) + (qr.cnt ? 1 : 0) - 1;

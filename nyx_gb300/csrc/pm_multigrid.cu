@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(kTailThreadsD) k_vcycle_tail_d(TailD A)
     pdl_trigger();
     __shared__ double r[kMaxBottom * kMaxBottom * kMaxBottom];
     __shared__ double g[kMaxBottom * kMaxBottom * kMaxBottom];
-    vcycle_tail<double>(A.lv, A.nl, A.nu1, A.nu2, A.G, A.nb, r, g, true);
+    vcycle_tail<double>(A.lv, A.nl, A.nu1, A.nu2, A.G, A.nb, r, g, A.nu1 > 0);
 }
 
 // g_d(c) = 0.5*((phi_c - phi_{c-e_d})*dxi + (phi_{c+e_d} - phi_c)*dxi), second product fused;

@@ -874,6 +874,94 @@ __global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items,
     }
 }
 
+// rows of level 0 per e_correct_v item: enough (row, pair) tasks to fill a block
+// of nthreads threads (n / 4 compact pairs per row)
+__host__ __device__ inline int correct_rows(int n, int nthreads)
+{
+    const int pairs = n >> 2;
+    const int r = pairs > 0 ? nthreads / pairs : n;
+    return r < 1 ? 1 : (r > n ? n : r);
+}
+
+// e_correct for boxes whose level-0 rows hold an even number of compact cells,
+// on items {box, 0, plane k, first row j0} of correct_rows(n) rows: one task per
+// compact pair of one row, so small boxes fill the block too.  The same
+// arithmetic per cell as e_correct (the k_mx_correct2 pattern).
+__global__ void __launch_bounds__(256) e_correct_v(const Item* __restrict__ items, int nitems,
+                                                   const EDesc* __restrict__ D,
+                                                   const EState* __restrict__ S, float c_hi, float c_lo)
+{
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;  // uniform across the block
+        const EDesc& d = D[it.box];
+        const int n = d.n, k = it.b;
+        const unsigned half = (unsigned)n >> 1;
+        const unsigned pairs = half >> 1;
+        const unsigned nh = (unsigned)n * (unsigned)n * half;
+        const int rows = correct_rows(n, nthreads);
+        const float* e_r = d.lv[0].phi_r;
+        const float* e_b = d.lv[0].phi_b;
+        float* rh_r = d.lv[0].beta_r;
+        float* rh_b = d.lv[0].beta_b;
+        float* rl = d.r_lo;
+        double* p_r = d.phi_r;
+        double* p_b = d.phi_b;
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        auto row = [&](int jj, int kk) -> unsigned { return ((unsigned)jj + (unsigned)n * (unsigned)kk) * half; };
+        float vmax = 0.f, emax = 0.f;
+        for (unsigned task = tid; task < (unsigned)rows * pairs; task += nthreads) {
+            const int j = it.c + (int)(task / pairs);
+            if (j >= n) break;                           // later tasks lie further down
+            const unsigned ih = 2 * (task % pairs);
+            const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+            const unsigned r0 = row(j, k), rym = row(jm, k), ryp = row(jp, k), rzm = row(j, km),
+                           rzp = row(j, kp);
+            const unsigned t = r0 + ih;
+#pragma unroll
+            for (int color = 0; color < 2; ++color) {
+                const int q = (j + k + color) & 1;
+                const float* other = color ? e_r : e_b;
+                const float2 em = *reinterpret_cast<const float2*>((color ? e_b : e_r) + t);
+                const float2 cc = *reinterpret_cast<const float2*>(other + t);
+                float xm0, xm1, xp0, xp1;
+                if (q) {
+                    const float e = other[r0 + (ih + 2 == half ? 0u : ih + 2)];
+                    xm0 = cc.x; xp0 = cc.y; xm1 = cc.y; xp1 = e;
+                } else {
+                    const float e = other[r0 + (ih == 0 ? half - 1 : ih - 1)];
+                    xm0 = e; xp0 = cc.x; xm1 = cc.x; xp1 = cc.y;
+                }
+                const float2 ym = *reinterpret_cast<const float2*>(other + rym + ih);
+                const float2 yp = *reinterpret_cast<const float2*>(other + ryp + ih);
+                const float2 zm = *reinterpret_cast<const float2*>(other + rzm + ih);
+                const float2 zp = *reinterpret_cast<const float2*>(other + rzp + ih);
+                float2* rh_p = reinterpret_cast<float2*>((color ? rh_b : rh_r) + t);
+                float2* rl_p = reinterpret_cast<float2*>(rl + (color ? nh : 0u) + t);
+                float2 rh = *rh_p, rlo = *rl_p;
+                const float v0[6] = {xm0, xp0, ym.x, yp.x, zm.x, zp.x};
+                const float v1[6] = {xm1, xp1, ym.y, yp.y, zm.y, zp.y};
+                df_residual_update(v0, em.x, c_hi, c_lo, rh.x, rlo.x);
+                df_residual_update(v1, em.y, c_hi, c_lo, rh.y, rlo.y);
+                *rh_p = rh;
+                *rl_p = rlo;
+                double2* pp = reinterpret_cast<double2*>((color ? p_b : p_r) + t);
+                double2 ph = *pp;
+                ph.x = ph.x + f32_to_f64(em.x);
+                ph.y = ph.y + f32_to_f64(em.y);
+                *pp = ph;
+                vmax = fmaxf(vmax, fmaxf(fabsf(rh.x), fabsf(rh.y)));
+                emax = fmaxf(emax, fmaxf(fabsf(em.x), fabsf(em.y)));
+            }
+        }
+        warp_umax_atomic(absbits(f32_to_f64(vmax)), d.norms + 1);
+        warp_umax_atomic(absbits(f32_to_f64(emax)), d.norms + 3);
+    }
+}
+
 // e = 0 on level 0 for the next inner solve (after e_correct), boxes still
 // iterating whose level 0 is cycled by e_tail
 __global__ void __launch_bounds__(256) e_zero_inner(const Item* __restrict__ items, int nitems,
@@ -1623,6 +1711,10 @@ struct nyxpm_ensemble {
     // rows per task where the coarse level is split, e_prolong4's items elsewhere
     Range r_prolong_quad[nyxpm::kMaxLev];
     Range r_prolong_rest[nyxpm::kMaxLev];
+    // e_correct's items: level-0 plane segments of correct_rows rows for boxes
+    // whose rows hold an even number of compact cells, rows of r_rows_split[0]
+    // for the others
+    Range r_correct_vec, r_correct_rest;
     nyxpm::EDesc* d_desc = nullptr;
     nyxpm::EState* d_state = nullptr;
     nyxpm::EStep* d_step = nullptr;
@@ -1760,6 +1852,20 @@ nyxpm_status rebuild(nyxpm_ctx* c, nyxpm_ensemble* E)
         for (long long t = 0; t < (nr + 7) / 8; ++t) items.push_back(Item{b, (int)t, 0, 0});
     }
     end(E->r_rows_rho);
+    for (int vec = 1; vec >= 0; --vec) {
+        auto& rg = vec ? E->r_correct_vec : E->r_correct_rest;
+        begin(rg);
+        for (int b = 0; b < nbox; ++b) {
+            const EnsSlot& s = E->slots[b];
+            if (!s.used || s.desc.nlev < 2) continue;
+            const int n = s.desc.n;
+            if ((((n >> 1) & 1) == 0) != (vec == 1)) continue;
+            const int step = vec ? correct_rows(n, 32 * R) : R;
+            for (int k = 0; k < n; ++k)
+                for (int j0 = 0; j0 < n; j0 += step) items.push_back(Item{b, 0, k, j0});
+        }
+        end(rg);
+    }
     for (int l = 0; l < kMaxLev; ++l) {
         begin(E->r_rows_split[l]);
         for (int b = 0; b < nbox; ++b) {
@@ -2088,7 +2194,11 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
         } else {
             const float c_hi = (float)(1.0 / 6.0);
             const float c_lo = (float)(1.0 / 6.0 - (double)c_hi);
-            e_correct<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, c_hi, c_lo);
+            const auto& cv = E->r_correct_vec;
+            const auto& cr = E->r_correct_rest;
+            if (cv.cnt) e_correct_v<<<pgrid(E, cv.cnt), rb, 0, s>>>(it + cv.off, cv.cnt, D, S, c_hi, c_lo);
+            if (cr.cnt) e_correct<<<pgrid(E, cr.cnt), rb, 0, s>>>(it + cr.off, cr.cnt, D, S, c_hi, c_lo);
+            c->launches += (cv.cnt ? 1 : 0) + (cr.cnt ? 1 : 0) - 1;
             e_zero_inner<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S,
                                                           c->p.nu1 > 0 ? 0 : 1);
         }

@@ -499,6 +499,7 @@ __global__ void __launch_bounds__(256) e_deposit(const Item* __restrict__ items,
                                                  const EDesc* __restrict__ D, const EState* __restrict__ S)
 {
     constexpr int KX = TX + 1, KY = TY + 1, KZ = TZ + 1, NK = KX * KY * KZ;
+    // corner-major: a warp's consecutive keys (or cells) touch consecutive banks
     __shared__ float part[NK * 8];
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const Item it = items[w];
@@ -511,7 +512,12 @@ __global__ void __launch_bounds__(256) e_deposit(const Item* __restrict__ items,
         __syncthreads();
         for (int kl = threadIdx.x; kl < NK; kl += blockDim.x) {
             const int ki = kl % KX, kj = (kl / KX) % KY, kk = kl / (KX * KY);
-            const long long K = cidx(wrapi(i0 + ki, n), wrapi(j0 + kj, n), wrapi(k0 + kk, n), n);
+            // window coordinates exceed n by less than a tile: wrap by subtraction
+            int wi = i0 + ki, wj = j0 + kj, wk = k0 + kk;
+            while (wi >= n) wi -= n;
+            while (wj >= n) wj -= n;
+            while (wk >= n) wk -= n;
+            const unsigned K = (unsigned)wi + (unsigned)n * ((unsigned)wj + (unsigned)n * (unsigned)wk);
             float s[8];
 #pragma unroll
             for (int c = 0; c < 8; ++c) s[c] = 0.f;
@@ -533,7 +539,7 @@ __global__ void __launch_bounds__(256) e_deposit(const Item* __restrict__ items,
                         for (int cx = 0; cx < 2; ++cx) s[cx + 2 * cy + 4 * cz] += (sx[cx] * sy[cy]) * sz[cz];
             }
 #pragma unroll
-            for (int c = 0; c < 8; ++c) part[kl * 8 + c] = s[c];
+            for (int c = 0; c < 8; ++c) part[c * NK + kl] = s[c];
         }
         __syncthreads();
         const float scale = d.dep_scale;
@@ -549,7 +555,7 @@ __global__ void __launch_bounds__(256) e_deposit(const Item* __restrict__ items,
 #pragma unroll
                     for (int di = 0; di < 2; ++di) {
                         const int kl = (ci + di) + KX * ((cj + dj) + KY * (ck + dk));
-                        acc += part[kl * 8 + (1 - di) + 2 * (1 - dj) + 4 * (1 - dk)];
+                        acc += part[((1 - di) + 2 * (1 - dj) + 4 * (1 - dk)) * NK + kl];
                     }
             d.frho[cidx(i, j, k, n)] = acc * scale;
         }

@@ -662,6 +662,15 @@ __global__ void __launch_bounds__(256) e_make_beta(const Item* __restrict__ item
     }
 }
 
+// rows of level 0 per e_correct_v and e_resid_v item: enough (row, pair) tasks to fill a block
+// of nthreads threads (n / 4 compact pairs per row)
+__host__ __device__ inline int correct_rows(int n, int nthreads)
+{
+    const int pairs = n >> 2;
+    const int r = pairs > 0 ? nthreads / pairs : n;
+    return r < 1 ? 1 : (r > n ? n : r);
+}
+
 template <typename T>
 __device__ __forceinline__ T nbr_sum_split(const T* other, int n, int half, int ih, int j, int k, int q)
 {
@@ -711,6 +720,84 @@ __global__ void __launch_bounds__(256) e_resid(const Item* __restrict__ items, i
                     const unsigned long long u = absbits(r);
                     vmax = u > vmax ? u : vmax;
                 }
+            }
+        }
+        warp_umax_atomic(vmax, d.norms + 1);
+    }
+}
+
+// e_resid for boxes whose level-0 rows hold an even number of compact cells, on
+// e_correct_v's items: one task per compact pair of one row (k_mx_resid2's
+// pattern: paired FP64 loads, the neighbour sum in nbr_sum_split's order), so
+// small boxes fill the block; the same bits as e_resid.
+__global__ void __launch_bounds__(256) e_resid_v(const Item* __restrict__ items, int nitems,
+                                                 const EDesc* __restrict__ D, const EState* __restrict__ S,
+                                                 int low_words)
+{
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;  // uniform across the block
+        const EDesc& d = D[it.box];
+        const int n = d.n, k = it.b;
+        const unsigned half = (unsigned)n >> 1;
+        const unsigned pairs = half >> 1;
+        const unsigned nh = (unsigned)n * (unsigned)n * half;
+        const int rows = correct_rows(n, nthreads);
+        const int km = k == 0 ? n - 1 : k - 1, kp = k == n - 1 ? 0 : k + 1;
+        auto row = [&](int jj, int kk) -> unsigned { return ((unsigned)jj + (unsigned)n * (unsigned)kk) * half; };
+        unsigned long long vmax = 0;
+        for (unsigned task = tid; task < (unsigned)rows * pairs; task += nthreads) {
+            const int j = it.c + (int)(task / pairs);
+            if (j >= n) break;
+            const unsigned ih = 2 * (task % pairs);
+            const int jm = j == 0 ? n - 1 : j - 1, jp = j == n - 1 ? 0 : j + 1;
+            const unsigned r0 = row(j, k);
+            const unsigned t = r0 + ih;
+#pragma unroll
+            for (int color = 0; color < 2; ++color) {
+                const int q = (j + k + color) & 1;
+                const double* other = color ? d.phi_r : d.phi_b;
+                const double* mine = color ? d.phi_b : d.phi_r;
+                const double* beta = color ? d.beta_b : d.beta_r;
+                const double2 c = __ldg(reinterpret_cast<const double2*>(other + t));
+                double xm0, xm1, xp0, xp1;
+                if (q) {   // neighbours ih, ih + 1
+                    const double e = __ldg(other + r0 + (ih + 2 == half ? 0u : ih + 2));
+                    xm0 = c.x; xp0 = c.y; xm1 = c.y; xp1 = e;
+                } else {   // neighbours ih - 1, ih
+                    const double e = __ldg(other + r0 + (ih == 0 ? half - 1 : ih - 1));
+                    xm0 = e; xp0 = c.x; xm1 = c.x; xp1 = c.y;
+                }
+                const double2 ym = __ldg(reinterpret_cast<const double2*>(other + row(jm, k) + ih));
+                const double2 yp = __ldg(reinterpret_cast<const double2*>(other + row(jp, k) + ih));
+                const double2 zm = __ldg(reinterpret_cast<const double2*>(other + row(j, km) + ih));
+                const double2 zp = __ldg(reinterpret_cast<const double2*>(other + row(j, kp) + ih));
+                const double2 b = __ldg(reinterpret_cast<const double2*>(beta + t));
+                const double2 m = __ldg(reinterpret_cast<const double2*>(mine + t));
+                double s0 = xm0 + xp0;
+                s0 = s0 + ym.x;
+                s0 = s0 + yp.x;
+                s0 = s0 + zm.x;
+                s0 = s0 + zp.x;
+                double s1 = xm1 + xp1;
+                s1 = s1 + ym.y;
+                s1 = s1 + yp.y;
+                s1 = s1 + zm.y;
+                s1 = s1 + zp.y;
+                const double r0v = b.x - fma(s0, kSixth, -m.x);
+                const double r1v = b.y - fma(s1, kSixth, -m.y);
+                const float h0 = f64_to_f32_rn(r0v), h1 = f64_to_f32_rn(r1v);
+                reinterpret_cast<float2*>((color ? d.lv[0].beta_b : d.lv[0].beta_r) + t)[0] = make_float2(h0, h1);
+                if (low_words)
+                    reinterpret_cast<float2*>(d.r_lo + (color ? nh : 0u) + t)[0] =
+                        make_float2(f64_to_f32_rn(r0v - f32_to_f64(h0)), f64_to_f32_rn(r1v - f32_to_f64(h1)));
+                reinterpret_cast<float2*>((color ? d.lv[0].phi_b : d.lv[0].phi_r) + t)[0] = make_float2(0.f, 0.f);
+                const unsigned long long u0 = absbits(r0v), u1 = absbits(r1v);
+                vmax = u0 > vmax ? u0 : vmax;
+                vmax = u1 > vmax ? u1 : vmax;
             }
         }
         warp_umax_atomic(vmax, d.norms + 1);
@@ -880,15 +967,6 @@ __global__ void __launch_bounds__(256) e_correct(const Item* __restrict__ items,
     }
 }
 
-// rows of level 0 per e_correct_v item: enough (row, pair) tasks to fill a block
-// of nthreads threads (n / 4 compact pairs per row)
-__host__ __device__ inline int correct_rows(int n, int nthreads)
-{
-    const int pairs = n >> 2;
-    const int r = pairs > 0 ? nthreads / pairs : n;
-    return r < 1 ? 1 : (r > n ? n : r);
-}
-
 // e_correct for boxes whose level-0 rows hold an even number of compact cells,
 // on items {box, 0, plane k, first row j0} of correct_rows(n) rows: one task per
 // compact pair of one row, so small boxes fill the block too.  The same
@@ -1011,6 +1089,40 @@ __global__ void __launch_bounds__(256) e_gsrb_zero(const Item* __restrict__ item
         const long long row = ((long long)j + (long long)n * k) * half;
         for (int ih = threadIdx.x; ih < half; ih += blockDim.x)
             d.lv[0].phi_r[row + ih] = fmaf(0.f, kSixthF, -d.lv[0].beta_r[row + ih]);
+    }
+}
+
+// e_gsrb_zero on e_correct_v's items: the plane segment's red cells are one
+// contiguous range of the level-0 red array, taken four at a time (level-0 rows
+// of a multiple of four compact cells; else one at a time); the same values.
+__global__ void __launch_bounds__(256) e_gsrb_zero_v(const Item* __restrict__ items, int nitems,
+                                                     const EDesc* __restrict__ D,
+                                                     const EState* __restrict__ S)
+{
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const Item it = items[w];
+        const EState st = S[it.box];
+        if (!(st.active && st.solve_active)) continue;
+        const EDesc& d = D[it.box];
+        if (d.tail_l == 0) continue;
+        const int n = d.n, k = it.b;
+        const unsigned half = (unsigned)n >> 1;
+        const int rows = min(correct_rows(n, nthreads), n - it.c);
+        const unsigned begin = ((unsigned)it.c + (unsigned)n * (unsigned)k) * half;
+        const unsigned cnt = (unsigned)rows * half;
+        float* phi = d.lv[0].phi_r + begin;
+        const float* beta = d.lv[0].beta_r + begin;
+        if ((half & 3u) == 0) {
+            for (unsigned q = tid; q < cnt / 4; q += nthreads) {
+                const float4 b = __ldg(reinterpret_cast<const float4*>(beta) + q);
+                reinterpret_cast<float4*>(phi)[q] = make_float4(fmaf(0.f, kSixthF, -b.x), fmaf(0.f, kSixthF, -b.y),
+                                                                fmaf(0.f, kSixthF, -b.z), fmaf(0.f, kSixthF, -b.w));
+            }
+        } else {
+            for (unsigned q = tid; q < cnt; q += nthreads) phi[q] = fmaf(0.f, kSixthF, -beta[q]);
+        }
     }
 }
 
@@ -2096,7 +2208,13 @@ void enqueue_solve_head(nyxpm_ctx* c, nyxpm_ensemble* E)
     const dim3 rb(32, E->tune.smooth_rows);
     const auto& r0 = E->r_rows_split[0];
     e_make_beta<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
-    e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, 1);
+    {
+        const auto& cv = E->r_correct_vec;
+        const auto& cr = E->r_correct_rest;
+        if (cv.cnt) e_resid_v<<<pgrid(E, cv.cnt), rb, 0, s>>>(it + cv.off, cv.cnt, D, S, 1);
+        if (cr.cnt) e_resid<<<pgrid(E, cr.cnt), rb, 0, s>>>(it + cr.off, cr.cnt, D, S, 1);
+        c->launches += (cv.cnt ? 1 : 0) + (cr.cnt ? 1 : 0) - 1;
+    }
     e_flags<<<bb, 128, 0, s>>>(nbox, D, S, c->p.rel_tol, 1);
     ep_end(c, NYXPM_ST_RHS);
     c->launches += 16;
@@ -2123,9 +2241,12 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
         const auto& rr = E->r_smooth_row[l];
         if (zero_start) {
             // the opening red half sweep of an inner solve on level 0
-            const auto& r0 = E->r_rows_split[0];
+            const auto& cv = E->r_correct_vec;
+            const auto& cr = E->r_correct_rest;
             ep_begin(c);
-            e_gsrb_zero<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
+            if (cv.cnt) e_gsrb_zero_v<<<pgrid(E, cv.cnt), rb, 0, s>>>(it + cv.off, cv.cnt, D, S);
+            if (cr.cnt) e_gsrb_zero<<<pgrid(E, cr.cnt), rb, 0, s>>>(it + cr.off, cr.cnt, D, S);
+            c->launches += (cv.cnt ? 1 : 0) + (cr.cnt ? 1 : 0) - 1;
             ep_end(c, NYXPM_ST_SMOOTH);
             c->launches += 1;
             return;
@@ -2196,7 +2317,11 @@ void enqueue_iterations(nyxpm_ctx* c, nyxpm_ensemble* E, int outer, int first)
         e_count_inner<<<bb, 128, 0, s>>>(nbox, S, E->tune.inner_vcycles);
         if (first && o == 0) {
             e_update<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S);
-            e_resid<<<pgrid(E, r0.cnt), rb, 0, s>>>(it + r0.off, r0.cnt, D, S, 1);
+            const auto& cv = E->r_correct_vec;
+            const auto& cr = E->r_correct_rest;
+            if (cv.cnt) e_resid_v<<<pgrid(E, cv.cnt), rb, 0, s>>>(it + cv.off, cv.cnt, D, S, 1);
+            if (cr.cnt) e_resid<<<pgrid(E, cr.cnt), rb, 0, s>>>(it + cr.off, cr.cnt, D, S, 1);
+            c->launches += (cv.cnt ? 1 : 0) + (cr.cnt ? 1 : 0) - 1;
         } else {
             const float c_hi = (float)(1.0 / 6.0);
             const float c_lo = (float)(1.0 / 6.0 - (double)c_hi);

@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(kPT) e_scatter(const Item* __restrict__ items,
     }
 }
 
-__global__ void __launch_bounds__(kPT) e_gather(const Item* __restrict__ items, int nitems,
+__global__ void __launch_bounds__(kPT, 8) e_gather(const Item* __restrict__ items, int nitems,
                                                  const EDesc* __restrict__ D, const EState* __restrict__ S,
                                                  int bucket)
 {

@@ -730,7 +730,7 @@ __global__ void __launch_bounds__(256) e_resid(const Item* __restrict__ items, i
 // e_correct_v's items: one task per compact pair of one row (k_mx_resid2's
 // pattern: paired FP64 loads, the neighbour sum in nbr_sum_split's order), so
 // small boxes fill the block; the same bits as e_resid.
-__global__ void __launch_bounds__(256) e_resid_v(const Item* __restrict__ items, int nitems,
+__global__ void __launch_bounds__(256, 5) e_resid_v(const Item* __restrict__ items, int nitems,
                                                  const EDesc* __restrict__ D, const EState* __restrict__ S,
                                                  int low_words)
 {
@@ -1193,7 +1193,7 @@ __host__ __device__ inline int vec_rows(int n, int nthreads)
 // holds exactly kMarchE planes.
 constexpr int kMarchE = 4;
 
-__global__ void __launch_bounds__(256) e_gsrb4(const Item* __restrict__ items, int nitems,
+__global__ void __launch_bounds__(256, 6) e_gsrb4(const Item* __restrict__ items, int nitems,
                                                const EDesc* __restrict__ D,
                                                const EState* __restrict__ S, int color)
 {
@@ -1401,7 +1401,7 @@ __global__ void __launch_bounds__(256) e_restrict4(const Item* __restrict__ item
 // right-hand side from the 4 red children of each coarse cell, whose residuals
 // are the only ones above round-off (pm_restrict.cuh, as k_restrict_f4_red),
 // summed in (dk, dj) order; half the loads and residual arithmetic.
-__global__ void __launch_bounds__(256) e_restrict4_red(const Item* __restrict__ items, int nitems,
+__global__ void __launch_bounds__(256, 5) e_restrict4_red(const Item* __restrict__ items, int nitems,
                                                        const EDesc* __restrict__ D,
                                                        const EState* __restrict__ S)
 {

@@ -487,6 +487,60 @@ nyxpm_status nyxpm_deposit_noalloc(const double* x, const double* y, const doubl
                                    double mass, int n, double L, double* rho, void* stream,
                                    char* errbuf, size_t errlen);
 
+/* ---- multilevel (AMR) PM without subcycling, FP64 ------------------------------------
+ * Nyx::advance_particles_only with finest_level > 0 and amr.subcycling_mode = None
+ * (Source/TimeStep/Nyx_advance_particles.cpp:9-272) on fixed grids, as the
+ * reference's Exec/ParticleOnlyTest/inputs.mass.nosub runs it (amr.regrid_file).
+ * Level l has n0 * 2^l cells per side (refinement ratio 2); levels 1 .. nlev-1
+ * (nlev <= 4) are lists of boxes given as 6 ints each (lo x y z, hi x y z,
+ * inclusive, in that level's index space), level by level, nbox[l-1] on level l.
+ * A box needs even lo and odd hi (coarsenable), boxes of a level must not
+ * overlap, and each box above level 1 must sit inside the coarser level with
+ * one coarse cell to spare.  A particle belongs to the finest level whose boxes
+ * hold its cell.  The multilevel deposit (AMReX AssignDensity) and the composite
+ * MLMG solve are AMReX's, absent from the reference tree; this library's
+ * definition of both is given in nyx_gb300/csrc/pm_amr.cu. */
+typedef struct nyxpm_amr nyxpm_amr;
+
+nyxpm_status nyxpm_amr_create(nyxpm_ctx* ctx, int n0, double L, int nlev, const int* nbox,
+                              const int* boxes, int64_t np, nyxpm_amr** out);
+nyxpm_status nyxpm_amr_destroy(nyxpm_ctx* ctx, nyxpm_amr* amr);
+/* pos, vel: np x 3; mass: np, or NULL with mass_scalar for equal masses.
+ * mass_offset = sum(m) / L^3 (Gravity::set_mass_offset, Gravity.cpp:975-1030). */
+nyxpm_status nyxpm_amr_upload(nyxpm_ctx* ctx, nyxpm_amr* amr, const double* pos,
+                              const double* vel, const double* mass, double mass_scalar);
+nyxpm_status nyxpm_amr_download(nyxpm_ctx* ctx, nyxpm_amr* amr, double* pos, double* vel);
+/* One step: particle levels, old-time multilevel deposit and solve
+ * (Gravity::multilevel_solve_for_old_phi, Gravity.cpp:572-600 ->
+ * actual_multilevel_solve, :602-779), moveKickDrift on every level, new-time
+ * deposit and solve (multilevel_solve_for_new_phi, :543-570), moveKick on every
+ * level (DarkMatterParticleContainer.cpp:76-247), the periodic shift of
+ * post_timestep (Nyx.cpp:1421-1437).  Both solves start from phi = 0, as the
+ * reference calls them (use_previous_phi_as_guess defaults to 0, Gravity.H:64-69).
+ * NYXPM_INVALID_ARG if a particle moved more than 2 cells of its level. */
+nyxpm_status nyxpm_amr_step(nyxpm_ctx* ctx, nyxpm_amr* amr, double a_old, double a_new,
+                            double dt, nyxpm_step_info* info);
+/* The parts of the step, for callers that drive it themselves:
+ * particle levels and boxes (box -1 on level 0) of the current positions; */
+nyxpm_status nyxpm_amr_assign(nyxpm_ctx* ctx, nyxpm_amr* amr, int* lev, int* box);
+/* multilevel CIC deposit with the levels of the last nyxpm_amr_assign
+ * (Gravity::AddParticlesToRhs, Gravity.cpp:1068-1102); */
+nyxpm_status nyxpm_amr_deposit(nyxpm_ctx* ctx, nyxpm_amr* amr);
+/* composite solve of the deposited density at a, from phi = 0; */
+nyxpm_status nyxpm_amr_solve(nyxpm_ctx* ctx, nyxpm_amr* amr, double a, nyxpm_solve_info* info);
+/* gravity vector of every level (Gravity::get_old_grav_vector / get_new_grav_vector); */
+nyxpm_status nyxpm_amr_grav_vector(nyxpm_ctx* ctx, nyxpm_amr* amr);
+/* kick (and drift when do_move) of every particle with its own level's g. */
+nyxpm_status nyxpm_amr_kick(nyxpm_ctx* ctx, nyxpm_amr* amr, double dt, double a_prev,
+                            double a_cur, int do_move);
+/* A field of level 0 (box -1: n0^3, x fastest) or of one box (its cells, x
+ * fastest); which: NYXPM_AMR_RHO .. NYXPM_AMR_MASS. */
+enum { NYXPM_AMR_RHO = 0, NYXPM_AMR_PHI = 1, NYXPM_AMR_GX = 2, NYXPM_AMR_GY = 3, NYXPM_AMR_GZ = 4,
+       NYXPM_AMR_MASS = 5 };
+nyxpm_status nyxpm_amr_field(nyxpm_ctx* ctx, nyxpm_amr* amr, int which, int box, double* out);
+/* Cells of level 0 (box -1) or of one box; -1 for a bad box. */
+int64_t nyxpm_amr_cells(const nyxpm_amr* amr, int box);
+
 /* ---- measurement ------------------------------------------------------------- */
 
 #define NYXPM_NUM_STAGES 12

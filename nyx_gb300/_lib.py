@@ -42,6 +42,9 @@ EXPORTS = [
     "nyxpm_cosmo_1ppc_particles", "nyxpm_cosmo_ic_factors", "nyxpm_box_init_cosmo_1ppc",
     "nyxpm_multifab_info_read", "nyxpm_multifab_boxes", "nyxpm_multifab_read",
     "nyxpm_multifab_write", "nyxpm_particles_info", "nyxpm_particles_read", "nyxpm_particles_write",
+    "nyxpm_amr_create", "nyxpm_amr_destroy", "nyxpm_amr_upload", "nyxpm_amr_download",
+    "nyxpm_amr_step", "nyxpm_amr_assign", "nyxpm_amr_deposit", "nyxpm_amr_solve",
+    "nyxpm_amr_grav_vector", "nyxpm_amr_kick", "nyxpm_amr_field", "nyxpm_amr_cells",
 ]
 NYXPM_MF_REJECT_NAN = 1
 
@@ -248,5 +251,19 @@ def load(path: str | None = None):
     L.nyxpm_ensemble_step.argtypes = [vp, vp, dp, dp, dp, C.POINTER(EnsembleInfo)]
     L.nyxpm_deposit_noalloc.argtypes = [vp, vp, vp, i64, d, C.c_int, d, vp, vp, C.c_char_p,
                                         C.c_size_t]
+    ip = C.POINTER(C.c_int)
+    L.nyxpm_amr_create.argtypes = [vp, C.c_int, d, C.c_int, ip, ip, i64, C.POINTER(vp)]
+    L.nyxpm_amr_destroy.argtypes = [vp, vp]
+    L.nyxpm_amr_upload.argtypes = [vp, vp, vp, vp, vp, d]
+    L.nyxpm_amr_download.argtypes = [vp, vp, vp, vp]
+    L.nyxpm_amr_step.argtypes = [vp, vp, d, d, d, C.POINTER(StepInfo)]
+    L.nyxpm_amr_assign.argtypes = [vp, vp, vp, vp]
+    L.nyxpm_amr_deposit.argtypes = [vp, vp]
+    L.nyxpm_amr_solve.argtypes = [vp, vp, d, C.POINTER(SolveInfo)]
+    L.nyxpm_amr_grav_vector.argtypes = [vp, vp]
+    L.nyxpm_amr_kick.argtypes = [vp, vp, d, d, d, C.c_int]
+    L.nyxpm_amr_field.argtypes = [vp, vp, C.c_int, C.c_int, vp]
+    L.nyxpm_amr_cells.argtypes = [vp, C.c_int]
+    L.nyxpm_amr_cells.restype = i64
     _lib = L
     return L

@@ -30,6 +30,7 @@ UNITS = {
     "pm_mixed.cu": [],
     "pm_ensemble.cu": [],
     "pm_noalloc.cu": ["--fmad=false"],
+    "pm_amr.cu": ["--fmad=false"],
     "pm_probe.cu": [],
     "pm_io.cpp": [],
     "pm_vismf.cpp": [],

@@ -546,6 +546,10 @@ nyxpm_status mg_solve(Ctx& c, Box& b, nyxpm_solve_info* info);
 nyxpm_status launch_grav_vector(Ctx& c, Box& b);
 nyxpm_status launch_phi_to_natural(Ctx& c, Box& b, double* d_out);
 nyxpm_status launch_phi_from_natural(Ctx& c, Box& b, const double* d_in);
+// one V-cycle of b's hierarchy from a zero guess for the right-hand side beta
+// (smoother units, natural layout), the correction into e (natural layout): the
+// base level's correction solve of the multilevel composite V-cycle
+nyxpm_status mg_vcycle_zero(Ctx& c, Box& b, const double* beta_nat, double* e_nat);
 
 // mixed-precision form
 nyxpm_status mixed_unpack(Ctx& c, Box& b, const double* d_pos, const double* d_vel,

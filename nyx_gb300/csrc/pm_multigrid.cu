@@ -478,6 +478,16 @@ __global__ void k_from_natural(LevelView L, const double* __restrict__ in)
     *lv_ptr<double>(L.phi_r, L.phi_b, n, L.split, i, j, k) = in[cidx(i, j, k, n)];
 }
 
+__global__ void k_beta_from_natural(LevelView L, const double* __restrict__ in)
+{
+    const int n = L.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n || j >= n) return;
+    *lv_ptr<double>(L.beta_r, L.beta_b, n, L.split, i, j, k) = in[cidx(i, j, k, n)];
+}
+
 inline unsigned norm_blocks(Ctx& c, long long cnt)
 {
     long long b = (cnt + kThreads - 1) / kThreads;
@@ -768,6 +778,19 @@ nyxpm_status launch_phi_from_natural(Ctx& c, Box& b, const double* d_in)
     k_from_natural<<<g.grid, g.block, 0, c.stream>>>(view(b.levels[0]), d_in);
     prof_end(c, NYXPM_ST_GATHER, 16.0 * nc);
     return check_launch(c, "phi from natural");
+}
+
+nyxpm_status mg_vcycle_zero(Ctx& c, Box& b, const double* beta_nat, double* e_nat)
+{
+    nyxpm_status st;
+    const long long nc = (long long)b.n * b.n * b.n;
+    const Geo g = geo3(b.n, b.n, b.n);
+    prof_begin(c);
+    k_beta_from_natural<<<g.grid, g.block, 0, c.stream>>>(view(b.levels[0]), beta_nat);
+    prof_end(c, NYXPM_ST_RHS, 16.0 * nc);
+    if ((st = launch_zero_phi(c, b)) != NYXPM_OK) return st;
+    if ((st = vcycle(c, b, 0)) != NYXPM_OK) return st;
+    return launch_phi_to_natural(c, b, e_nat);
 }
 
 }  // namespace nyxpm

@@ -24,8 +24,9 @@ _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 def build(force: bool = False) -> str:
     """Compile the oracle shared library with its Makefile (g++ + OpenMP)."""
+    srcs = [os.path.join(_HERE, f) for f in ("pm_oracle.cpp", "pm_amr_oracle.cpp")]
     if force or not os.path.exists(_LIB_PATH) or (
-        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "pm_oracle.cpp"))
+        os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(f) for f in srcs)
     ):
         subprocess.run(["make", "-s", "-C", _HERE, "liboracle_pm.so"], check=True)
     return _LIB_PATH
@@ -42,6 +43,17 @@ class _Cfg(C.Structure):
         ("nu1", C.c_int),
         ("nu2", C.c_int),
         ("reuse_field", C.c_int),
+    ]
+
+
+class _AmrCfg(C.Structure):
+    _fields_ = [
+        ("mass_offset", C.c_double),
+        ("ggrav", C.c_double),
+        ("rel_tol", C.c_double),
+        ("max_cycles", C.c_int),
+        ("nu1", C.c_int),
+        ("nu2", C.c_int),
     ]
 
 
@@ -86,6 +98,28 @@ def lib():
         L.orc_step.argtypes = [C.POINTER(_Cfg), C.c_long, _dp, _dp, _dp, _dp, _dp, _dp, C.c_void_p,
                                C.c_double, C.c_void_p, C.c_double, C.c_double, C.c_double, _dp, _dp,
                                C.c_void_p, _ip]
+        L.orc_amr_create.restype = C.c_void_p
+        L.orc_amr_create.argtypes = [C.c_int, C.c_double, C.c_int, _ip, _ip, C.c_char_p, C.c_int]
+        L.orc_amr_destroy.argtypes = [C.c_void_p]
+        L.orc_amr_assign.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, _ip, _ip]
+        L.orc_amr_deposit.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, C.c_void_p, C.c_double,
+                                      _ip]
+        L.orc_amr_solve.restype = C.c_int
+        L.orc_amr_solve.argtypes = [C.c_void_p, C.POINTER(_AmrCfg), C.c_double,
+                                    C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double)]
+        L.orc_amr_grav.argtypes = [C.c_void_p]
+        L.orc_amr_move.restype = C.c_int
+        L.orc_amr_move.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip,
+                                   C.c_double, C.c_double, C.c_double, C.c_int]
+        L.orc_amr_step.restype = C.c_int
+        L.orc_amr_step.argtypes = [C.c_void_p, C.POINTER(_AmrCfg), C.c_long, _dp, _dp, _dp, _dp,
+                                   _dp, _dp, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                   C.c_double, _ip, _ip, _ip]
+        L.orc_amr_field.restype = C.c_int
+        L.orc_amr_field.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp]
+        L.orc_amr_total_mass.restype = C.c_double
+        L.orc_amr_total_mass.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -288,3 +322,85 @@ class PMOracle:
         if st == 1:
             raise ValueError("grid size not supported by the multigrid hierarchy")
         return st
+
+
+class AmrOracle:
+    """The multilevel (AMR) FP64 PM step without subcycling
+    (Nyx_advance_particles.cpp:9-272 with finest_level > 0 and
+    amr.subcycling_mode = None; Gravity::actual_multilevel_solve,
+    Gravity.cpp:602-779).  ``boxes`` lists, for each level above 0, its boxes as
+    ((lo_x, lo_y, lo_z), (hi_x, hi_y, hi_z)) in that level's index space."""
+
+    FIELDS = {"rho": 0, "phi": 1, "gx": 2, "gy": 3, "gz": 4, "mass": 5}
+
+    def __init__(self, n0, L, boxes, particles: Particles, rel_tol=1e-10, max_cycles=100, nu1=2,
+                 nu2=2):
+        self.n0, self.L, self.p = n0, L, particles
+        self.nlev = len(boxes) + 1
+        self.boxes = [[(tuple(lo), tuple(hi)) for lo, hi in lv] for lv in boxes]
+        nbox = np.array([len(lv) for lv in boxes] or [0], dtype=np.int32)
+        flat = np.array([c for lv in boxes for lo, hi in lv for c in (*lo, *hi)] or [0],
+                        dtype=np.int32)
+        err = C.create_string_buffer(256)
+        self.h = lib().orc_amr_create(n0, L, self.nlev, nbox, flat, err, 256)
+        if not self.h:
+            raise ValueError(err.value.decode())
+        self.cfg = _AmrCfg(mass_offset=particles.total_mass() / (L * L * L),
+                           ggrav=-4.0 * np.pi * gconst(), rel_tol=rel_tol, max_cycles=max_cycles,
+                           nu1=nu1, nu2=nu2)
+        self.cycles = np.zeros(2, dtype=np.int32)
+        self.lev = np.zeros(particles.np, dtype=np.int32)
+        self.box = np.zeros(particles.np, dtype=np.int32)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_amr_destroy(self.h)
+            self.h = None
+
+    def box_shape(self, b):
+        flat = [bx for lv in self.boxes for bx in lv]
+        lo, hi = flat[b]
+        return tuple(hi[d] - lo[d] + 1 for d in (2, 1, 0))
+
+    def assign(self):
+        p = self.p
+        lib().orc_amr_assign(self.h, p.np, p.x, p.y, p.z, self.lev, self.box)
+        return self.lev.copy(), self.box.copy()
+
+    def deposit(self):
+        p = self.p
+        lib().orc_amr_deposit(self.h, p.np, p.x, p.y, p.z, _ptr(p.m), p.mscalar, self.lev)
+
+    def solve(self, a):
+        nc, r0, r = C.c_int(0), C.c_double(0), C.c_double(0)
+        st = lib().orc_amr_solve(self.h, C.byref(self.cfg), a, C.byref(nc), C.byref(r0),
+                                 C.byref(r))
+        return st, nc.value, r0.value, r.value
+
+    def grav(self):
+        lib().orc_amr_grav(self.h)
+
+    def move(self, dt, a_prev, a_cur, do_move):
+        p = self.p
+        return lib().orc_amr_move(self.h, p.np, p.x, p.y, p.z, p.vx, p.vy, p.vz, self.lev,
+                                  self.box, dt, a_prev, a_cur, do_move)
+
+    def step(self, a_old, a_new, dt):
+        p = self.p
+        st = lib().orc_amr_step(self.h, C.byref(self.cfg), p.np, p.x, p.y, p.z, p.vx, p.vy, p.vz,
+                                _ptr(p.m), p.mscalar, a_old, a_new, dt, self.cycles, self.lev,
+                                self.box)
+        if st == 1:
+            raise ValueError("grid size not supported by the multigrid hierarchy")
+        return st
+
+    def field(self, name, box=-1):
+        """A field on level 0 (box -1, (n0, n0, n0) z-major) or on one box."""
+        shape = (self.n0,) * 3 if box < 0 else self.box_shape(box)
+        out = np.zeros(int(np.prod(shape)))
+        if lib().orc_amr_field(self.h, self.FIELDS[name], box, out):
+            raise ValueError("bad field or box")
+        return out.reshape(shape)
+
+    def total_mass(self):
+        return lib().orc_amr_total_mass(self.h)

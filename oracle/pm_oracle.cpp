@@ -589,6 +589,21 @@ int orc_mg_solve(int n, double L, const double* rhs, double* phi, double rel_tol
     return status;
 }
 
+// One V(nu1,nu2) cycle of the periodic hierarchy from a zero initial guess for
+// the right-hand side beta given in smoother units (n^3, natural order); the
+// result in e.  The base level's correction solve of the multilevel (AMR)
+// composite V-cycle.  Returns 1 on bad n.
+int orc_mg_vcycle_zero(int n, double L, const double* beta, double* e, int nu1, int nu2)
+{
+    Hierarchy H;
+    if (!build_hierarchy(n, L, H)) return 1;
+    const long nc = (long)n * n * n;
+    std::memcpy(H.lv[0].beta.data(), beta, sizeof(double) * nc);
+    vcycle(H, 0, nu1, nu2);
+    std::memcpy(e, H.lv[0].phi.data(), sizeof(double) * nc);
+    return 0;
+}
+
 // Cell-centred gravity vector g = average of the two face gradients
 // (Gravity.cpp:817-850): g_d(c) = 0.5*((phi_c - phi_{c-e_d})*dxi + (phi_{c+e_d} - phi_c)*dxi),
 // the second product fused with the sum.  g holds the three components one

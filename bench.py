@@ -74,11 +74,18 @@ def parse():
     ap.add_argument("--fraction", type=float, default=1.0,
                     help="with --quick: particles per cell (profiling the grid kernels of a "
                          "larger grid within a few GB)")
+    ap.add_argument("--no-amr", action="store_true",
+                    help="skip the multilevel (AMR) step object")
+    ap.add_argument("--amr-only", action="store_true",
+                    help="only the multilevel (AMR) step object, as its own JSON line")
+    ap.add_argument("--amr-n0", type=int, default=128,
+                    help="base grid of the multilevel workload (each level holds n0^3 cells)")
     ap.add_argument("--accuracy-n", type=int, default=512)
     ap.add_argument("--accuracy-steps", type=str, default="1,10,50")
     a = ap.parse_args()
     if a.quick:
         a.no_cpu_baseline = a.no_e2e = a.no_reuse = a.no_ensemble = a.no_serving = a.no_c3 = True
+        a.no_amr = True
     else:
         a.no_reuse = False
         if a.precision != "fp64" or a.fraction != 1.0:
@@ -574,6 +581,103 @@ def run_c3_form(ctx, stream, n=512, steps=NSTEPS_CFG):
     }
 
 
+def amr_workload(n0, seed=7):
+    """A zoom-shaped multilevel workload: n0^3 Zel'dovich particles (P(k)~k^-2,
+    rms displacement 0.2 cell at a = 0.02) plus n0^3/8 particles in a Gaussian
+    cluster (sigma 0.1, central overdensity about 8) at the centre with
+    velocities of the same spread (clipped at 2.5 sigma), equal masses; level 1
+    refines [0.25, 0.75)^3 and level 2 [0.375, 0.625)^3 (one box each, n0^3
+    cells each)."""
+    import numpy as np
+    from nyx_gb300.ics import zeldovich_ics
+    ic = zeldovich_ics(n0, 1.0, -2.0, seed, A_START, rms_disp_cells=0.2)
+    rng = np.random.default_rng(seed)
+    nc = n0 ** 3 // 8
+    sig = float(np.std(ic.vel))
+    pos = np.concatenate([ic.pos, (0.5 + rng.normal(0, 0.1, (nc, 3))) % 1.0])
+    vel = np.concatenate([ic.vel, np.clip(rng.normal(0, sig, (nc, 3)), -2.5 * sig, 2.5 * sig)])
+    boxes = [[((n0 // 2,) * 3, (3 * n0 // 2 - 1,) * 3)], [((3 * n0 // 2,) * 3, (5 * n0 // 2 - 1,) * 3)]]
+    return pos, vel, float(ic.mass), boxes
+
+
+AMR_A_END, AMR_STEPS = 0.04, 40
+
+
+def run_amr_form(ctx, stream, n0=128, warmup=2, timed=10, cpu_n0=32, cpu_seconds=20.0):
+    """The multilevel step without subcycling (nyxpm_amr_step) on amr_workload(n0):
+    warmup + timed steps of a 0.02 -> 0.1 in 20 equal-da steps, each timed by a
+    CUDA event pair on the library stream; the CPU oracle of the same step on the
+    same-shaped workload at n0 = cpu_n0 as a bounded sample."""
+    import numpy as np
+    import torch
+    from nyx_gb300.amr import AmrHierarchy
+    from oracle import oracle as O
+    pos, vel, mass, boxes = amr_workload(n0)
+    npart = len(pos)
+    H = AmrHierarchy(ctx, n0, 1.0, boxes, npart)
+    H.upload(pos, vel, mass)
+    lev, _ = H.assign()
+    per_level = np.bincount(lev, minlength=3).tolist()
+    sched = ctx.step_schedule(A_START, AMR_A_END, AMR_STEPS)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ms, vc, launches = [], [], 0
+    for k, (a0, a1, dt) in enumerate(sched[:warmup + timed]):
+        l0 = ctx.launch_count()
+        e[0].record(stream)
+        info = H.step(a0, a1, dt)
+        e[1].record(stream)
+        e[1].synchronize()
+        if k >= warmup:
+            ms.append(e[0].elapsed_time(e[1]))
+            vc.append((info["old_solve"]["vcycles"], info["new_solve"]["vcycles"]))
+            launches += ctx.launch_count() - l0
+    H.close()
+    # the oracle (one thread) on the same-shaped workload at cpu_n0
+    cpos, cvel, cmass, cboxes = amr_workload(cpu_n0)
+    p = O.Particles(cpos, cvel, cmass)
+    A = O.AmrOracle(cpu_n0, 1.0, cboxes, p)
+    done, secs = 0, 0.0
+    for a0, a1, dt in sched:
+        t0 = time.perf_counter()
+        A.step(a0, a1, dt)
+        secs += time.perf_counter() - t0
+        done += 1
+        if secs >= cpu_seconds:
+            break
+    tot = sum(ms)
+    cells = [n0 ** 3, n0 ** 3, n0 ** 3]
+    return {
+        "workload": f"{n0}^3 Zel'dovich particles (P(k)~k^-2) + {n0 ** 3 // 8} in a central Gaussian "
+                    f"cluster, base grid {n0}^3, level 1 [0.25,0.75)^3 and level 2 [0.375,0.625)^3 "
+                    f"({n0}^3 cells each, ratio 2), a {A_START}->{AMR_A_END} in {AMR_STEPS} equal-da "
+                    f"steps, no subcycling, two multilevel solves per step from phi = 0, rel tol 1e-10",
+        "n_particles": npart, "particles_per_level": per_level, "cells_per_level": cells,
+        "steps": timed, "warmup": warmup,
+        "value": npart * timed / (tot / 1e3), "unit": UNIT, "ms_per_step": tot / timed,
+        "vcycles_per_solve_mean": float(np.mean(vc)), "launches_per_step": launches / timed,
+        "dtype": "f64",
+        "cpu_baseline": {"value": len(cpos) * done / secs, "unit": UNIT, "cores": 1, "kind": "port",
+                         "seconds": secs,
+                         "sample": f"{done} steps of the same-shaped workload at base grid {cpu_n0}^3 "
+                                   f"({len(cpos)} particles), the multilevel C++ oracle on one thread"},
+        "note": "each step timed by its own CUDA event pair on the library stream; the solves read "
+                "their residual norm on the host after every composite V-cycle",
+    }
+
+
+def run_amr_only(args):
+    import torch
+    from nyx_gb300 import _lib
+    _lib.load()
+    from nyx_gb300.pm import Context
+    ctx = Context(device=0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    out = run_amr_form(ctx, stream, n0=args.amr_n0)
+    ctx.close()
+    print(json.dumps({"amr": out}), flush=True)
+    return 0
+
+
 def run_reference(args):
     ws, rank, _ = dist_init("gloo")
     if rank != 0:
@@ -929,6 +1033,8 @@ def run_ours(args):
         box.close()
         box = None
         line["c3"] = run_c3_form(ctx, stream)
+    if rank == 0 and ws == 1 and not args.no_amr:
+        line["amr"] = run_amr_form(ctx, stream, n0=args.amr_n0)
 
     # ---- CPU baseline: the oracle on a bounded sample, rank 0 at N=1 ----
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -1058,6 +1164,8 @@ def main():
         return run_accuracy(args)
     if args.ensemble_only:
         return run_ensemble_only(args)
+    if args.amr_only:
+        return run_amr_only(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

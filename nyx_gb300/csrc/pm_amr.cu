@@ -108,6 +108,12 @@ struct Range {
 
 inline unsigned nblk(long long n) { return (unsigned)std::max<long long>(1, (n + kT - 1) / kT); }
 
+// grid-stride reductions: at most 4 blocks per SM
+inline unsigned norm_grid(const Ctx& c, long long n)
+{
+    return (unsigned)std::min<long long>(nblk(n), (long long)std::max(1, c.sm_count) * 4);
+}
+
 __host__ __device__ inline long long box_idx(const ABox& B, int i, int j, int k)
 {
     return B.off + (long long)(i - B.lo[0] + kGW) +
@@ -467,26 +473,77 @@ __device__ __forceinline__ double nbr_fine(const double* __restrict__ u, long lo
     return s;
 }
 
-__global__ void k_amr_residf(long long nc, const ACell* __restrict__ cells, const ABox* __restrict__ boxes,
-                             const double* __restrict__ u, const double* __restrict__ rhs, double* out)
+// Fine cells are numbered box by box (x fastest), boxes in level order;
+// pref[b] is the number of fine cells in the boxes before b (every box has an
+// even number of cells per row, so each colour holds half of each row and
+// pref[b] / 2 numbers the cells of one colour).  find_box: the box of fine cell
+// (or colour cell) g among the boxes [b0, b0 + nb).
+__device__ __forceinline__ int find_box(const long long* __restrict__ pref, int b0, int nb, long long g, int half)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nc) return;
-    const ACell c = cells[t];
-    const ABox& B = boxes[c.box];
-    const long long sx = B.d[0], sxy = (long long)B.d[0] * B.d[1];
-    out[c.q] = rhs[c.q] - fma(nbr_fine(u, c.q, sx, sxy), kSixth, -u[c.q]);
+    int lo = b0, hi = b0 + nb - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const long long pm = half ? (pref[mid] >> 1) : pref[mid];
+        if (pm <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
-__global__ void k_amr_gsrbf(long long nc, const ACell* __restrict__ cells, const ABox* __restrict__ boxes,
-                            double* e, const double* __restrict__ R)
+// composite index of fine cell g (numbered from the first cell of box b0)
+__device__ __forceinline__ long long fine_cell(const ABox* __restrict__ boxes, const long long* __restrict__ pref,
+                                              int b0, int nb, long long t, int& b)
+{
+    const long long g = pref[b0] + t;
+    b = find_box(pref, b0, nb, g, 0);
+    const ABox& B = boxes[b];
+    const long long r = g - pref[b];
+    const int nx = B.hi[0] - B.lo[0] + 1, ny = B.hi[1] - B.lo[1] + 1;
+    const long long row = r / nx;
+    const int u = (int)(r - row * nx);
+    const int j = (int)(row % ny), k = (int)(row / ny);
+    return box_idx(B, B.lo[0] + u, B.lo[1] + j, B.lo[2] + k);
+}
+
+// composite index of the t-th cell of colour col (numbered from box b0)
+__device__ __forceinline__ long long fine_color_cell(const ABox* __restrict__ boxes, const long long* __restrict__ pref,
+                                                    int b0, int nb, long long t, int col, int& b)
+{
+    const long long g = (pref[b0] >> 1) + t;
+    b = find_box(pref, b0, nb, g, 1);
+    const ABox& B = boxes[b];
+    const long long r = g - (pref[b] >> 1);
+    const int hx = (B.hi[0] - B.lo[0] + 1) >> 1, ny = B.hi[1] - B.lo[1] + 1;
+    const long long row = r / hx;
+    const int tp = (int)(r - row * hx);
+    const int j = B.lo[1] + (int)(row % ny), k = B.lo[2] + (int)(row / ny);
+    const int i = B.lo[0] + 2 * tp + ((col - B.lo[0] - j - k) & 1);
+    return box_idx(B, i, j, k);
+}
+
+// out = rhs - (s/6 - u) on the n fine cells from box b0
+__global__ void k_amr_residf(long long n, int b0, int nb, const long long* __restrict__ pref,
+                             const ABox* __restrict__ boxes, const double* __restrict__ u,
+                             const double* __restrict__ rhs, double* out)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nc) return;
-    const ACell c = cells[t];
-    const ABox& B = boxes[c.box];
-    const long long sx = B.d[0], sxy = (long long)B.d[0] * B.d[1];
-    e[c.q] = fma(nbr_fine(e, c.q, sx, sxy), kSixth, -R[c.q]);
+    if (t >= n) return;
+    int b;
+    const long long q = fine_cell(boxes, pref, b0, nb, t, b);
+    const long long sx = boxes[b].d[0], sxy = (long long)boxes[b].d[0] * boxes[b].d[1];
+    out[q] = rhs[q] - fma(nbr_fine(u, q, sx, sxy), kSixth, -u[q]);
+}
+
+// one colour of a Gauss-Seidel sweep on the n colour cells from box b0
+__global__ void k_amr_gsrbf(long long n, int b0, int nb, const long long* __restrict__ pref,
+                            const ABox* __restrict__ boxes, int col, double* e, const double* __restrict__ R)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int b;
+    const long long q = fine_color_cell(boxes, pref, b0, nb, t, col, b);
+    const long long sx = boxes[b].d[0], sxy = (long long)boxes[b].d[0] * boxes[b].d[1];
+    e[q] = fma(nbr_fine(e, q, sx, sxy), kSixth, -R[q]);
 }
 
 // R(C) -= ((sum_k (u(f_k) - u(g_k))) / 2 - (u(N) - u(C))) / 6 at each coarse/fine face of C
@@ -540,27 +597,52 @@ __global__ void k_amr_add(long long n, double* phi, const double* __restrict__ e
 }
 
 // max |f| * inv_scale over the uncovered cells into out (as the bits of a
-// non-negative double)
+// non-negative double): a block maximum, then one atomic per block
+__device__ __forceinline__ void block_umax(unsigned long long v, unsigned long long* out)
+{
+    __shared__ unsigned long long part[kT / 32];
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, off);
+        v = o > v ? o : v;
+    }
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = part[w] > v ? part[w] : v;
+        if (v != 0ULL) atomicMax(out, v);
+    }
+}
+
+// (the maximum is taken over the bit patterns: equal to the maximum of the
+// non-negative values, and a NaN, whose bits are above every number's, wins)
+__device__ __forceinline__ unsigned long long umax_bits(unsigned long long v, double x)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    return u > v ? u : v;
+}
+
 __global__ void k_amr_absmax0(long long n3, const double* __restrict__ f, const unsigned char* __restrict__ cov,
                               double inv_scale, unsigned long long* out)
 {
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0.0;
-    if (q < n3 && !cov[q]) v = fabs(f[q]) * inv_scale;
-    warp_umax_atomic((unsigned long long)__double_as_longlong(v), out);
+    unsigned long long v = 0ULL;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n3; q += (long long)gridDim.x * blockDim.x)
+        if (!cov[q]) v = umax_bits(v, fabs(f[q]) * inv_scale);
+    block_umax(v, out);
 }
 
-__global__ void k_amr_absmaxf(long long nc, const ACell* __restrict__ cells, const ABox* __restrict__ boxes,
-                              const double* __restrict__ f, const unsigned char* __restrict__ cov,
-                              const double* __restrict__ inv_scale, unsigned long long* out)
+__global__ void k_amr_absmaxf(long long n, int b0, int nb, const long long* __restrict__ pref,
+                              const ABox* __restrict__ boxes, const double* __restrict__ f,
+                              const unsigned char* __restrict__ cov, const double* __restrict__ inv_scale,
+                              unsigned long long* out)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0.0;
-    if (t < nc) {
-        const ACell c = cells[t];
-        if (!cov[c.q]) v = fabs(f[c.q]) * inv_scale[boxes[c.box].lev];
+    unsigned long long v = 0ULL;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int b;
+        const long long q = fine_cell(boxes, pref, b0, nb, t, b);
+        if (!cov[q]) v = umax_bits(v, fabs(f[q]) * inv_scale[boxes[b].lev]);
     }
-    warp_umax_atomic((unsigned long long)__double_as_longlong(v), out);
+    block_umax(v, out);
 }
 
 // the single-level cell-centred gravity vector on level 0 / on fine cells
@@ -623,14 +705,13 @@ struct nyxpm_amr {
     BoxTab tab{};                       // device pointer to the box table
     long long ntot = 0;
     // per level: ranges in the device lists
-    Range cells[kMaxLevels], color[kMaxLevels][2], ghost1[kMaxLevels], ghost23[kMaxLevels], rrec[kMaxLevels],
-        frec[kMaxLevels];
+    Range cells[kMaxLevels], ghost1[kMaxLevels], ghost23[kMaxLevels], rrec[kMaxLevels], frec[kMaxLevels];
     Range fine_cells, all_ghost1, all_ghost23, all_frec;
     double scale[kMaxLevels], inv_scale[kMaxLevels], hcube[kMaxLevels], dxi[kMaxLevels];
     // device lists
     ABox* d_boxes = nullptr;
     ACell* d_cells = nullptr;      // every fine cell, level by level
-    ACell* d_color = nullptr;      // the same split by colour, [level][colour] ranges
+    long long* d_pref = nullptr;   // fine cells in the boxes before box b (b = 0 .. nboxes)
     APar* d_par = nullptr;         // aligned with d_cells
     AGhost* d_ghost = nullptr;
     AEnt* d_ent = nullptr;
@@ -745,7 +826,8 @@ nyxpm_status build_lists(nyxpm_ctx* c, nyxpm_amr* a)
     nyxpm_amr& A = *a;
     Builder Bd(A);
     const int n0 = A.n0;
-    std::vector<ACell> cells, color;
+    std::vector<ACell> cells;
+    std::vector<long long> pref(1, 0);
     std::vector<APar> par;
     std::vector<AGhost> ghost;
     std::vector<AEnt> ent;
@@ -774,14 +856,9 @@ nyxpm_status build_lists(nyxpm_ctx* c, nyxpm_amr* a)
                         }
                         par.push_back(P);
                     }
+            pref.push_back((long long)cells.size());
         }
         A.cells[l].count = (long long)cells.size() - A.cells[l].first;
-        for (int col = 0; col < 2; ++col) {
-            A.color[l][col].first = (long long)color.size();
-            for (long long t = A.cells[l].first; t < A.cells[l].first + A.cells[l].count; ++t)
-                if (((cells[t].i + cells[t].j + cells[t].k) & 1) == col) color.push_back(cells[t]);
-            A.color[l][col].count = (long long)color.size() - A.color[l][col].first;
-        }
     }
     A.fine_cells = Range{0, (long long)cells.size()};
     // covered flags
@@ -871,7 +948,7 @@ nyxpm_status build_lists(nyxpm_ctx* c, nyxpm_amr* a)
     A.all_frec = Range{0, (long long)frec.size()};
     nyxpm_status st;
     if ((st = upload_vec(c, a, &A.d_cells, cells)) != NYXPM_OK) return st;
-    if ((st = upload_vec(c, a, &A.d_color, color)) != NYXPM_OK) return st;
+    if ((st = upload_vec(c, a, &A.d_pref, pref)) != NYXPM_OK) return st;
     if ((st = upload_vec(c, a, &A.d_par, par)) != NYXPM_OK) return st;
     if ((st = upload_vec(c, a, &A.d_ghost, ghost)) != NYXPM_OK) return st;
     if ((st = upload_vec(c, a, &A.d_ent, ent)) != NYXPM_OK) return st;
@@ -945,8 +1022,8 @@ nyxpm_status comp_resid(Ctx& c, nyxpm_amr& A, int slot)
     prof_end(c, NYXPM_ST_NORM, 24.0 * n3);
     if (A.fine_cells.count) {
         prof_begin(c);
-        k_amr_residf<<<nblk(A.fine_cells.count), kT, 0, c.stream>>>(A.fine_cells.count, A.d_cells, A.d_boxes,
-                                                                     A.phi, A.beta, A.R);
+        k_amr_residf<<<nblk(A.fine_cells.count), kT, 0, c.stream>>>(A.fine_cells.count, 0, (int)A.boxes.size(),
+                                                                     A.d_pref, A.d_boxes, A.phi, A.beta, A.R);
         prof_end(c, NYXPM_ST_NORM, 48.0 * A.fine_cells.count);
     }
     if (A.all_frec.count) {
@@ -957,12 +1034,13 @@ nyxpm_status comp_resid(Ctx& c, nyxpm_amr& A, int slot)
     }
     cudaMemsetAsync(A.norms + slot, 0, sizeof(unsigned long long), c.stream);
     prof_begin(c);
-    k_amr_absmax0<<<nblk(n3), kT, 0, c.stream>>>(n3, A.R, A.d_cov, A.inv_scale[0], A.norms + slot);
+    k_amr_absmax0<<<norm_grid(c, n3), kT, 0, c.stream>>>(n3, A.R, A.d_cov, A.inv_scale[0], A.norms + slot);
     prof_end(c, NYXPM_ST_NORM, 9.0 * n3);
     if (A.fine_cells.count) {
         prof_begin(c);
-        k_amr_absmaxf<<<nblk(A.fine_cells.count), kT, 0, c.stream>>>(A.fine_cells.count, A.d_cells, A.d_boxes, A.R,
-                                                                      A.d_cov, A.d_level + 8, A.norms + slot);
+        k_amr_absmaxf<<<norm_grid(c, A.fine_cells.count), kT, 0, c.stream>>>(
+            A.fine_cells.count, 0, (int)A.boxes.size(), A.d_pref, A.d_boxes, A.R, A.d_cov, A.d_level + 8,
+            A.norms + slot);
         prof_end(c, NYXPM_ST_NORM, 33.0 * A.fine_cells.count);
     }
     return check_launch(c, "composite residual");
@@ -973,10 +1051,11 @@ nyxpm_status smooth_level(Ctx& c, nyxpm_amr& A, int l)
     nyxpm_status st;
     for (int col = 0; col < 2; ++col) {
         if ((st = ghost_fill(c, A, A.e, A.ghost1[l])) != NYXPM_OK) return st;
-        const Range& r = A.color[l][col];
+        const long long half = A.cells[l].count / 2;
         prof_begin(c);
-        k_amr_gsrbf<<<nblk(r.count), kT, 0, c.stream>>>(r.count, A.d_color + r.first, A.d_boxes, A.e, A.R);
-        prof_end(c, NYXPM_ST_SMOOTH, 48.0 * r.count, 1);
+        k_amr_gsrbf<<<nblk(half), kT, 0, c.stream>>>(half, A.tab.first[l], A.tab.count[l], A.d_pref, A.d_boxes, col,
+                                                     A.e, A.R);
+        prof_end(c, NYXPM_ST_SMOOTH, 24.0 * half, 1);
     }
     return check_launch(c, "fine smoother");
 }
@@ -993,7 +1072,8 @@ nyxpm_status vcycle(nyxpm_ctx* cx, nyxpm_amr& A)
         if ((st = ghost_fill(c, A, A.e, A.ghost1[l])) != NYXPM_OK) return st;
         const Range& r = A.cells[l];
         prof_begin(c);
-        k_amr_residf<<<nblk(r.count), kT, 0, c.stream>>>(r.count, A.d_cells + r.first, A.d_boxes, A.e, A.R, A.T);
+        k_amr_residf<<<nblk(r.count), kT, 0, c.stream>>>(r.count, A.tab.first[l], A.tab.count[l], A.d_pref,
+                                                         A.d_boxes, A.e, A.R, A.T);
         prof_end(c, NYXPM_ST_RESTRICT, 48.0 * r.count);
         prof_begin(c);
         k_amr_sum8<<<nblk(A.rrec[l].count), kT, 0, c.stream>>>(A.rrec[l].count, A.d_rrec + A.rrec[l].first, A.T,
@@ -1068,12 +1148,13 @@ nyxpm_status solve(nyxpm_ctx* cx, nyxpm_amr& A, double a, nyxpm_solve_info* info
     cudaMemsetAsync(A.phi, 0, sizeof(double) * A.ntot, c.stream);
     cudaMemsetAsync(A.norms, 0, sizeof(unsigned long long), c.stream);
     prof_begin(c);
-    k_amr_absmax0<<<nblk(n3), kT, 0, c.stream>>>(n3, A.beta, A.d_cov, A.inv_scale[0], A.norms);
+    k_amr_absmax0<<<norm_grid(c, n3), kT, 0, c.stream>>>(n3, A.beta, A.d_cov, A.inv_scale[0], A.norms);
     prof_end(c, NYXPM_ST_NORM, 9.0 * n3);
     if (A.fine_cells.count) {
         prof_begin(c);
-        k_amr_absmaxf<<<nblk(A.fine_cells.count), kT, 0, c.stream>>>(A.fine_cells.count, A.d_cells, A.d_boxes,
-                                                                      A.beta, A.d_cov, A.d_level + 8, A.norms);
+        k_amr_absmaxf<<<norm_grid(c, A.fine_cells.count), kT, 0, c.stream>>>(
+            A.fine_cells.count, 0, (int)A.boxes.size(), A.d_pref, A.d_boxes, A.beta, A.d_cov, A.d_level + 8,
+            A.norms);
         prof_end(c, NYXPM_ST_NORM, 33.0 * A.fine_cells.count);
     }
     if ((st = comp_resid(c, A, 1)) != NYXPM_OK) return st;

@@ -57,6 +57,7 @@ struct ABox {
     int lev;
     int lo[3], hi[3];
     int d[3];          // padded extents
+    int pbox;          // the coarser box holding this box's parents (-1: level 0; -2: several)
     long long off;     // first padded cell in the composite layout
 };
 
@@ -507,7 +508,7 @@ __device__ __forceinline__ long long fine_cell(const ABox* __restrict__ boxes, c
 
 // composite index of the t-th cell of colour col (numbered from box b0)
 __device__ __forceinline__ long long fine_color_cell(const ABox* __restrict__ boxes, const long long* __restrict__ pref,
-                                                    int b0, int nb, long long t, int col, int& b)
+                                                    int b0, int nb, long long t, int col, int& b, int* ijk = nullptr)
 {
     const long long g = (pref[b0] >> 1) + t;
     b = find_box(pref, b0, nb, g, 1);
@@ -518,6 +519,11 @@ __device__ __forceinline__ long long fine_color_cell(const ABox* __restrict__ bo
     const int tp = (int)(r - row * hx);
     const int j = B.lo[1] + (int)(row % ny), k = B.lo[2] + (int)(row / ny);
     const int i = B.lo[0] + 2 * tp + ((col - B.lo[0] - j - k) & 1);
+    if (ijk) {
+        ijk[0] = i;
+        ijk[1] = j;
+        ijk[2] = k;
+    }
     return box_idx(B, i, j, k);
 }
 
@@ -588,6 +594,38 @@ __global__ void k_amr_prolong(long long nc, const ACell* __restrict__ cells, con
                 s = fma(kAmrProlongW[u + 2 * a + 4 * b], e[src], s);
             }
     e[c.q] = e[c.q] + s;
+}
+
+// the same on the black cells only (the red ones are overwritten by the red half
+// sweep that follows), for levels whose boxes each have their parents in one
+// coarser box (or on level 0)
+__global__ void k_amr_prolong_black(long long n, int b0, int nb, const long long* __restrict__ pref,
+                                    const ABox* __restrict__ boxes, int n0, double* e)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int b, c[3];
+    const long long q = fine_color_cell(boxes, pref, b0, nb, t, 1, b, c);
+    const ABox& B = boxes[b];
+    const int I = c[0] >> 1, J = c[1] >> 1, K = c[2] >> 1;
+    const int di = (c[0] & 1) ? 1 : -1, dj = (c[1] & 1) ? 1 : -1, dk = (c[2] & 1) ? 1 : -1;
+    long long pc = 0, sx = 0, sxy = 0;
+    if (B.pbox >= 0) {
+        const ABox& P = boxes[B.pbox];
+        pc = box_idx(P, I, J, K);
+        sx = P.d[0];
+        sxy = (long long)P.d[0] * P.d[1];
+    }
+    double s = 0.0;
+    for (int bz = 0; bz < 2; ++bz)
+        for (int a = 0; a < 2; ++a)
+            for (int u = 0; u < 2; ++u) {
+                const long long src = B.pbox < 0
+                    ? cidx(wrapi(I + u * di, n0), wrapi(J + a * dj, n0), wrapi(K + bz * dk, n0), n0)
+                    : pc + (long long)(u * di) + (long long)(a * dj) * sx + (long long)(bz * dk) * sxy;
+                s = fma(kAmrProlongW[u + 2 * a + 4 * bz], e[src], s);
+            }
+    e[q] = e[q] + s;
 }
 
 __global__ void k_amr_add(long long n, double* phi, const double* __restrict__ e)
@@ -705,7 +743,11 @@ struct nyxpm_amr {
     BoxTab tab{};                       // device pointer to the box table
     long long ntot = 0;
     // per level: ranges in the device lists
-    Range cells[kMaxLevels], ghost1[kMaxLevels], ghost23[kMaxLevels], rrec[kMaxLevels], frec[kMaxLevels];
+    // ghost1[l]: the ring-1 ghosts of level l, its copies of same-level cells first
+    // (ghost1_same[l]), then the ones interpolated from coarser levels
+    Range cells[kMaxLevels], ghost1[kMaxLevels], ghost1_same[kMaxLevels], ghost23[kMaxLevels], rrec[kMaxLevels],
+        frec[kMaxLevels];
+    int prolong_black_ok[kMaxLevels] = {0, 0, 0, 0};
     Range fine_cells, all_ghost1, all_ghost23, all_frec;
     double scale[kMaxLevels], inv_scale[kMaxLevels], hcube[kMaxLevels], dxi[kMaxLevels];
     // device lists
@@ -873,6 +915,7 @@ nyxpm_status build_lists(nyxpm_ctx* c, nyxpm_amr* a)
         for (int l = 1; l < A.nlev; ++l) {
             Range& R = pass == 0 ? A.ghost1[l] : A.ghost23[l];
             R.first = (long long)ghost.size();
+            std::vector<AGhost> same, interp;
             for (int b = A.tab.first[l]; b < A.tab.first[l] + A.tab.count[l]; ++b) {
                 const ABox& B = A.boxes[b];
                 for (int k = B.lo[2] - kGW; k <= B.hi[2] + kGW; ++k)
@@ -884,9 +927,12 @@ nyxpm_status build_lists(nyxpm_ctx* c, nyxpm_amr* a)
                             AGhost G{box_idx(B, i, j, k), (int)ent.size(), 0};
                             Bd.gen(l, i, j, k, 1.0, ent);
                             G.count = (int)ent.size() - G.first;
-                            ghost.push_back(G);
+                            (Bd.vidx(l, i, j, k) >= 0 ? same : interp).push_back(G);
                         }
             }
+            if (pass == 0) A.ghost1_same[l] = Range{(long long)ghost.size(), (long long)same.size()};
+            ghost.insert(ghost.end(), same.begin(), same.end());
+            ghost.insert(ghost.end(), interp.begin(), interp.end());
             R.count = (long long)ghost.size() - R.first;
         }
     A.all_ghost1 = Range{0, A.nlev > 1 ? A.ghost1[A.nlev - 1].first + A.ghost1[A.nlev - 1].count : 0};
@@ -1046,17 +1092,24 @@ nyxpm_status comp_resid(Ctx& c, nyxpm_amr& A, int slot)
     return check_launch(c, "composite residual");
 }
 
-nyxpm_status smooth_level(Ctx& c, nyxpm_amr& A, int l)
+// nsweeps red-black sweeps of level l's correction.  A ring-1 ghost is either a
+// copy of a same-level cell or an interpolation of coarser levels, and those do
+// not change while level l smooths: the interpolated ghosts are filled once, at
+// the start (fill_interp; not on the way down, where every coarser correction
+// and so every such ghost is still zero), the copies before each colour.
+nyxpm_status smooth_level(Ctx& c, nyxpm_amr& A, int l, int nsweeps, int fill_interp)
 {
     nyxpm_status st;
-    for (int col = 0; col < 2; ++col) {
-        if ((st = ghost_fill(c, A, A.e, A.ghost1[l])) != NYXPM_OK) return st;
-        const long long half = A.cells[l].count / 2;
-        prof_begin(c);
-        k_amr_gsrbf<<<nblk(half), kT, 0, c.stream>>>(half, A.tab.first[l], A.tab.count[l], A.d_pref, A.d_boxes, col,
-                                                     A.e, A.R);
-        prof_end(c, NYXPM_ST_SMOOTH, 24.0 * half, 1);
-    }
+    const long long half = A.cells[l].count / 2;
+    for (int s = 0; s < nsweeps; ++s)
+        for (int col = 0; col < 2; ++col) {
+            const bool all = fill_interp && s == 0 && col == 0;
+            if ((st = ghost_fill(c, A, A.e, all ? A.ghost1[l] : A.ghost1_same[l])) != NYXPM_OK) return st;
+            prof_begin(c);
+            k_amr_gsrbf<<<nblk(half), kT, 0, c.stream>>>(half, A.tab.first[l], A.tab.count[l], A.d_pref, A.d_boxes,
+                                                         col, A.e, A.R);
+            prof_end(c, NYXPM_ST_SMOOTH, 24.0 * half, 1);
+        }
     return check_launch(c, "fine smoother");
 }
 
@@ -1067,9 +1120,8 @@ nyxpm_status vcycle(nyxpm_ctx* cx, nyxpm_amr& A)
     const int nu1 = c.p.nu1, nu2 = c.p.nu2;
     cudaMemsetAsync(A.e, 0, sizeof(double) * A.ntot, c.stream);
     for (int l = A.nlev - 1; l >= 1; --l) {
-        for (int s = 0; s < nu1; ++s)
-            if ((st = smooth_level(c, A, l)) != NYXPM_OK) return st;
-        if ((st = ghost_fill(c, A, A.e, A.ghost1[l])) != NYXPM_OK) return st;
+        if ((st = smooth_level(c, A, l, nu1, 0)) != NYXPM_OK) return st;
+        if ((st = ghost_fill(c, A, A.e, A.ghost1_same[l])) != NYXPM_OK) return st;
         const Range& r = A.cells[l];
         prof_begin(c);
         k_amr_residf<<<nblk(r.count), kT, 0, c.stream>>>(r.count, A.tab.first[l], A.tab.count[l], A.d_pref,
@@ -1089,15 +1141,22 @@ nyxpm_status vcycle(nyxpm_ctx* cx, nyxpm_amr& A)
     }
     if ((st = mg_vcycle_zero(c, *A.mg, A.R, A.e)) != NYXPM_OK) return st;
     for (int l = 1; l < A.nlev; ++l) {
-        if (l - 1 >= 1 && (st = ghost_fill(c, A, A.e, A.ghost1[l - 1])) != NYXPM_OK) return st;
+        // the parents' neighbours are valid coarser cells: in the parent's box or
+        // in the copies of its ring
+        if (l - 1 >= 1 && (st = ghost_fill(c, A, A.e, A.ghost1_same[l - 1])) != NYXPM_OK) return st;
         const Range& r = A.cells[l];
         prof_begin(c);
-        k_amr_prolong<<<nblk(r.count), kT, 0, c.stream>>>(r.count, A.d_cells + r.first, A.d_par + r.first, A.n0,
-                                                          A.e);
-        prof_end(c, NYXPM_ST_PROLONG, 96.0 * r.count);
+        if (nu2 > 0 && A.prolong_black_ok[l]) {
+            k_amr_prolong_black<<<nblk(r.count / 2), kT, 0, c.stream>>>(r.count / 2, A.tab.first[l], A.tab.count[l],
+                                                                       A.d_pref, A.d_boxes, A.n0, A.e);
+            prof_end(c, NYXPM_ST_PROLONG, 48.0 * r.count);
+        } else {
+            k_amr_prolong<<<nblk(r.count), kT, 0, c.stream>>>(r.count, A.d_cells + r.first, A.d_par + r.first, A.n0,
+                                                              A.e);
+            prof_end(c, NYXPM_ST_PROLONG, 96.0 * r.count);
+        }
         if ((st = check_launch(c, "composite prolongation")) != NYXPM_OK) return st;
-        for (int s = 0; s < nu2; ++s)
-            if ((st = smooth_level(c, A, l)) != NYXPM_OK) return st;
+        if ((st = smooth_level(c, A, l, nu2, 1)) != NYXPM_OK) return st;
     }
     prof_begin(c);
     k_amr_add<<<nblk(A.ntot), kT, 0, c.stream>>>(A.ntot, A.phi, A.e);
@@ -1334,6 +1393,21 @@ nyxpm_status nyxpm_amr_create(nyxpm_ctx* c, int n0, double L, int nlev, const in
                             return cleanup(afail(c, NYXPM_INVALID_ARG,
                                                  "a box is not nested in the coarser level with one cell to spare"));
         }
+    }
+    for (ABox& B : a->boxes) {
+        B.pbox = -1;
+        if (B.lev < 2) continue;
+        B.pbox = -2;
+        for (int o = a->tab.first[B.lev - 1]; o < a->tab.first[B.lev - 1] + a->tab.count[B.lev - 1]; ++o) {
+            const ABox& P = a->boxes[o];
+            if (box_has(P, B.lo[0] / 2, B.lo[1] / 2, B.lo[2] / 2) && box_has(P, B.hi[0] / 2, B.hi[1] / 2, B.hi[2] / 2))
+                B.pbox = o;
+        }
+    }
+    for (int l = 1; l < nlev; ++l) {
+        a->prolong_black_ok[l] = 1;
+        for (int b = a->tab.first[l]; b < a->tab.first[l] + a->tab.count[l]; ++b)
+            if (a->boxes[b].pbox == -2) a->prolong_black_ok[l] = 0;
     }
     for (int l = 0; l < nlev; ++l) {
         const double h = L / (n0 << l);

@@ -92,10 +92,15 @@ def test_parts_of_the_step_match_the_oracle(ctx):
     assert _rel(vg - vel, p.vel() - vel) <= 1e-8
 
 
-@pytest.mark.parametrize("seed", [41, 42])
-def test_steps_match_the_oracle(ctx, seed):
+# two level-1 boxes sharing a face (their ghosts copy each other's cells) and a
+# level-2 box whose parents lie in both (the prolongation's general path)
+TOUCHING = [[((8, 8, 8), (15, 23, 23)), ((16, 8, 8), (23, 23, 23))], [((28, 20, 20), (35, 27, 27))]]
+
+
+@pytest.mark.parametrize("seed, layout", [(41, "reference"), (42, "reference"), (43, "touching")])
+def test_steps_match_the_oracle(ctx, seed, layout):
     n0, L = 16, 1.0
-    boxes = reference_boxes()
+    boxes = reference_boxes() if layout == "reference" else TOUCHING
     ic = zeldovich_ics(n0, L, -2.0, seed, 0.05, rms_disp_cells=0.5)
     H = AmrHierarchy(ctx, n0, L, boxes, len(ic.pos))
     H.upload(ic.pos, ic.vel, ic.mass)

@@ -605,8 +605,9 @@ AMR_A_END, AMR_STEPS = 0.04, 40
 
 def run_amr_form(ctx, stream, n0=128, warmup=2, timed=10, cpu_n0=32, cpu_seconds=20.0):
     """The multilevel step without subcycling (nyxpm_amr_step) on amr_workload(n0):
-    warmup + timed steps of a 0.02 -> 0.1 in 20 equal-da steps, each timed by a
-    CUDA event pair on the library stream; the CPU oracle of the same step on the
+    warmup + timed steps of a 0.02 -> 0.04 in 40 equal-da steps, each timed by a
+    CUDA event pair on the library stream, then one profiled step for the
+    smoothers' FP64 roofline; the CPU oracle of the same step on the
     same-shaped workload at n0 = cpu_n0 as a bounded sample."""
     import numpy as np
     import torch
@@ -631,6 +632,26 @@ def run_amr_form(ctx, stream, n0=128, warmup=2, timed=10, cpu_n0=32, cpu_seconds
             ms.append(e[0].elapsed_time(e[1]))
             vc.append((info["old_solve"]["vcycles"], info["new_solve"]["vcycles"]))
             launches += ctx.launch_count() - l0
+    # one more step with per-launch events: the red-black half sweeps of every
+    # level (k_amr_gsrbf on the fine levels, k_gsrb on level 0's hierarchy) against
+    # the FP64 rates of this GPU, as the headline's roofline does
+    ctx.set_profiling(True)
+    ctx.profile(reset=True)
+    H.step(*sched[warmup + timed])
+    prof = ctx.profile(reset=True)
+    ctx.set_profiling(False)
+    fs = prof["fine_smooth"]
+    stage_ms = sum(v["ms"] for v in prof["stages"].values())
+    fp64_peak, fp64_add = ctx.measure_fp64_peak()
+    updates = fs["bytes"] / 24.0
+    ops = 6.0 * updates / (fs["ms"] * 1e-3) / 1e12
+    peak_ops = 6.0 / (5.0 / fp64_add + 1.0 / (fp64_peak / 2.0))
+    roofline = {"bound": "fp64", "kernel": "red-black half sweeps of every level (k_amr_gsrbf, level 0's k_gsrb)",
+                "achieved": round(ops, 4), "peak": round(peak_ops, 4), "frac": round(ops / peak_ops, 4),
+                "unit": "T FP64 op/s (an add or an FMA is one op; 6 per updated cell)",
+                "peak_source": "measured: nyxpm_measure_fp64_peak on this GPU, weighted 5 adds : 1 FMA",
+                "launches": fs["launches"], "ms": round(fs["ms"], 3),
+                "share_of_step": round(fs["ms"] / stage_ms, 3) if stage_ms > 0 else None}
     H.close()
     # the oracle (one thread) on the same-shaped workload at cpu_n0
     cpos, cvel, cmass, cboxes = amr_workload(cpu_n0)
@@ -655,7 +676,7 @@ def run_amr_form(ctx, stream, n0=128, warmup=2, timed=10, cpu_n0=32, cpu_seconds
         "steps": timed, "warmup": warmup,
         "value": npart * timed / (tot / 1e3), "unit": UNIT, "ms_per_step": tot / timed,
         "vcycles_per_solve_mean": float(np.mean(vc)), "launches_per_step": launches / timed,
-        "dtype": "f64",
+        "dtype": "f64", "roofline": roofline,
         "cpu_baseline": {"value": len(cpos) * done / secs, "unit": UNIT, "cores": 1, "kind": "port",
                          "seconds": secs,
                          "sample": f"{done} steps of the same-shaped workload at base grid {cpu_n0}^3 "

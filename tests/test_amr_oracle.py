@@ -72,6 +72,43 @@ def test_full_domain_level_equals_single_level_at_twice_the_resolution():
     assert A.cycles[0] == S.cycles[0]
 
 
+def test_two_full_domain_levels_equal_single_level_at_four_times_the_resolution():
+    n0, L = 8, 1.0
+    ic = zeldovich_ics(4 * n0, L, -2.0, 17, 0.05, rms_disp_cells=0.3)
+    a0, a1, dt = _cfl_step(ic.vel, L / (4 * n0))
+    pa = O.Particles(ic.pos, ic.vel, ic.mass)
+    ps = O.Particles(ic.pos, ic.vel, ic.mass)
+    A = O.AmrOracle(n0, L, [[((0, 0, 0), (2 * n0 - 1,) * 3)], [((0, 0, 0), (4 * n0 - 1,) * 3)]], pa)
+    assert A.step(a0, a1, dt) == 0
+    assert np.all(A.lev == 2)
+    S = O.PMOracle(4 * n0, L, ps)
+    S.step(a0, a1, dt)
+    xa, va = pa.by_id()
+    xs, vs = ps.by_id()
+    assert _rel(xa, xs) < 1e-14
+    assert _rel(va - ic.vel, vs - ic.vel) < 1e-8
+
+
+THREE = [[((8, 8, 8), (23, 23, 23))], [((20, 20, 20), (43, 43, 43))], [((44, 44, 44), (83, 83, 83))]]
+
+
+def test_three_refined_levels_conserve_mass_and_step():
+    n0, L = 16, 1.0
+    rng = np.random.default_rng(3)
+    ic = zeldovich_ics(n0, L, -2.0, 44, 0.05, rms_disp_cells=0.5)
+    pos = np.concatenate([ic.pos, (0.5 + rng.normal(0, 0.05, (3000, 3))) % 1.0])
+    vel = np.concatenate([ic.vel, np.zeros((3000, 3))])
+    p = O.Particles(pos, vel, float(ic.mass))
+    A = O.AmrOracle(n0, L, THREE, p)
+    lev, _ = A.assign()
+    assert set(np.unique(lev)) == {0, 1, 2, 3}
+    A.deposit()
+    assert abs(A.total_mass() - float(ic.mass) * len(pos)) <= 1e-13 * float(ic.mass) * len(pos)
+    a0, a1, dt = _cfl_step(vel, L / (8 * n0))
+    assert A.step(a0, a1, dt) == 0
+    assert A.cycles[0] < 20 and A.cycles[1] < 20
+
+
 def test_one_level_equals_single_level():
     n0, L = 16, 1.0
     ic = zeldovich_ics(n0, L, -2.0, 12, 0.05, rms_disp_cells=0.3)

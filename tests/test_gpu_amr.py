@@ -97,16 +97,26 @@ def test_parts_of_the_step_match_the_oracle(ctx):
 TOUCHING = [[((8, 8, 8), (15, 23, 23)), ((16, 8, 8), (23, 23, 23))], [((28, 20, 20), (35, 27, 27))]]
 
 
-@pytest.mark.parametrize("seed, layout", [(41, "reference"), (42, "reference"), (43, "touching")])
+# three refined levels (the most the library takes), nested about the centre
+THREE = [[((8, 8, 8), (23, 23, 23))], [((20, 20, 20), (43, 43, 43))], [((44, 44, 44), (83, 83, 83))]]
+
+
+@pytest.mark.parametrize("seed, layout", [(41, "reference"), (42, "reference"), (43, "touching"),
+                                          (44, "three")])
 def test_steps_match_the_oracle(ctx, seed, layout):
     n0, L = 16, 1.0
-    boxes = reference_boxes() if layout == "reference" else TOUCHING
+    boxes = {"reference": reference_boxes(), "touching": TOUCHING, "three": THREE}[layout]
     ic = zeldovich_ics(n0, L, -2.0, seed, 0.05, rms_disp_cells=0.5)
-    H = AmrHierarchy(ctx, n0, L, boxes, len(ic.pos))
-    H.upload(ic.pos, ic.vel, ic.mass)
-    p = O.Particles(ic.pos, ic.vel, ic.mass)
+    pos, vel = ic.pos, ic.vel
+    if layout == "three":
+        rng = np.random.default_rng(3)
+        pos = np.concatenate([pos, (0.5 + rng.normal(0, 0.05, (3000, 3))) % 1.0])
+        vel = np.concatenate([vel, np.zeros((3000, 3))])
+    H = AmrHierarchy(ctx, n0, L, boxes, len(pos))
+    H.upload(pos, vel, ic.mass)
+    p = O.Particles(pos, vel, ic.mass)
     A = O.AmrOracle(n0, L, boxes, p)
-    a0, a1, dt = _cfl_step(ctx, ic.vel, L / (4 * n0))
+    a0, a1, dt = _cfl_step(ctx, vel, L / (2 ** len(boxes) * n0))
     for _ in range(3):
         v_before = p.vel().copy()
         info = H.step(a0, a1, dt)
@@ -134,6 +144,24 @@ def test_reference_particle_test(ctx):
     xg, vg = H.download()
     assert _rel(xg, p.pos()) <= 1e-13
     assert _rel(vg - vel, p.vel() - vel) <= 1e-8
+
+
+def test_two_full_domain_levels_equal_single_level_box(ctx):
+    n0, L = 8, 1.0
+    ic = zeldovich_ics(4 * n0, L, -2.0, 17, 0.05, rms_disp_cells=0.3)
+    H = AmrHierarchy(ctx, n0, L, [[((0, 0, 0), (2 * n0 - 1,) * 3)], [((0, 0, 0), (4 * n0 - 1,) * 3)]],
+                     len(ic.pos))
+    H.upload(ic.pos, ic.vel, ic.mass)
+    B = Box(ctx, 4 * n0, L, len(ic.pos))
+    B.upload(ic.pos, ic.vel, ic.mass)
+    a0, a1, dt = _cfl_step(ctx, ic.vel, L / (4 * n0))
+    H.step(a0, a1, dt)
+    B.step(a0, a1, dt)
+    xa, va = H.download()
+    xb, vb = B.download()
+    assert _rel(xa, xb) <= 1e-14
+    assert _rel(va - ic.vel, vb - ic.vel) <= 1e-8
+    B.close()
 
 
 def test_full_domain_level_equals_single_level_box(ctx):

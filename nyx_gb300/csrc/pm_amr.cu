@@ -498,12 +498,14 @@ __device__ __forceinline__ long long fine_cell(const ABox* __restrict__ boxes, c
     const long long g = pref[b0] + t;
     b = find_box(pref, b0, nb, g, 0);
     const ABox& B = boxes[b];
-    const long long r = g - pref[b];
-    const int nx = B.hi[0] - B.lo[0] + 1, ny = B.hi[1] - B.lo[1] + 1;
-    const long long row = r / nx;
+    // a box holds fewer than 2^31 cells: 32-bit index arithmetic
+    const unsigned r = (unsigned)(g - pref[b]);
+    const unsigned nx = (unsigned)(B.hi[0] - B.lo[0] + 1), ny = (unsigned)(B.hi[1] - B.lo[1] + 1);
+    const unsigned row = r / nx;
     const int u = (int)(r - row * nx);
-    const int j = (int)(row % ny), k = (int)(row / ny);
-    return box_idx(B, B.lo[0] + u, B.lo[1] + j, B.lo[2] + k);
+    const unsigned k = row / ny;
+    const int j = (int)(row - k * ny);
+    return box_idx(B, B.lo[0] + u, B.lo[1] + j, B.lo[2] + (int)k);
 }
 
 // composite index of the t-th cell of colour col (numbered from box b0)
@@ -513,11 +515,12 @@ __device__ __forceinline__ long long fine_color_cell(const ABox* __restrict__ bo
     const long long g = (pref[b0] >> 1) + t;
     b = find_box(pref, b0, nb, g, 1);
     const ABox& B = boxes[b];
-    const long long r = g - (pref[b] >> 1);
-    const int hx = (B.hi[0] - B.lo[0] + 1) >> 1, ny = B.hi[1] - B.lo[1] + 1;
-    const long long row = r / hx;
+    const unsigned r = (unsigned)(g - (pref[b] >> 1));
+    const unsigned hx = (unsigned)(B.hi[0] - B.lo[0] + 1) >> 1, ny = (unsigned)(B.hi[1] - B.lo[1] + 1);
+    const unsigned row = r / hx;
     const int tp = (int)(r - row * hx);
-    const int j = B.lo[1] + (int)(row % ny), k = B.lo[2] + (int)(row / ny);
+    const unsigned kk = row / ny;
+    const int j = B.lo[1] + (int)(row - kk * ny), k = B.lo[2] + (int)kk;
     const int i = B.lo[0] + 2 * tp + ((col - B.lo[0] - j - k) & 1);
     if (ijk) {
         ijk[0] = i;
@@ -1370,6 +1373,8 @@ nyxpm_status nyxpm_amr_create(nyxpm_ctx* c, int n0, double L, int nlev, const in
                                          "box outside its level, empty, or not aligned to the refinement ratio"));
                 B.d[d] = B.hi[d] - B.lo[d] + 1 + 2 * kGW;
             }
+            if ((long long)B.d[0] * B.d[1] * B.d[2] >= (1LL << 31))
+                return cleanup(afail(c, NYXPM_INVALID_ARG, "a box of 2^31 cells or more"));
             for (int o = a->tab.first[l]; o < (int)a->boxes.size(); ++o) {
                 const ABox& O = a->boxes[o];
                 bool sep = false;

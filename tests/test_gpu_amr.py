@@ -181,6 +181,23 @@ def test_full_domain_level_equals_single_level_box(ctx):
     B.close()
 
 
+def test_one_level_equals_single_level_box(ctx):
+    n0, L = 16, 1.0
+    ic = zeldovich_ics(n0, L, -2.0, 12, 0.05, rms_disp_cells=0.3)
+    H = AmrHierarchy(ctx, n0, L, [], len(ic.pos))
+    H.upload(ic.pos, ic.vel, ic.mass)
+    B = Box(ctx, n0, L, len(ic.pos))
+    B.upload(ic.pos, ic.vel, ic.mass)
+    a0, a1, dt = _cfl_step(ctx, ic.vel, L / n0)
+    H.step(a0, a1, dt)
+    B.step(a0, a1, dt)
+    xa, va = H.download()
+    xb, vb = B.download()
+    assert _rel(xa, xb) <= 1e-14
+    assert _rel(va - ic.vel, vb - ic.vel) <= 1e-8
+    B.close()
+
+
 @pytest.mark.parametrize("boxes", [
     [[((1, 0, 0), (8, 7, 7))]],
     [[((0, 0, 0), (7, 7, 7)), ((6, 6, 6), (9, 9, 9))]],

@@ -335,7 +335,10 @@ bool build(Amr& A, int n0, double L, int nlev, const int* nbox, const int* boxes
 
 void ghost_fill(Amr& A, std::vector<double>& f, const std::vector<Ghost>& gl)
 {
-    for (const Ghost& gh : gl) {
+    // sources are valid cells, destinations ghost cells: the ghosts are independent
+#pragma omp parallel for schedule(static)
+    for (long t = 0; t < (long)gl.size(); ++t) {
+        const Ghost& gh = gl[t];
         double v = 0.0;
         for (int t = 0; t < gh.count; ++t) v = std::fma(A.ent[gh.first + t].w, f[A.ent[gh.first + t].src], v);
         f[gh.dst] = v;
@@ -355,7 +358,9 @@ void ghost_fill_all(Amr& A, std::vector<double>& f, int rings3)
 // the covered cells of level l-1 take the average of their 8 children
 void avg_down(Amr& A, std::vector<double>& f, int l)
 {
-    for (const RRec& r : A.rrec[l]) {
+#pragma omp parallel for schedule(static)
+    for (long t = 0; t < (long)A.rrec[l].size(); ++t) {
+        const RRec& r = A.rrec[l][t];
         double s = 0.0;
         for (int dk = 0; dk < 2; ++dk)
             for (int dj = 0; dj < 2; ++dj)
@@ -395,6 +400,7 @@ void resid_level(Amr& A, const std::vector<double>& u, const std::vector<double>
 {
     if (l == 0) {
         const int n = A.n0;
+#pragma omp parallel for schedule(static)
         for (int k = 0; k < n; ++k)
             for (int j = 0; j < n; ++j)
                 for (int i = 0; i < n; ++i) {
@@ -403,13 +409,18 @@ void resid_level(Amr& A, const std::vector<double>& u, const std::vector<double>
                 }
         return;
     }
-    for (const Cell& c : A.cells[l]) out[c.q] = rhs[c.q] - std::fma(nbrf(A, u, c), kSixth, -u[c.q]);
+    const std::vector<Cell>& cl = A.cells[l];
+#pragma omp parallel for schedule(static)
+    for (long t = 0; t < (long)cl.size(); ++t)
+        out[cl[t].q] = rhs[cl[t].q] - std::fma(nbrf(A, u, cl[t]), kSixth, -u[cl[t].q]);
 }
 
 // refluxing at the faces between the uncovered cells of level l-1 and level l
 void reflux(Amr& A, const std::vector<double>& u, std::vector<double>& R, int l)
 {
-    for (const FRec& r : A.frec[l]) {
+#pragma omp parallel for schedule(static)
+    for (long t = 0; t < (long)A.frec[l].size(); ++t) {
+        const FRec& r = A.frec[l][t];
         double v = R[r.C];
         for (const Face& f : r.faces) {
             double s = u[f.f[0]] - u[f.g[0]];
@@ -427,11 +438,14 @@ double level_absmax(const Amr& A, const std::vector<double>& f, int l)
     double mx = 0.0;
     if (l == 0) {
         const long nc = (long)A.n0 * A.n0 * A.n0;
+#pragma omp parallel for schedule(static) reduction(max : mx)
         for (long q = 0; q < nc; ++q)
             if (!A.cov[q]) mx = std::max(mx, std::fabs(f[q]));
     } else {
-        for (const Cell& c : A.cells[l])
-            if (!A.cov[c.q]) mx = std::max(mx, std::fabs(f[c.q]));
+        const std::vector<Cell>& cl = A.cells[l];
+#pragma omp parallel for schedule(static) reduction(max : mx)
+        for (long t = 0; t < (long)cl.size(); ++t)
+            if (!A.cov[cl[t].q]) mx = std::max(mx, std::fabs(f[cl[t].q]));
     }
     return mx;
 }
@@ -458,13 +472,18 @@ void gsrb_level(Amr& A, int l)
 {
     for (int col = 0; col < 2; ++col) {
         ghost_fill_level(A, A.e, l);
-        for (const Cell& c : A.color[col][l]) A.e[c.q] = std::fma(nbrf(A, A.e, c), kSixth, -A.R[c.q]);
+        const std::vector<Cell>& cl = A.color[col][l];
+#pragma omp parallel for schedule(static)
+        for (long t = 0; t < (long)cl.size(); ++t)
+            A.e[cl[t].q] = std::fma(nbrf(A, A.e, cl[t]), kSixth, -A.R[cl[t].q]);
     }
 }
 
 void prolong_level(Amr& A, int l)
 {
-    for (const Cell& c : A.cells[l]) {
+#pragma omp parallel for schedule(static)
+    for (long ci = 0; ci < (long)A.cells[l].size(); ++ci) {
+        const Cell& c = A.cells[l][ci];
         const int I = c.i >> 1, J = c.j >> 1, K = c.k >> 1;
         const int Is[2] = {I, (c.i & 1) ? I + 1 : I - 1};
         const int Js[2] = {J, (c.j & 1) ? J + 1 : J - 1};
@@ -485,7 +504,9 @@ int vcycle(Amr& A, int nu1, int nu2)
         for (int s = 0; s < nu1; ++s) gsrb_level(A, l);
         ghost_fill_level(A, A.e, l);
         resid_level(A, A.e, A.R, A.T, l);
-        for (const RRec& r : A.rrec[l]) {
+#pragma omp parallel for schedule(static)
+        for (long t = 0; t < (long)A.rrec[l].size(); ++t) {
+            const RRec& r = A.rrec[l][t];
             double s = 0.0;
             for (int dk = 0; dk < 2; ++dk)
                 for (int dj = 0; dj < 2; ++dj)
@@ -503,6 +524,7 @@ int vcycle(Amr& A, int nu1, int nu2)
         prolong_level(A, l);
         for (int s = 0; s < nu2; ++s) gsrb_level(A, l);
     }
+#pragma omp parallel for schedule(static)
     for (long q = 0; q < A.ntot; ++q) A.phi[q] = A.phi[q] + A.e[q];
     return 0;
 }

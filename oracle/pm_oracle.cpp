@@ -595,10 +595,20 @@ int orc_mg_solve(int n, double L, const double* rhs, double* phi, double rel_tol
 // composite V-cycle.  Returns 1 on bad n.
 int orc_mg_vcycle_zero(int n, double L, const double* beta, double* e, int nu1, int nu2)
 {
-    Hierarchy H;
-    if (!build_hierarchy(n, L, H)) return 1;
+    // the hierarchy of the last (n, L), kept between calls (one V-cycle per call)
+    static Hierarchy H;
+    static int Hn = 0;
+    static double HL = 0.0;
+    if (Hn != n || HL != L) {
+        H = Hierarchy();
+        Hn = 0;
+        if (!build_hierarchy(n, L, H)) return 1;
+        Hn = n;
+        HL = L;
+    }
     const long nc = (long)n * n * n;
     std::memcpy(H.lv[0].beta.data(), beta, sizeof(double) * nc);
+    std::fill(H.lv[0].phi.begin(), H.lv[0].phi.end(), 0.0);
     vcycle(H, 0, nu1, nu2);
     std::memcpy(e, H.lv[0].phi.data(), sizeof(double) * nc);
     return 0;

@@ -8,8 +8,15 @@
 // field from a raw float64 file (3 n^3 values, component-major, x fastest) by
 // nyxpm_set_grav_vector, one moveKickDrift, then the AsciiFile out.
 //
+// A third mode takes multilevel steps without subcycling on fixed grids, as
+// Nyx::advance_particles_only at level 0 would through the shim: the boxes of
+// levels 1 .. nlev-1 on the command line (6 ints each, in each level's own index
+// space), steps at constant a with a given dt, then the AsciiFile out.
+//
 // usage: pm_driver <in.ascii> <n> <L> <a0> <steps> <out.ascii>
 //        pm_driver kick <in.ascii> <n> <L> <acc.f64> <dt> <a_old> <a_half> <out.ascii>
+//        pm_driver amr <in.ascii> <n0> <L> <a> <dt> <steps> <out.ascii> <nlev>
+//                  <boxes on level 1> ... <boxes on level nlev-1> <6 ints per box ...>
 #include "nyxpm.h"
 
 #include <cstdio>
@@ -82,8 +89,50 @@ static int kick_with_callers_field(char** argv)
     return 0;
 }
 
+static int amr_steps(int argc, char** argv)
+{
+    const int n0 = std::atoi(argv[3]);
+    const double L = std::atof(argv[4]), a = std::atof(argv[5]), dt = std::atof(argv[6]);
+    const int steps = std::atoi(argv[7]);
+    const int nlev = std::atoi(argv[9]);
+    if (nlev < 1 || argc < 10 + nlev - 1) return 2;
+    std::vector<int> nbox(nlev > 1 ? nlev - 1 : 1, 0), boxes;
+    int total = 0;
+    for (int l = 1; l < nlev; ++l) total += (nbox[l - 1] = std::atoi(argv[9 + l]));
+    if (argc != 10 + (nlev - 1) + 6 * total) return 2;
+    for (int t = 0; t < 6 * total; ++t) boxes.push_back(std::atoi(argv[9 + nlev + t]));
+    std::vector<double> pos, vel, mass;
+    int64_t np = 0;
+    if (read_particles(argv[2], pos, vel, mass, &np)) return 1;
+    nyxpm_params p;
+    nyxpm_default_params(&p);
+    nyxpm_ctx* c = nullptr;
+    if (check(nullptr, nyxpm_create(&p, &c), "nyxpm_create")) return 1;
+    nyxpm_amr* h = nullptr;
+    if (check(c, nyxpm_amr_create(c, n0, L, nlev, nbox.data(), boxes.empty() ? nullptr : boxes.data(), np, &h),
+              "nyxpm_amr_create"))
+        return 1;
+    if (check(c, nyxpm_amr_upload(c, h, pos.data(), vel.data(), mass.data(), 0.0), "nyxpm_amr_upload")) return 1;
+    for (int s = 0; s < steps; ++s) {
+        nyxpm_step_info info;
+        if (check(c, nyxpm_amr_step(c, h, a, a, dt, &info), "nyxpm_amr_step")) return 1;
+        std::printf("step %d vcycles %d %d\n", s + 1, info.old_solve.vcycles, info.new_solve.vcycles);
+    }
+    if (check(c, nyxpm_amr_download(c, h, pos.data(), vel.data()), "nyxpm_amr_download")) return 1;
+    nyxpm_amr_destroy(c, h);
+    nyxpm_destroy(c);
+    char err[256];
+    if (nyxpm_particle_file_write(argv[8], NYXPM_FILE_ASCII, np, pos.data(), vel.data(), mass.data(), 0.0,
+                                  err, sizeof(err)) != NYXPM_OK) {
+        std::fprintf(stderr, "%s\n", err);
+        return 1;
+    }
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
+    if (argc >= 10 && std::strcmp(argv[1], "amr") == 0) return amr_steps(argc, argv);
     if (argc == 10 && std::strcmp(argv[1], "kick") == 0) return kick_with_callers_field(argv);
     if (argc != 7) {
         std::fprintf(stderr, "usage: %s in.ascii n L a0 steps out.ascii\n"

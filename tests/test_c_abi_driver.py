@@ -94,3 +94,35 @@ def test_driver_kicks_with_the_callers_acceleration(tmp_path):
     O.move(n, L, p, g, dt, a_old, a_half, 1)
     opos, ovel = p.by_id()
     assert np.array_equal(cpos, opos) and np.array_equal(cvel, ovel)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no GPU")
+def test_driver_runs_the_reference_multilevel_test(tmp_path):
+    """The reference's Exec/ParticleOnlyTest/inputs.mass.nosub setup through the C
+    ABI from C++: its AsciiFile particles on its fixed grids (amr.regrid_file), no
+    subcycling, a = 1; three multilevel steps against the multilevel oracle
+    (positions 1e-13, velocity change 1e-8: the GPU deposit adds with atomics)."""
+    from nyx_gb300.amr import regrid_file_boxes
+    from oracle import oracle as O
+    exe = build_driver(str(tmp_path))
+    golden = os.path.join(REPO, "tests", "golden")
+    with open(os.path.join(golden, "particle_only_fixed_grids.mass")) as f:
+        boxes = regrid_file_boxes(f)
+    inp = os.path.join(golden, "particle_only_particle_file.mass")
+    out = str(tmp_path / "out.ascii")
+    args = [exe, "amr", inp, "16", "32.0", "1.0", "0.05", "3", out, str(len(boxes) + 1)]
+    args += [str(len(lv)) for lv in boxes]
+    args += [str(v) for lv in boxes for lo, hi in lv for v in (*lo, *hi)]
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert len(r.stdout.strip().splitlines()) == 3
+    cpos, cvel, _ = read_particle_file(out)
+    pos, vel, mass = read_particle_file(inp)
+    p = O.Particles(pos, vel, mass)
+    A = O.AmrOracle(16, 32.0, boxes, p)
+    for _ in range(3):
+        assert A.step(1.0, 1.0, 0.05) == 0
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    assert rel(cpos, p.pos()) <= 1e-13
+    assert rel(cvel - vel, p.vel() - vel) <= 1e-8

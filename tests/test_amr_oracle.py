@@ -52,6 +52,22 @@ def test_regrid_file_boxes_are_refined_and_nested():
     O.AmrOracle(16, 32.0, boxes, p)   # accepted: aligned, disjoint, nested
 
 
+def test_regrid_file_forms():
+    """Regrid files as AMReX writes and reads them: the level count, then per level
+    the box count and the boxes ((lo) (hi) (type)), spaces anywhere, each box in the
+    index space of the level below; a box of coarse cells lo..hi becomes the fine
+    cells 2 lo .. 2 hi + 1."""
+    text = ["1", "2", "((0,0,0) (3,3,3) (0,0,0))", "(( 4 , 6 , 8 )   ( 5,7,9 ) ( 0, 0, 0 ))"]
+    assert regrid_file_boxes(text) == [[((0, 0, 0), (7, 7, 7)), ((8, 12, 16), (11, 15, 19))]]
+    text = ["3", "1", "((2,2,2) (5,5,5) (0,0,0))", "1", "((6,6,6) (9,9,9) (0,0,0))", "1",
+            "((14,14,14) (17,17,17) (0,0,0))"]
+    boxes = regrid_file_boxes(text)
+    assert boxes == [[((4, 4, 4), (11, 11, 11))], [((12, 12, 12), (19, 19, 19))],
+                     [((28, 28, 28), (35, 35, 35))]]
+    p = O.Particles(np.full((1, 3), 0.5), np.zeros((1, 3)), 1.0)
+    O.AmrOracle(8, 1.0, boxes, p)   # three refined levels, nested
+
+
 def test_full_domain_level_equals_single_level_at_twice_the_resolution():
     n0, L = 16, 1.0
     ic = zeldovich_ics(2 * n0, L, -2.0, 11, 0.05, rms_disp_cells=0.3)

@@ -49,3 +49,22 @@ def test_ctypes_mirrors_match_the_header(tmp_path):
         assert int(got[cname]) == C.sizeof(st), cname
         for field, _ in st._fields_:
             assert int(got[f"{cname}.{field}"]) == getattr(st, field).offset, (cname, field)
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="no host C compiler")
+def test_multilevel_field_codes_match_the_header(tmp_path):
+    """nyx_gb300.amr.FIELDS (the `which` argument of nyxpm_amr_field) against the
+    NYXPM_AMR_* constants of the header, through a probe compiled against it."""
+    from nyx_gb300.amr import FIELDS
+    names = {"rho": "NYXPM_AMR_RHO", "phi": "NYXPM_AMR_PHI", "gx": "NYXPM_AMR_GX",
+             "gy": "NYXPM_AMR_GY", "gz": "NYXPM_AMR_GZ", "mass": "NYXPM_AMR_MASS"}
+    assert set(names) == set(FIELDS)
+    src = tmp_path / "codes.c"
+    src.write_text("#include <stdio.h>\n#include \"nyxpm.h\"\nint main(void) {\n" +
+                   "".join(f'    printf("{k} %d\\n", (int){v});\n' for k, v in names.items()) +
+                   "    return 0;\n}\n")
+    exe = tmp_path / "codes"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert {out[i]: int(out[i + 1]) for i in range(0, len(out), 2)} == FIELDS

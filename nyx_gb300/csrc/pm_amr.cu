@@ -28,9 +28,12 @@
 //     residual restricted onto covered coarse cells and the fine flux change
 //     refluxed, one V-cycle of the periodic single-level hierarchy on level 0
 //     (mg_vcycle_zero), trilinear prolongation back up.
-// Every index structure (cell lists, ghost stencils, restriction and face
-// records) is built once on the host when the hierarchy is created; the kernels
-// walk flat lists, one thread per cell, ghost cell, record or particle.
+// Every index structure (ghost stencils with the same-level copies first,
+// restriction and coarse/fine face records, per-cell parents, a prefix of fine
+// cells per box) is built once on the host when the hierarchy is created.  The
+// smoother, residual and norms number the fine cells box by box (a binary search
+// over the prefix finds the box); the other kernels walk flat lists, one thread
+// per cell, ghost cell, record or particle.
 // Built with --fmad=false: only the explicit fma() calls fuse.
 #include "pm_common.cuh"
 
